@@ -1,0 +1,366 @@
+"""Benchmark: batched all-pairs PCC2 on one GB300 (correlations/s), with the plain
+per-pair drop-in, end-to-end host-buffer throughput, latency, roofline and the
+CPU baseline on the same line.
+
+Workload (all-pairs): 64 synthetic stations x 48 windows of 18,000 float32
+samples (noise + a shared band-passed component with per-station delays), all
+2016 station pairs x 48 windows = 96,768 PCC2 correlations per step, lags
++-2000 (4001 lags).  One step = station stage (phase spectra of the 3072 station
+windows) + pair stage (96,768 fused cross-spectrum / inverse-transform / lag
+kernels), inputs resident in HBM.  Inputs (221 MB) and outputs (1.55 GB) exceed
+the 129 MB L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PCC2 correlations/s + p99 latency, served-batched vs plain, 1 GB300, err≤1e-4"
+UNIT = "correlations/s"
+N_STA, N_WIN, N_SAMP, LAG = 64, 48, 18000, 2000
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--stations", type=int, default=N_STA)
+    ap.add_argument("--windows", type=int, default=N_WIN)
+    ap.add_argument("--fmt", default="f32", choices=["f32", "f16"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def all_pairs_index(n_sta, n_win):
+    """(station-window row of station 1, of station 2) for all i<j pairs, window-major;
+    station-window rows are station*n_win + window."""
+    iu, ju = np.triu_indices(n_sta, k=1)
+    w = np.repeat(np.arange(n_win), iu.size)
+    a = np.tile(iu, n_win) * n_win + w
+    b = np.tile(ju, n_win) * n_win + w
+    return np.ascontiguousarray(np.stack([a, b], axis=1).astype(np.int32))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the pair kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "pcc2_pairs_allpairs.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_full_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(x, pairs, budget_s=12.0):
+    """The oracle's PCC2 on host cores over a bounded sample of the workload."""
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    rng = np.random.default_rng(7)
+    done, t0 = 0, time.perf_counter()
+    batch = max(threads, 16)
+    while time.perf_counter() - t0 < budget_s:
+        sel = rng.choice(pairs.shape[0], batch, replace=False)
+        O.pcc2(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)
+        done += batch
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{done} random pair-windows of the all-pairs workload (FP64 oracle, "
+                      f"reference padding 2^ceil(log2(N+M)), OpenMP over windows), {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from fastpcc_gb300 import synth
+    n_sta, n_win = args.stations, args.windows
+    x, _ = synth.all_pairs(n_stations=n_sta, n_windows=n_win, N=N_SAMP)
+    x = x.reshape(n_sta * n_win, N_SAMP)
+    pairs = all_pairs_index(n_sta, n_win)
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(11)
+    per_step = max(2 * threads, 32)
+    for _ in range(args.warmup):
+        sel = rng.choice(pairs.shape[0], threads, replace=False)
+        O.pcc2(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)
+    times = []
+    for _ in range(args.steps):
+        sel = rng.choice(pairs.shape[0], per_step, replace=False)
+        t0 = time.perf_counter()
+        O.pcc2(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = per_step * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded noise + shared band-passed component)",
+        "config": {"workload": f"all-pairs PCC2: {n_sta} stations x {n_win} windows x {N_SAMP} samples, "
+                               f"lags +-{LAG}", "sample_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{per_step} random pair-windows per step (FP64 oracle port of "
+                                   f"src/FFTapps.c pcc2_set; the reference's own source is absent on this host)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import fastpcc_gb300 as F
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    F.build()
+    n_sta, n_win = args.stations, args.windows
+    from fastpcc_gb300 import synth
+    # weak scaling: rank r correlates its own block of windows
+    x, _ = synth.all_pairs(n_stations=n_sta, n_windows=n_win, N=N_SAMP, tag=f"all-pairs/rank{rank}")
+    x = np.ascontiguousarray(x.reshape(n_sta * n_win, N_SAMP))
+    pairs = all_pairs_index(n_sta, n_win)
+    P = pairs.shape[0]
+    L = 2 * LAG + 1
+    fmt = F.F16 if args.fmt == "f16" else F.F32
+    Nz = F.choose_nz(N_SAMP, -LAG, LAG, F.NZ_FAST)
+    esz = 4 if fmt == F.F16 else 8
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    ctx = F.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    d_x = torch.from_numpy(x).to(dev)
+    d_pairs = torch.from_numpy(pairs).to(dev)
+    d_spec = torch.empty((x.shape[0], Nz * esz // 4), dtype=torch.float32, device=dev)
+    d_y = torch.empty((P, L), dtype=torch.float32, device=dev)
+
+    def step():
+        ctx.station_stage(F.PCC2, d_x.data_ptr(), N_SAMP, x.shape[0], N_SAMP, Nz, fmt, F.AMP_F_REG,
+                          d_spec.data_ptr(), Nz)
+        ctx.pair_stage(F.PCC2, d_spec.data_ptr(), Nz, fmt, d_pairs.data_ptr(), P, N_SAMP, Nz, -LAG, LAG,
+                       d_y=d_y.data_ptr(), ldy=L)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    # --- timed: device-resident step ---
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = F.launch_count()
+    with ClockSampler(local) as clk:
+        barrier()
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        barrier()
+    launches = F.launch_count() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = sum(step_ms) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_total], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt.item())
+    value = P * world * args.steps / t_total
+
+    # --- roofline: the pair kernel alone, timed on its stream ---
+    ctx.station_stage(F.PCC2, d_x.data_ptr(), N_SAMP, x.shape[0], N_SAMP, Nz, fmt, F.AMP_F_REG,
+                      d_spec.data_ptr(), Nz)
+    reps = max(3, args.steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(reps):
+        ctx.pair_stage(F.PCC2, d_spec.data_ptr(), Nz, fmt, d_pairs.data_ptr(), P, N_SAMP, Nz, -LAG, LAG,
+                       d_y=d_y.data_ptr(), ldy=L)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    t_pair = e0.elapsed_time(e1) / 1e3 / reps
+    alg_bytes = P * (2 * Nz * esz + 4 * L)
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / t_pair / 1e9
+    traffic = profiled_traffic()
+
+    # --- parity spot check against the oracle ---
+    err = None
+    if rank == 0:
+        from oracle import oracle as O
+        sel = np.random.default_rng(3).choice(P, 8, replace=False)
+        y_gpu = d_y[torch.from_numpy(sel).to(dev)].cpu().numpy()
+        y64 = O.pcc2(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)
+        err = float(O.relerr(y_gpu, y64).max())
+
+    # --- end to end through the C ABI with host buffers (pinned) ---
+    hx = torch.from_numpy(x).pin_memory()
+    hp = torch.from_numpy(pairs).pin_memory()
+    hy = torch.empty((P, L), dtype=torch.float32).pin_memory()
+    hxn, hpn, hyn = hx.numpy(), hp.numpy(), hy.numpy()
+    ctx.allpairs_host(F.PCC2, hxn, hpn, -LAG, LAG, hyn, fmt=fmt)   # warm
+    e2e_steps = max(2, min(args.steps, 5))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.allpairs_host(F.PCC2, hxn, hpn, -LAG, LAG, hyn, fmt=fmt)
+    barrier()
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": P * world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(hxn.nbytes + hpn.nbytes),
+           "d2h_bytes_per_step": int(hyn.nbytes)}
+
+    # --- plain per-pair drop-in (one launch sequence per pair-window), bounded sample ---
+    plain = None
+    if rank == 0:
+        n_plain = 256
+        sel = np.random.default_rng(5).choice(P, n_plain, replace=False)
+        a, b = x[pairs[sel, 0]], x[pairs[sel, 1]]
+        F.pcc2_highlevel(a[:4], b[:4], -LAG, LAG)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        F.pcc2_highlevel(a, b, -LAG, LAG)
+        dt = time.perf_counter() - t0
+        plain = {"value": n_plain / dt, "unit": UNIT, "sample": f"{n_plain} pair-windows through pcc2_highlevel"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(x, pairs)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if fmt == F.F32 else "f32 (f16 spectra)",
+            "data": "synthetic (seeded noise + shared band-passed component, per-station delays)",
+            "config": {"workload": f"all-pairs PCC2: {n_sta} stations x {n_win} windows x {N_SAMP} samples, "
+                                   f"{P} pair-windows per step, lags +-{LAG}",
+                       "Nz": Nz, "spectra": args.fmt, "l2": "inputs 221 MB and outputs 1.55 GB exceed L2; no flush",
+                       "parallelism": f"replicas x{world}"},
+            "max_rel_err": err,
+            "latency_ms": {"p50": statistics.median(step_ms), "p99": float(np.percentile(step_ms, 99)),
+                           "what": "batched step (3072 station windows + 96768 correlations)"},
+            "plain": plain,
+            "gpu_launches": int(launches),
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_pairs (PCC2 pair stage)", "kernel_ms": t_pair * 1e3,
+                         "alg_bytes_per_launch": alg_bytes},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

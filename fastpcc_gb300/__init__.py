@@ -1,0 +1,222 @@
+"""fastpcc_gb300 — GB300-native interstation correlations behind a C ABI.
+
+The compute path is the native library ``libfastpcc_gb300.so`` (sm_103a CUDA
+kernels + C ABI, see include/fastpcc_gb300.h).  This module is the host-side
+mirror of the reference's method layer (FastPCC src/FFTapps.c): the ``*_set``
+functions take the same arguments as the reference's ``pcc2_set``, ``pcc1_set``,
+``pcc_set``, ``ccgn_set``, ``cc1b_set`` — windows of station 1 and station 2 and a
+lag window — with numpy arrays in place of row-pointer arrays, and raise
+``FpccError`` with the library's message where the reference returns a negative
+code.  There is no CPU fallback: without the native library every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfastpcc_gb300.so")
+
+# methods (enum fpcc_method)
+PCC2, GNCC, CC1B, CC1B_POPCOUNT, PCC1, PCCV, WPCC = 0, 1, 2, 3, 4, 5, 6
+# amplitude-normalisation rules (enum fpcc_amp_rule)
+AMP_F_REG, AMP_D_REG, AMP_PURE, AMP_THRESH, AMP_SUMTHR = 0, 1, 2, 3, 4
+F32, F16 = 0, 1
+SIGN_GE, SIGN_GT = 0, 1
+NZ_REFERENCE, NZ_FAST = 0, 1
+
+_lock = threading.Lock()
+_lib = None
+
+
+class FpccError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"fastpcc_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def build(force: bool = False) -> str:
+    from . import native_build
+    return native_build.build(force=force)
+
+
+def lib():
+    """The loaded native library (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise FpccError(-4, f"native library missing: {LIB_PATH} (run fastpcc_gb300.build)")
+            L = C.CDLL(LIB_PATH)
+            i, u, f, i64, vp = C.c_int, C.c_uint, C.c_float, C.c_int64, C.c_void_p
+            fpp = C.POINTER(C.POINTER(C.c_float))
+            L.fpcc_create.argtypes = [C.POINTER(vp), i]
+            L.fpcc_destroy.argtypes = [vp]
+            L.fpcc_set_stream.argtypes = [vp, vp]
+            L.fpcc_get_stream.argtypes = [vp]
+            L.fpcc_get_stream.restype = vp
+            L.fpcc_sync.argtypes = [vp]
+            L.fpcc_last_error.restype = C.c_char_p
+            L.fpcc_version.restype = C.c_char_p
+            L.fpcc_launch_count.restype = i64
+            L.fpcc_choose_nz.argtypes = [i, i, i, i]
+            L.fpcc_max_block_len.restype = i
+            L.fpcc_station_row_elems.argtypes = [i, i, i]
+            L.fpcc_station_row_elems.restype = i64
+            L.fpcc_station_stage.argtypes = [vp, i, vp, i64, i, i, i, i, i, vp, i64]
+            L.fpcc_energy_stage.argtypes = [vp, vp, i64, i, i, vp, i64]
+            L.fpcc_pair_stage.argtypes = [vp, i, vp, i64, i, vp, i, i, i, i, i, f, vp, i64, vp, i64, vp]
+            L.fpcc_host_batched.argtypes = [i, fpp, fpp, fpp, u, u, i, i, f, i, i]
+            L.fpcc_host_plain.argtypes = [i, fpp, fpp, fpp, u, u, i, i, f, i, i]
+            L.fpcc_allpairs_host.argtypes = [vp, i, vp, i, i, vp, i, i, i, f, i, i, vp]
+            for name in ("pcc2_highlevel", "ccgn_highlevel", "cc1b_highlevel"):
+                getattr(L, name).argtypes = [fpp, fpp, fpp, u, u, i, i]
+            L.cc1b_popcount_highlevel.argtypes = [C.POINTER(C.POINTER(C.c_int64)), fpp, fpp, u, u, i, i]
+            _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        raise FpccError(rc, lib().fpcc_last_error().decode(errors="replace"))
+
+
+def launch_count() -> int:
+    return int(lib().fpcc_launch_count())
+
+
+def choose_nz(N: int, Lag1: int, Lag2: int, mode: int = NZ_FAST) -> int:
+    nz = lib().fpcc_choose_nz(N, Lag1, Lag2, mode)
+    if nz <= 0:
+        raise FpccError(-4, f"no supported correlation length for N={N}, lags [{Lag1},{Lag2}]")
+    return nz
+
+
+def lag_count(Lag1: int, Lag2: int) -> int:
+    return abs(Lag2 - Lag1) + 1
+
+
+def _rows(a, ctype=C.c_float):
+    rows = (C.POINTER(ctype) * a.shape[0])()
+    for k in range(a.shape[0]):
+        rows[k] = a[k].ctypes.data_as(C.POINTER(ctype))
+    return rows
+
+
+def _windows(x1, x2):
+    x1 = np.ascontiguousarray(np.atleast_2d(x1), dtype=np.float32)
+    x2 = np.ascontiguousarray(np.atleast_2d(x2), dtype=np.float32)
+    if x1.shape != x2.shape:
+        raise ValueError("x1 and x2 must have the same shape (Tr, N)")
+    return x1, x2, x1.shape[0], x1.shape[1]
+
+
+def correlate(method, x1, x2, Lag1, Lag2, v=2.0, plain=False, nz_mode=NZ_FAST, fmt=F32):
+    """Correlate same-index windows of two stations on the GPU (host arrays in and out)."""
+    x1, x2, Tr, N = _windows(x1, x2)
+    L = lag_count(Lag1, Lag2)
+    y = np.zeros((Tr, L), np.float32)
+    fn = lib().fpcc_host_plain if plain else lib().fpcc_host_batched
+    check(fn(method, _rows(y), _rows(x1), _rows(x2), N, Tr, Lag1, Lag2, float(v), nz_mode, fmt))
+    return y
+
+
+# --- mirror of the reference method layer (src/FFTapps.c) -----------------------
+def pcc2_set(x1, x2, Lag1, Lag2, **kw):
+    """PCC at power 2 (reference pcc2_set, src/FFTapps.c:785)."""
+    return correlate(PCC2, x1, x2, Lag1, Lag2, **kw)
+
+
+def pcc1_set(x1, x2, Lag1, Lag2, **kw):
+    """PCC at power 1 by direct lag sums (reference pcc1_set, src/FFTapps.c:611)."""
+    return correlate(PCC1, x1, x2, Lag1, Lag2, v=1.0, **kw)
+
+
+def pcc_set(x1, x2, v, Lag1, Lag2, **kw):
+    """PCC at power v by direct lag sums, GPU normalisation 2(N-|lag|) (src/ccs_cuda.cu:452)."""
+    return correlate(PCCV, x1, x2, Lag1, Lag2, v=v, **kw)
+
+
+def ccgn_set(x1, x2, Lag1, Lag2, **kw):
+    """Geometrically normalised cross-correlation (reference ccgn_set, src/FFTapps.c:883)."""
+    return correlate(GNCC, x1, x2, Lag1, Lag2, v=0.0, **kw)
+
+
+def cc1b_set(x1, x2, Lag1, Lag2, popcount=False, **kw):
+    """1-bit GNCC (reference cc1b_set, src/FFTapps.c:980); popcount=True uses exact
+    integer numerators from packed sign bits."""
+    return correlate(CC1B_POPCOUNT if popcount else CC1B, x1, x2, Lag1, Lag2, v=0.0, **kw)
+
+
+def cc1b_numerators(x1, x2, Lag1, Lag2):
+    """Exact int64 numerators sum_n s1[n] s2[n+lag] of 1-bit GNCC."""
+    x1, x2, Tr, N = _windows(x1, x2)
+    num = np.zeros((Tr, lag_count(Lag1, Lag2)), np.int64)
+    check(lib().cc1b_popcount_highlevel(_rows(num, C.c_int64), _rows(x1), _rows(x2), N, Tr, Lag1, Lag2))
+    return num
+
+
+def pcc2_highlevel(x1, x2, Lag1, Lag2):
+    """The plain per-pair drop-in (one launch sequence per window) through its C symbol."""
+    x1, x2, Tr, N = _windows(x1, x2)
+    y = np.zeros((Tr, lag_count(Lag1, Lag2)), np.float32)
+    check(lib().pcc2_highlevel(_rows(y), _rows(x1), _rows(x2), N, Tr, Lag1, Lag2))
+    return y
+
+
+class Context:
+    """A device context: its own CUDA stream and workspace (device pointers as ints)."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        check(lib().fpcc_create(C.byref(self._h), device))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().fpcc_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int | None):
+        check(lib().fpcc_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    def stream(self) -> int:
+        return int(lib().fpcc_get_stream(self._h) or 0)
+
+    def sync(self):
+        check(lib().fpcc_sync(self._h))
+
+    def station_stage(self, method, d_x, ldx, nrows, N, Nz, fmt, rule, d_out, ldo):
+        check(lib().fpcc_station_stage(self._h, method, C.c_void_p(d_x), ldx, nrows, N, Nz, fmt, rule,
+                                       C.c_void_p(d_out), ldo))
+
+    def energy_stage(self, d_x, ldx, nrows, N, d_E, ldE):
+        check(lib().fpcc_energy_stage(self._h, C.c_void_p(d_x), ldx, nrows, N, C.c_void_p(d_E), ldE))
+
+    def pair_stage(self, method, d_station, lds, fmt, d_pairs, npairs, N, Nz, Lag1, Lag2, v=0.0,
+                   d_E=0, ldE=0, d_y=0, ldy=0, d_num=0):
+        check(lib().fpcc_pair_stage(self._h, method, C.c_void_p(d_station), lds, fmt, C.c_void_p(d_pairs),
+                                    npairs, N, Nz, Lag1, Lag2, float(v), C.c_void_p(d_E or 0), ldE,
+                                    C.c_void_p(d_y or 0), ldy, C.c_void_p(d_num or 0)))
+
+    def allpairs_host(self, method, x, pairs, Lag1, Lag2, y, v=0.0, nz_mode=NZ_FAST, fmt=F32):
+        """x: (nsta, N) float32 host array (pinned or pageable); pairs (npairs, 2) int32;
+        y: (npairs, L) float32 host output."""
+        assert x.dtype == np.float32 and x.flags.c_contiguous
+        assert pairs.dtype == np.int32 and pairs.flags.c_contiguous
+        assert y.dtype == np.float32 and y.flags.c_contiguous
+        check(lib().fpcc_allpairs_host(self._h, method, C.c_void_p(x.ctypes.data), x.shape[0], x.shape[1],
+                                       C.c_void_p(pairs.ctypes.data), pairs.shape[0], Lag1, Lag2, float(v),
+                                       nz_mode, fmt, C.c_void_p(y.ctypes.data)))

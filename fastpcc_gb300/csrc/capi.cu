@@ -1,0 +1,605 @@
+// C ABI of the correlation engine: contexts, device-resident stages and the
+// host-buffer entry points (batched and plain per-window drop-ins).
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/fastpcc_gb300.h"
+#include "direct.cuh"
+#include "engine.h"
+#include "kernels.cuh"
+#include "menu.cuh"
+
+using namespace fpcc;
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<int64_t> g_launches{0};
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(FPCC_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call)                                              \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);       \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+};
+
+}  // namespace
+
+struct fpcc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  DevBuf dev[16];
+  DevBuf pin[4];
+  std::map<int, float2*> twiddles;   // device tables exp(-2 pi i t/n), per n
+  std::mutex mu;
+};
+
+namespace {
+
+int dev_buf(fpcc_ctx* c, int slot, size_t bytes, void** out) {
+  DevBuf& b = c->dev[slot];
+  if (b.n < bytes) {
+    if (b.p) {
+      cudaStreamSynchronize(c->stream);
+      cudaFree(b.p);
+    }
+    b.p = nullptr;
+    b.n = 0;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) return fail(FPCC_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    b.n = bytes;
+  }
+  *out = b.p;
+  return 0;
+}
+
+int pin_buf(fpcc_ctx* c, int slot, size_t bytes, void** out) {
+  DevBuf& b = c->pin[slot];
+  if (b.n < bytes) {
+    if (b.p) {
+      cudaStreamSynchronize(c->stream);
+      cudaFreeHost(b.p);
+    }
+    b.p = nullptr;
+    b.n = 0;
+    cudaError_t e = cudaMallocHost(&b.p, bytes);
+    if (e != cudaSuccess) return fail(FPCC_ENOMEM, "cudaMallocHost(%zu): %s", bytes, cudaGetErrorString(e));
+    b.n = bytes;
+  }
+  *out = b.p;
+  return 0;
+}
+
+void lag_window(int Lag1, int Lag2, int* lag0, int* L) {
+  if (Lag2 >= Lag1) { *lag0 = Lag1; *L = Lag2 - Lag1 + 1; }
+  else { *lag0 = Lag2; *L = Lag1 - Lag2 + 1; }
+}
+
+bool is_fft_method(int m) { return m == FPCC_PCC2 || m == FPCC_GNCC || m == FPCC_CC1B; }
+
+int check_lags(int N, int Lag1, int Lag2) {
+  if (N <= 0) return fail(FPCC_EARG, "N must be positive");
+  if (abs(Lag1) >= N || abs(Lag2) >= N)
+    return fail(FPCC_EARG, "|lag| must be below N (Lag1=%d Lag2=%d N=%d)", Lag1, Lag2, N);
+  return 0;
+}
+
+fpcc_ctx* g_default = nullptr;
+std::mutex g_default_mu;
+
+int default_ctx(fpcc_ctx** out) {
+  std::lock_guard<std::mutex> lk(g_default_mu);
+  if (!g_default) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int rc = fpcc_create(&g_default, dev);
+    if (rc) return rc;
+  }
+  *out = g_default;
+  return 0;
+}
+
+}  // namespace
+
+// ============================================================== context
+extern "C" int fpcc_create(fpcc_ctx** out, int device) {
+  if (!out) return fail(FPCC_EARG, "null output pointer");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return fail(FPCC_ECUDA, "no CUDA device available");
+  if (device < 0 || device >= ndev) return fail(FPCC_EARG, "device %d out of range", device);
+  CK(cudaSetDevice(device));
+  fpcc_ctx* c = new fpcc_ctx();
+  c->device = device;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  c->own_stream = true;
+  *out = c;
+  return 0;
+}
+
+extern "C" int fpcc_destroy(fpcc_ctx* c) {
+  if (!c) return 0;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& b : c->dev) if (b.p) cudaFree(b.p);
+  for (auto& b : c->pin) if (b.p) cudaFreeHost(b.p);
+  for (auto& kv : c->twiddles) cudaFree(kv.second);
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  {
+    std::lock_guard<std::mutex> lk(g_default_mu);
+    if (c == g_default) g_default = nullptr;
+  }
+  delete c;
+  return 0;
+}
+
+extern "C" int fpcc_set_stream(fpcc_ctx* c, void* stream) {
+  if (!c) return fail(FPCC_EARG, "null context");
+  if (stream == nullptr) {
+    if (!c->own_stream) {
+      CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+      c->own_stream = true;
+    }
+    return 0;
+  }
+  if (c->own_stream) {
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+  }
+  c->stream = (cudaStream_t)stream;
+  c->own_stream = false;
+  return 0;
+}
+
+extern "C" void* fpcc_get_stream(fpcc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" int fpcc_sync(fpcc_ctx* c) {
+  if (!c) return fail(FPCC_EARG, "null context");
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+extern "C" const char* fpcc_last_error(void) { return g_err.c_str(); }
+extern "C" const char* fpcc_version(void) { return "fastpcc_gb300 0.1 (sm_103a)"; }
+extern "C" int64_t fpcc_launch_count(void) { return g_launches.load(); }
+
+// ============================================================== planning
+extern "C" int fpcc_choose_nz(int N, int Lag1, int Lag2, int mode) {
+  const int M = abs(Lag1) > abs(Lag2) ? abs(Lag1) : abs(Lag2);
+  return choose_nz(N, M, mode);
+}
+
+extern "C" int fpcc_max_block_len(void) { return kMenu[kMenuLen - 1]; }
+
+extern "C" int64_t fpcc_station_row_elems(int method, int N, int Nz) {
+  switch (method) {
+    case FPCC_PCC2: return Nz;
+    case FPCC_PCC1:
+    case FPCC_PCCV: return N;
+    case FPCC_GNCC:
+    case FPCC_CC1B: return Nz / 2 + 1;
+    case FPCC_CC1B_POPCOUNT: return (N + 31) / 32;
+    default: return -1;
+  }
+}
+
+// ============================================================== device stages
+namespace {
+
+// Workspace slots of the context.
+enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_PAIRS = 5, S_ANA_A = 6,
+            S_ANA_B = 7, S_RSTAT = 8 };
+
+int twiddle_table(fpcc_ctx* c, int n, const float2** out) {
+  auto it = c->twiddles.find(n);
+  if (it != c->twiddles.end()) { *out = it->second; return 0; }
+  std::vector<float2> h(n);
+  for (int t = 0; t < n; t++) {
+    const double a = -2.0 * M_PI * (double)t / (double)n;
+    h[t] = make_float2((float)cos(a), (float)sin(a));
+  }
+  float2* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, (size_t)n * sizeof(float2));
+  if (e != cudaSuccess) return fail(FPCC_ENOMEM, "twiddle table: %s", cudaGetErrorString(e));
+  e = cudaMemcpy(d, h.data(), (size_t)n * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(d); return cuda_fail(e, "twiddle upload"); }
+  c->twiddles[n] = d;
+  *out = d;
+  return 0;
+}
+
+// Analytic signal of nrows real rows (src/FFTapps.c:104-124): DFT_N, mask,
+// IDFT_N, by generic passes.  Leaves the rows (stride N) in *out and the row
+// statistics (max and sum of |a|^2) in *rmax / *rsum.
+int analytic_rows(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, const float2** out,
+                  const float** rmax, const float** rsum) {
+  FftPlan p;
+  if (!make_plan(N, &p)) return fail(FPCC_EUNSUP, "window length N=%d is not 2,3,5-smooth", N);
+  const float2* tw = nullptr;
+  int rc = twiddle_table(c, N, &tw);
+  if (rc) return rc;
+  void *A, *B, *S;
+  const size_t bytes = (size_t)nrows * N * sizeof(float2);
+  if ((rc = dev_buf(c, S_ANA_A, bytes, &A)) || (rc = dev_buf(c, S_ANA_B, bytes, &B)) ||
+      (rc = dev_buf(c, S_RSTAT, (size_t)2 * nrows * sizeof(float), &S)))
+    return rc;
+  float2* bufs[2] = {(float2*)A, (float2*)B};
+  int cur = 0;   // buffer holding the current data (after the first pass)
+  for (int dir = -1; dir <= 1; dir += 2) {
+    int Ns = 1;
+    for (int i = 0; i < p.npass; i++) {
+      const int R = p.rad[i];
+      const bool first = (dir < 0 && i == 0);
+      float2* dst = first ? bufs[0] : bufs[cur ^ 1];
+      const void* src = first ? (const void*)d_x : (const void*)bufs[cur];
+      CK(launch_gpass(R, dir, src, first, ldx, dst, N, N, Ns, nrows, tw, c->stream));
+      g_launches++;
+      cur = first ? 0 : (cur ^ 1);
+      Ns *= R;
+    }
+    if (p.npass == 0 && dir < 0) {
+      // N == 1: copy the real sample in through a radix-free pass is not possible; unsupported
+      return fail(FPCC_EUNSUP, "N=1");
+    }
+    if (dir < 0) {
+      CK(launch_analytic_mask(bufs[cur], N, N, nrows, c->stream));
+      g_launches++;
+    }
+  }
+  float* st = (float*)S;
+  CK(launch_rowstats(bufs[cur], N, N, nrows, st, st + nrows, c->stream));
+  g_launches++;
+  *out = bufs[cur];
+  *rmax = st;
+  *rsum = st + nrows;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int fpcc_station_stage(fpcc_ctx* c, int method, const float* d_x, int64_t ldx, int nrows, int N,
+                                  int Nz, int fmt, int rule, void* d_out, int64_t ldo) {
+  if (!c) return fail(FPCC_EARG, "null context");
+  if (nrows <= 0) return 0;
+  if (N <= 0) return fail(FPCC_EARG, "N must be positive");
+  int rc;
+  if (method == FPCC_CC1B_POPCOUNT) {
+    CK(launch_sign_bits(d_x, ldx, nrows, N, (uint32_t*)d_out, ldo, rule == FPCC_SIGN_GE ? 1 : 0, nullptr,
+                        c->stream));
+    g_launches++;
+    return 0;
+  }
+  if (method == FPCC_PCC1 || method == FPCC_PCCV) {
+    const float2 *an; const float *rmax, *rsum;
+    if ((rc = analytic_rows(c, d_x, ldx, nrows, N, &an, &rmax, &rsum))) return rc;
+    PhaseArgs a{};
+    a.in = an; a.ldin = N; a.nrows = nrows; a.N = N; a.rule = rule;
+    a.rowstat = (rule == FPCC_AMP_SUMTHR) ? rsum : rmax;
+    a.fmt = fmt; a.out = d_out; a.ldo = ldo;
+    CK(launch_phase_store(a, c->stream));
+    g_launches++;
+    return 0;
+  }
+  if (method != FPCC_PCC2 && method != FPCC_GNCC && method != FPCC_CC1B)
+    return fail(FPCC_EUNSUP, "method %d has no station stage", method);
+  if (Nz < N || (Nz & 1)) return fail(FPCC_EARG, "Nz=%d must be even and >= N=%d", Nz, N);
+  if (!spec_supported(Nz)) return fail(FPCC_EUNSUP, "Nz=%d is not a supported transform length", Nz);
+  if ((method == FPCC_GNCC || method == FPCC_CC1B) && fmt != FPCC_F32)
+    return fail(FPCC_EUNSUP, "real-trace spectra are stored in F32");
+  SpecArgs a{};
+  a.nrows = nrows; a.N = N; a.Nz = Nz; a.fmt = fmt; a.out = d_out; a.ldo = ldo;
+  if (method == FPCC_PCC2) {
+    const float2 *an; const float *rmax, *rsum;
+    if ((rc = analytic_rows(c, d_x, ldx, nrows, N, &an, &rmax, &rsum))) return rc;
+    a.in = an; a.ldin = N; a.mode = SPEC_PHASE; a.rule = rule;
+    a.rowstat = (rule == FPCC_AMP_SUMTHR) ? rsum : rmax;
+  } else {
+    a.in = d_x; a.ldin = ldx;
+    a.mode = (method == FPCC_GNCC) ? SPEC_REAL : SPEC_SIGN;
+    a.sign_ge = (rule == FPCC_SIGN_GE) ? 1 : 0;
+  }
+  CK(launch_spec(a, c->stream));
+  g_launches++;
+  return 0;
+}
+
+extern "C" int fpcc_energy_stage(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, double* d_E,
+                                 int64_t ldE) {
+  if (!c) return fail(FPCC_EARG, "null context");
+  CK(launch_energy_prefix(d_x, ldx, nrows, N, d_E, ldE, c->stream));
+  g_launches++;
+  return 0;
+}
+
+extern "C" int fpcc_pair_stage(fpcc_ctx* c, int method, const void* d_station, int64_t lds, int fmt,
+                               const int32_t* d_pairs, int npairs, int N, int Nz, int Lag1, int Lag2, float v,
+                               const double* d_E, int64_t ldE, float* d_y, int64_t ldy, int64_t* d_num) {
+  if (!c) return fail(FPCC_EARG, "null context");
+  if (npairs <= 0) return 0;
+  int rc = check_lags(N, Lag1, Lag2);
+  if (rc) return rc;
+  int lag0, L;
+  lag_window(Lag1, Lag2, &lag0, &L);
+  const int M = abs(Lag1) > abs(Lag2) ? abs(Lag1) : abs(Lag2);
+  if (is_fft_method(method)) {
+    if (Nz < N + M || (Nz & 1)) return fail(FPCC_EARG, "Nz=%d must be even and >= N+M=%d", Nz, N + M);
+    PairArgs a{};
+    a.spec = d_station;
+    a.ldspec = lds;
+    a.fmt = fmt;
+    a.pairs = reinterpret_cast<const int2*>(d_pairs);
+    a.npairs = npairs;
+    a.Nz = Nz;
+    if (!pair_supported(Nz)) return fail(FPCC_EUNSUP, "Nz=%d is not a supported correlation length", Nz);
+    a.lag0 = lag0;
+    a.L = L;
+    a.y = d_y;
+    a.ldy = ldy;
+    a.N = N;
+    if (method == FPCC_PCC2) {
+      a.norm = 0;
+      a.scale = 1.0f / ((float)Nz * (float)N);   // src/FFTapps.c:832
+    } else if (method == FPCC_GNCC) {
+      if (!d_E) return fail(FPCC_EARG, "GNCC needs the energy prefix sums");
+      a.norm = 1;
+      a.energy = d_E;
+      a.ldE = ldE;
+      a.scale = (float)(1.0 / (double)Nz);       // src/FFTapps.c:340
+      if (fmt != FPCC_F32) return fail(FPCC_EUNSUP, "GNCC spectra are F32");
+    } else {
+      a.norm = 2;
+      a.scale = (float)(1.0 / (double)Nz);       // src/FFTapps.c:357
+      if (fmt != FPCC_F32) return fail(FPCC_EUNSUP, "1-bit spectra are F32");
+    }
+    CK(launch_pairs(a, c->stream));
+    g_launches++;
+    return 0;
+  }
+  if (method == FPCC_PCC1 || method == FPCC_PCCV) {
+    PccvArgs a{};
+    a.phase = d_station;
+    a.ldp = lds;
+    a.half = (fmt == FPCC_F16);
+    a.pairs = reinterpret_cast<const int2*>(d_pairs);
+    a.npairs = npairs;
+    a.N = N;
+    a.Lag1 = lag0;
+    a.L = L;
+    a.v = (method == FPCC_PCC1) ? 1.0f : v;
+    // the PCC1 path and the GPU PCC_v path divide by 2(N-|lag|) (src/FFTapps.c:276,
+    // src/ccs_cuda.cu:452); the CPU PCC_v path by 2^(v/2)(N-|lag|) (src/FFTapps.c:334)
+    a.norm_gpu = 1;
+    a.y = d_y;
+    a.ldy = ldy;
+    CK(launch_pccv(a, c->stream));
+    g_launches++;
+    return 0;
+  }
+  if (method == FPCC_CC1B_POPCOUNT) {
+    Cc1bArgs a{};
+    a.bits = (const uint32_t*)d_station;
+    a.ldb = lds;
+    a.pairs = reinterpret_cast<const int2*>(d_pairs);
+    a.npairs = npairs;
+    a.N = N;
+    a.lag0 = lag0;
+    a.L = L;
+    a.y = d_y;
+    a.num = reinterpret_cast<long long*>(d_num);
+    a.ldy = ldy;
+    CK(launch_cc1b_popcount(a, c->stream));
+    g_launches++;
+    return 0;
+  }
+  return fail(FPCC_EUNSUP, "method %d has no pair stage", method);
+}
+
+// ============================================================== host entry points
+namespace {
+
+struct Layout {
+  int method, N, Nz, lag0, L, fmt;
+  int64_t lds;      // station row elements
+  size_t esz;       // station element bytes
+  bool two_rules;   // 1-bit: station 1 and 2 rows use different sign rules
+};
+
+int make_layout(int method, int N, int Lag1, int Lag2, int nz_mode, int fmt, Layout* o) {
+  int rc = check_lags(N, Lag1, Lag2);
+  if (rc) return rc;
+  o->method = method;
+  o->N = N;
+  lag_window(Lag1, Lag2, &o->lag0, &o->L);
+  o->Nz = is_fft_method(method) ? fpcc_choose_nz(N, Lag1, Lag2, nz_mode) : N;
+  if (o->Nz <= 0) return fail(FPCC_EUNSUP, "no padded length for N=%d", N);
+  if (method == FPCC_GNCC || method == FPCC_CC1B) fmt = FPCC_F32;
+  o->fmt = fmt;
+  o->lds = fpcc_station_row_elems(method, N, o->Nz);
+  if (o->lds < 0) return fail(FPCC_EUNSUP, "method %d not available here", method);
+  o->esz = (method == FPCC_CC1B_POPCOUNT) ? 4 : (fmt == FPCC_F16 ? 4 : 8);
+  o->two_rules = (method == FPCC_CC1B || method == FPCC_CC1B_POPCOUNT);
+  return 0;
+}
+
+// Station stage then pair stage on the context stream.  For the 1-bit methods
+// the sign rule depends on the role of the trace (src/FFTapps.c:1037,1042):
+// split >= 0 gives rows [0, split) the station-1 rule and the rest the station-2
+// rule; split < 0 computes both variants (rows [0,nsta) and [nsta,2 nsta)) and
+// expects each pair's station-2 index to point into the second half.
+int run_device(fpcc_ctx* c, const Layout& Ly, const float* d_x, int nsta, const int32_t* d_pairs, int npairs,
+               float v, float* d_y, int64_t* d_num, int split) {
+  void* d_st = nullptr;
+  int rc;
+  const int method = Ly.method;
+  const bool both = Ly.two_rules && split < 0;
+  const int nrows_st = both ? 2 * nsta : nsta;
+  if ((rc = dev_buf(c, S_STATION, (size_t)nrows_st * Ly.lds * Ly.esz, &d_st))) return rc;
+  char* base = (char*)d_st;
+  const size_t rowb = (size_t)Ly.lds * Ly.esz;
+  if (Ly.two_rules) {
+    const int n1 = both ? nsta : split;
+    if (n1 > 0 && (rc = fpcc_station_stage(c, method, d_x, Ly.N, n1, Ly.N, Ly.Nz, Ly.fmt, FPCC_SIGN_GE, base,
+                                           Ly.lds)))
+      return rc;
+    if (both) {
+      if ((rc = fpcc_station_stage(c, method, d_x, Ly.N, nsta, Ly.N, Ly.Nz, Ly.fmt, FPCC_SIGN_GT,
+                                   base + (size_t)nsta * rowb, Ly.lds)))
+        return rc;
+    } else if (nsta - split > 0) {
+      if ((rc = fpcc_station_stage(c, method, d_x + (size_t)split * Ly.N, Ly.N, nsta - split, Ly.N, Ly.Nz, Ly.fmt,
+                                   FPCC_SIGN_GT, base + (size_t)split * rowb, Ly.lds)))
+        return rc;
+    }
+  } else {
+    if ((rc = fpcc_station_stage(c, method, d_x, Ly.N, nsta, Ly.N, Ly.Nz, Ly.fmt, FPCC_AMP_F_REG, d_st, Ly.lds)))
+      return rc;
+  }
+  double* d_E = nullptr;
+  if (method == FPCC_GNCC) {
+    void* p = nullptr;
+    if ((rc = dev_buf(c, S_ENERGY, (size_t)nsta * (Ly.N + 1) * sizeof(double), &p))) return rc;
+    d_E = (double*)p;
+    if ((rc = fpcc_energy_stage(c, d_x, Ly.N, nsta, Ly.N, d_E, Ly.N + 1))) return rc;
+  }
+  return fpcc_pair_stage(c, method, d_st, Ly.lds, Ly.fmt, d_pairs, npairs, Ly.N, Ly.Nz, Ly.lag0,
+                         Ly.lag0 + Ly.L - 1, v, d_E, Ly.N + 1, d_y, Ly.L, d_num);
+}
+
+int host_windows(int method, float** y, int64_t** num, float** x1, float** x2, unsigned N, unsigned Tr, int Lag1,
+                 int Lag2, float v, int nz_mode, int fmt, bool plain) {
+  if (!x1 || !x2 || (!y && !num)) return fail(FPCC_EARG, "null row arrays");
+  if (Tr == 0) return 0;
+  fpcc_ctx* c = nullptr;
+  int rc = default_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  Layout Ly;
+  if ((rc = make_layout(method, (int)N, Lag1, Lag2, nz_mode, fmt, &Ly))) return rc;
+  const unsigned nwin = plain ? 1u : Tr;   // windows per launch sequence
+  const size_t xbytes = (size_t)2 * nwin * N * sizeof(float);
+  const size_t ybytes = (size_t)nwin * Ly.L * (num ? sizeof(int64_t) : sizeof(float));
+  void *h_x, *h_y, *d_x, *d_y, *d_pairs;
+  if ((rc = pin_buf(c, 0, xbytes, &h_x)) || (rc = pin_buf(c, 1, ybytes, &h_y))) return rc;
+  if ((rc = dev_buf(c, S_HOST_X, xbytes, &d_x)) || (rc = dev_buf(c, S_Y, ybytes, &d_y)) ||
+      (rc = dev_buf(c, S_PAIRS, (size_t)2 * nwin * sizeof(int32_t), &d_pairs)))
+    return rc;
+  std::vector<int32_t> pairs(2 * nwin);
+  for (unsigned t = 0; t < nwin; t++) { pairs[2 * t] = (int32_t)t; pairs[2 * t + 1] = (int32_t)(nwin + t); }
+  CK(cudaMemcpyAsync(d_pairs, pairs.data(), pairs.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  for (unsigned t0 = 0; t0 < Tr; t0 += nwin) {
+    float* hx = (float*)h_x;
+    for (unsigned t = 0; t < nwin; t++) {
+      memcpy(hx + (size_t)t * N, x1[t0 + t], N * sizeof(float));
+      memcpy(hx + (size_t)(nwin + t) * N, x2[t0 + t], N * sizeof(float));
+    }
+    CK(cudaMemcpyAsync(d_x, h_x, xbytes, cudaMemcpyHostToDevice, c->stream));
+    if (num) {
+      if ((rc = run_device(c, Ly, (const float*)d_x, 2 * nwin, (const int32_t*)d_pairs, nwin, v, nullptr,
+                           (int64_t*)d_y, (int)nwin)))
+        return rc;
+    } else {
+      if ((rc = run_device(c, Ly, (const float*)d_x, 2 * nwin, (const int32_t*)d_pairs, nwin, v, (float*)d_y,
+                           nullptr, (int)nwin)))
+        return rc;
+    }
+    CK(cudaMemcpyAsync(h_y, d_y, ybytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (unsigned t = 0; t < nwin; t++) {
+      if (num) memcpy(num[t0 + t], (int64_t*)h_y + (size_t)t * Ly.L, Ly.L * sizeof(int64_t));
+      else memcpy(y[t0 + t], (float*)h_y + (size_t)t * Ly.L, Ly.L * sizeof(float));
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int fpcc_host_batched(int method, float** y, float** x1, float** x2, unsigned N, unsigned Tr, int Lag1,
+                                 int Lag2, float v, int nz_mode, int fmt) {
+  return host_windows(method, y, nullptr, x1, x2, N, Tr, Lag1, Lag2, v, nz_mode, fmt, false);
+}
+
+extern "C" int fpcc_host_plain(int method, float** y, float** x1, float** x2, unsigned N, unsigned Tr, int Lag1,
+                               int Lag2, float v, int nz_mode, int fmt) {
+  return host_windows(method, y, nullptr, x1, x2, N, Tr, Lag1, Lag2, v, nz_mode, fmt, true);
+}
+
+extern "C" int fpcc_allpairs_host(fpcc_ctx* c, int method, const float* h_x, int nsta, int N, const int32_t* h_pairs,
+                                  int npairs, int Lag1, int Lag2, float v, int nz_mode, int fmt, float* h_y) {
+  if (!c || !h_x || !h_pairs || !h_y) return fail(FPCC_EARG, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  Layout Ly;
+  int rc = make_layout(method, N, Lag1, Lag2, nz_mode, fmt, &Ly);
+  if (rc) return rc;
+  const size_t xbytes = (size_t)nsta * N * sizeof(float);
+  const size_t ybytes = (size_t)npairs * Ly.L * sizeof(float);
+  const size_t pbytes = (size_t)npairs * 2 * sizeof(int32_t);
+  void *d_x, *d_y, *d_p;
+  if ((rc = dev_buf(c, S_HOST_X, xbytes, &d_x)) || (rc = dev_buf(c, S_Y, ybytes, &d_y)) ||
+      (rc = dev_buf(c, S_PAIRS, pbytes, &d_p)))
+    return rc;
+  CK(cudaMemcpyAsync(d_x, h_x, xbytes, cudaMemcpyHostToDevice, c->stream));
+  if (Ly.two_rules) {
+    // station 2 of each pair reads the station-2-rule variant (second half of the rows)
+    std::vector<int32_t> hp(h_pairs, h_pairs + 2 * (size_t)npairs);
+    for (int i = 0; i < npairs; i++) hp[2 * i + 1] += nsta;
+    CK(cudaMemcpyAsync(d_p, hp.data(), pbytes, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  } else {
+    CK(cudaMemcpyAsync(d_p, h_pairs, pbytes, cudaMemcpyHostToDevice, c->stream));
+  }
+  if ((rc = run_device(c, Ly, (const float*)d_x, nsta, (const int32_t*)d_p, npairs, v, (float*)d_y, nullptr, -1)))
+    return rc;
+  CK(cudaMemcpyAsync(h_y, d_y, ybytes, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+// Drop-in siblings of the reference's per-pair GPU calls (plain form).
+extern "C" int pcc2_highlevel(float** y, float** x1, float** x2, unsigned N, unsigned Tr, int Lag1, int Lag2) {
+  return host_windows(FPCC_PCC2, y, nullptr, x1, x2, N, Tr, Lag1, Lag2, 2.0f, FPCC_NZ_FAST, FPCC_F32, true);
+}
+extern "C" int ccgn_highlevel(float** y, float** x1, float** x2, unsigned N, unsigned Tr, int Lag1, int Lag2) {
+  return host_windows(FPCC_GNCC, y, nullptr, x1, x2, N, Tr, Lag1, Lag2, 0.0f, FPCC_NZ_FAST, FPCC_F32, true);
+}
+extern "C" int cc1b_highlevel(float** y, float** x1, float** x2, unsigned N, unsigned Tr, int Lag1, int Lag2) {
+  return host_windows(FPCC_CC1B, y, nullptr, x1, x2, N, Tr, Lag1, Lag2, 0.0f, FPCC_NZ_FAST, FPCC_F32, true);
+}
+extern "C" int cc1b_popcount_highlevel(int64_t** num, float** x1, float** x2, unsigned N, unsigned Tr, int Lag1,
+                                       int Lag2) {
+  return host_windows(FPCC_CC1B_POPCOUNT, nullptr, num, x1, x2, N, Tr, Lag1, Lag2, 0.0f, FPCC_NZ_FAST, FPCC_F32,
+                      true);
+}

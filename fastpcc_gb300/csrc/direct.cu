@@ -1,0 +1,214 @@
+// Direct (non-FFT) kernels:
+//   - FP64 prefix sums of x^2 per station window (GNCC overlap energies,
+//     reference gn_lowlevel src/FFTapps.c:372-399 updates the same sums
+//     incrementally),
+//   - PCC at power v by direct lag sums over phase signals
+//     (src/FFTapps.c:223-336, src/ccs_cuda.cu:260-321,388-453),
+//   - 1-bit GNCC numerators as exact popcounts of packed sign bits.
+#include "direct.cuh"
+
+namespace fpcc {
+
+namespace {
+
+// ---------------------------------------------------------------- energies
+__global__ void __launch_bounds__(256) k_energy_prefix(const float* __restrict__ x, int64_t ldx, int N,
+                                                       double* __restrict__ E, int64_t ldE) {
+  __shared__ double wsum[8];
+  __shared__ double carry_s;
+  const float* xr = x + (int64_t)blockIdx.x * ldx;
+  double* Er = E + (int64_t)blockIdx.x * ldE;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) { Er[0] = 0.0; carry_s = 0.0; }
+  __syncthreads();
+  for (int t0 = 0; t0 < N; t0 += 256) {
+    const int n = t0 + threadIdx.x;
+    double v = 0.0;
+    if (n < N) { const double f = (double)__ldg(xr + n); v = f * f; }
+    // inclusive warp scan
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      double u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    double off = carry_s;
+    for (int i = 0; i < w; i++) off += wsum[i];
+    if (n < N) Er[n + 1] = off + v;
+    __syncthreads();
+    if (threadIdx.x == 255) carry_s = off + v;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- PCC_v direct
+// One thread per lag, 256 lags per block; phase signals staged in shared memory
+// in tiles of TILE samples (zeros outside [0,N), which contribute nothing since
+// |0+b| - |0-b| = 0).  Each tile's terms are summed in FP32 and the tile sums
+// are accumulated in FP64.
+constexpr int kLagBlock = 256;
+constexpr int kTile = 512;
+
+template <int MODE, bool HALF>   // MODE 1: v = 1, 2: v = 2, 0: general power
+__global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
+  __shared__ float2 s1[kTile];
+  __shared__ float2 s2[kTile + kLagBlock];
+  const int p = blockIdx.x;
+  const int2 pr = a.pairs[p];
+  const int N = a.N;
+  const int lblk = blockIdx.y * kLagBlock;       // first lag index of the block
+  const int l = lblk + threadIdx.x;
+  const int lagb = a.Lag1 + lblk;                 // lag of thread 0
+  const float V = 0.5f * a.v;
+  double acc = 0.0;
+  const float2* P1f = reinterpret_cast<const float2*>(a.phase) + (int64_t)pr.x * a.ldp;
+  const float2* P2f = reinterpret_cast<const float2*>(a.phase) + (int64_t)pr.y * a.ldp;
+  const __half2* P1h = reinterpret_cast<const __half2*>(a.phase) + (int64_t)pr.x * a.ldp;
+  const __half2* P2h = reinterpret_cast<const __half2*>(a.phase) + (int64_t)pr.y * a.ldp;
+  // samples n of station 1 that overlap any lag of the block
+  int nlo = -(lagb + kLagBlock - 1);
+  if (nlo < 0) nlo = 0;
+  int nhi = N - lagb;
+  if (nhi > N) nhi = N;
+  for (int n0 = nlo; n0 < nhi; n0 += kTile) {
+    for (int i = threadIdx.x; i < kTile; i += kLagBlock) {
+      const int n = n0 + i;
+      float2 v = make_float2(0.f, 0.f);
+      if (n < N) v = HALF ? __half22float2(P1h[n]) : P1f[n];
+      s1[i] = v;
+    }
+    for (int i = threadIdx.x; i < kTile + kLagBlock; i += kLagBlock) {
+      const int n = n0 + lagb + i;
+      float2 v = make_float2(0.f, 0.f);
+      if (n >= 0 && n < N) v = HALF ? __half22float2(P2h[n]) : P2f[n];
+      s2[i] = v;
+    }
+    __syncthreads();
+    float part = 0.0f;
+    const float2* b = s2 + threadIdx.x;
+#pragma unroll 8
+    for (int i = 0; i < kTile; i++) {
+      const float2 u = s1[i];
+      const float2 w = b[i];
+      const float sx = u.x + w.x, sy = u.y + w.y;
+      const float dx = u.x - w.x, dy = u.y - w.y;
+      const float s2v = sx * sx + sy * sy;
+      const float d2v = dx * dx + dy * dy;
+      if (MODE == 1) part += sqrtf(s2v) - sqrtf(d2v);
+      else if (MODE == 2) part += s2v - d2v;
+      else part += powf(s2v, V) - powf(d2v, V);
+    }
+    acc += (double)part;
+    __syncthreads();
+  }
+  if (l < a.L) {
+    const int lag = a.Lag1 + l;
+    float* y = a.y + (int64_t)p * a.ldy;
+    if (lag < -N || lag > N) { y[l] = 0.0f; return; }
+    const double cnt = (double)(N - abs(lag));
+    const double D = a.norm_gpu ? 2.0 * cnt : exp2((double)V) * cnt;
+    y[l] = (float)(acc / D);
+  }
+}
+
+// ---------------------------------------------------------------- 1-bit bits
+// bit i of word w is 1 when sample 32w+i maps to -1: x < 0 for the station-1
+// rule (x >= 0 -> +1), x <= 0 for the station-2 rule (x > 0 -> +1).
+__global__ void k_sign_bits(const float* __restrict__ x, int64_t ldx, int N, uint32_t* __restrict__ bits,
+                            int64_t ldb, int pos_ge, const int8_t* __restrict__ sel) {
+  // one warp per 32-sample word (blockDim is a multiple of 32)
+  const int row = blockIdx.x;
+  const int n = blockIdx.y * blockDim.x + threadIdx.x;
+  const int nw = (N + 31) >> 5;
+  const int ge = sel ? sel[row] : pos_ge;
+  const float* xr = x + (int64_t)row * ldx;
+  bool neg = false;
+  if (n < N) {
+    const float v = __ldg(xr + n);
+    neg = ge ? !(v >= 0.0f) : !(v > 0.0f);
+  }
+  const uint32_t m = __ballot_sync(0xffffffffu, neg);
+  if ((threadIdx.x & 31) == 0 && (n >> 5) < nw) bits[(int64_t)row * ldb + (n >> 5)] = m;
+}
+
+// 32 bits of a packed stream starting at bit position b (b >= 0); words beyond
+// the row read as zero.
+__device__ __forceinline__ uint32_t bits_at(const uint32_t* r, int nw, int b) {
+  const int w = b >> 5, s = b & 31;
+  const uint32_t lo = (w < nw) ? __ldg(r + w) : 0u;
+  const uint32_t hi = (w + 1 < nw) ? __ldg(r + w + 1) : 0u;
+  return __funnelshift_r(lo, hi, s);
+}
+
+// numerator(lag) = overlap - 2 * popcount(b1[n] xor b2[n+lag]) over the overlap.
+__global__ void __launch_bounds__(256) k_cc1b_popcount(Cc1bArgs a) {
+  const int p = blockIdx.x;
+  const int l = blockIdx.y * blockDim.x + threadIdx.x;
+  if (l >= a.L) return;
+  const int2 pr = a.pairs[p];
+  const int N = a.N, nw = (N + 31) >> 5;
+  const uint32_t* B1 = a.bits + (int64_t)pr.x * a.ldb;
+  const uint32_t* B2 = a.bits + (int64_t)pr.y * a.ldb;
+  const int lag = a.lag0 + l;
+  const int n1 = lag < 0 ? -lag : 0;
+  const int n2 = lag < 0 ? N : N - lag;
+  const int cnt = n2 - n1;
+  int mism = 0;
+  for (int n = n1; n < n2; n += 32) {
+    const uint32_t u = bits_at(B1, nw, n);
+    const uint32_t v = bits_at(B2, nw, n + lag);
+    uint32_t d = u ^ v;
+    const int rem = n2 - n;
+    if (rem < 32) d &= (1u << rem) - 1u;
+    mism += __popc(d);
+  }
+  const long long num = (long long)cnt - 2LL * mism;
+  if (a.num) a.num[(int64_t)p * a.ldy + l] = num;
+  if (a.y) a.y[(int64_t)p * a.ldy + l] = (float)((double)num / (double)cnt);
+}
+
+}  // namespace
+
+cudaError_t launch_energy_prefix(const float* x, int64_t ldx, int nrows, int N, double* E, int64_t ldE,
+                                 cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  k_energy_prefix<<<nrows, 256, 0, st>>>(x, ldx, N, E, ldE);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st) {
+  if (a.npairs <= 0 || a.L <= 0) return cudaSuccess;
+  if ((a.L + kLagBlock - 1) / kLagBlock > 65535) return cudaErrorInvalidValue;
+  dim3 grid(a.npairs, (a.L + kLagBlock - 1) / kLagBlock);
+  const int mode = (a.v == 1.0f) ? 1 : (a.v == 2.0f ? 2 : 0);
+  if (a.half) {
+    if (mode == 1) k_pccv<1, true><<<grid, kLagBlock, 0, st>>>(a);
+    else if (mode == 2) k_pccv<2, true><<<grid, kLagBlock, 0, st>>>(a);
+    else k_pccv<0, true><<<grid, kLagBlock, 0, st>>>(a);
+  } else {
+    if (mode == 1) k_pccv<1, false><<<grid, kLagBlock, 0, st>>>(a);
+    else if (mode == 2) k_pccv<2, false><<<grid, kLagBlock, 0, st>>>(a);
+    else k_pccv<0, false><<<grid, kLagBlock, 0, st>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sign_bits(const float* x, int64_t ldx, int nrows, int N, uint32_t* bits, int64_t ldb,
+                             int pos_ge, const int8_t* sel, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  if ((N + 255) / 256 > 65535) return cudaErrorInvalidValue;
+  dim3 grid(nrows, (N + 255) / 256);
+  k_sign_bits<<<grid, 256, 0, st>>>(x, ldx, N, bits, ldb, pos_ge, sel);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cc1b_popcount(const Cc1bArgs& a, cudaStream_t st) {
+  if (a.npairs <= 0 || a.L <= 0) return cudaSuccess;
+  if ((a.L + 255) / 256 > 65535) return cudaErrorInvalidValue;
+  dim3 grid(a.npairs, (a.L + 255) / 256);
+  k_cc1b_popcount<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace fpcc

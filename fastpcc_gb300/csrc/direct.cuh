@@ -1,0 +1,45 @@
+// Direct (non-FFT) kernels: energies, PCC_v lag sums, 1-bit popcounts.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fpcc {
+
+struct PccvArgs {
+  const void* phase;   // phase signals, N complex per row (float2 or half2)
+  int64_t ldp;
+  int half;            // 1: half2 storage
+  const int2* pairs;   // (row of station 1, row of station 2)
+  int npairs;
+  int N;
+  int Lag1;            // lag of output 0 (Lag1 <= Lag2)
+  int L;               // number of outputs
+  float v;             // power
+  int norm_gpu;        // 1: divide by 2(N-|lag|); 0: by 2^(v/2)(N-|lag|)
+  float* y;
+  int64_t ldy;
+};
+
+struct Cc1bArgs {
+  const uint32_t* bits;  // packed sign bits, ldb words per row
+  int64_t ldb;
+  const int2* pairs;
+  int npairs;
+  int N;
+  int lag0;
+  int L;
+  float* y;              // optional normalised output (num / overlap)
+  long long* num;        // optional exact numerators
+  int64_t ldy;
+};
+
+cudaError_t launch_energy_prefix(const float* x, int64_t ldx, int nrows, int N, double* E, int64_t ldE,
+                                 cudaStream_t st);
+cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st);
+cudaError_t launch_sign_bits(const float* x, int64_t ldx, int nrows, int N, uint32_t* bits, int64_t ldb,
+                             int pos_ge, const int8_t* sel, cudaStream_t st);
+cudaError_t launch_cc1b_popcount(const Cc1bArgs& a, cudaStream_t st);
+
+}  // namespace fpcc

@@ -1,0 +1,85 @@
+// Host-side planning: radix schedules and padded correlation lengths.
+#include <math.h>
+
+#include "engine.h"
+#include "menu.cuh"
+
+namespace fpcc {
+
+bool factor235(int n, int* a, int* b, int* c) {
+  if (n < 1) return false;
+  *a = *b = *c = 0;
+  while (n % 2 == 0) { n /= 2; (*a)++; }
+  while (n % 3 == 0) { n /= 3; (*b)++; }
+  while (n % 5 == 0) { n /= 5; (*c)++; }
+  return n == 1;
+}
+
+static void encode(FftPlan* p) {
+  p->code = 0;
+  for (int i = p->npass - 1; i >= 0; i--) p->code = (p->code << 5) | (uint64_t)p->rad[i];
+}
+
+bool make_plan(int n, FftPlan* p, const int* forced, int nforced) {
+  const bool ok = make_plan_raw(n, p, forced, nforced);
+  encode(p);
+  return ok;
+}
+
+bool make_plan_raw(int n, FftPlan* p, const int* forced, int nforced) {
+  p->n = n;
+  p->npass = 0;
+  if (forced) {
+    long prod = 1;
+    for (int i = 0; i < nforced && i < kMaxPass; i++) {
+      p->rad[p->npass++] = forced[i];
+      prod *= forced[i];
+    }
+    return prod == n;
+  }
+  int a, b, c;
+  if (!factor235(n, &a, &b, &c)) return false;
+  if (n == 1) return true;
+  const int np2 = (a + 3) / 4;
+  for (int i = 0; i < np2; i++) {
+    // spread the exponent a over np2 passes as evenly as possible
+    const int e = a / np2 + (i < a % np2 ? 1 : 0);
+    p->rad[p->npass++] = 1 << e;
+  }
+  for (int i = 0; i < c; i++) p->rad[p->npass++] = 5;
+  for (int i = 0; i < b; i++) p->rad[p->npass++] = 3;
+  return p->npass <= kMaxPass;
+}
+
+double plan_cost(int n) {
+  FftPlan p;
+  if (!make_plan(n, &p)) return 1e30;
+  double c = 0;
+  for (int i = 0; i < p.npass; i++) {
+    // one shared-memory round trip per pass plus the butterfly work per point
+    const int R = p.rad[i];
+    c += 1.0 + 0.35 * log2((double)R) + (R == 3 || R == 5 ? 0.6 : 0.0);
+  }
+  return c * (double)n;
+}
+
+int choose_nz(int N, int M, int mode) {
+  const int need = N + M;
+  if (mode == 0) {
+    const int nz = 1 << (int)ceil(log2((double)need));
+    return (on_menu(nz) && on_menu(nz / 2)) ? nz : -1;
+  }
+  // menu lengths whose half is also on the menu; the pair transform (Nz/2)
+  // dominates the cost of a batch of correlations
+  int best = -1;
+  double bc = 1e300;
+  for (int i = 0; i < kMenuLen; i++) {
+    const int nz = kMenu[i];
+    if (nz < need || !on_menu(nz / 2)) continue;
+    const double cost = plan_cost(nz / 2) + 0.1 * plan_cost(nz);
+    if (cost < bc) { bc = cost; best = nz; }
+  }
+  return best;
+}
+
+}  // namespace fpcc

@@ -1,0 +1,32 @@
+// Host-side planning: radix schedules and padded correlation lengths.
+#pragma once
+
+#include <stdint.h>
+
+#include "fft_core.cuh"
+
+namespace fpcc {
+
+// Largest length one thread block transforms in shared memory.
+constexpr int kMaxCtaLen = 21120;
+
+// Factor n into 2^a 3^b 5^c; false for any other prime factor.
+bool factor235(int n, int* a, int* b, int* c);
+
+// Radix schedule for an in-block transform of length n (2,3,5-smooth):
+// ceil(a/4) power-of-two passes with the exponent spread evenly, then the 5s
+// and 3s.  When `forced` is non-null it lists the radices to use instead.
+bool make_plan(int n, FftPlan* p, const int* forced = nullptr, int nforced = 0);
+bool make_plan_raw(int n, FftPlan* p, const int* forced, int nforced);
+
+// Padded correlation length for a window of N samples and max |lag| M.
+//   mode 0: the reference rule 2^ceil(log2(N+M))   (src/FFTapps.c:805)
+//   mode 1: the cheapest even 2,3,5-smooth length >= N+M whose half length fits
+//           one block, by a per-pass cost model (results are identical for any
+//           length >= N+M: the correlation is linear).
+int choose_nz(int N, int M, int mode);
+
+// Estimated relative cost of an in-block transform of length n.
+double plan_cost(int n);
+
+}  // namespace fpcc

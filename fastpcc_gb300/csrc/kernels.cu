@@ -1,0 +1,392 @@
+// FFT-based correlation kernels (PCC2, GNCC, 1-bit GNCC) and the generic
+// transform passes.
+//
+// Station spectrum stage, one block per station window, length Nz on the size
+// menu (reference src/FFTapps.c):
+//   SPEC_PHASE : analytic signal -> amplitude normalisation (:178-205 or the GPU
+//                rules of src/ccs_cuda.cu) -> zero pad -> DFT_Nz, all Nz bins
+//   SPEC_REAL  : trace -> zero pad -> DFT_Nz, bins 0..Nz/2              (:940-946)
+//   SPEC_SIGN  : 1-bit signs (:1037,1042) -> zero pad -> DFT_Nz, bins 0..Nz/2
+// Pair stage, one block per (station pair, window):
+//   Z = conj(X1) X2 (:851, :347), y = Re IDFT_Nz(Z) at the requested lags, as one
+//   complex IDFT of Nz/2 points of the packed Hermitian part of Z; scaled
+//   (:832,855-856) and, for GNCC / 1-bit, divided by the overlap norms (:372-429).
+// Generic passes: one radix-R Stockham pass per launch over all rows, for window
+// lengths N that are not on the menu (the N-point analytic signal, :104-124).
+#include <float.h>
+
+#include "kernels.cuh"
+#include "menu.cuh"
+
+namespace fpcc {
+
+namespace {
+
+__device__ __forceinline__ bool f_isnormal_pos(float v) { return v >= FLT_MIN && v <= FLT_MAX; }
+
+// Reference threshold / regulariser from the row statistic.
+__device__ __forceinline__ float amp_eps(int rule, float ref) {
+  if (rule == AMP_F_REG) return (float)(1e-6 * sqrt((double)ref));   // src/FFTapps.c:191
+  if (rule == AMP_PURE) return 0.0f;                                  // src/ccs_cuda.cu:582
+  return 1e-6f * ref;                                                 // :160, ccs_cuda.cu:197
+}
+
+// Factor that maps a sample of squared modulus m2 to its phase-signal value.
+__device__ __forceinline__ float amp_factor(int rule, float m2, float eps) {
+  float f;
+  if (rule == AMP_F_REG) {
+    f = 1.0f / (sqrtf(m2) + eps);   // src/FFTapps.c:196-203
+    return f_isnormal_pos(f) ? f : 0.0f;
+  }
+  if (rule == AMP_D_REG) {
+    f = rsqrtf(m2 + eps);           // src/FFTapps.c:166-173
+    return f_isnormal_pos(f) ? f : 0.0f;
+  }
+  return (m2 > eps) ? rsqrtf(m2) : 0.0f;   // src/ccs_cuda.cu:201-208, 223-230
+}
+
+template <int FMT>
+__device__ __forceinline__ float2 load_bin(const void* base, int i) {
+  if constexpr (FMT == SPEC_F16) {
+    return __half22float2(reinterpret_cast<const __half2*>(base)[i]);
+  } else {
+    return reinterpret_cast<const float2*>(base)[i];
+  }
+}
+
+template <int... Rs>
+constexpr int rad_len(Radices<Rs...>) {
+  return prod_radices<Rs...>();
+}
+
+// ------------------------------------------------------------ station spectra
+template <int T, typename RAD>
+__global__ void __launch_bounds__(T, 1) k_spec(SpecArgs a) {
+  constexpr int NZ = rad_len(RAD{});
+  extern __shared__ float4 smem_raw[];
+  float2* s = reinterpret_cast<float2*>(smem_raw);
+  float2* lo = s + padded_len(NZ);
+  float2* hi = lo + 128;
+  build_twiddles(lo, hi, NZ);
+  const int row = blockIdx.x;
+  const int N = a.N;
+  if (a.mode == SPEC_PHASE) {
+    const float2* x = reinterpret_cast<const float2*>(a.in) + (int64_t)row * a.ldin;
+    const int rule = a.rule;
+    const float eps = amp_eps(rule, a.rowstat[row]);
+    for (int n = threadIdx.x; n < N; n += T) {
+      const float2 v = x[n];
+      s[PADI(n)] = cscale(v, amp_factor(rule, v.x * v.x + v.y * v.y, eps));
+    }
+  } else {
+    const float* x = reinterpret_cast<const float*>(a.in) + (int64_t)row * a.ldin;
+    const bool sgn = (a.mode == SPEC_SIGN);
+    const bool ge = a.sign_ge != 0;
+    for (int n = threadIdx.x; n < N; n += T) {
+      float v = __ldg(x + n);
+      if (sgn) v = (ge ? (v >= 0.0f) : (v > 0.0f)) ? 1.0f : -1.0f;
+      s[PADI(n)] = make_float2(v, 0.0f);
+    }
+  }
+  for (int n = N + threadIdx.x; n < NZ; n += T) s[PADI(n)] = make_float2(0.0f, 0.0f);
+  __syncthreads();
+  ct_fft<-1, T, 1>(s, 1, 0, TwTab{lo, hi}, RAD{});
+  const int nout = (a.mode == SPEC_PHASE) ? NZ : (NZ / 2 + 1);
+  if (a.fmt == SPEC_F16) {
+    __half2* o = reinterpret_cast<__half2*>(a.out) + (int64_t)row * a.ldo;
+    for (int k = threadIdx.x; k < nout; k += T) o[k] = __float22half2_rn(s[PADI(k)]);
+  } else {
+    float2* o = reinterpret_cast<float2*>(a.out) + (int64_t)row * a.ldo;
+    for (int k = threadIdx.x; k < nout; k += T) o[k] = s[PADI(k)];
+  }
+}
+
+// ------------------------------------------------------------ pairs
+// Cross-spectrum bin at position p in [0, Nz).  Full storage holds Nz bins;
+// Hermitian storage (real traces) holds bins 0..Nz/2.
+template <int FMT, bool HERM>
+__device__ __forceinline__ float2 zbin(const void* X1, const void* X2, int p, int Nz) {
+  if constexpr (HERM) {
+    const int h = Nz >> 1;
+    if (p <= h) return cconjmul(load_bin<FMT>(X1, p), load_bin<FMT>(X2, p));
+    return cconj(cconjmul(load_bin<FMT>(X1, Nz - p), load_bin<FMT>(X2, Nz - p)));
+  } else {
+    return cconjmul(load_bin<FMT>(X1, p), load_bin<FMT>(X2, p));
+  }
+}
+
+template <int T, typename RAD, int FMT, bool HERM>
+__global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
+  constexpr int H = rad_len(RAD{});
+  constexpr int NZ = 2 * H;
+  extern __shared__ float4 smem_raw[];
+  float2* s = reinterpret_cast<float2*>(smem_raw);
+  float2* hlo = s + padded_len(H);
+  float2* hhi = hlo + 128;
+  float2* zlo = hhi + tw_hi_len(H);
+  float2* zhi = zlo + 128;
+  build_twiddles(hlo, hhi, H);
+  build_twiddles(zlo, zhi, NZ);
+  __syncthreads();
+  const TwTab twZ{zlo, zhi};
+  const int p = blockIdx.x;
+  const int2 pr = a.pairs[p];
+  constexpr int esz = (FMT == SPEC_F16) ? 4 : 8;
+  const char* X1 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.x * a.ldspec * esz;
+  const char* X2 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.y * a.ldspec * esz;
+
+  // F[k] = (H[k] + H[k+h]) + i w^k (H[k] - H[k+h]), H = Hermitian part of Z,
+  // w = exp(2 pi i / Nz); the group {k, h-k} reads Z at k, h-k, h+k, Nz-k.
+  for (int k = threadIdx.x; k <= (H >> 1); k += T) {
+    const int k2 = H - k;
+    const float2 z0 = zbin<FMT, HERM>(X1, X2, k, NZ);
+    const float2 z1 = zbin<FMT, HERM>(X1, X2, k2, NZ);
+    const float2 z2 = zbin<FMT, HERM>(X1, X2, H + k, NZ);
+    const float2 z3 = zbin<FMT, HERM>(X1, X2, (k == 0) ? 0 : NZ - k, NZ);
+    const float2 Hk = cscale(cadd(z0, cconj(z3)), 0.5f);
+    const float2 Hkh = cscale(cadd(z2, cconj(z1)), 0.5f);
+    float2 w = twiddle(twZ, k);
+    w.y = -w.y;
+    const float2 e = cadd(Hk, Hkh);
+    const float2 o = cmul(w, csub(Hk, Hkh));
+    s[PADI(k)] = make_float2(e.x - o.y, e.y + o.x);
+    if (k2 != k && k2 < H) {
+      // H[k2] = conj(H[k+h]), H[k2+h] = conj(H[k])
+      float2 w2 = twiddle(twZ, k2);
+      w2.y = -w2.y;
+      const float2 e2 = cconj(cadd(Hkh, Hk));
+      const float2 o2 = cmul(w2, cconj(csub(Hkh, Hk)));
+      s[PADI(k2)] = make_float2(e2.x - o2.y, e2.y + o2.x);
+    }
+  }
+  __syncthreads();
+  ct_fft<+1, T, 1>(s, 1, 0, TwTab{hlo, hhi}, RAD{});
+
+  float* y = a.y + (int64_t)p * a.ldy;
+  const int N = a.N;
+  const double* E1 = (a.norm == 1) ? a.energy + (int64_t)pr.x * a.ldE : nullptr;
+  const double* E2 = (a.norm == 1) ? a.energy + (int64_t)pr.y * a.ldE : nullptr;
+  for (int l = threadIdx.x; l < a.L; l += T) {
+    const int lag = a.lag0 + l;
+    const int idx = lag < 0 ? lag + NZ : lag;
+    const float2 zz = s[PADI(idx >> 1)];
+    float v = ((idx & 1) ? zz.y : zz.x) * a.scale;
+    if (a.norm == 1) {
+      // overlap x1[n11,n12), x2[n21,n22) (src/FFTapps.c:896-902)
+      int n11 = 0, n21 = 0, n12 = N, n22 = N;
+      if (lag > 0) { n21 = lag; n12 -= lag; }
+      else { n11 = -lag; n22 += lag; }
+      const double e1 = E1[n12] - E1[n11];
+      const double e2 = E2[n22] - E2[n21];
+      v = (float)((double)v / sqrt(e1 * e2));
+    } else if (a.norm == 2) {
+      v = (float)((double)v / (double)(N - abs(lag)));
+    }
+    y[l] = v;
+  }
+}
+
+// ------------------------------------------------------------ phase store
+__global__ void __launch_bounds__(256) k_phase_store(PhaseArgs a) {
+  const int row = blockIdx.x;
+  const int n = blockIdx.y * blockDim.x + threadIdx.x;
+  if (n >= a.N) return;
+  const float eps = amp_eps(a.rule, a.rowstat[row]);
+  const float2 v = a.in[(int64_t)row * a.ldin + n];
+  const float2 p = cscale(v, amp_factor(a.rule, v.x * v.x + v.y * v.y, eps));
+  if (a.fmt == 1) reinterpret_cast<__half2*>(a.out)[(int64_t)row * a.ldo + n] = __float22half2_rn(p);
+  else reinterpret_cast<float2*>(a.out)[(int64_t)row * a.ldo + n] = p;
+}
+
+// ------------------------------------------------------------ generic passes
+template <int R, int DIR, bool REAL_IN>
+__global__ void __launch_bounds__(256) k_gpass(const void* __restrict__ in, int64_t ldr, float2* __restrict__ out,
+                                               int64_t ld, int n, int Ns, int nrows,
+                                               const float2* __restrict__ tw) {
+  const int m = n / R;
+  const int64_t total = (int64_t)m * nrows;
+  const int tstride = n / (Ns * R);
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int row = (int)(g / m);
+    const int j = (int)(g - (int64_t)row * m);
+    float2 v[R];
+    if constexpr (REAL_IN) {
+      const float* x = reinterpret_cast<const float*>(in) + (int64_t)row * ldr;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[r] = make_float2(__ldg(x + j + r * m), 0.0f);
+    } else {
+      const float2* x = reinterpret_cast<const float2*>(in) + (int64_t)row * ld;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[r] = x[j + r * m];
+    }
+    const int k = j % Ns;
+    if (k != 0) {
+      float2 w1 = __ldg(tw + k * tstride);
+      if (DIR > 0) w1.y = -w1.y;
+      float2 w = w1;
+#pragma unroll
+      for (int r = 1; r < R; r++) {
+        v[r] = cmul(v[r], w);
+        if (r + 1 < R) w = cmul(w, w1);
+      }
+    }
+    dft<R, DIR>(v);
+    float2* o = out + (int64_t)row * ld + (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) o[r * Ns] = v[dft_perm<R>(r)];
+  }
+}
+
+__global__ void k_analytic_mask(float2* a, int64_t ld, int n, int nrows) {
+  const int row = blockIdx.x;
+  const float d = 1.0f / (float)n;
+  const int half = (n + 1) >> 1;
+  for (int k = blockIdx.y * blockDim.x + threadIdx.x; k < n; k += gridDim.y * blockDim.x) {
+    float f;
+    if (k == 0) f = d;
+    else if (k < half) f = 2.0f * d;
+    else if (!(n & 1) && k == (n >> 1)) f = d;
+    else f = 0.0f;
+    float2* p = a + (int64_t)row * ld + k;
+    *p = cscale(*p, f);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_rowstats(const float2* a, int64_t ld, int n, float* rmax, float* rsum) {
+  __shared__ float sm[32], ss[32];
+  const float2* r = a + (int64_t)blockIdx.x * ld;
+  float mx = 0.0f, sum = 0.0f;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const float2 v = r[k];
+    const float m2 = v.x * v.x + v.y * v.y;
+    mx = fmaxf(mx, m2);
+    sum += m2;
+  }
+  mx = warp_max(mx);
+  sum = warp_sum(sum);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { sm[w] = mx; ss[w] = sum; }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    mx = (l < nw) ? sm[l] : 0.0f;
+    sum = (l < nw) ? ss[l] : 0.0f;
+    mx = warp_max(mx);
+    sum = warp_sum(sum);
+    if (l == 0) {
+      if (rmax) rmax[blockIdx.x] = mx;
+      if (rsum) rsum[blockIdx.x] = sum;
+    }
+  }
+}
+
+template <typename K>
+cudaError_t launch_k(K kern, int grid, int T, size_t smem, cudaStream_t st, const void* args) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  void* argv[] = {const_cast<void*>(args)};
+  return cudaLaunchKernel((const void*)kern, dim3(grid), dim3(T), argv, smem, st);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+bool spec_supported(int Nz) { return on_menu(Nz); }
+bool pair_supported(int Nz) { return (Nz % 2 == 0) && on_menu(Nz / 2); }
+
+size_t spec_smem_bytes(int Nz) {
+  return ((size_t)padded_len(Nz) + 128 + tw_hi_len(Nz)) * sizeof(float2);
+}
+
+size_t pair_smem_bytes(int Nz) {
+  const int h = Nz / 2;
+  return ((size_t)padded_len(h) + 128 + tw_hi_len(h) + 128 + tw_hi_len(Nz)) * sizeof(float2);
+}
+
+cudaError_t launch_spec(const SpecArgs& a, cudaStream_t st) {
+  if (a.nrows <= 0) return cudaSuccess;
+  const size_t smem = spec_smem_bytes(a.Nz);
+  switch (a.Nz) {
+#define FPCC_SPEC_CASE(SZ, T, ...) \
+  case SZ: return launch_k(k_spec<T, Radices<__VA_ARGS__>>, a.nrows, T, smem, st, &a);
+    FPCC_SIZE_MENU(FPCC_SPEC_CASE)
+#undef FPCC_SPEC_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int FMT, bool HERM>
+static cudaError_t launch_pairs_t(const PairArgs& a, cudaStream_t st) {
+  const size_t smem = pair_smem_bytes(a.Nz);
+  switch (a.Nz / 2) {
+#define FPCC_PAIR_CASE(SZ, T, ...) \
+  case SZ: return launch_k(k_pairs<T, Radices<__VA_ARGS__>, FMT, HERM>, a.npairs, T, smem, st, &a);
+    FPCC_SIZE_MENU(FPCC_PAIR_CASE)
+#undef FPCC_PAIR_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_pairs(const PairArgs& a, cudaStream_t st) {
+  if (a.npairs <= 0) return cudaSuccess;
+  const bool herm = (a.norm != 0);
+  if (a.fmt == SPEC_F16) return herm ? launch_pairs_t<SPEC_F16, true>(a, st) : launch_pairs_t<SPEC_F16, false>(a, st);
+  return herm ? launch_pairs_t<SPEC_F32, true>(a, st) : launch_pairs_t<SPEC_F32, false>(a, st);
+}
+
+cudaError_t launch_phase_store(const PhaseArgs& a, cudaStream_t st) {
+  if (a.nrows <= 0) return cudaSuccess;
+  if ((a.N + 255) / 256 > 65535) return cudaErrorInvalidValue;
+  dim3 grid(a.nrows, (a.N + 255) / 256);
+  k_phase_store<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+static int grid_for(int64_t work) {
+  int64_t b = (work + 255) / 256;
+  const int64_t cap = 152 * 16;   // a few waves of 256-thread blocks on 152 SMs
+  return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
+}
+
+cudaError_t launch_gpass(int R, int dir, const void* in, bool real_in, int64_t ldr, float2* out, int64_t ld, int n,
+                         int Ns, int nrows, const float2* tw, cudaStream_t st) {
+  const int grid = grid_for((int64_t)(n / R) * nrows);
+#define FPCC_GP(RR)                                                                                   \
+  if (R == RR) {                                                                                      \
+    if (real_in) {                                                                                    \
+      if (dir < 0) k_gpass<RR, -1, true><<<grid, 256, 0, st>>>(in, ldr, out, ld, n, Ns, nrows, tw);  \
+      else k_gpass<RR, 1, true><<<grid, 256, 0, st>>>(in, ldr, out, ld, n, Ns, nrows, tw);           \
+    } else {                                                                                          \
+      if (dir < 0) k_gpass<RR, -1, false><<<grid, 256, 0, st>>>(in, ldr, out, ld, n, Ns, nrows, tw); \
+      else k_gpass<RR, 1, false><<<grid, 256, 0, st>>>(in, ldr, out, ld, n, Ns, nrows, tw);          \
+    }                                                                                                 \
+    return cudaGetLastError();                                                                        \
+  }
+  FPCC_GP(16)
+  FPCC_GP(8)
+  FPCC_GP(5)
+  FPCC_GP(4)
+  FPCC_GP(3)
+  FPCC_GP(2)
+#undef FPCC_GP
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_analytic_mask(float2* a, int64_t ld, int n, int nrows, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  dim3 grid(nrows, (n + 255) / 256 < 64 ? (n + 255) / 256 : 64);
+  k_analytic_mask<<<grid, 256, 0, st>>>(a, ld, n, nrows);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rowstats(const float2* a, int64_t ld, int n, int nrows, float* rmax, float* rsum,
+                            cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  k_rowstats<<<nrows, 256, 0, st>>>(a, ld, n, rmax, rsum);
+  return cudaGetLastError();
+}
+
+}  // namespace fpcc

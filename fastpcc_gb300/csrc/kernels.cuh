@@ -1,0 +1,96 @@
+// Kernel argument blocks and launchers shared by the host engine.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_core.cuh"
+
+namespace fpcc {
+
+// Amplitude-normalisation rules of the reference.
+enum AmpRule : int {
+  AMP_F_REG = 0,   // AmpNormf  (src/FFTapps.c:178-205): x / (|x| + 1e-6 max|x|)
+  AMP_D_REG = 1,   // AmpNorm   (src/FFTapps.c:147-175): x / sqrt(|x|^2 + 1e-6 max|x|^2)
+  AMP_PURE = 2,    // GPU_AmpNormf with mabs = 0 (src/ccs_cuda.cu:212-232): x / |x|
+  AMP_THRESH = 3,  // GPU_AmpNormf2 on the max (src/ccs_cuda.cu:190-210): x/|x| above 1e-6 max|x|^2
+  AMP_SUMTHR = 4   // cuda_AmpNormf2 on the sum (src/ccs_cuda.cu:493-511): x/|x| above 1e-6 sum|x|^2
+};
+
+enum SpecFmt : int { SPEC_F32 = 0, SPEC_F16 = 1 };
+
+// Station spectrum stage input modes.
+enum SpecMode : int {
+  SPEC_PHASE = 0,  // complex analytic signal rows -> amplitude-normalised phase signal
+  SPEC_REAL = 1,   // real trace rows
+  SPEC_SIGN = 2    // 1-bit signs of real trace rows
+};
+
+struct SpecArgs {
+  const void* in;        // SPEC_PHASE: float2 rows; otherwise float rows
+  int64_t ldin;
+  int nrows;
+  int N;                 // samples per row
+  int Nz;                // transform length (on the size menu)
+  int mode;              // SpecMode
+  int rule;              // AmpRule (SPEC_PHASE)
+  const float* rowstat;  // SPEC_PHASE: per-row max |a|^2, or sum |a|^2 for AMP_SUMTHR
+  int sign_ge;           // SPEC_SIGN: 1 -> x >= 0 is +1, 0 -> x > 0 is +1
+  int fmt;               // SpecFmt of the output
+  void* out;             // nrows x ldo complex; SPEC_PHASE stores Nz bins, else 0..Nz/2
+  int64_t ldo;
+};
+
+struct PairArgs {
+  const void* spec;      // station spectra
+  int64_t ldspec;
+  int fmt;               // SpecFmt
+  const int2* pairs;     // (station-1 row, station-2 row) per output row
+  int npairs;
+  int Nz;                // 2 * (menu length)
+  int lag0;              // first lag
+  int L;                 // number of lags
+  float scale;           // output scale
+  float* y;              // npairs x ldy
+  int64_t ldy;
+  int norm;              // 0 none, 1 GNCC energies (FP64 prefix sums), 2 overlap counts
+  const double* energy;  // per station row: N+1 prefix sums of x^2
+  int64_t ldE;
+  int N;
+};
+
+// Per-row phase signal store for the direct-sum methods.
+struct PhaseArgs {
+  const float2* in;      // analytic signal rows
+  int64_t ldin;
+  int nrows;
+  int N;
+  int rule;
+  const float* rowstat;
+  int fmt;               // 0: float2, 1: half2
+  void* out;
+  int64_t ldo;
+};
+
+bool spec_supported(int Nz);
+bool pair_supported(int Nz);
+size_t spec_smem_bytes(int Nz);
+size_t pair_smem_bytes(int Nz);
+
+cudaError_t launch_spec(const SpecArgs& a, cudaStream_t st);
+cudaError_t launch_pairs(const PairArgs& a, cudaStream_t st);
+cudaError_t launch_phase_store(const PhaseArgs& a, cudaStream_t st);
+
+// Generic transforms for any 2,3,5-smooth length: one kernel per radix pass,
+// reading `in` and writing `out` (rows of n complex, row stride ld).  The first
+// pass may read real rows (real_in) of stride ldr.  tw is the device table
+// exp(-2 pi i t / n), t in [0, n).
+cudaError_t launch_gpass(int R, int dir, const void* in, bool real_in, int64_t ldr, float2* out, int64_t ld,
+                         int n, int Ns, int nrows, const float2* tw, cudaStream_t st);
+// Analytic mask with the 1/n of the inverse (src/FFTapps.c:63-67), in place.
+cudaError_t launch_analytic_mask(float2* a, int64_t ld, int n, int nrows, cudaStream_t st);
+// Per-row max |a|^2 and sum |a|^2.
+cudaError_t launch_rowstats(const float2* a, int64_t ld, int n, int nrows, float* rmax, float* rsum,
+                            cudaStream_t st);
+
+}  // namespace fpcc

@@ -1,0 +1,140 @@
+/*
+ * fastpcc_gb300 — GB300-native interstation correlations (C ABI).
+ *
+ * Methods (reference: FastPCC src/FFTapps.c):
+ *   FPCC_PCC2   phase cross-correlation at power 2 via DFTs of unit-modulus
+ *               analytic phase signals                     (pcc2_set  :785-881)
+ *   FPCC_GNCC   geometrically normalised cross-correlation  (ccgn_set  :883-978)
+ *   FPCC_CC1B   1-bit GNCC, DFT path                        (cc1b_set  :980-1073)
+ *   FPCC_CC1B_POPCOUNT  1-bit GNCC with exact integer numerators from
+ *               popcounts of packed sign bits (same outputs as cc1b_set)
+ *   FPCC_PCC1   PCC at power 1 by direct lag sums           (pcc1_set  :611-783)
+ *   FPCC_PCCV   PCC at power v by direct lag sums           (pcc_set   :475-608)
+ *   FPCC_WPCC   wavelet PCC                                 (tspcc2_set :1076-1255)
+ *
+ * Lag conventions follow the reference: a window [Lag1, Lag2] (either order)
+ * yields L = |Lag2-Lag1|+1 outputs, output l <-> lag min(Lag1,Lag2)+l, with
+ * out[lag] = sum_n conj(a1[n]) a2[n+lag]; |Lag1|,|Lag2| < N.
+ *
+ * All calls return 0 on success and a negative FPCC_E* code on failure (the
+ * message is available from fpcc_last_error()).  No call resets the device.
+ *
+ * The reference's own GPU entry points (src/ccs_cuda.h) are declared, with
+ * identical signatures, in ccs_cuda.h beside this header.
+ */
+#ifndef FASTPCC_GB300_H
+#define FASTPCC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FPCC_OK 0
+#define FPCC_ECUDA (-1)    /* CUDA runtime failure (the reference's -1)          */
+#define FPCC_ENOMEM (-2)   /* allocation failure                                  */
+#define FPCC_EARG (-3)     /* invalid argument, e.g. |lag| >= N (reference's -3)  */
+#define FPCC_EUNSUP (-4)   /* size or option not supported by this build          */
+
+enum fpcc_method {
+  FPCC_PCC2 = 0,
+  FPCC_GNCC = 1,
+  FPCC_CC1B = 2,
+  FPCC_CC1B_POPCOUNT = 3,
+  FPCC_PCC1 = 4,
+  FPCC_PCCV = 5,
+  FPCC_WPCC = 6
+};
+
+/* Amplitude-normalisation rules of the reference (phase signals). */
+enum fpcc_amp_rule {
+  FPCC_AMP_F_REG = 0,  /* AmpNormf, src/FFTapps.c:178-205 (CPU PCC paths, default) */
+  FPCC_AMP_D_REG = 1,  /* AmpNorm,  src/FFTapps.c:147-175 (CPU WPCC)               */
+  FPCC_AMP_PURE = 2,   /* x/|x|, src/ccs_cuda.cu:212-232 with mabs = 0 (GPU PCC)   */
+  FPCC_AMP_THRESH = 3, /* x/|x| above 1e-6 max|x|^2, src/ccs_cuda.cu:190-210 (GPU WPCC) */
+  FPCC_AMP_SUMTHR = 4  /* x/|x| above 1e-6 sum|x|^2, src/ccs_cuda.cu:493-511        */
+};
+
+/* Storage formats of cached station products. */
+enum fpcc_format { FPCC_F32 = 0, FPCC_F16 = 1 };
+
+/* 1-bit sign rules: the reference maps x1 >= 0 -> +1 but x2 > 0 -> +1
+ * (src/FFTapps.c:1037,1042). */
+enum fpcc_sign_rule { FPCC_SIGN_GE = 0, FPCC_SIGN_GT = 1 };
+
+/* Padded correlation length rules. */
+enum fpcc_nz_mode { FPCC_NZ_REFERENCE = 0, FPCC_NZ_FAST = 1 };
+
+typedef struct fpcc_ctx fpcc_ctx;
+
+/* ---- context ------------------------------------------------------------ */
+int fpcc_create(fpcc_ctx **out, int device);
+int fpcc_destroy(fpcc_ctx *ctx);
+/* Run subsequent work on this CUDA stream (cudaStream_t; NULL = the context's own). */
+int fpcc_set_stream(fpcc_ctx *ctx, void *stream);
+void *fpcc_get_stream(fpcc_ctx *ctx);
+int fpcc_sync(fpcc_ctx *ctx);
+const char *fpcc_last_error(void);
+const char *fpcc_version(void);
+/* Kernel launches issued by this process so far (all contexts). */
+int64_t fpcc_launch_count(void);
+
+/* ---- planning ----------------------------------------------------------- */
+/* Padded correlation length for N samples and the lag window (mode: fpcc_nz_mode). */
+int fpcc_choose_nz(int N, int Lag1, int Lag2, int mode);
+/* Largest length an in-block transform of this build supports. */
+int fpcc_max_block_len(void);
+/* Elements per row of the station product of a method (for sizing buffers). */
+int64_t fpcc_station_row_elems(int method, int N, int Nz);
+
+/* ---- device-resident stages (all pointers are device memory) -------------
+ * Station stage: one output row per input row.
+ *   PCC2:            DFT_Nz of the zero-padded phase signal, Nz complex (fmt F32/F16), rule = fpcc_amp_rule
+ *   PCC1, PCCV:      phase signal, N complex (fmt F32 float2 / F16 half2), rule = fpcc_amp_rule
+ *   GNCC:            DFT_Nz of the zero-padded trace, bins 0..Nz/2 (F32)
+ *   CC1B:            DFT_Nz of the zero-padded 1-bit signs, bins 0..Nz/2 (F32), rule = fpcc_sign_rule
+ *   CC1B_POPCOUNT:   packed sign bits, ceil(N/32) uint32 words, rule = fpcc_sign_rule
+ */
+int fpcc_station_stage(fpcc_ctx *ctx, int method, const float *d_x, int64_t ldx, int nrows, int N,
+                       int Nz, int fmt, int rule, void *d_out, int64_t ldo);
+/* FP64 prefix sums E[n] = sum_{m<n} x[m]^2, N+1 per row (GNCC normalisation). */
+int fpcc_energy_stage(fpcc_ctx *ctx, const float *d_x, int64_t ldx, int nrows, int N, double *d_E,
+                      int64_t ldE);
+/* Pair stage: output row p correlates station rows pairs[2p] (station 1) and
+ * pairs[2p+1] (station 2).  v is the power for PCCV; d_E/ldE the energies for
+ * GNCC; d_num (optional, CC1B_POPCOUNT) receives exact int64 numerators. */
+int fpcc_pair_stage(fpcc_ctx *ctx, int method, const void *d_station, int64_t lds, int fmt,
+                    const int32_t *d_pairs, int npairs, int N, int Nz, int Lag1, int Lag2, float v,
+                    const double *d_E, int64_t ldE, float *d_y, int64_t ldy, int64_t *d_num);
+
+/* ---- host-buffer entry points (row-pointer arrays like the reference's *_set)
+ * x1, x2: Tr rows of N floats (station 1 / station 2 windows); y: Tr rows of L.
+ * The "batched" calls run each stage once over all windows; the plain drop-ins
+ * below run one launch sequence per window. */
+int fpcc_host_batched(int method, float **y, float **x1, float **x2, unsigned N, unsigned Tr,
+                      int Lag1, int Lag2, float v, int nz_mode, int fmt);
+int fpcc_host_plain(int method, float **y, float **x1, float **x2, unsigned N, unsigned Tr, int Lag1,
+                    int Lag2, float v, int nz_mode, int fmt);
+
+/* Contiguous host arrays (pinned or pageable): x is nsta x N, pairs 2*npairs,
+ * y npairs x L.  Host<->device copies happen inside the call. */
+int fpcc_allpairs_host(fpcc_ctx *ctx, int method, const float *h_x, int nsta, int N,
+                       const int32_t *h_pairs, int npairs, int Lag1, int Lag2, float v, int nz_mode,
+                       int fmt, float *h_y);
+
+/* Drop-in siblings of the reference's GPU calls for the methods it runs on the
+ * CPU (raw float traces in, y rows out; semantics of pcc2_set, ccgn_set,
+ * cc1b_set).  Plain form: one launch sequence per pair and window. */
+int pcc2_highlevel(float **y, float **x1, float **x2, unsigned N, unsigned Tr, int Lag1, int Lag2);
+int ccgn_highlevel(float **y, float **x1, float **x2, unsigned N, unsigned Tr, int Lag1, int Lag2);
+int cc1b_highlevel(float **y, float **x1, float **x2, unsigned N, unsigned Tr, int Lag1, int Lag2);
+/* Exact integer numerators of 1-bit GNCC (num rows of L int64). */
+int cc1b_popcount_highlevel(int64_t **num, float **x1, float **x2, unsigned N, unsigned Tr, int Lag1,
+                            int Lag2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,115 @@
+"""GPU parity: every method through the C ABI against the FP64 oracle.
+
+Error metric: max over lags of |y - y64| divided by max |y64| of the same
+correlation (relative to its own peak).  Tolerance 1e-4 for every FP32 path;
+FP16 spectrum storage is held to 3e-4 (its measured error sits near 1e-4); the
+1-bit popcount numerators must be bit-exact.
+"""
+import numpy as np
+import pytest
+
+from fastpcc_gb300 import synth
+from gpu_util import fp, need_gpu, relerr
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+CASES = [
+    # N, Tr, Lag1, Lag2, delay
+    (1000, 3, -100, 100, 37),
+    (1200, 2, -400, -20, -150),
+    (2048, 2, 10, 300, 120),
+    (3000, 2, 250, -250, 60),
+    (4500, 2, -450, 450, -200),
+]
+
+
+@pytest.fixture(scope="module")
+def F():
+    need_gpu()
+    return fp()
+
+
+def _data(N, Tr, d, tag):
+    return synth.plain_pair(N=N, n_windows=Tr, delay=d, tag=f"gpu/{tag}/{N}")
+
+
+@pytest.mark.parametrize("N,Tr,l1,l2,d", CASES)
+def test_pcc2(F, orc, N, Tr, l1, l2, d):
+    a, b = _data(N, Tr, d, "pcc2")
+    y64 = orc.pcc2(a, b, l1, l2)
+    assert relerr(F.pcc2_set(a, b, l1, l2), y64) < TOL
+    assert relerr(F.pcc2_set(a, b, l1, l2, plain=True), y64) < TOL
+    assert relerr(F.pcc2_highlevel(a, b, l1, l2), y64) < TOL
+
+
+@pytest.mark.parametrize("N,Tr,l1,l2,d", CASES)
+def test_gncc(F, orc, N, Tr, l1, l2, d):
+    a, b = _data(N, Tr, d, "gncc")
+    assert relerr(F.ccgn_set(a, b, l1, l2), orc.gncc(a, b, l1, l2)) < TOL
+
+
+@pytest.mark.parametrize("N,Tr,l1,l2,d", CASES)
+def test_cc1b_fft(F, orc, N, Tr, l1, l2, d):
+    a, b = _data(N, Tr, d, "cc1b")
+    assert relerr(F.cc1b_set(a, b, l1, l2), orc.cc1b(a, b, l1, l2)) < TOL
+
+
+@pytest.mark.parametrize("N,Tr,l1,l2,d", CASES)
+def test_cc1b_popcount_bit_exact(F, orc, N, Tr, l1, l2, d):
+    a, b = _data(N, Tr, d, "cc1b")
+    a[:, ::97] = 0.0   # exact zeros exercise the asymmetric sign rule
+    b[:, ::89] = 0.0
+    num = F.cc1b_numerators(a, b, l1, l2)
+    ref = orc.cc1b_num(a, b, l1, l2)
+    assert np.array_equal(num, ref)
+    y = F.cc1b_set(a, b, l1, l2, popcount=True)
+    assert np.max(np.abs(y - orc.cc1b(a, b, l1, l2))) < 1e-6
+
+
+@pytest.mark.parametrize("N,Tr,l1,l2,d", [c for c in CASES if c[2] <= c[3]])
+def test_pcc1(F, orc, N, Tr, l1, l2, d):
+    a, b = _data(N, Tr, d, "pcc1")
+    assert relerr(F.pcc1_set(a, b, l1, l2), orc.pcc1(a, b, l1, l2)) < TOL
+
+
+def test_pccv_gpu_normalisation(F, orc):
+    a, b = _data(2000, 2, 40, "pccv")
+    y64 = orc.pccv(a, b, 1.5, -150, 150, norm_gpu=True)
+    assert relerr(F.pcc_set(a, b, 1.5, -150, 150), y64) < TOL
+
+
+def test_pcc2_fp16_storage(F, orc):
+    a, b = _data(4500, 3, -200, "f16")
+    y64 = orc.pcc2(a, b, -450, 450)
+    assert relerr(F.pcc2_set(a, b, -450, 450, fmt=F.F16), y64) < 3e-4
+
+
+def test_pcc2_reference_padding_rule(F, orc):
+    a, b = _data(3000, 2, 60, "nzref")
+    y64 = orc.pcc2(a, b, -500, 500)
+    assert relerr(F.pcc2_set(a, b, -500, 500, nz_mode=F.NZ_REFERENCE), y64) < TOL
+
+
+def test_all_pairs_size_window(F, orc):
+    """One window of the all-pairs workload size (N = 18000, lags +-2000)."""
+    x, _ = synth.all_pairs(n_stations=3, n_windows=1, N=18000, tag="gpu/allpairs-size")
+    a = x[[0, 0, 1], 0]
+    b = x[[1, 2, 2], 0]
+    for name, f, o in (("pcc2", F.pcc2_set, orc.pcc2), ("cc1b", F.cc1b_set, orc.cc1b)):
+        assert relerr(f(a, b, -2000, 2000), o(a, b, -2000, 2000)) < TOL, name
+
+
+def test_identity_and_shift(F):
+    a, b = synth.plain_pair(N=3000, n_windows=1, delay=37, snr=3.0, tag="gpu/shift")
+    y = F.pcc2_set(a, a, -50, 50)
+    assert abs(y[0, 50] - 1.0) < 1e-4
+    for f in (F.pcc2_set, F.ccgn_set, F.cc1b_set, F.pcc1_set):
+        y = f(a, b, -200, 200)
+        assert int(np.argmax(y[0])) - 200 == 37, f.__name__
+
+
+def test_bad_lags_raise(F):
+    a, b = _data(1000, 1, 0, "bad")
+    with pytest.raises(F.FpccError):
+        F.pcc2_set(a, b, -1000, 10)
