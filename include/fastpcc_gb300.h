@@ -134,6 +134,24 @@ int cc1b_highlevel(float **y, float **x1, float **x2, unsigned N, unsigned Tr, i
 int cc1b_popcount_highlevel(int64_t **num, float **x1, float **x2, unsigned N, unsigned Tr, int Lag1,
                             int Lag2);
 
+/* ---- allocation-free PCC2 ------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a host whose pool allocator owns all device memory, plugin frameworks that
+ * forbid device allocation, latency-critical loops that must not synchronise
+ * the device): PCC2 of the same-index windows of d_x1 and d_x2 (Tr rows of N
+ * floats, row stride ldx, device memory) into d_y (Tr rows, stride ldy >= L),
+ * on `stream` (a cudaStream_t; NULL = legacy default stream).  Every
+ * intermediate lives in one fixed device array of fpcc_noalloc_scratch_bytes()
+ * (64 MiB) that each GPU loading the library holds until exit; calls needing
+ * more are rejected with FPCC_EARG and a message.  The first call on a device
+ * looks up that array's address (make it before any stream capture).  Calls
+ * share the array: calls whose work overlaps on the GPU race and must be
+ * serialised by the caller.  Errors: fpcc_noalloc_last_error(). */
+int fpcc_pcc2_noalloc(const float *d_x1, const float *d_x2, int64_t ldx, int N, int Tr, int Lag1, int Lag2,
+                      float *d_y, int64_t ldy, void *stream);
+size_t fpcc_noalloc_scratch_bytes(void);
+const char *fpcc_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
