@@ -15,6 +15,7 @@
 #include "direct.cuh"
 #include "engine.h"
 #include "kernels.cuh"
+#include "large.cuh"
 #include "menu.cuh"
 
 using namespace fpcc;
@@ -219,7 +220,74 @@ namespace {
 
 // Workspace slots of the context.
 enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_PAIRS = 5, S_ANA_A = 6,
-            S_ANA_B = 7, S_RSTAT = 8 };
+            S_ANA_B = 7, S_RSTAT = 8, S_LARGE_T = 9 };
+
+constexpr size_t kLargeChunkBytes = size_t(512) << 20;   // four-step intermediate per chunk
+
+// Station products of a length above the in-block menu: four-step forward DFT
+// of each zero-padded row, in chunks of rows whose intermediate stays small.
+int large_station(fpcc_ctx* c, int cmode, const void* in, size_t in_esz, int64_t ldin, int nrows, int N, int Nz,
+                  int rule, const float* rowstat, int sign_ge, int fmt, int half, void* out, int64_t ldo) {
+  int n1, n2;
+  if (!large_supported(Nz, &n1, &n2)) return fail(FPCC_EUNSUP, "Nz=%d is not a supported transform length", Nz);
+  int64_t chunk = (int64_t)(kLargeChunkBytes / ((size_t)Nz * sizeof(float2)));
+  if (chunk < 1) chunk = 1;
+  if (chunk > 65535) chunk = 65535;
+  if (chunk > nrows) chunk = nrows;
+  void* T = nullptr;
+  int rc = dev_buf(c, S_LARGE_T, (size_t)chunk * Nz * sizeof(float2), &T);
+  if (rc) return rc;
+  const size_t out_esz = (fmt == FPCC_F16) ? 4 : 8;
+  for (int r0 = 0; r0 < nrows; r0 += (int)chunk) {
+    LargeArgs a{};
+    a.n = Nz; a.n1 = n1; a.n2 = n2; a.dir = -1;
+    a.nrows = (int)((nrows - r0) < chunk ? (nrows - r0) : chunk);
+    a.cmode = cmode;
+    a.in = (const char*)in + (size_t)r0 * ldin * in_esz;
+    a.ldin = ldin; a.N = N; a.in_off = 0; a.rule = rule;
+    a.rowstat = rowstat ? rowstat + r0 : nullptr;
+    a.sign_ge = sign_ge; a.in_scale = 1.0f;
+    a.T = (float2*)T;
+    a.rmode = ROW_SPEC;
+    a.out = (char*)out + (size_t)r0 * ldo * out_esz;
+    a.ldo = ldo; a.out_fmt = fmt; a.out_half = half;
+    CK(launch_large(a, c->stream));
+    g_launches += 2;
+  }
+  return 0;
+}
+
+// Pair stage for Nz/2 above the in-block menu: four-step inverse transform of the
+// packed Hermitian cross-spectrum, lags written from the row pass.
+int large_pairs(fpcc_ctx* c, const PairArgs& q, int herm) {
+  const int h = q.Nz / 2;
+  int n1, n2;
+  if (!large_supported(h, &n1, &n2)) return fail(FPCC_EUNSUP, "Nz=%d is not a supported correlation length", q.Nz);
+  int64_t chunk = (int64_t)(kLargeChunkBytes / ((size_t)h * sizeof(float2)));
+  if (chunk < 1) chunk = 1;
+  if (chunk > 65535) chunk = 65535;
+  if (chunk > q.npairs) chunk = q.npairs;
+  void* T = nullptr;
+  int rc = dev_buf(c, S_LARGE_T, (size_t)chunk * h * sizeof(float2), &T);
+  if (rc) return rc;
+  for (int p0 = 0; p0 < q.npairs; p0 += (int)chunk) {
+    LargeArgs a{};
+    a.n = h; a.n1 = n1; a.n2 = n2; a.dir = +1;
+    a.nrows = (int)((q.npairs - p0) < chunk ? (q.npairs - p0) : chunk);
+    a.cmode = COL_PAIR;
+    a.spec = q.spec; a.ldspec = q.ldspec; a.fmt = q.fmt; a.herm = herm;
+    a.pairs = q.pairs + p0;
+    a.Nz = q.Nz;
+    a.T = (float2*)T;
+    a.rmode = ROW_LAGS;
+    a.lag0 = q.lag0; a.L = q.L; a.scale = q.scale; a.norm = q.norm;
+    a.energy = q.energy; a.ldE = q.ldE; a.N = q.N;
+    a.y = q.y + (size_t)p0 * q.ldy; a.ldy = q.ldy;
+    CK(launch_large(a, c->stream));
+    g_launches += 2;
+  }
+  return 0;
+}
 
 int twiddle_table(fpcc_ctx* c, int n, const float2** out) {
   auto it = c->twiddles.find(n);
@@ -314,9 +382,18 @@ extern "C" int fpcc_station_stage(fpcc_ctx* c, int method, const float* d_x, int
   if (method != FPCC_PCC2 && method != FPCC_GNCC && method != FPCC_CC1B)
     return fail(FPCC_EUNSUP, "method %d has no station stage", method);
   if (Nz < N || (Nz & 1)) return fail(FPCC_EARG, "Nz=%d must be even and >= N=%d", Nz, N);
-  if (!spec_supported(Nz)) return fail(FPCC_EUNSUP, "Nz=%d is not a supported transform length", Nz);
   if ((method == FPCC_GNCC || method == FPCC_CC1B) && fmt != FPCC_F32)
     return fail(FPCC_EUNSUP, "real-trace spectra are stored in F32");
+  if (!spec_supported(Nz)) {
+    if (method == FPCC_PCC2) {
+      const float2 *an; const float *rmax, *rsum;
+      if ((rc = analytic_rows(c, d_x, ldx, nrows, N, &an, &rmax, &rsum))) return rc;
+      return large_station(c, COL_PHASE, an, sizeof(float2), N, nrows, N, Nz, rule,
+                           (rule == FPCC_AMP_SUMTHR) ? rsum : rmax, 0, fmt, 0, d_out, ldo);
+    }
+    return large_station(c, method == FPCC_GNCC ? COL_REAL : COL_SIGN, d_x, sizeof(float), ldx, nrows, N, Nz, 0,
+                         nullptr, rule == FPCC_SIGN_GE ? 1 : 0, FPCC_F32, 1, d_out, ldo);
+  }
   SpecArgs a{};
   a.nrows = nrows; a.N = N; a.Nz = Nz; a.fmt = fmt; a.out = d_out; a.ldo = ldo;
   if (method == FPCC_PCC2) {
@@ -361,7 +438,7 @@ extern "C" int fpcc_pair_stage(fpcc_ctx* c, int method, const void* d_station, i
     a.pairs = reinterpret_cast<const int2*>(d_pairs);
     a.npairs = npairs;
     a.Nz = Nz;
-    if (!pair_supported(Nz)) return fail(FPCC_EUNSUP, "Nz=%d is not a supported correlation length", Nz);
+    const bool inblock = pair_supported(Nz);
     a.lag0 = lag0;
     a.L = L;
     a.y = d_y;
@@ -382,6 +459,7 @@ extern "C" int fpcc_pair_stage(fpcc_ctx* c, int method, const void* d_station, i
       a.scale = (float)(1.0 / (double)Nz);       // src/FFTapps.c:357
       if (fmt != FPCC_F32) return fail(FPCC_EUNSUP, "1-bit spectra are F32");
     }
+    if (!inblock) return large_pairs(c, a, method == FPCC_PCC2 ? 0 : 1);
     CK(launch_pairs(a, c->stream));
     g_launches++;
     return 0;

@@ -3,6 +3,7 @@
 
 #include "engine.h"
 #include "menu.cuh"
+#include "large.cuh"
 
 namespace fpcc {
 
@@ -63,20 +64,41 @@ double plan_cost(int n) {
   return c * (double)n;
 }
 
+// A transform length is usable when it runs in one block (menu) or as a
+// four-step transform; the cost model charges the four-step form its two extra
+// global-memory passes.
+static bool usable(int n) {
+  int n1, n2;
+  return on_menu(n) || large_supported(n, &n1, &n2);
+}
+
+static double length_cost(int n) {
+  if (on_menu(n)) return plan_cost(n);
+  int n1, n2;
+  if (!large_supported(n, &n1, &n2)) return 1e30;
+  return plan_cost(n1) * (double)(n / n1) + plan_cost(n2) * (double)(n / n2) + 4.0 * (double)n;
+}
+
+bool nz_usable(int nz) { return nz > 0 && (nz % 2) == 0 && usable(nz) && usable(nz / 2); }
+
 int choose_nz(int N, int M, int mode) {
   const int need = N + M;
+  if (mode >= 2) {
+    // explicit padded length
+    return (mode >= need && nz_usable(mode)) ? mode : -1;
+  }
   if (mode == 0) {
     const int nz = 1 << (int)ceil(log2((double)need));
-    return (on_menu(nz) && on_menu(nz / 2)) ? nz : -1;
+    return nz_usable(nz) ? nz : -1;
   }
-  // menu lengths whose half is also on the menu; the pair transform (Nz/2)
-  // dominates the cost of a batch of correlations
+  // candidates: menu lengths and four-step lengths 2^a 3^b 5^c up to 2^20
   int best = -1;
   double bc = 1e300;
-  for (int i = 0; i < kMenuLen; i++) {
-    const int nz = kMenu[i];
-    if (nz < need || !on_menu(nz / 2)) continue;
-    const double cost = plan_cost(nz / 2) + 0.1 * plan_cost(nz);
+  for (int nz = need + (need & 1); nz <= 2 * need + 64 && nz <= (1 << 21); nz += 2) {
+    int a2, b3, c5;
+    if (!factor235(nz, &a2, &b3, &c5) || !nz_usable(nz)) continue;
+    // the pair transform (Nz/2) dominates a batch of correlations
+    const double cost = length_cost(nz / 2) + 0.1 * length_cost(nz);
     if (cost < bc) { bc = cost; best = nz; }
   }
   return best;

@@ -24,7 +24,10 @@ bool make_plan_raw(int n, FftPlan* p, const int* forced, int nforced);
 //   mode 1: the cheapest even 2,3,5-smooth length >= N+M whose half length fits
 //           one block, by a per-pass cost model (results are identical for any
 //           length >= N+M: the correlation is linear).
+//   mode >= 2: that explicit length, if usable and >= N+M.
 int choose_nz(int N, int M, int mode);
+// Nz and Nz/2 both run in one block or as four-step transforms.
+bool nz_usable(int nz);
 
 // Estimated relative cost of an in-block transform of length n.
 double plan_cost(int n);

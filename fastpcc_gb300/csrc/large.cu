@@ -1,0 +1,292 @@
+// Four-step transforms for lengths above the in-block menu (see large.cuh).
+#include <float.h>
+
+#include "large.cuh"
+
+namespace fpcc {
+namespace {
+
+constexpr int kColVecs = 16;   // columns per column-kernel block
+constexpr int kRowVecs = 8;    // rows per row-kernel block
+
+__host__ __device__ constexpr int cpadded(int n) { return n + (n >> 5) + 1; }
+__host__ __device__ constexpr int ctw_hi(int n) { return (n + 127) / 128; }
+
+template <int... Rs>
+constexpr int rlen(Radices<Rs...>) {
+  return prod_radices<Rs...>();
+}
+
+__device__ __forceinline__ bool isnormal_pos(float v) { return v >= FLT_MIN && v <= FLT_MAX; }
+
+__device__ __forceinline__ float eps_of(int rule, float ref) {
+  if (rule == AMP_F_REG) return (float)(1e-6 * sqrt((double)ref));
+  if (rule == AMP_PURE) return 0.0f;
+  return 1e-6f * ref;
+}
+
+__device__ __forceinline__ float factor_of(int rule, float m2, float eps) {
+  if (rule == AMP_F_REG) {
+    const float f = 1.0f / (sqrtf(m2) + eps);
+    return isnormal_pos(f) ? f : 0.0f;
+  }
+  if (rule == AMP_D_REG) {
+    const float f = rsqrtf(m2 + eps);
+    return isnormal_pos(f) ? f : 0.0f;
+  }
+  return (m2 > eps) ? rsqrtf(m2) : 0.0f;
+}
+
+__device__ __forceinline__ float2 ld_bin(const void* base, int fmt, int64_t i) {
+  if (fmt == SPEC_F16) return __half22float2(reinterpret_cast<const __half2*>(base)[i]);
+  return reinterpret_cast<const float2*>(base)[i];
+}
+
+// Cross-spectrum bin p of a pair: herm 0 = full spectra, 1 = bins 0..Nz/2 of real
+// traces, 2 = precomputed cross-spectrum rows (spec row = pair index).
+__device__ __forceinline__ float2 pair_bin(const LargeArgs& a, int row, int p) {
+  const int Nz = a.Nz;
+  if (a.herm == 2) return ld_bin(a.spec, a.fmt, (int64_t)row * a.ldspec + p);
+  const int2 pr = a.pairs[row];
+  const int64_t b1 = (int64_t)pr.x * a.ldspec, b2 = (int64_t)pr.y * a.ldspec;
+  if (a.herm == 1 && p > (Nz >> 1)) {
+    const int q = Nz - p;
+    return cconj(cconjmul(ld_bin(a.spec, a.fmt, b1 + q), ld_bin(a.spec, a.fmt, b2 + q)));
+  }
+  return cconjmul(ld_bin(a.spec, a.fmt, b1 + p), ld_bin(a.spec, a.fmt, b2 + p));
+}
+
+__device__ __forceinline__ float2 col_load(const LargeArgs& a, int row, int j, float eps) {
+  switch (a.cmode) {
+    case COL_REAL:
+    case COL_SIGN: {
+      const int jj = j - a.in_off;
+      if (jj < 0 || jj >= a.N) return make_float2(0.f, 0.f);
+      float v = __ldg(reinterpret_cast<const float*>(a.in) + (int64_t)row * a.ldin + jj);
+      if (a.cmode == COL_SIGN) v = (a.sign_ge ? (v >= 0.0f) : (v > 0.0f)) ? 1.0f : -1.0f;
+      return make_float2(v * a.in_scale, 0.f);
+    }
+    case COL_PHASE: {
+      if (j >= a.N) return make_float2(0.f, 0.f);
+      const float2 v = reinterpret_cast<const float2*>(a.in)[(int64_t)row * a.ldin + j];
+      return cscale(v, factor_of(a.rule, v.x * v.x + v.y * v.y, eps));
+    }
+    case COL_COMPLEX:
+      return reinterpret_cast<const float2*>(a.in)[(int64_t)row * a.ldin + j];
+    case COL_NORMALISE: {
+      const float2 v = reinterpret_cast<const float2*>(a.in)[(int64_t)row * a.ldin + j];
+      return cscale(v, factor_of(a.rule, v.x * v.x + v.y * v.y, eps));
+    }
+    case COL_PRODUCT: {
+      const int g = a.filt_of_row_div;
+      const float2 x = reinterpret_cast<const float2*>(a.in)[(int64_t)(row / g) * a.ldin + j];
+      const float2 w = a.filt[(int64_t)(row % g) * a.ldfilt + j];
+      return cscale(cmul(x, w), a.in_scale);
+    }
+    default: {  // COL_PAIR: F[j] = (H[j] + H[j+h]) + i w^j (H[j] - H[j+h]), w = exp(2 pi i / Nz)
+      const int h = a.n;
+      const int Nz = a.Nz;
+      const float2 z0 = pair_bin(a, row, j);
+      const float2 z3 = pair_bin(a, row, j == 0 ? 0 : Nz - j);
+      const float2 z2 = pair_bin(a, row, j + h);
+      const float2 z1 = pair_bin(a, row, h - j);
+      const float2 Hk = cscale(cadd(z0, cconj(z3)), 0.5f);
+      const float2 Hkh = cscale(cadd(z2, cconj(z1)), 0.5f);
+      float s, c;
+      sincospif((float)j / (float)h, &s, &c);   // exp(2 pi i j / Nz), Nz = 2h
+      const float2 e = cadd(Hk, Hkh);
+      const float2 o = cmul(make_float2(c, s), csub(Hk, Hkh));
+      return make_float2(e.x - o.y, e.y + o.x);
+    }
+  }
+}
+
+template <int T, typename RAD, int DIR>
+__global__ void __launch_bounds__(T) k_cols(LargeArgs a) {
+  constexpr int N1 = rlen(RAD{});
+  constexpr int C = kColVecs;
+  constexpr int VS = cpadded(N1);
+  extern __shared__ float4 smem_raw[];
+  float2* s = reinterpret_cast<float2*>(smem_raw);
+  float2* lo1 = s + C * VS;
+  float2* hi1 = lo1 + 128;
+  float2* loN = hi1 + ctw_hi(N1);
+  float2* hiN = loN + 128;
+  const int n = a.n, n2 = a.n2;
+  build_twiddles(lo1, hi1, N1);
+  build_twiddles(loN, hiN, n);
+  const int row = blockIdx.y;
+  const int c0 = blockIdx.x * C;
+  const float eps = (a.cmode == COL_PHASE || a.cmode == COL_NORMALISE) ? eps_of(a.rule, a.rowstat[row]) : 0.f;
+  for (int e = threadIdx.x; e < C * N1; e += T) {
+    const int c = e % C, j1 = e / C;
+    s[c * VS + PADI(j1)] = col_load(a, row, j1 * n2 + c0 + c, eps);
+  }
+  __syncthreads();
+  ct_fft<DIR, T, C>(s, C, VS, TwTab{lo1, hi1}, RAD{});
+  float2* out = a.T + (int64_t)row * n;
+  const TwTab twN{loN, hiN};
+  for (int e = threadIdx.x; e < C * N1; e += T) {
+    const int c = e % C, k1 = e / C;
+    const int j2 = c0 + c;
+    const int t = (int)(((int64_t)j2 * k1) % n);
+    float2 w = twiddle(twN, t);
+    if (DIR > 0) w.y = -w.y;
+    out[(int64_t)k1 * n2 + j2] = cmul(s[c * VS + PADI(k1)], w);
+  }
+}
+
+template <int T, typename RAD, int DIR>
+__global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
+  constexpr int N2 = rlen(RAD{});
+  constexpr int C = kRowVecs;
+  constexpr int VS = cpadded(N2);
+  extern __shared__ float4 smem_raw[];
+  float2* s = reinterpret_cast<float2*>(smem_raw);
+  float2* lo = s + C * VS;
+  float2* hi = lo + 128;
+  __shared__ float red[32];
+  build_twiddles(lo, hi, N2);
+  const int n = a.n, n1 = a.n1;
+  const int row = blockIdx.y;
+  const int r0 = blockIdx.x * C;
+  const float2* in = a.T + (int64_t)row * n;
+  for (int e = threadIdx.x; e < C * N2; e += T) {
+    const int c = e / N2, j2 = e - c * N2;
+    s[c * VS + PADI(j2)] = in[(int64_t)(r0 + c) * N2 + j2];
+  }
+  __syncthreads();
+  ct_fft<DIR, T, C>(s, C, VS, TwTab{lo, hi}, RAD{});
+  float mx = 0.f;
+  for (int e = threadIdx.x; e < C * N2; e += T) {
+    const int c = e % C, k2 = e / C;
+    const int k = (r0 + c) + n1 * k2;
+    const float2 v = s[c * VS + PADI(k2)];
+    if (a.rmode == ROW_SPEC) {
+      if (a.out_half && k > (n >> 1)) continue;
+      if (a.out_fmt == SPEC_F16)
+        reinterpret_cast<__half2*>(a.out)[(int64_t)row * a.ldo + k] = __float22half2_rn(v);
+      else
+        reinterpret_cast<float2*>(a.out)[(int64_t)row * a.ldo + k] = v;
+    } else if (a.rmode == ROW_COMPLEX) {
+      reinterpret_cast<float2*>(a.out)[(int64_t)row * a.ldo + k] = v;
+      mx = fmaxf(mx, v.x * v.x + v.y * v.y);
+    } else {
+      // y_full[2k] = Re z[k], y_full[2k+1] = Im z[k]; lag = idx or idx - Nz
+      const int Nz = 2 * n;
+      const int N = a.N;
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        const int idx = 2 * k + q;
+        const int lag = (idx <= (Nz >> 1)) ? idx : idx - Nz;
+        const int l = lag - a.lag0;
+        if (l < 0 || l >= a.L) continue;
+        float val = (q ? v.y : v.x) * a.scale;
+        if (a.norm == 1) {
+          const int2 pr = a.pairs[row];
+          const double* E1 = a.energy + (int64_t)pr.x * a.ldE;
+          const double* E2 = a.energy + (int64_t)pr.y * a.ldE;
+          int n11 = 0, n21 = 0, n12 = N, n22 = N;
+          if (lag > 0) { n21 = lag; n12 -= lag; }
+          else { n11 = -lag; n22 += lag; }
+          val = (float)((double)val / sqrt((E1[n12] - E1[n11]) * (E2[n22] - E2[n21])));
+        } else if (a.norm == 2) {
+          val = (float)((double)val / (double)(N - abs(lag)));
+        }
+        a.y[(int64_t)row * a.ldy + l] = val;
+      }
+    }
+  }
+  if (a.rmode == ROW_COMPLEX && a.rowmax) {
+    mx = warp_max(mx);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      float v = (threadIdx.x < T / 32) ? red[threadIdx.x] : 0.f;
+      v = warp_max(v);
+      if (threadIdx.x == 0) atomicMax(reinterpret_cast<int*>(a.rowmax) + row, __float_as_int(v));
+    }
+  }
+}
+
+template <typename K>
+cudaError_t launch_k2(K kern, dim3 grid, int T, size_t smem, cudaStream_t st, const LargeArgs& a) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  void* argv[] = {const_cast<LargeArgs*>(&a)};
+  return cudaLaunchKernel((const void*)kern, grid, dim3(T), argv, smem, st);
+}
+
+// column sub-lengths and row sub-lengths with their radix schedules
+#define FPCC_COL_MENU(X) X(32, 128, 8, 4) X(64, 128, 16, 4) X(128, 128, 16, 8) X(256, 256, 16, 16)
+#define FPCC_ROW_MENU(X)                                                                               \
+  X(64, 128, 16, 4) X(128, 128, 16, 8) X(256, 128, 16, 16) X(320, 160, 16, 4, 5) X(384, 192, 16, 8, 3) \
+  X(512, 256, 16, 8, 4) X(640, 320, 16, 8, 5) X(768, 384, 16, 16, 3) X(1024, 512, 16, 16, 4)           \
+  X(1280, 640, 16, 16, 5) X(1536, 768, 16, 8, 4, 3) X(2048, 1024, 16, 16, 8)
+
+bool in_col_menu(int n) {
+#define FPCC_C(SZ, T, ...) if (n == SZ) return true;
+  FPCC_COL_MENU(FPCC_C)
+#undef FPCC_C
+  return false;
+}
+bool in_row_menu(int n) {
+#define FPCC_R(SZ, T, ...) if (n == SZ) return true;
+  FPCC_ROW_MENU(FPCC_R)
+#undef FPCC_R
+  return false;
+}
+
+}  // namespace
+
+bool large_supported(int n, int* n1, int* n2) {
+  for (int c : {256, 128, 64, 32}) {
+    if (n % c == 0 && in_row_menu(n / c) && n / c >= kRowVecs) {
+      *n1 = c;
+      *n2 = n / c;
+      return true;
+    }
+  }
+  return false;
+}
+
+cudaError_t launch_large(const LargeArgs& a, cudaStream_t st) {
+  if (a.nrows <= 0) return cudaSuccess;
+  if (a.nrows > 65535) return cudaErrorInvalidValue;
+  cudaError_t e = cudaErrorInvalidValue;
+  // column pass
+  {
+    dim3 grid(a.n2 / kColVecs, a.nrows);
+    const size_t smem = ((size_t)kColVecs * cpadded(a.n1) + 128 + ctw_hi(a.n1) + 128 + ctw_hi(a.n)) * sizeof(float2);
+    bool done = false;
+#define FPCC_CL(SZ, T, ...)                                                                            \
+  if (!done && a.n1 == SZ) {                                                                         \
+    e = (a.dir < 0) ? launch_k2(k_cols<T, Radices<__VA_ARGS__>, -1>, grid, T, smem, st, a)             \
+                    : launch_k2(k_cols<T, Radices<__VA_ARGS__>, 1>, grid, T, smem, st, a);             \
+    done = true;                                                                                     \
+  }
+    FPCC_COL_MENU(FPCC_CL)
+#undef FPCC_CL
+    if (!done || e != cudaSuccess) return done ? e : cudaErrorInvalidValue;
+  }
+  // row pass
+  {
+    dim3 grid(a.n1 / kRowVecs, a.nrows);
+    const size_t smem = ((size_t)kRowVecs * cpadded(a.n2) + 128 + ctw_hi(a.n2)) * sizeof(float2);
+    bool done = false;
+#define FPCC_RW(SZ, T, ...)                                                                            \
+  if (!done && a.n2 == SZ) {                                                                         \
+    e = (a.dir < 0) ? launch_k2(k_rows<T, Radices<__VA_ARGS__>, -1>, grid, T, smem, st, a)             \
+                    : launch_k2(k_rows<T, Radices<__VA_ARGS__>, 1>, grid, T, smem, st, a);             \
+    done = true;                                                                                     \
+  }
+    FPCC_ROW_MENU(FPCC_RW)
+#undef FPCC_RW
+    if (!done) return cudaErrorInvalidValue;
+  }
+  return e;
+}
+
+}  // namespace fpcc

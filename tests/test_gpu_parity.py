@@ -113,3 +113,27 @@ def test_bad_lags_raise(F):
     a, b = _data(1000, 1, 0, "bad")
     with pytest.raises(F.FpccError):
         F.pcc2_set(a, b, -1000, 10)
+
+
+# ---- lengths above the in-block menu (four-step transforms) --------------------
+@pytest.mark.parametrize("nz", [0, 131072])
+def test_plain_pair_config_sizes(F, orc, nz):
+    """36,000-sample windows, lags +-3000: default padding and 2^17 (four-step)."""
+    a, b = synth.plain_pair(N=36000, n_windows=2, delay=150, tag="gpu/plain36k")
+    mode = nz if nz else F.NZ_FAST
+    y64 = orc.pcc2(a, b, -3000, 3000)
+    assert relerr(F.pcc2_set(a, b, -3000, 3000, nz_mode=mode), y64) < TOL
+    assert relerr(F.ccgn_set(a, b, -3000, 3000, nz_mode=mode), orc.gncc(a, b, -3000, 3000)) < TOL
+    assert relerr(F.cc1b_set(a, b, -3000, 3000, nz_mode=mode), orc.cc1b(a, b, -3000, 3000)) < TOL
+
+
+def test_long_window_pcc2(F, orc):
+    a, b = synth.plain_pair(N=65536, n_windows=1, delay=-300, fs=20.0, band=(0.02, 5.0), tag="gpu/long")
+    assert relerr(F.pcc2_set(a, b, -4000, 4000), orc.pcc2(a, b, -4000, 4000)) < TOL
+
+
+def test_explicit_padding_lengths(F, orc):
+    a, b = _data(4500, 2, 80, "explicit-nz")
+    y64 = orc.pcc2(a, b, -450, 450)
+    for nz in (6144, 8192, 16384, 32768):   # in-block and four-step pair transforms
+        assert relerr(F.pcc2_set(a, b, -450, 450, nz_mode=nz), y64) < TOL, nz
