@@ -74,6 +74,13 @@ def lib():
             L.fpcc_allpairs_host.argtypes = [vp, i, vp, i, i, vp, i, i, i, f, i, i, vp]
             for name in ("pcc2_highlevel", "ccgn_highlevel", "cc1b_highlevel"):
                 getattr(L, name).argtypes = [fpp, fpp, fpp, u, u, i, i]
+            d = C.c_double
+            L.fpcc_wpcc_host.argtypes = [fpp, fpp, fpp, u, u, i, i, d, d, u, i, d, i, i]
+            L.fpcc_wpcc_plan_create.argtypes = [vp, C.POINTER(vp), u, i, i, d, d, u, i, d, i, i]
+            L.fpcc_wpcc_plan_info.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]
+            L.fpcc_wpcc_plan_destroy.argtypes = [vp]
+            L.fpcc_wpcc_station_stage.argtypes = [vp, vp, vp, i64, i, vp, i]
+            L.fpcc_wpcc_pair_stage.argtypes = [vp, vp, vp, i, vp, i, vp, i64]
             L.cc1b_popcount_highlevel.argtypes = [C.POINTER(C.POINTER(C.c_int64)), fpp, fpp, u, u, i, i]
             _lib = L
     return _lib
@@ -149,6 +156,16 @@ def cc1b_set(x1, x2, Lag1, Lag2, popcount=False, **kw):
     """1-bit GNCC (reference cc1b_set, src/FFTapps.c:980); popcount=True uses exact
     integer numerators from packed sign bits."""
     return correlate(CC1B_POPCOUNT if popcount else CC1B, x1, x2, Lag1, Lag2, v=0.0, **kw)
+
+
+def wpcc_set(x1, x2, Lag1, Lag2, pmin, pmax, V=2, type=-3, op1=0.0, rule=AMP_D_REG, nz_mode=NZ_FAST):
+    """Wavelet PCC (reference tspcc2_set, src/FFTapps.c:1076): pmin/pmax in samples,
+    V voices per octave, type -1 Morlet / -2 complete Morlet / -3 complex Mexican hat."""
+    x1, x2, Tr, N = _windows(x1, x2)
+    y = np.zeros((Tr, abs(Lag2 - Lag1 + 1)), np.float32)
+    check(lib().fpcc_wpcc_host(_rows(y), _rows(x1), _rows(x2), N, Tr, Lag1, Lag2, float(pmin), float(pmax),
+                               V, type, float(op1), rule, nz_mode))
+    return y
 
 
 def cc1b_numerators(x1, x2, Lag1, Lag2):

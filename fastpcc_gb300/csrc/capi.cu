@@ -17,6 +17,8 @@
 #include "kernels.cuh"
 #include "large.cuh"
 #include "menu.cuh"
+#include "wavelet.h"
+#include "wpcc.h"
 
 using namespace fpcc;
 
@@ -220,7 +222,8 @@ namespace {
 
 // Workspace slots of the context.
 enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_PAIRS = 5, S_ANA_A = 6,
-            S_ANA_B = 7, S_RSTAT = 8, S_LARGE_T = 9 };
+            S_ANA_B = 7, S_RSTAT = 8, S_LARGE_T = 9, S_WP_X = 10, S_WP_BAND = 11, S_WP_RMAX = 12,
+            S_WP_Y = 13, S_WP_STAGE = 14 };
 
 constexpr size_t kLargeChunkBytes = size_t(512) << 20;   // four-step intermediate per chunk
 
@@ -680,4 +683,198 @@ extern "C" int cc1b_popcount_highlevel(int64_t** num, float** x1, float** x2, un
                                        int Lag2) {
   return host_windows(FPCC_CC1B_POPCOUNT, nullptr, num, x1, x2, N, Tr, Lag1, Lag2, 0.0f, FPCC_NZ_FAST, FPCC_F32,
                       true);
+}
+
+// ============================================================== wavelet PCC
+struct fpcc_wpcc_plan {
+  fpcc::WpccSetup su;
+  fpcc::WpccPlanDev dev;
+  float2* W = nullptr;
+  float* a = nullptr;
+  int device = 0;
+};
+
+namespace {
+
+int wpcc_plan_build(fpcc_ctx* c, const WaveletFamily& wf, int Nz, unsigned N, int lag0, int L, double C, int rule,
+                    int filt_conj, fpcc_wpcc_plan* p) {
+  int n1, n2;
+  if (!large_supported(Nz, &n1, &n2) || !large_supported(Nz / 2, &n1, &n2))
+    return fail(FPCC_EUNSUP, "WPCC length Nz=%d is not supported", Nz);
+  const unsigned S = wf.S;
+  CK(cudaMalloc(&p->W, (size_t)S * Nz * sizeof(float2)));
+  CK(cudaMalloc(&p->a, (size_t)S * sizeof(float)));
+  std::vector<float> a(S);
+  for (unsigned s = 0; s < S; s++) a[s] = (float)(1.0 / (wf.scale[s] * (double)Nz));   // src/FFTapps.c:1217
+  CK(cudaMemcpyAsync(p->a, a.data(), S * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  void *T, *stage;
+  int rc;
+  if ((rc = dev_buf(c, S_LARGE_T, (size_t)S * Nz * sizeof(float2), &T)) ||
+      (rc = dev_buf(c, S_WP_STAGE, (size_t)S * Nz * sizeof(float2), &stage)))
+    return rc;
+  CK(wpcc_filters(wf, Nz, p->W, (float2*)T, (float2*)stage, c->stream));
+  g_launches += 2;
+  p->dev.N = (int)N;
+  p->dev.Nz = Nz;
+  p->dev.S = (int)S;
+  p->dev.Ls0 = (int)wf.Ls[S - 1];
+  p->dev.lag0 = lag0;
+  p->dev.L = L;
+  p->dev.rule = rule;
+  p->dev.filt_conj = filt_conj;
+  p->dev.C = (float)C;
+  p->dev.d_W = p->W;
+  p->dev.d_a = p->a;
+  cudaGetDevice(&p->device);
+  return 0;
+}
+
+int wpcc_station_run(fpcc_ctx* c, const fpcc_wpcc_plan* p, const float* d_x, int64_t ldx, int nrows, void* d_P,
+                     int fmt) {
+  const int Nz = p->dev.Nz, S = p->dev.S;
+  int chunk = (int)(kLargeChunkBytes / ((size_t)S * Nz * sizeof(float2)));
+  if (chunk < 1) chunk = 1;
+  if (chunk * S > 65535) chunk = 65535 / S;
+  if (chunk > nrows) chunk = nrows;
+  void *X, *T, *band, *rmax;
+  int rc;
+  if ((rc = dev_buf(c, S_WP_X, (size_t)chunk * Nz * sizeof(float2), &X)) ||
+      (rc = dev_buf(c, S_LARGE_T, (size_t)chunk * S * Nz * sizeof(float2), &T)) ||
+      (rc = dev_buf(c, S_WP_BAND, (size_t)chunk * S * Nz * sizeof(float2), &band)) ||
+      (rc = dev_buf(c, S_WP_RMAX, (size_t)chunk * S * sizeof(float), &rmax)))
+    return rc;
+  CK(wpcc_station(p->dev, d_x, ldx, nrows, d_P, fmt, (float2*)X, (float2*)T, (float2*)band, (float*)rmax, chunk,
+                  c->stream));
+  g_launches += 6 * ((nrows + chunk - 1) / chunk);
+  return 0;
+}
+
+int wpcc_pairs_run(fpcc_ctx* c, const fpcc_wpcc_plan* p, const void* d_P, int fmt, const int32_t* d_pairs,
+                   int npairs, float* d_y, int64_t ldy) {
+  const int Nz = p->dev.Nz;
+  int chunk = (int)(kLargeChunkBytes / ((size_t)Nz * sizeof(float2)));
+  if (chunk < 1) chunk = 1;
+  if (chunk > 65535) chunk = 65535;
+  if (chunk > npairs) chunk = npairs;
+  void *Y, *T;
+  int rc;
+  if ((rc = dev_buf(c, S_WP_Y, (size_t)chunk * Nz * sizeof(float2), &Y)) ||
+      (rc = dev_buf(c, S_LARGE_T, (size_t)chunk * (Nz / 2) * sizeof(float2), &T)))
+    return rc;
+  CK(wpcc_pairs(p->dev, d_P, fmt, reinterpret_cast<const int2*>(d_pairs), npairs, d_y, ldy, (float2*)Y,
+                (float2*)T, chunk, c->stream));
+  g_launches += 3 * ((npairs + chunk - 1) / chunk);
+  return 0;
+}
+
+// x1, x2 rows -> y rows through the WPCC plan (one batched pass over all windows).
+int wpcc_host_rows(fpcc_ctx* c, const fpcc_wpcc_plan* p, float** y, float** x1, float** x2, unsigned N,
+                   unsigned Tr) {
+  const int L = p->dev.L, S = p->dev.S, Nz = p->dev.Nz;
+  const size_t xbytes = (size_t)2 * Tr * N * sizeof(float);
+  const size_t ybytes = (size_t)Tr * L * sizeof(float);
+  void *h_x, *h_y, *d_x, *d_y, *d_pairs, *d_P;
+  int rc;
+  if ((rc = pin_buf(c, 0, xbytes, &h_x)) || (rc = pin_buf(c, 1, ybytes, &h_y))) return rc;
+  if ((rc = dev_buf(c, S_HOST_X, xbytes, &d_x)) || (rc = dev_buf(c, S_Y, ybytes, &d_y)) ||
+      (rc = dev_buf(c, S_PAIRS, (size_t)2 * Tr * sizeof(int32_t), &d_pairs)) ||
+      (rc = dev_buf(c, S_STATION, (size_t)2 * Tr * S * Nz * sizeof(float2), &d_P)))
+    return rc;
+  float* hx = (float*)h_x;
+  for (unsigned t = 0; t < Tr; t++) {
+    memcpy(hx + (size_t)t * N, x1[t], N * sizeof(float));
+    memcpy(hx + (size_t)(Tr + t) * N, x2[t], N * sizeof(float));
+  }
+  std::vector<int32_t> pairs(2 * Tr);
+  for (unsigned t = 0; t < Tr; t++) { pairs[2 * t] = (int32_t)t; pairs[2 * t + 1] = (int32_t)(Tr + t); }
+  CK(cudaMemcpyAsync(d_x, h_x, xbytes, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(d_pairs, pairs.data(), pairs.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  if ((rc = wpcc_station_run(c, p, (const float*)d_x, N, 2 * (int)Tr, d_P, FPCC_F32))) return rc;
+  if ((rc = wpcc_pairs_run(c, p, d_P, FPCC_F32, (const int32_t*)d_pairs, (int)Tr, (float*)d_y, L))) return rc;
+  CK(cudaMemcpyAsync(h_y, d_y, ybytes, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (unsigned t = 0; t < Tr; t++) memcpy(y[t], (float*)h_y + (size_t)t * L, L * sizeof(float));
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int fpcc_wpcc_plan_create(fpcc_ctx* c, fpcc_wpcc_plan** out, unsigned N, int Lag1, int Lag2, double pmin,
+                                     double pmax, unsigned V, int type, double op1, int rule, int nz_mode) {
+  if (!c || !out) return fail(FPCC_EARG, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  fpcc_wpcc_plan* p = new fpcc_wpcc_plan();
+  if (wpcc_setup(N, Lag1, Lag2, pmin, pmax, V, type, op1, &p->su) != 0) {
+    delete p;
+    return fail(FPCC_EARG, "invalid WPCC parameters (lags below N, pmin/pmax > 0, type -1/-2/-3)");
+  }
+  const int Nz = wpcc_choose_nz(p->su, N, nz_mode);
+  if (Nz <= 0) {
+    delete p;
+    return fail(FPCC_EUNSUP, "no supported WPCC transform length");
+  }
+  int lag0, L;
+  lag_window(Lag1, Lag2, &lag0, &L);
+  int rc = wpcc_plan_build(c, p->su.wf, Nz, N, lag0, L, p->su.C, rule, 0, p);
+  if (rc) {
+    cudaFree(p->W);
+    cudaFree(p->a);
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return 0;
+}
+
+extern "C" int fpcc_wpcc_plan_info(const fpcc_wpcc_plan* p, int* Nz, int* S, int* L) {
+  if (!p) return fail(FPCC_EARG, "null plan");
+  if (Nz) *Nz = p->dev.Nz;
+  if (S) *S = p->dev.S;
+  if (L) *L = p->dev.L;
+  return 0;
+}
+
+extern "C" int fpcc_wpcc_plan_destroy(fpcc_wpcc_plan* p) {
+  if (!p) return 0;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(p->device);
+  cudaDeviceSynchronize();
+  cudaFree(p->W);
+  cudaFree(p->a);
+  cudaSetDevice(cur);
+  delete p;
+  return 0;
+}
+
+extern "C" int fpcc_wpcc_station_stage(fpcc_ctx* c, const fpcc_wpcc_plan* p, const float* d_x, int64_t ldx,
+                                       int nrows, void* d_P, int fmt) {
+  if (!c || !p) return fail(FPCC_EARG, "null argument");
+  if (nrows <= 0) return 0;
+  return wpcc_station_run(c, p, d_x, ldx, nrows, d_P, fmt);
+}
+
+extern "C" int fpcc_wpcc_pair_stage(fpcc_ctx* c, const fpcc_wpcc_plan* p, const void* d_P, int fmt,
+                                    const int32_t* d_pairs, int npairs, float* d_y, int64_t ldy) {
+  if (!c || !p) return fail(FPCC_EARG, "null argument");
+  if (npairs <= 0) return 0;
+  return wpcc_pairs_run(c, p, d_P, fmt, d_pairs, npairs, d_y, ldy);
+}
+
+extern "C" int fpcc_wpcc_host(float** y, float** x1, float** x2, unsigned N, unsigned Tr, int Lag1, int Lag2,
+                              double pmin, double pmax, unsigned V, int type, double op1, int rule, int nz_mode) {
+  if (!y || !x1 || !x2) return fail(FPCC_EARG, "null row arrays");
+  if (Tr == 0) return 0;
+  fpcc_ctx* c = nullptr;
+  int rc = default_ctx(&c);
+  if (rc) return rc;
+  fpcc_wpcc_plan* p = nullptr;
+  if ((rc = fpcc_wpcc_plan_create(c, &p, N, Lag1, Lag2, pmin, pmax, V, type, op1, rule, nz_mode))) return rc;
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    rc = wpcc_host_rows(c, p, y, x1, x2, N, Tr);
+  }
+  fpcc_wpcc_plan_destroy(p);
+  return rc;
 }

@@ -80,7 +80,8 @@ __device__ __forceinline__ float2 col_load(const LargeArgs& a, int row, int j, f
     case COL_PRODUCT: {
       const int g = a.filt_of_row_div;
       const float2 x = reinterpret_cast<const float2*>(a.in)[(int64_t)(row / g) * a.ldin + j];
-      const float2 w = a.filt[(int64_t)(row % g) * a.ldfilt + j];
+      float2 w = a.filt[(int64_t)(row % g) * a.ldfilt + j];
+      if (a.filt_conj) w.y = -w.y;
       return cscale(cmul(x, w), a.in_scale);
     }
     default: {  // COL_PAIR: F[j] = (H[j] + H[j+h]) + i w^j (H[j] - H[j+h]), w = exp(2 pi i / Nz)

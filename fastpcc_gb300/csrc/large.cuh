@@ -56,7 +56,8 @@ struct LargeArgs {
   // COL_PRODUCT: row r uses filter filt[(r / rows_per_filter) ... ] — see large.cu
   const float2* filt;
   int64_t ldfilt;
-  int filt_of_row_div; // row r multiplies by filter row (r % filt_of_row_div)
+  int filt_of_row_div; // row r reads input row r / div and filter row r % div
+  int filt_conj;       // multiply by conj(filter) instead
   float in_scale;
   // intermediate
   float2* T;          // nrows x n

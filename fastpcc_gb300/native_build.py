@@ -31,7 +31,7 @@ def nvcc() -> str:
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def _newest_input() -> float:
@@ -54,7 +54,7 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
     flags = NVCC_FLAGS + ARCH + list(extra or [])
 
     def one(src):
-        obj = os.path.join(OBJDIR, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(OBJDIR, os.path.splitext(os.path.basename(src))[0] + ".o")
         cmd = [cc, *flags, "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)

@@ -134,6 +134,26 @@ int cc1b_highlevel(float **y, float **x1, float **x2, unsigned N, unsigned Tr, i
 int cc1b_popcount_highlevel(int64_t **num, float **x1, float **x2, unsigned N, unsigned Tr, int Lag1,
                             int Lag2);
 
+/* ---- wavelet PCC (reference tspcc2_set, src/FFTapps.c:1076-1255) ---------
+ * A plan holds the complex wavelet family (type -1 Morlet, -2 complete Morlet,
+ * -3 complex Mexican hat; scales from pmin/pmax in samples, V voices), its
+ * spectra on the device and the padded length (nz_mode as fpcc_nz_mode or an
+ * explicit length).  rule: FPCC_AMP_D_REG (the reference CPU path) or
+ * FPCC_AMP_THRESH (the reference GPU path).  Station products are S x Nz complex
+ * per station window (the per-scale phase spectra). */
+typedef struct fpcc_wpcc_plan fpcc_wpcc_plan;
+int fpcc_wpcc_plan_create(fpcc_ctx *ctx, fpcc_wpcc_plan **out, unsigned N, int Lag1, int Lag2, double pmin,
+                          double pmax, unsigned V, int type, double op1, int rule, int nz_mode);
+int fpcc_wpcc_plan_info(const fpcc_wpcc_plan *p, int *Nz, int *S, int *L);
+int fpcc_wpcc_plan_destroy(fpcc_wpcc_plan *p);
+int fpcc_wpcc_station_stage(fpcc_ctx *ctx, const fpcc_wpcc_plan *p, const float *d_x, int64_t ldx, int nrows,
+                            void *d_P, int fmt);
+int fpcc_wpcc_pair_stage(fpcc_ctx *ctx, const fpcc_wpcc_plan *p, const void *d_P, int fmt, const int32_t *d_pairs,
+                         int npairs, float *d_y, int64_t ldy);
+/* Host rows in and out, arguments of tspcc2_set plus rule and nz_mode. */
+int fpcc_wpcc_host(float **y, float **x1, float **x2, unsigned N, unsigned Tr, int Lag1, int Lag2, double pmin,
+                   double pmax, unsigned V, int type, double op1, int rule, int nz_mode);
+
 /* ---- allocation-free PCC2 ------------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a host whose pool allocator owns all device memory, plugin frameworks that

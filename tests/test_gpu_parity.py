@@ -137,3 +137,33 @@ def test_explicit_padding_lengths(F, orc):
     y64 = orc.pcc2(a, b, -450, 450)
     for nz in (6144, 8192, 16384, 32768):   # in-block and four-step pair transforms
         assert relerr(F.pcc2_set(a, b, -450, 450, nz_mode=nz), y64) < TOL, nz
+
+
+# ---- wavelet PCC -----------------------------------------------------------------
+def test_wpcc_golden(F, orc):
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_wpcc_n3000.npz"))
+    x1, x2 = g["x1"], g["x2"]
+    l1, l2, pmin, pmax, V = int(g["Lag1"]), int(g["Lag2"]), float(g["pmin"]), float(g["pmax"]), int(g["V"])
+    for key, wt in (("wpcc_mexhat", -3), ("wpcc_morlet", -1)):
+        y64 = orc.wpcc(x1, x2, l1, l2, pmin, pmax, V=V, wtype=wt)
+        assert relerr(g[key], y64) < 1e-6, key          # oracle pinned to the reference
+        y = F.wpcc_set(x1, x2, l1, l2, pmin, pmax, V=V, type=wt)
+        assert relerr(y, y64) < TOL, key
+        y_ref_len = F.wpcc_set(x1, x2, l1, l2, pmin, pmax, V=V, type=wt, nz_mode=F.NZ_REFERENCE)
+        assert relerr(y_ref_len, y64) < TOL, key
+
+
+def test_wpcc_gpu_rule(F, orc):
+    a, b = synth.plain_pair(N=4000, n_windows=2, delay=-60, fs=20.0, band=(0.02, 5.0), tag="gpu/wpcc-thr")
+    y64 = orc.wpcc(a, b, -300, 300, 4.0, 80.0, V=3, wtype=-1, rule=orc.AMP_THRESH)
+    assert relerr(F.wpcc_set(a, b, -300, 300, 4.0, 80.0, V=3, type=-1, rule=F.AMP_THRESH), y64) < TOL
+
+
+def test_wpcc_wavelet_config_size(F, orc):
+    """65,536 samples at 20 Hz, Morlet, 40 scales (V=5, 4 to 1000 samples), lags +-4000."""
+    x1, x2, _ = synth.wavelet_pairs(n_pairs=1, n_windows=1, tag="gpu/wpcc-c3")
+    a, b = x1[0], x2[0]
+    y64 = orc.wpcc(a, b, -4000, 4000, 4.0, 1000.0, V=5, wtype=-1)
+    y = F.wpcc_set(a, b, -4000, 4000, 4.0, 1000.0, V=5, type=-1)
+    assert relerr(y, y64) < TOL
