@@ -7,6 +7,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <semaphore.h>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -58,8 +59,9 @@ struct fpcc_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  DevBuf dev[16];
-  DevBuf pin[4];
+  DevBuf dev[24];
+  DevBuf pin[8];
+  cudaStream_t stream2 = nullptr;   // second stream of the pipelined drop-ins
   std::map<int, float2*> twiddles;   // device tables exp(-2 pi i t/n), per n
   std::mutex mu;
 };
@@ -159,6 +161,7 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
   for (auto& b : c->pin) if (b.p) cudaFreeHost(b.p);
   for (auto& kv : c->twiddles) cudaFree(kv.second);
   if (c->own_stream) cudaStreamDestroy(c->stream);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
   {
     std::lock_guard<std::mutex> lk(g_default_mu);
     if (c == g_default) g_default = nullptr;
@@ -877,4 +880,183 @@ extern "C" int fpcc_wpcc_host(float** y, float** x1, float** x2, unsigned N, uns
   }
   fpcc_wpcc_plan_destroy(p);
   return rc;
+}
+
+// ============================================================== reference GPU boundary
+// The four entry points of the reference's src/ccs_cuda.h with its signatures.
+namespace {
+
+enum CcSlot { S_CC_AN = 15, S_CC_PH = 17, S_CC_Y = 19, S_CC_ZERO = 21 };
+
+// PCC_v on analytic signals produced concurrently by the caller: windows are
+// consumed in groups of 16 (the reference's 16 streams, src/ccs_cuda.cu:570-592)
+// on two alternating streams with double-buffered pinned staging, so the copy
+// of one group overlaps the kernels of the previous one.
+int pcc_from_analytic(float** y, const float2* const* x1, const float2* const* x2, int N, unsigned Tr, float v,
+                      int Lag1, int Lag2, sem_t* anok, bool pcc1) {
+  if (!y || !x1 || !x2 || N <= 0) return FPCC_ECUDA;
+  // lag handling of src/ccs_cuda.cu:544-551
+  int L = abs(Lag2 - Lag1 + 1);
+  if (Lag2 > N) L -= (Lag2 - N);
+  const int l1 = (Lag1 >= -N) ? 0 : -(Lag1 + N);
+  if (L <= 0 || Tr == 0) return 0;
+  fpcc_ctx* c = nullptr;
+  if (default_ctx(&c)) return FPCC_ECUDA;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (cudaSetDevice(c->device) != cudaSuccess) return FPCC_ECUDA;
+  if (!c->stream2 && cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) return FPCC_ECUDA;
+  const unsigned G = 16;
+  const size_t xb = (size_t)2 * G * N * sizeof(float2);
+  const size_t yb = (size_t)G * L * sizeof(float);
+  void *hx[2], *hy[2], *dx[2], *dp[2], *dy[2], *zero, *dpairs;
+  for (int k = 0; k < 2; k++) {
+    if (pin_buf(c, 2 + k, xb, &hx[k]) || pin_buf(c, 4 + k, yb, &hy[k]) || dev_buf(c, S_CC_AN + k, xb, &dx[k]) ||
+        dev_buf(c, S_CC_PH + k, xb, &dp[k]) || dev_buf(c, S_CC_Y + k, yb, &dy[k]))
+      return FPCC_ECUDA;
+  }
+  if (dev_buf(c, S_CC_ZERO, (size_t)2 * G * sizeof(float), &zero) ||
+      dev_buf(c, S_PAIRS, (size_t)2 * G * sizeof(int32_t), &dpairs))
+    return FPCC_ECUDA;
+  std::vector<int32_t> pr(2 * G);
+  for (unsigned t = 0; t < G; t++) { pr[2 * t] = (int32_t)t; pr[2 * t + 1] = (int32_t)(G + t); }
+  cudaStream_t st[2] = {c->stream, c->stream2};
+  if (cudaMemsetAsync(zero, 0, 2 * G * sizeof(float), st[0]) != cudaSuccess ||
+      cudaMemcpyAsync(dpairs, pr.data(), pr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st[0]) != cudaSuccess ||
+      cudaStreamSynchronize(st[0]) != cudaSuccess)
+    return FPCC_ECUDA;
+  unsigned pending_base[2] = {0, 0}, pending_n[2] = {0, 0};
+  auto drain = [&](int k) -> int {
+    if (!pending_n[k]) return 0;
+    if (cudaStreamSynchronize(st[k]) != cudaSuccess) return FPCC_ECUDA;
+    for (unsigned t = 0; t < pending_n[k]; t++)
+      for (int l = l1; l < L; l++) y[pending_base[k] + t][l] = ((float*)hy[k])[(size_t)t * L + l];
+    pending_n[k] = 0;
+    return 0;
+  };
+  unsigned grp = 0;
+  for (unsigned t0 = 0; t0 < Tr; t0 += G, grp++) {
+    const int k = grp & 1;
+    if (drain(k)) return FPCC_ECUDA;
+    const unsigned n = (Tr - t0) < G ? (Tr - t0) : G;
+    float2* h = (float2*)hx[k];
+    for (unsigned t = 0; t < n; t++) {
+      if (anok) sem_wait(&anok[t0 + t]);   // src/ccs_cuda.cu:575,693
+      memcpy(h + (size_t)t * N, x1[t0 + t], (size_t)N * sizeof(float2));
+      memcpy(h + (size_t)(G + t) * N, x2[t0 + t], (size_t)N * sizeof(float2));
+    }
+    if (cudaMemcpyAsync(dx[k], hx[k], xb, cudaMemcpyHostToDevice, st[k]) != cudaSuccess) return FPCC_ECUDA;
+    PhaseArgs a{};
+    a.in = (const float2*)dx[k]; a.ldin = N; a.nrows = 2 * G; a.N = N; a.rule = AMP_PURE;
+    a.rowstat = (const float*)zero; a.fmt = 0; a.out = dp[k]; a.ldo = N;
+    if (launch_phase_store(a, st[k]) != cudaSuccess) return FPCC_ECUDA;
+    PccvArgs q{};
+    q.phase = dp[k]; q.ldp = N; q.half = 0; q.pairs = (const int2*)dpairs; q.npairs = (int)n; q.N = N;
+    q.Lag1 = Lag1; q.L = L; q.v = pcc1 ? 1.0f : v; q.norm_gpu = 1; q.y = (float*)dy[k]; q.ldy = L;
+    if (launch_pccv(q, st[k]) != cudaSuccess) return FPCC_ECUDA;
+    if (cudaMemcpyAsync(hy[k], dy[k], (size_t)n * L * sizeof(float), cudaMemcpyDeviceToHost, st[k]) != cudaSuccess)
+      return FPCC_ECUDA;
+    g_launches += 2;
+    pending_base[k] = t0;
+    pending_n[k] = n;
+  }
+  if (drain(0) || drain(1)) return FPCC_ECUDA;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int pcc_highlevel(float** y, float2** x1, float2** x2, int N, unsigned int Tr, float v, int Lag1, int Lag2,
+                             sem_t* anok) {
+  return pcc_from_analytic(y, x1, x2, N, Tr, v, Lag1, Lag2, anok, false) ? -1 : 0;
+}
+
+extern "C" int pcc1_highlevel(float** y, float2** x1, float2** x2, int N, unsigned int Tr, int Lag1, int Lag2,
+                              sem_t* anok) {
+  return pcc_from_analytic(y, x1, x2, N, Tr, 1.0f, Lag1, Lag2, anok, true) ? -1 : 0;
+}
+
+// Raw traces in: analytic signals on the GPU, amplitude threshold 1e-6 of the
+// sum of |x|^2 (cuda_AmpNormf2, src/ccs_cuda.cu:493-511), PCC1.  The reference's
+// GPU_analytic (src/ccs_cuda.cu:13-30) does not apply the one-sided mask of
+// src/FFTapps.c:114-118; this one applies that mask.
+extern "C" void pcc1_highlevel2(float** y, float** x1, float** x2, int N, unsigned int Tr, int Lag1, int Lag2) {
+  if (!y || !x1 || !x2 || N <= 0 || Tr == 0) return;
+  int L = abs(Lag2 - Lag1 + 1);
+  if (Lag2 > N) L -= (Lag2 - N);
+  const int l1 = (Lag1 >= -N) ? 0 : -(Lag1 + N);
+  if (L <= 0) return;
+  fpcc_ctx* c = nullptr;
+  if (default_ctx(&c)) return;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  const size_t xb = (size_t)2 * Tr * N * sizeof(float), yb = (size_t)Tr * L * sizeof(float);
+  void *hx, *hy, *dx, *dy, *dp, *dpairs;
+  if (pin_buf(c, 0, xb, &hx) || pin_buf(c, 1, yb, &hy) || dev_buf(c, S_HOST_X, xb, &dx) ||
+      dev_buf(c, S_Y, yb, &dy) || dev_buf(c, S_STATION, (size_t)2 * Tr * N * sizeof(float2), &dp) ||
+      dev_buf(c, S_PAIRS, (size_t)2 * Tr * sizeof(int32_t), &dpairs))
+    return;
+  float* h = (float*)hx;
+  for (unsigned t = 0; t < Tr; t++) {
+    memcpy(h + (size_t)t * N, x1[t], N * sizeof(float));
+    memcpy(h + (size_t)(Tr + t) * N, x2[t], N * sizeof(float));
+  }
+  std::vector<int32_t> pr(2 * Tr);
+  for (unsigned t = 0; t < Tr; t++) { pr[2 * t] = (int32_t)t; pr[2 * t + 1] = (int32_t)(Tr + t); }
+  if (cudaMemcpyAsync(dx, hx, xb, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) return;
+  if (cudaMemcpyAsync(dpairs, pr.data(), pr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+    return;
+  const float2* an;
+  const float *rmax, *rsum;
+  if (analytic_rows(c, (const float*)dx, N, 2 * (int)Tr, N, &an, &rmax, &rsum)) return;
+  PhaseArgs a{};
+  a.in = an; a.ldin = N; a.nrows = 2 * (int)Tr; a.N = N; a.rule = AMP_SUMTHR; a.rowstat = rsum;
+  a.fmt = 0; a.out = dp; a.ldo = N;
+  if (launch_phase_store(a, c->stream) != cudaSuccess) return;
+  PccvArgs q{};
+  q.phase = dp; q.ldp = N; q.pairs = (const int2*)dpairs; q.npairs = (int)Tr; q.N = N; q.Lag1 = Lag1; q.L = L;
+  q.v = 1.0f; q.norm_gpu = 1; q.y = (float*)dy; q.ldy = L;
+  if (launch_pccv(q, c->stream) != cudaSuccess) return;
+  g_launches += 2;
+  if (cudaMemcpyAsync(hy, dy, yb, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) return;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return;
+  for (unsigned t = 0; t < Tr; t++)
+    for (int l = l1; l < L; l++) y[t][l] = ((float*)hy)[(size_t)t * L + l];
+}
+
+// WPCC with the caller's wavelet family, the GPU path's conventions: bands from
+// conj(W_s) (GPU_prod, src/ccs_cuda.cu:874-884) and the threshold normalisation
+// on the band maximum (cuda_AmpNormf3, :513-531).
+extern "C" int cuda_tspcc2_set_freq(float** y0, float** x01, float** x02, unsigned int N, unsigned int Tr,
+                                    unsigned int Nz, const int Lag1, const int Lag2, unsigned int S, double* scale,
+                                    double2** wc, unsigned int* Ls, int* center, unsigned int* Down_smp, float C) {
+  if (!y0 || !x01 || !x02 || !scale || !wc || !Ls || !center || !Down_smp || S == 0) return -1;
+  for (unsigned s = 0; s < S; s++)
+    if (Down_smp[s] != 1) return -2;   // src/ccs_cuda.cu:940-941
+  WaveletFamily wf;
+  wf.S = S;
+  wf.scale.assign(scale, scale + S);
+  wf.Ls.assign(Ls, Ls + S);
+  wf.center.assign(center, center + S);
+  wf.taps.resize(S);
+  for (unsigned s = 0; s < S; s++) {
+    wf.taps[s].resize(Ls[s]);
+    for (unsigned n = 0; n < Ls[s]; n++) wf.taps[s][n] = std::complex<double>(wc[s][n].x, wc[s][n].y);
+  }
+  int lag0, L;
+  lag_window(Lag1, Lag2, &lag0, &L);
+  fpcc_ctx* c = nullptr;
+  if (default_ctx(&c)) return -1;
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (cudaSetDevice(c->device) != cudaSuccess) return -1;
+  fpcc_wpcc_plan p;
+  if (wpcc_plan_build(c, wf, (int)Nz, N, lag0, L, (double)C, AMP_THRESH, 1, &p)) {
+    cudaFree(p.W);
+    cudaFree(p.a);
+    return -1;
+  }
+  const int rc = wpcc_host_rows(c, &p, y0, x01, x02, N, Tr);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(p.W);
+  cudaFree(p.a);
+  return rc ? -1 : 0;
 }

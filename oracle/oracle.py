@@ -24,7 +24,7 @@ import threading
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-AMP_F_REG, AMP_D_REG, AMP_PURE, AMP_THRESH = 0, 1, 2, 3
+AMP_F_REG, AMP_D_REG, AMP_PURE, AMP_THRESH, AMP_SUMTHR = 0, 1, 2, 3, 4
 
 _lock = threading.Lock()
 _lib = None

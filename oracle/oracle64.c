@@ -45,12 +45,14 @@ int orc_analytic(double complex *y, const float *x, unsigned N) {
 }
 
 void orc_ampnorm(double complex *y, unsigned N, int rule) {
-    double mx = 0;   /* max |y|^2 */
+    double mx = 0, sm = 0;   /* max and sum of |y|^2 */
     for (unsigned n = 0; n < N; n++) {
         double a = creal(y[n]), b = cimag(y[n]);
         double m = a * a + b * b;
         if (mx < m) mx = m;
+        sm += m;
     }
+    if (rule == ORC_AMP_SUMTHR) mx = sm;
     if (rule == ORC_AMP_F_REG) {
         /* src/FFTapps.c:185-204 */
         double eps = 1e-6 * sqrt(mx);
@@ -68,8 +70,8 @@ void orc_ampnorm(double complex *y, unsigned N, int rule) {
             y[n] = isnormal(f) ? y[n] * f : 0;
         }
     } else {
-        /* src/ccs_cuda.cu:190-232: threshold e = 1e-6*mabs, mabs = 0 or max|y|^2 */
-        double e = (rule == ORC_AMP_THRESH) ? 1e-6 * mx : 0.0;
+        /* src/ccs_cuda.cu:190-232: threshold e = 1e-6*mabs, mabs = 0, max|y|^2 or sum|y|^2 */
+        double e = (rule == ORC_AMP_THRESH || rule == ORC_AMP_SUMTHR) ? 1e-6 * mx : 0.0;
         for (unsigned n = 0; n < N; n++) {
             double a = creal(y[n]), b = cimag(y[n]);
             double m = a * a + b * b;
