@@ -28,7 +28,7 @@ enum {
     ORC_AMP_PURE = 2,    /* GPU_AmpNormf, mabs=0  src/ccs_cuda.cu:212-232: x/|x| if |x|>0  */
     ORC_AMP_THRESH = 3,  /* GPU_AmpNormf2 + max   src/ccs_cuda.cu:190-210,513-531:
                             x/|x| if |x|^2 > 1e-6*max|x|^2, else 0                        */
-  ORC_AMP_SUMTHR = 4   /* GPU_AmpNormf2 + sum   src/ccs_cuda.cu:107-146,493-511:
+    ORC_AMP_SUMTHR = 4   /* GPU_AmpNormf2 + sum   src/ccs_cuda.cu:107-146,493-511:
                             x/|x| if |x|^2 > 1e-6*sum|x|^2, else 0                        */
 };
 
