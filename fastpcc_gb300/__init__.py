@@ -32,6 +32,17 @@ _lock = threading.Lock()
 _lib = None
 
 
+class Request(C.Structure):
+    """fpcc_request of include/fastpcc_gb300.h."""
+    _fields_ = [("method", C.c_int), ("sta1", C.c_int32), ("sta2", C.c_int32), ("window", C.c_int32),
+                ("Lag1", C.c_int), ("Lag2", C.c_int), ("v", C.c_float), ("y", C.c_void_p), ("num", C.c_void_p)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("batches", C.c_int64), ("station_rows", C.c_int64),
+                ("hbm_used", C.c_int64), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double)]
+
+
 class FpccError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"fastpcc_gb300 error {code}: {msg}")
@@ -81,6 +92,19 @@ def lib():
             L.fpcc_wpcc_plan_destroy.argtypes = [vp]
             L.fpcc_wpcc_station_stage.argtypes = [vp, vp, vp, i64, i, vp, i]
             L.fpcc_wpcc_pair_stage.argtypes = [vp, vp, vp, i, vp, i, vp, i64]
+            L.fpcc_server_create.argtypes = [C.POINTER(vp), i, C.c_size_t, i]
+            L.fpcc_server_destroy.argtypes = [vp]
+            L.fpcc_put_station_window.argtypes = [vp, C.c_int32, C.c_int32, vp, i]
+            L.fpcc_submit.argtypes = [vp, C.POINTER(Request)]
+            L.fpcc_submit.restype = i64
+            L.fpcc_submit_many.argtypes = [vp, C.POINTER(Request), i, C.POINTER(i64)]
+            L.fpcc_server_offer_poisson.argtypes = [vp, C.POINTER(Request), i, C.c_double, C.c_uint64,
+                                                    C.POINTER(i64)]
+            L.fpcc_poll.argtypes = [vp, i64]
+            L.fpcc_wait.argtypes = [vp, i64, C.c_double]
+            L.fpcc_server_drain.argtypes = [vp]
+            L.fpcc_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
+            L.fpcc_server_reset_stats.argtypes = [vp]
             L.cc1b_popcount_highlevel.argtypes = [C.POINTER(C.POINTER(C.c_int64)), fpp, fpp, u, u, i, i]
             _lib = L
     return _lib
@@ -237,3 +261,78 @@ class Context:
         check(lib().fpcc_allpairs_host(self._h, method, C.c_void_p(x.ctypes.data), x.shape[0], x.shape[1],
                                        C.c_void_p(pairs.ctypes.data), pairs.shape[0], Lag1, Lag2, float(v),
                                        nz_mode, fmt, C.c_void_p(y.ctypes.data)))
+
+
+class Server:
+    """Continuous-batching correlation server (fpcc_server_* of the C ABI).
+
+    Outputs are written into numpy arrays owned by the caller; keep them alive
+    until the request completes (``wait``/``drain``)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 150 << 30, max_batch: int = 4096):
+        self._h = C.c_void_p()
+        check(lib().fpcc_server_create(C.byref(self._h), device, hbm_budget, max_batch))
+        self._keep = {}
+
+    def close(self):
+        if self._h:
+            lib().fpcc_server_destroy(self._h)
+            self._h = C.c_void_p()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def put(self, sta: int, window: int, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        check(lib().fpcc_put_station_window(self._h, sta, window, x.ctypes.data, x.shape[0]))
+
+    @staticmethod
+    def request(method, sta1, sta2, window, Lag1, Lag2, out, v=0.0):
+        r = Request(method, sta1, sta2, window, Lag1, Lag2, float(v), None, None)
+        if method == CC1B_POPCOUNT:
+            r.num = out.ctypes.data
+        else:
+            r.y = out.ctypes.data
+        return r
+
+    def submit(self, method, sta1, sta2, window, Lag1, Lag2, out, v=0.0) -> int:
+        r = self.request(method, sta1, sta2, window, Lag1, Lag2, out, v)
+        rid = int(lib().fpcc_submit(self._h, C.byref(r)))
+        if rid < 0:
+            check(rid)
+        self._keep[rid] = out
+        return rid
+
+    def submit_many(self, reqs, outs=None, poisson_rate=None, seed=1):
+        arr = (Request * len(reqs))(*reqs)
+        ids = np.zeros(len(reqs), np.int64)
+        idp = ids.ctypes.data_as(C.POINTER(C.c_int64))
+        if poisson_rate:
+            rc = lib().fpcc_server_offer_poisson(self._h, arr, len(reqs), float(poisson_rate), seed, idp)
+        else:
+            rc = lib().fpcc_submit_many(self._h, arr, len(reqs), idp)
+        check(rc)
+        return ids
+
+    def wait(self, rid: int, timeout: float = 0.0) -> int:
+        st = lib().fpcc_wait(self._h, rid, float(timeout))
+        if st < 0:
+            check(st)
+        self._keep.pop(rid, None)
+        return st
+
+    def drain(self):
+        check(lib().fpcc_server_drain(self._h))
+        self._keep.clear()
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        check(lib().fpcc_server_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def reset_stats(self):
+        check(lib().fpcc_server_reset_stats(self._h))

@@ -244,7 +244,7 @@ bool in_row_menu(int n) {
 
 bool large_supported(int n, int* n1, int* n2) {
   for (int c : {256, 128, 64, 32}) {
-    if (n % c == 0 && in_row_menu(n / c) && n / c >= kRowVecs) {
+    if (n % c == 0 && in_col_menu(c) && in_row_menu(n / c) && n / c >= kRowVecs) {
       *n1 = c;
       *n2 = n / c;
       return true;

@@ -1,0 +1,735 @@
+// Serving loop: continuous batching of correlation requests over station
+// products kept resident in HBM.
+//
+// Requests (method, station pair, window, lag window) arrive from any host
+// thread.  A worker thread repeatedly takes everything pending (up to max_batch
+// requests), groups it by (method, window length, padded length, lag window,
+// power), computes the station products the group lacks — uploading raw windows
+// first — and launches one pair stage per group.  While a batch's kernels and
+// output copy run, the worker is already forming the next batch: requests that
+// arrive meanwhile join it.  Completion is detected from CUDA events; the
+// worker copies each result into the caller's buffer and records its latency.
+//
+// Device memory: raw windows and station products live in slabs (one per
+// product class) whose rows are recycled least-recently-used first; the total
+// never exceeds the HBM budget given at creation.  Rows used by a batch in
+// flight are never evicted.  Each result depends only on its own request (the
+// same kernels and padded length whatever the batch holds), so a result is the
+// same alone and in any mix.
+#include <algorithm>
+#include <cmath>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <list>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/fastpcc_gb300.h"
+#include "engine.h"
+#include "large.cuh"
+#include "serve.h"
+
+namespace fpcc {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+__global__ void k_copy_rows(const char* __restrict__ src, int64_t lds, const int* __restrict__ sidx, char* __restrict__ dst,
+                            int64_t ldd, const int* __restrict__ didx, int64_t row_bytes) {
+  const int r = blockIdx.y;
+  const char* s = src + (int64_t)(sidx ? sidx[r] : r) * lds;
+  char* d = dst + (int64_t)(didx ? didx[r] : r) * ldd;
+  const int64_t n16 = row_bytes / 16;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += (int64_t)gridDim.x * blockDim.x)
+    reinterpret_cast<int4*>(d)[i] = reinterpret_cast<const int4*>(s)[i];
+  const int64_t tail = row_bytes - n16 * 16;
+  if (blockIdx.x == 0 && threadIdx.x < tail) d[n16 * 16 + threadIdx.x] = s[n16 * 16 + threadIdx.x];
+}
+
+// rows of row_bytes (multiple of 16 for the vector path; strides multiples of 16)
+cudaError_t copy_rows(const void* src, int64_t lds, const int* sidx, void* dst, int64_t ldd, const int* didx, int n,
+                      int64_t row_bytes, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  int gx = (int)std::min<int64_t>((row_bytes / 16 + 255) / 256, 64);
+  if (gx < 1) gx = 1;
+  k_copy_rows<<<dim3(gx, n), 256, 0, st>>>((const char*)src, lds, sidx, (char*)dst, ldd, didx, row_bytes);
+  return cudaGetLastError();
+}
+
+// A slab of equal rows with least-recently-used recycling.
+struct Slab {
+  void* base = nullptr;
+  int64_t row_bytes = 0;
+  int cap = 0;
+  std::vector<int64_t> key_of;     // row -> key (-1 free)
+  std::vector<int> pin;            // in-flight references
+  std::list<int> lru;              // front = most recent
+  std::vector<std::list<int>::iterator> pos;
+  std::unordered_map<int64_t, int> row_of;
+};
+
+struct Product {  // identifies a product class
+  int kind;       // 0 raw window, 1 phase spectrum, 2 real half spectrum, 3 sign half spectrum (GE),
+                  // 4 sign half spectrum (GT), 5 energies, 6 phase signal, 7 bits GE, 8 bits GT
+  int N, Nz, fmt;
+  bool operator<(const Product& o) const {
+    return std::tie(kind, N, Nz, fmt) < std::tie(o.kind, o.N, o.Nz, o.fmt);
+  }
+};
+
+struct Req {
+  int64_t id;
+  fpcc_request r;
+  Clock::time_point t_submit;
+  int N = 0, Nz = 0, lag0 = 0, L = 0;
+};
+
+struct InFlight {
+  cudaEvent_t done = nullptr;
+  std::vector<Req> reqs;
+  std::vector<int64_t> out_off;    // offset of each request's output in the pinned buffer (floats or int64)
+  void* h_out = nullptr;           // pinned
+  size_t h_bytes = 0;
+  std::vector<std::pair<Slab*, int>> pinned_rows;
+};
+
+}  // namespace
+
+struct Server {
+  int device = 0;
+  size_t budget = 0, used = 0;
+  int max_batch = 4096;
+  cudaStream_t st = nullptr;
+  fpcc_ctx* ctx = nullptr;
+  // host copies of registered windows
+  std::mutex mu;
+  std::condition_variable cv, cv_done;
+  std::map<std::pair<int, int>, std::vector<float>> windows;   // (sta, win) -> samples
+  std::deque<Req> pending;
+  std::unordered_map<int64_t, int> status;                     // id -> 0 pending, 1 done, <0 error
+  int64_t next_id = 0;
+  bool stop = false;
+  std::thread worker;
+  // device state (worker thread only)
+  std::map<Product, Slab> slabs;
+  std::deque<InFlight> inflight;
+  // scratch (worker only)
+  void* d_tmp_x = nullptr; size_t n_tmp_x = 0;
+  void* d_tmp_p = nullptr; size_t n_tmp_p = 0;
+  void* d_idx = nullptr; size_t n_idx = 0;
+  void* d_y = nullptr; size_t n_y = 0;
+  void* d_pl = nullptr; size_t n_pl = 0;
+  std::vector<void*> pinned_pool;
+  // stats
+  std::vector<double> lat_ms;
+  int64_t completed = 0, batches = 0, station_rows = 0;
+  double busy_s = 0;
+  int last_error = 0;
+};
+
+namespace {
+
+int64_t wkey(int sta, int win) { return ((int64_t)sta << 32) | (uint32_t)win; }
+
+size_t product_row_bytes(const Product& p) {
+  switch (p.kind) {
+    case 0: return (size_t)p.N * 4;
+    case 1: return (size_t)p.Nz * (p.fmt ? 4 : 8);
+    case 2: case 3: case 4: return (size_t)(p.Nz / 2 + 1) * 8;
+    case 5: return (size_t)(p.N + 1) * 8;
+    case 6: return (size_t)p.N * (p.fmt ? 4 : 8);
+    default: return (size_t)((p.N + 31) / 32) * 4;
+  }
+}
+
+int64_t round16(int64_t b) { return (b + 15) & ~int64_t(15); }
+
+bool grow(Server* s, Slab& sl, int need_rows) {
+  if (sl.cap >= need_rows) return true;
+  int ncap = std::max(need_rows, std::max(64, sl.cap * 2));
+  size_t add = (size_t)(ncap - sl.cap) * sl.row_bytes;
+  if (s->used + add > s->budget) {
+    // a tight budget: grow only to what is needed now, else recycle rows
+    ncap = need_rows;
+    add = (size_t)(ncap - sl.cap) * sl.row_bytes;
+    if (s->used + add > s->budget) return false;
+  }
+  void* nb = nullptr;
+  if (cudaMalloc(&nb, (size_t)ncap * sl.row_bytes) != cudaSuccess) return false;
+  if (sl.base) {
+    cudaMemcpyAsync(nb, sl.base, (size_t)sl.cap * sl.row_bytes, cudaMemcpyDeviceToDevice, s->st);
+    cudaStreamSynchronize(s->st);
+    cudaFree(sl.base);
+  }
+  sl.base = nb;
+  sl.key_of.resize(ncap, -1);
+  sl.pin.resize(ncap, 0);
+  sl.pos.resize(ncap);
+  for (int r = sl.cap; r < ncap; r++) {
+    sl.lru.push_back(r);
+    sl.pos[r] = std::prev(sl.lru.end());
+  }
+  sl.cap = ncap;
+  s->used += add;
+  return true;
+}
+
+Slab& slab_of(Server* s, const Product& p) {
+  Slab& sl = s->slabs[p];
+  if (!sl.row_bytes) sl.row_bytes = round16((int64_t)product_row_bytes(p));
+  return sl;
+}
+
+void touch(Slab& sl, int r) {
+  sl.lru.erase(sl.pos[r]);
+  sl.lru.push_front(r);
+  sl.pos[r] = sl.lru.begin();
+}
+
+// Row holding `key`, or -1.
+int find_row(Slab& sl, int64_t key) {
+  auto it = sl.row_of.find(key);
+  if (it == sl.row_of.end()) return -1;
+  touch(sl, it->second);
+  return it->second;
+}
+
+// A free or least-recently-used unpinned row for `key` (grows the slab first).
+int claim_row(Server* s, Slab& sl, int64_t key, int rows_needed_now) {
+  if ((int)sl.row_of.size() + rows_needed_now > sl.cap) grow(s, sl, std::max(sl.cap * 2, (int)sl.row_of.size() + rows_needed_now));
+  for (auto it = sl.lru.rbegin(); it != sl.lru.rend(); ++it) {
+    const int r = *it;
+    if (sl.pin[r]) continue;
+    if (sl.key_of[r] >= 0) sl.row_of.erase(sl.key_of[r]);
+    sl.key_of[r] = key;
+    sl.row_of[key] = r;
+    touch(sl, r);
+    return r;
+  }
+  return -1;
+}
+
+void* dbuf(void** p, size_t* n, size_t need) {
+  if (*n < need) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *n = 0;
+    if (cudaMalloc(p, need) != cudaSuccess) return nullptr;
+    *n = need;
+  }
+  return *p;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- batch execution
+namespace {
+
+struct GroupKey {
+  int method, N, Nz, lag0, L, fmt;
+  float v;
+  bool operator<(const GroupKey& o) const {
+    return std::tie(method, N, Nz, lag0, L, fmt, v) < std::tie(o.method, o.N, o.Nz, o.lag0, o.L, o.fmt, o.v);
+  }
+};
+
+// Ensure raw windows of the listed (sta, win) are on the device; returns rows.
+int ensure_raw(Server* s, int N, const std::vector<int64_t>& keys, std::vector<int>& rows, InFlight& fl) {
+  Slab& sl = slab_of(s, Product{0, N, 0, 0});
+  rows.resize(keys.size());
+  std::vector<int> miss;
+  for (size_t i = 0; i < keys.size(); i++) {
+    int r = find_row(sl, keys[i]);
+    if (r < 0) {
+      r = claim_row(s, sl, keys[i], 1);
+      if (r < 0) return FPCC_ENOMEM;
+      miss.push_back((int)i);
+    }
+    rows[i] = r;
+    sl.pin[r]++;
+    fl.pinned_rows.push_back({&sl, r});
+  }
+  for (int i : miss) {
+    std::vector<float>* w;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      auto it = s->windows.find({(int)(keys[i] >> 32), (int)(uint32_t)keys[i]});
+      if (it == s->windows.end()) return FPCC_EARG;
+      w = &it->second;
+    }
+    cudaMemcpyAsync((char*)sl.base + (int64_t)rows[i] * sl.row_bytes, w->data(), (size_t)N * 4,
+                    cudaMemcpyHostToDevice, s->st);
+  }
+  return 0;
+}
+
+// Ensure products of `kind` for the keys; computes the missing ones from raw rows.
+int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& keys, std::vector<int>& rows,
+                    InFlight& fl) {
+  Slab& sl = slab_of(s, pk);
+  rows.resize(keys.size());
+  std::vector<int64_t> miss_keys;
+  std::vector<int> miss_rows;
+  for (size_t i = 0; i < keys.size(); i++) {
+    int r = find_row(sl, keys[i]);
+    if (r < 0) {
+      r = claim_row(s, sl, keys[i], (int)(keys.size() - i));
+      if (r < 0) return FPCC_ENOMEM;
+      miss_keys.push_back(keys[i]);
+      miss_rows.push_back(r);
+    }
+    rows[i] = r;
+    sl.pin[r]++;
+    fl.pinned_rows.push_back({&sl, r});
+  }
+  if (miss_keys.empty()) return 0;
+  const int n = (int)miss_keys.size();
+  std::vector<int> raw_rows;
+  int rc = ensure_raw(s, pk.N, miss_keys, raw_rows, fl);
+  if (rc) return rc;
+  Slab& raw = slab_of(s, Product{0, pk.N, 0, 0});
+  // gather raw rows contiguously, compute, scatter into the slab
+  const int64_t N = pk.N;
+  void* dx = dbuf(&s->d_tmp_x, &s->n_tmp_x, (size_t)n * round16(N * 4));
+  void* dp = dbuf(&s->d_tmp_p, &s->n_tmp_p, (size_t)n * sl.row_bytes);
+  void* di = dbuf(&s->d_idx, &s->n_idx, (size_t)2 * n * sizeof(int) + 64);
+  if (!dx || !dp || !di) return FPCC_ENOMEM;
+  std::vector<int> idx(2 * n);
+  for (int i = 0; i < n; i++) { idx[i] = raw_rows[i]; idx[n + i] = miss_rows[i]; }
+  cudaMemcpyAsync(di, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, s->st);
+  const int64_t ldx = round16(N * 4) / 4;
+  if (copy_rows(raw.base, raw.row_bytes, (const int*)di, dx, ldx * 4, nullptr, n, N * 4, s->st) != cudaSuccess)
+    return FPCC_ECUDA;
+  int method = FPCC_PCC2, rule = FPCC_AMP_F_REG;
+  int64_t ldo = sl.row_bytes / (pk.fmt ? 4 : 8);
+  switch (pk.kind) {
+    case 1: method = FPCC_PCC2; break;
+    case 2: method = FPCC_GNCC; break;
+    case 3: method = FPCC_CC1B; rule = FPCC_SIGN_GE; break;
+    case 4: method = FPCC_CC1B; rule = FPCC_SIGN_GT; break;
+    case 6: method = FPCC_PCC1; break;
+    case 7: method = FPCC_CC1B_POPCOUNT; rule = FPCC_SIGN_GE; ldo = sl.row_bytes / 4; break;
+    case 8: method = FPCC_CC1B_POPCOUNT; rule = FPCC_SIGN_GT; ldo = sl.row_bytes / 4; break;
+    default: break;
+  }
+  if (pk.kind == 5) {
+    rc = fpcc_energy_stage(s->ctx, (const float*)dx, ldx, n, pk.N, (double*)dp, sl.row_bytes / 8);
+  } else {
+    rc = fpcc_station_stage(s->ctx, method, (const float*)dx, ldx, n, pk.N, pk.Nz, pk.fmt, rule, dp, ldo);
+  }
+  if (rc) return rc;
+  if (copy_rows(dp, sl.row_bytes, nullptr, sl.base, sl.row_bytes, (const int*)di + n, n, sl.row_bytes, s->st) !=
+      cudaSuccess)
+    return FPCC_ECUDA;
+  s->station_rows += n;
+  return 0;
+}
+
+int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base) {
+  const int n = (int)reqs.size();
+  const int m = g.method;
+  std::vector<int64_t> k1(n), k2(n);
+  for (int i = 0; i < n; i++) {
+    k1[i] = wkey(reqs[i]->r.sta1, reqs[i]->r.window);
+    k2[i] = wkey(reqs[i]->r.sta2, reqs[i]->r.window);
+  }
+  int kind1, kind2;
+  switch (m) {
+    case FPCC_PCC2: kind1 = kind2 = 1; break;
+    case FPCC_GNCC: kind1 = kind2 = 2; break;
+    case FPCC_CC1B: kind1 = 3; kind2 = 4; break;
+    case FPCC_CC1B_POPCOUNT: kind1 = 7; kind2 = 8; break;
+    default: kind1 = kind2 = 6; break;
+  }
+  const int Nz = (m == FPCC_PCC1 || m == FPCC_PCCV || m == FPCC_CC1B_POPCOUNT) ? 0 : g.Nz;
+  Product p1{kind1, g.N, Nz, g.fmt}, p2{kind2, g.N, Nz, g.fmt};
+  std::vector<int> r1, r2;
+  int rc;
+  if (kind1 == kind2) {
+    std::vector<int64_t> all(k1);
+    all.insert(all.end(), k2.begin(), k2.end());
+    std::vector<int> rr;
+    if ((rc = ensure_products(s, p1, all, rr, fl))) return rc;
+    r1.assign(rr.begin(), rr.begin() + n);
+    r2.assign(rr.begin() + n, rr.end());
+  } else {
+    if ((rc = ensure_products(s, p1, k1, r1, fl)) || (rc = ensure_products(s, p2, k2, r2, fl))) return rc;
+  }
+  std::vector<int> e1, e2;
+  if (m == FPCC_GNCC) {
+    std::vector<int64_t> all(k1);
+    all.insert(all.end(), k2.begin(), k2.end());
+    std::vector<int> rr;
+    if ((rc = ensure_products(s, Product{5, g.N, 0, 0}, all, rr, fl))) return rc;
+    e1.assign(rr.begin(), rr.begin() + n);
+    e2.assign(rr.begin() + n, rr.end());
+  }
+  // pair list: rows in one slab (both roles share a slab except the 1-bit methods,
+  // whose station-2 rows are offset by the station-1 slab capacity after a merge)
+  Slab& s1 = slab_of(s, p1);
+  Slab& s2 = slab_of(s, p2);
+  const void* base = s1.base;
+  std::vector<int32_t> pairs(2 * n);
+  if (&s1 != &s2) {
+    // stage the station-2 rows behind the station-1 rows in the temporary buffer
+    const int64_t rb = s1.row_bytes;
+    void* merged = dbuf(&s->d_tmp_p, &s->n_tmp_p, (size_t)2 * n * rb);
+    void* di = dbuf(&s->d_idx, &s->n_idx, (size_t)2 * n * sizeof(int) + 64);
+    if (!merged || !di) return FPCC_ENOMEM;
+    std::vector<int> idx(2 * n);
+    for (int i = 0; i < n; i++) { idx[i] = r1[i]; idx[n + i] = r2[i]; }
+    cudaMemcpyAsync(di, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, s->st);
+    if (copy_rows(s1.base, rb, (const int*)di, merged, rb, nullptr, n, rb, s->st) != cudaSuccess ||
+        copy_rows(s2.base, rb, (const int*)di + n, (char*)merged + (size_t)n * rb, rb, nullptr, n, rb, s->st) !=
+            cudaSuccess)
+      return FPCC_ECUDA;
+    base = merged;
+    for (int i = 0; i < n; i++) { pairs[2 * i] = i; pairs[2 * i + 1] = n + i; }
+  } else {
+    for (int i = 0; i < n; i++) { pairs[2 * i] = r1[i]; pairs[2 * i + 1] = r2[i]; }
+  }
+  const double* E = nullptr;
+  int64_t ldE = 0;
+  std::vector<int32_t> epairs;
+  if (m == FPCC_GNCC) {
+    // energies are indexed by the same pair entries: rewrite both lists onto one index space
+    Slab& se = slab_of(s, Product{5, g.N, 0, 0});
+    // the pair kernel reads energy rows by the pair's station rows, so stage both
+    // spectra and energies in pair order
+    const int64_t rb = s1.row_bytes, eb = se.row_bytes;
+    void* tmp = dbuf(&s->d_tmp_p, &s->n_tmp_p, (size_t)2 * n * (rb + eb));
+    void* di = dbuf(&s->d_idx, &s->n_idx, (size_t)4 * n * sizeof(int) + 64);
+    if (!tmp || !di) return FPCC_ENOMEM;
+    std::vector<int> idx(4 * n);
+    for (int i = 0; i < n; i++) { idx[i] = r1[i]; idx[n + i] = r2[i]; idx[2 * n + i] = e1[i]; idx[3 * n + i] = e2[i]; }
+    cudaMemcpyAsync(di, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, s->st);
+    char* spec = (char*)tmp;
+    char* en = spec + (size_t)2 * n * rb;
+    if (copy_rows(s1.base, rb, (const int*)di, spec, rb, nullptr, 2 * n, rb, s->st) != cudaSuccess ||
+        copy_rows(se.base, eb, (const int*)di + 2 * n, en, eb, nullptr, 2 * n, eb, s->st) != cudaSuccess)
+      return FPCC_ECUDA;
+    base = spec;
+    E = (const double*)en;
+    ldE = eb / 8;
+    for (int i = 0; i < n; i++) { pairs[2 * i] = i; pairs[2 * i + 1] = n + i; }
+  }
+  // device pair list (its own buffer: the index buffer may still feed queued copies) and output
+  const size_t ybytes = (size_t)n * g.L * (m == FPCC_CC1B_POPCOUNT ? 8 : 4);
+  void* dpl = dbuf(&s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
+  void* dy = dbuf(&s->d_y, &s->n_y, ybytes);
+  if (!dpl || !dy) return FPCC_ENOMEM;
+  cudaMemcpyAsync(dpl, pairs.data(), pairs.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s->st);
+  const int64_t lds = slab_of(s, p1).row_bytes / ((m == FPCC_CC1B_POPCOUNT) ? 4 : (g.fmt ? 4 : 8));
+  if (m == FPCC_CC1B_POPCOUNT) {
+    rc = fpcc_pair_stage(s->ctx, m, base, lds, 0, (const int32_t*)dpl, n, g.N, 0, g.lag0, g.lag0 + g.L - 1, 0.f,
+                         nullptr, 0, nullptr, g.L, (int64_t*)dy);
+  } else {
+    rc = fpcc_pair_stage(s->ctx, m, base, lds, g.fmt, (const int32_t*)dpl, n, g.N, Nz ? Nz : g.N, g.lag0,
+                         g.lag0 + g.L - 1, g.v, E, ldE, (float*)dy, g.L, nullptr);
+  }
+  if (rc) return rc;
+  cudaMemcpyAsync((char*)fl.h_out + out_base, dy, ybytes, cudaMemcpyDeviceToHost, s->st);
+  return 0;
+}
+
+void* pinned_get(Server* s, size_t bytes, size_t* got) {
+  for (size_t i = 0; i < s->pinned_pool.size(); i += 2) {
+    if ((size_t)s->pinned_pool[i + 1] >= bytes) {
+      void* p = s->pinned_pool[i];
+      *got = (size_t)s->pinned_pool[i + 1];
+      s->pinned_pool.erase(s->pinned_pool.begin() + i, s->pinned_pool.begin() + i + 2);
+      return p;
+    }
+  }
+  void* p = nullptr;
+  const size_t b = std::max(bytes, (size_t)1 << 20);
+  if (cudaMallocHost(&p, b) != cudaSuccess) return nullptr;
+  *got = b;
+  return p;
+}
+
+void pinned_put(Server* s, void* p, size_t bytes) {
+  s->pinned_pool.push_back(p);
+  s->pinned_pool.push_back((void*)bytes);
+}
+
+void finish(Server* s, InFlight& fl, int err) {
+  const auto now = Clock::now();
+  for (size_t i = 0; i < fl.reqs.size(); i++) {
+    Req& q = fl.reqs[i];
+    if (!err) {
+      if (q.r.method == FPCC_CC1B_POPCOUNT) {
+        if (q.r.num) memcpy(q.r.num, (char*)fl.h_out + fl.out_off[i], (size_t)q.L * 8);
+      } else if (q.r.y) {
+        memcpy(q.r.y, (char*)fl.h_out + fl.out_off[i], (size_t)q.L * 4);
+      }
+    }
+  }
+  for (auto& pr : fl.pinned_rows) pr.first->pin[pr.second]--;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (auto& q : fl.reqs) {
+      s->status[q.id] = err ? err : 1;
+      s->lat_ms.push_back(std::chrono::duration<double, std::milli>(now - q.t_submit).count());
+    }
+    s->completed += (int64_t)fl.reqs.size();
+  }
+  s->cv_done.notify_all();
+  pinned_put(s, fl.h_out, fl.h_bytes);
+  if (fl.done) cudaEventDestroy(fl.done);
+}
+
+void worker_main(Server* s) {
+  cudaSetDevice(s->device);
+  for (;;) {
+    std::vector<Req> batch;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      if (s->pending.empty() && s->inflight.empty()) {
+        s->cv.wait(lk, [&] { return s->stop || !s->pending.empty(); });
+      }
+      if (s->stop && s->pending.empty() && s->inflight.empty()) return;
+      while (!s->pending.empty() && (int)batch.size() < s->max_batch) {
+        batch.push_back(std::move(s->pending.front()));
+        s->pending.pop_front();
+      }
+    }
+    // retire finished batches (all but the newest are waited for, keeping two in flight)
+    while (!s->inflight.empty()) {
+      InFlight& fl = s->inflight.front();
+      const bool must_wait = s->inflight.size() > 1 || batch.empty();
+      cudaError_t q = must_wait ? cudaEventSynchronize(fl.done) : cudaEventQuery(fl.done);
+      if (q == cudaErrorNotReady) break;
+      finish(s, fl, q == cudaSuccess ? 0 : FPCC_ECUDA);
+      s->inflight.pop_front();
+    }
+    if (batch.empty()) continue;
+    // group and launch
+    InFlight fl;
+    std::map<GroupKey, std::vector<Req*>> groups;
+    for (auto& q : batch) {
+      GroupKey g{q.r.method, q.N, q.Nz, q.lag0, q.L, 0, q.r.method == FPCC_PCCV ? q.r.v : 0.f};
+      groups[g].push_back(&q);
+    }
+    size_t total = 0;
+    for (auto& q : batch) total += (size_t)q.L * (q.r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
+    fl.h_out = pinned_get(s, total, &fl.h_bytes);
+    int err = fl.h_out ? 0 : FPCC_ENOMEM;
+    fl.reqs.reserve(batch.size());
+    size_t off = 0;
+    for (auto& kv : groups) {
+      if (err) break;
+      const size_t base = off;
+      for (Req* q : kv.second) {
+        fl.reqs.push_back(*q);
+        fl.out_off.push_back(off);
+        off += (size_t)q->L * (q->r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
+      }
+      err = run_group(s, kv.first, kv.second, fl, base);
+    }
+    if (!err) {
+      cudaEventCreateWithFlags(&fl.done, cudaEventDisableTiming);
+      cudaEventRecord(fl.done, s->st);
+      s->batches++;
+      s->inflight.push_back(std::move(fl));
+    } else {
+      cudaStreamSynchronize(s->st);
+      s->last_error = err;
+      if (fl.reqs.empty())
+        for (auto& q : batch) fl.reqs.push_back(q);
+      finish(s, fl, err);
+    }
+  }
+}
+
+}  // namespace
+}  // namespace fpcc
+
+using namespace fpcc;
+
+extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budget_bytes, int max_batch) {
+  if (!out) return FPCC_EARG;
+  Server* s = new Server();
+  s->device = device;
+  s->budget = hbm_budget_bytes ? hbm_budget_bytes : (size_t)150 << 30;
+  s->max_batch = max_batch > 0 ? max_batch : 4096;
+  if (fpcc_create(&s->ctx, device)) {
+    delete s;
+    return FPCC_ECUDA;
+  }
+  s->st = (cudaStream_t)fpcc_get_stream(s->ctx);
+  s->worker = std::thread(worker_main, s);
+  *out = reinterpret_cast<fpcc_server*>(s);
+  return 0;
+}
+
+extern "C" int fpcc_server_destroy(fpcc_server* h) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s) return 0;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_all();
+  s->worker.join();
+  cudaSetDevice(s->device);
+  cudaStreamSynchronize(s->st);
+  for (auto& kv : s->slabs) if (kv.second.base) cudaFree(kv.second.base);
+  for (void** p : {&s->d_tmp_x, &s->d_tmp_p, &s->d_idx, &s->d_y, &s->d_pl}) if (*p) cudaFree(*p);
+  for (size_t i = 0; i < s->pinned_pool.size(); i += 2) cudaFreeHost(s->pinned_pool[i]);
+  fpcc_destroy(s->ctx);
+  delete s;
+  return 0;
+}
+
+extern "C" int fpcc_put_station_window(fpcc_server* h, int32_t sta, int32_t window, const float* x, int N) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s || !x || N <= 0) return FPCC_EARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto& w = s->windows[{sta, window}];
+  w.assign(x, x + N);
+  return 0;
+}
+
+extern "C" int64_t fpcc_submit(fpcc_server* h, const fpcc_request* req) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s || !req) return FPCC_EARG;
+  Req q;
+  q.r = *req;
+  q.t_submit = Clock::now();
+  int N = 0;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto a = s->windows.find({req->sta1, req->window});
+    auto b = s->windows.find({req->sta2, req->window});
+    if (a == s->windows.end() || b == s->windows.end()) return FPCC_EARG;
+    N = (int)a->second.size();
+    if ((int)b->second.size() != N) return FPCC_EARG;
+  }
+  const int M = std::max(std::abs(req->Lag1), std::abs(req->Lag2));
+  if (M >= N) return FPCC_EARG;
+  q.N = N;
+  q.lag0 = std::min(req->Lag1, req->Lag2);
+  q.L = std::abs(req->Lag2 - req->Lag1) + 1;
+  const int m = req->method;
+  if (m == FPCC_PCC2 || m == FPCC_GNCC || m == FPCC_CC1B) {
+    q.Nz = choose_nz(N, M, FPCC_NZ_FAST);
+    if (q.Nz <= 0) return FPCC_EUNSUP;
+  } else if (m == FPCC_PCC1 || m == FPCC_PCCV || m == FPCC_CC1B_POPCOUNT) {
+    q.Nz = 0;
+    if ((m == FPCC_PCC1 || m == FPCC_PCCV) && req->Lag1 > req->Lag2) return FPCC_EARG;
+  } else {
+    return FPCC_EUNSUP;
+  }
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    q.id = s->next_id++;
+    s->status[q.id] = 0;
+    s->pending.push_back(q);
+  }
+  s->cv.notify_one();
+  return q.id;
+}
+
+extern "C" int fpcc_poll(fpcc_server* h, int64_t id) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s) return FPCC_EARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->status.find(id);
+  if (it == s->status.end()) return FPCC_EARG;
+  return it->second;
+}
+
+extern "C" int fpcc_wait(fpcc_server* h, int64_t id, double timeout_s) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s) return FPCC_EARG;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto pred = [&] {
+    auto it = s->status.find(id);
+    return it == s->status.end() || it->second != 0;
+  };
+  if (timeout_s > 0) {
+    if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) return 0;
+  } else {
+    s->cv_done.wait(lk, pred);
+  }
+  auto it = s->status.find(id);
+  return it == s->status.end() ? FPCC_EARG : it->second;
+}
+
+extern "C" int fpcc_server_drain(fpcc_server* h) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s) return FPCC_EARG;
+  std::unique_lock<std::mutex> lk(s->mu);
+  s->cv_done.wait(lk, [&] { return s->pending.empty() && s->completed >= s->next_id; });
+  return s->last_error;
+}
+
+extern "C" int fpcc_server_get_stats(fpcc_server* h, fpcc_server_stats* o) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s || !o) return FPCC_EARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  std::vector<double> v = s->lat_ms;
+  std::sort(v.begin(), v.end());
+  auto pct = [&](double p) { return v.empty() ? 0.0 : v[std::min(v.size() - 1, (size_t)(p * (v.size() - 1) + 0.5))]; };
+  o->completed = s->completed;
+  o->batches = s->batches;
+  o->station_rows = s->station_rows;
+  o->hbm_used = (int64_t)s->used;
+  o->p50_ms = pct(0.50);
+  o->p99_ms = pct(0.99);
+  o->max_ms = v.empty() ? 0.0 : v.back();
+  return 0;
+}
+
+extern "C" int fpcc_server_reset_stats(fpcc_server* h) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s) return FPCC_EARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->lat_ms.clear();
+  s->batches = 0;
+  s->station_rows = 0;
+  return 0;
+}
+
+extern "C" int fpcc_submit_many(fpcc_server* h, const fpcc_request* reqs, int n, int64_t* ids) {
+  if (!h || !reqs || n < 0) return FPCC_EARG;
+  for (int i = 0; i < n; i++) {
+    const int64_t id = fpcc_submit(h, reqs + i);
+    if (ids) ids[i] = id;
+    if (id < 0) return (int)id;
+  }
+  return 0;
+}
+
+// Offer the requests at Poisson arrival times of the given rate (requests/s)
+// from the calling thread; returns when the last one has been submitted.
+extern "C" int fpcc_server_offer_poisson(fpcc_server* h, const fpcc_request* reqs, int n, double rate,
+                                         uint64_t seed, int64_t* ids) {
+  if (!h || !reqs || n < 0 || !(rate > 0)) return FPCC_EARG;
+  uint64_t x = seed ? seed : 0x9E3779B97F4A7C15ull;
+  auto next = [&]() {   // xorshift64* uniform in (0,1)
+    x ^= x >> 12; x ^= x << 25; x ^= x >> 27;
+    return ((x * 2685821657736338717ull) >> 11) * (1.0 / 9007199254740992.0) + 1e-18;
+  };
+  const auto t0 = Clock::now();
+  double t = 0;
+  for (int i = 0; i < n; i++) {
+    t += -std::log(next()) / rate;
+    const auto due = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(t));
+    while (Clock::now() < due) {
+      const auto left = due - Clock::now();
+      if (left > std::chrono::microseconds(200)) std::this_thread::sleep_for(left - std::chrono::microseconds(100));
+    }
+    const int64_t id = fpcc_submit(h, reqs + i);
+    if (ids) ids[i] = id;
+    if (id < 0) return (int)id;
+  }
+  return 0;
+}

@@ -54,11 +54,6 @@ __global__ void __launch_bounds__(256) k_wpcc_accum(const void* __restrict__ P, 
   }
 }
 
-int wpcc_fail(char* buf, size_t n, int code, const char* msg) {
-  snprintf(buf, n, "%s", msg);
-  return code;
-}
-
 }  // namespace
 
 // A usable WPCC length: both Nz and Nz/2 run as four-step transforms.

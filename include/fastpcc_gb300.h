@@ -154,6 +154,48 @@ int fpcc_wpcc_pair_stage(fpcc_ctx *ctx, const fpcc_wpcc_plan *p, const void *d_P
 int fpcc_wpcc_host(float **y, float **x1, float **x2, unsigned N, unsigned Tr, int Lag1, int Lag2, double pmin,
                    double pmax, unsigned V, int type, double op1, int rule, int nz_mode);
 
+/* ---- serving loop -----------------------------------------------------------
+ * A server keeps station products (phase spectra, real/sign spectra, energies,
+ * phase signals, sign bits) resident in HBM under a byte budget and runs a
+ * worker thread that batches requests continuously: everything pending when the
+ * worker is free forms the next batch, grouped by method and lengths; requests
+ * that arrive while a batch is on the GPU join the following one.  Each result
+ * depends only on its request, so it is the same alone and in any mix.
+ * Station windows are registered once (host samples, copied); products are
+ * computed on first use and recycled least-recently-used. */
+typedef struct fpcc_server fpcc_server;
+typedef struct {
+  int method;            /* FPCC_PCC2, GNCC, CC1B, CC1B_POPCOUNT, PCC1, PCCV          */
+  int32_t sta1, sta2;    /* station ids (station 1 = virtual source)                  */
+  int32_t window;        /* window id, registered for both stations                   */
+  int Lag1, Lag2;
+  float v;               /* power for FPCC_PCCV                                       */
+  float *y;              /* host output, L floats (written before completion)         */
+  int64_t *num;          /* host output for FPCC_CC1B_POPCOUNT, L int64               */
+} fpcc_request;
+typedef struct {
+  int64_t completed, batches, station_rows, hbm_used;
+  double p50_ms, p99_ms, max_ms;   /* submit -> result latency of completed requests */
+} fpcc_server_stats;
+int fpcc_server_create(fpcc_server **out, int device, size_t hbm_budget_bytes, int max_batch);
+int fpcc_server_destroy(fpcc_server *s);
+int fpcc_put_station_window(fpcc_server *s, int32_t sta, int32_t window, const float *x, int N);
+/* Returns a request id (>= 0) or a negative FPCC_E* code. */
+int64_t fpcc_submit(fpcc_server *s, const fpcc_request *req);
+/* n requests at once; ids[i] receives each id (or a negative code, which stops the call). */
+int fpcc_submit_many(fpcc_server *s, const fpcc_request *reqs, int n, int64_t *ids);
+/* Submits the requests at Poisson arrival times of `rate` per second (load generator). */
+int fpcc_server_offer_poisson(fpcc_server *s, const fpcc_request *reqs, int n, double rate, uint64_t seed,
+                              int64_t *ids);
+/* 1 done, 0 pending, < 0 failed. */
+int fpcc_poll(fpcc_server *s, int64_t id);
+/* Blocks until done (timeout_s <= 0: no limit); returns as fpcc_poll. */
+int fpcc_wait(fpcc_server *s, int64_t id, double timeout_s);
+/* Blocks until every submitted request has completed. */
+int fpcc_server_drain(fpcc_server *s);
+int fpcc_server_get_stats(fpcc_server *s, fpcc_server_stats *out);
+int fpcc_server_reset_stats(fpcc_server *s);
+
 /* ---- allocation-free PCC2 ------------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a host whose pool allocator owns all device memory, plugin frameworks that
