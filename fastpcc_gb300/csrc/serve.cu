@@ -94,10 +94,22 @@ struct InFlight {
   cudaEvent_t done = nullptr;
   std::vector<Req> reqs;
   std::vector<int64_t> out_off;    // offset of each request's output in the pinned buffer (floats or int64)
-  void* h_out = nullptr;           // pinned
+  void* h_out = nullptr;           // pinned result buffer
   size_t h_bytes = 0;
+  char* h_up = nullptr;            // pinned upload staging (index arrays), bump-allocated
+  size_t up_bytes = 0, up_used = 0;
   std::vector<std::pair<Slab*, int>> pinned_rows;
+  int err = 0;
 };
+
+// Copy a small host array into the batch's pinned staging and queue its upload.
+cudaError_t upload(InFlight& fl, void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  const size_t off = (fl.up_used + 255) & ~size_t(255);
+  if (off + bytes > fl.up_bytes) return cudaErrorMemoryAllocation;
+  memcpy(fl.h_up + off, src, bytes);
+  fl.up_used = off + bytes;
+  return cudaMemcpyAsync(dst, fl.h_up + off, bytes, cudaMemcpyHostToDevice, st);
+}
 
 }  // namespace
 
@@ -110,12 +122,21 @@ struct Server {
   // host copies of registered windows
   std::mutex mu;
   std::condition_variable cv, cv_done;
-  std::map<std::pair<int, int>, std::vector<float>> windows;   // (sta, win) -> samples
+  std::map<std::pair<int, int>, std::pair<float*, int>> windows;   // (sta, win) -> pinned samples, N
+  std::vector<char*> arena;                                       // pinned chunks holding the windows
+  size_t arena_left = 0;
+  char* arena_ptr = nullptr;
   std::deque<Req> pending;
   std::unordered_map<int64_t, int> status;                     // id -> 0 pending, 1 done, <0 error
   int64_t next_id = 0;
   bool stop = false;
   std::thread worker;
+  std::vector<std::thread> completers;
+  std::mutex mu_c;
+  std::condition_variable cv_c;
+  std::deque<InFlight*> launched;     // worker -> completers
+  std::deque<InFlight*> retired;      // completers -> worker
+  int in_flight = 0;                  // launched, not yet retired by the worker
   // device state (worker thread only)
   std::map<Product, Slab> slabs;
   std::deque<InFlight> inflight;
@@ -256,15 +277,16 @@ int ensure_raw(Server* s, int N, const std::vector<int64_t>& keys, std::vector<i
     fl.pinned_rows.push_back({&sl, r});
   }
   for (int i : miss) {
-    std::vector<float>* w;
+    const float* w;
     {
       std::lock_guard<std::mutex> lk(s->mu);
       auto it = s->windows.find({(int)(keys[i] >> 32), (int)(uint32_t)keys[i]});
       if (it == s->windows.end()) return FPCC_EARG;
-      w = &it->second;
+      w = it->second.first;
     }
-    cudaMemcpyAsync((char*)sl.base + (int64_t)rows[i] * sl.row_bytes, w->data(), (size_t)N * 4,
-                    cudaMemcpyHostToDevice, s->st);
+    if (cudaMemcpyAsync((char*)sl.base + (int64_t)rows[i] * sl.row_bytes, w, (size_t)N * 4, cudaMemcpyHostToDevice,
+                        s->st) != cudaSuccess)
+      return FPCC_ECUDA;
   }
   return 0;
 }
@@ -302,7 +324,7 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   if (!dx || !dp || !di) return FPCC_ENOMEM;
   std::vector<int> idx(2 * n);
   for (int i = 0; i < n; i++) { idx[i] = raw_rows[i]; idx[n + i] = miss_rows[i]; }
-  cudaMemcpyAsync(di, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, s->st);
+  if (upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st) != cudaSuccess) return FPCC_ECUDA;
   const int64_t ldx = round16(N * 4) / 4;
   if (copy_rows(raw.base, raw.row_bytes, (const int*)di, dx, ldx * 4, nullptr, n, N * 4, s->st) != cudaSuccess)
     return FPCC_ECUDA;
@@ -384,7 +406,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
     if (!merged || !di) return FPCC_ENOMEM;
     std::vector<int> idx(2 * n);
     for (int i = 0; i < n; i++) { idx[i] = r1[i]; idx[n + i] = r2[i]; }
-    cudaMemcpyAsync(di, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, s->st);
+    if (upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st) != cudaSuccess) return FPCC_ECUDA;
     if (copy_rows(s1.base, rb, (const int*)di, merged, rb, nullptr, n, rb, s->st) != cudaSuccess ||
         copy_rows(s2.base, rb, (const int*)di + n, (char*)merged + (size_t)n * rb, rb, nullptr, n, rb, s->st) !=
             cudaSuccess)
@@ -408,7 +430,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
     if (!tmp || !di) return FPCC_ENOMEM;
     std::vector<int> idx(4 * n);
     for (int i = 0; i < n; i++) { idx[i] = r1[i]; idx[n + i] = r2[i]; idx[2 * n + i] = e1[i]; idx[3 * n + i] = e2[i]; }
-    cudaMemcpyAsync(di, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, s->st);
+    if (upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st) != cudaSuccess) return FPCC_ECUDA;
     char* spec = (char*)tmp;
     char* en = spec + (size_t)2 * n * rb;
     if (copy_rows(s1.base, rb, (const int*)di, spec, rb, nullptr, 2 * n, rb, s->st) != cudaSuccess ||
@@ -424,7 +446,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
   void* dpl = dbuf(&s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
   void* dy = dbuf(&s->d_y, &s->n_y, ybytes);
   if (!dpl || !dy) return FPCC_ENOMEM;
-  cudaMemcpyAsync(dpl, pairs.data(), pairs.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s->st);
+  if (upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st) != cudaSuccess) return FPCC_ECUDA;
   const int64_t lds = slab_of(s, p1).row_bytes / ((m == FPCC_CC1B_POPCOUNT) ? 4 : (g.fmt ? 4 : 8));
   if (m == FPCC_CC1B_POPCOUNT) {
     rc = fpcc_pair_stage(s->ctx, m, base, lds, 0, (const int32_t*)dpl, n, g.N, 0, g.lag0, g.lag0 + g.L - 1, 0.f,
@@ -459,19 +481,18 @@ void pinned_put(Server* s, void* p, size_t bytes) {
   s->pinned_pool.push_back((void*)bytes);
 }
 
-void finish(Server* s, InFlight& fl, int err) {
+// Deliver a batch's results and record its latencies (completer threads).
+void deliver(Server* s, InFlight& fl) {
+  const int err = fl.err;
   const auto now = Clock::now();
-  for (size_t i = 0; i < fl.reqs.size(); i++) {
+  for (size_t i = 0; i < fl.reqs.size() && !err; i++) {
     Req& q = fl.reqs[i];
-    if (!err) {
-      if (q.r.method == FPCC_CC1B_POPCOUNT) {
-        if (q.r.num) memcpy(q.r.num, (char*)fl.h_out + fl.out_off[i], (size_t)q.L * 8);
-      } else if (q.r.y) {
-        memcpy(q.r.y, (char*)fl.h_out + fl.out_off[i], (size_t)q.L * 4);
-      }
+    if (q.r.method == FPCC_CC1B_POPCOUNT) {
+      if (q.r.num) memcpy(q.r.num, (char*)fl.h_out + fl.out_off[i], (size_t)q.L * 8);
+    } else if (q.r.y) {
+      memcpy(q.r.y, (char*)fl.h_out + fl.out_off[i], (size_t)q.L * 4);
     }
   }
-  for (auto& pr : fl.pinned_rows) pr.first->pin[pr.second]--;
   {
     std::lock_guard<std::mutex> lk(s->mu);
     for (auto& q : fl.reqs) {
@@ -479,39 +500,97 @@ void finish(Server* s, InFlight& fl, int err) {
       s->lat_ms.push_back(std::chrono::duration<double, std::milli>(now - q.t_submit).count());
     }
     s->completed += (int64_t)fl.reqs.size();
+    if (err) s->last_error = err;
   }
   s->cv_done.notify_all();
-  pinned_put(s, fl.h_out, fl.h_bytes);
-  if (fl.done) cudaEventDestroy(fl.done);
 }
+
+void completer_main(Server* s) {
+  cudaSetDevice(s->device);
+  for (;;) {
+    InFlight* fl = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(s->mu_c);
+      s->cv_c.wait(lk, [&] { return !s->launched.empty() || s->stop; });
+      if (s->launched.empty()) return;
+      fl = s->launched.front();
+      s->launched.pop_front();
+    }
+    if (fl->done && cudaEventSynchronize(fl->done) != cudaSuccess) fl->err = FPCC_ECUDA;
+    deliver(s, *fl);
+    {
+      std::lock_guard<std::mutex> lk(s->mu_c);
+      s->retired.push_back(fl);
+    }
+    s->cv_c.notify_all();
+    s->cv.notify_all();
+  }
+}
+
+// Worker side: release pins and pinned buffers of retired batches.
+void release_retired(Server* s) {
+  std::deque<InFlight*> done;
+  {
+    std::lock_guard<std::mutex> lk(s->mu_c);
+    done.swap(s->retired);
+  }
+  for (InFlight* fl : done) {
+    for (auto& pr : fl->pinned_rows) pr.first->pin[pr.second]--;
+    if (fl->h_out) pinned_put(s, fl->h_out, fl->h_bytes);
+    if (fl->h_up) pinned_put(s, fl->h_up, fl->up_bytes);
+    if (fl->done) cudaEventDestroy(fl->done);
+    delete fl;
+    s->in_flight--;
+  }
+}
+
+constexpr int kMaxInFlight = 3;
+constexpr auto kLingerStep = std::chrono::microseconds(25);
+constexpr auto kLingerMax = std::chrono::microseconds(400);
 
 void worker_main(Server* s) {
   cudaSetDevice(s->device);
   for (;;) {
+    release_retired(s);
     std::vector<Req> batch;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      if (s->pending.empty() && s->inflight.empty()) {
-        s->cv.wait(lk, [&] { return s->stop || !s->pending.empty(); });
+      if (s->pending.empty()) {
+        s->cv.wait_for(lk, std::chrono::milliseconds(2), [&] { return s->stop || !s->pending.empty(); });
+        if (s->pending.empty()) {
+          if (s->stop) {
+            lk.unlock();
+            // wait for the completers to drain what is in flight
+            for (;;) {
+              release_retired(s);
+              if (s->in_flight == 0) return;
+              std::this_thread::sleep_for(std::chrono::microseconds(200));
+            }
+          }
+          continue;
+        }
       }
-      if (s->stop && s->pending.empty() && s->inflight.empty()) return;
+      // While earlier batches keep the GPU busy and requests keep arriving,
+      // let this batch grow (continuous batching); an idle GPU starts at once.
+      const auto t0 = Clock::now();
+      while (s->in_flight > 0 && (int)s->pending.size() < s->max_batch && Clock::now() - t0 < kLingerMax) {
+        const size_t before = s->pending.size();
+        s->cv.wait_for(lk, kLingerStep);
+        if (s->pending.size() == before) break;
+      }
       while (!s->pending.empty() && (int)batch.size() < s->max_batch) {
         batch.push_back(std::move(s->pending.front()));
         s->pending.pop_front();
       }
     }
-    // retire finished batches (all but the newest are waited for, keeping two in flight)
-    while (!s->inflight.empty()) {
-      InFlight& fl = s->inflight.front();
-      const bool must_wait = s->inflight.size() > 1 || batch.empty();
-      cudaError_t q = must_wait ? cudaEventSynchronize(fl.done) : cudaEventQuery(fl.done);
-      if (q == cudaErrorNotReady) break;
-      finish(s, fl, q == cudaSuccess ? 0 : FPCC_ECUDA);
-      s->inflight.pop_front();
+    // bound the number of batches in flight
+    while (s->in_flight >= kMaxInFlight) {
+      std::unique_lock<std::mutex> lk(s->mu_c);
+      s->cv_c.wait_for(lk, std::chrono::milliseconds(1), [&] { return !s->retired.empty(); });
+      lk.unlock();
+      release_retired(s);
     }
-    if (batch.empty()) continue;
-    // group and launch
-    InFlight fl;
+    InFlight* fl = new InFlight();
     std::map<GroupKey, std::vector<Req*>> groups;
     for (auto& q : batch) {
       GroupKey g{q.r.method, q.N, q.Nz, q.lag0, q.L, 0, q.r.method == FPCC_PCCV ? q.r.v : 0.f};
@@ -519,32 +598,37 @@ void worker_main(Server* s) {
     }
     size_t total = 0;
     for (auto& q : batch) total += (size_t)q.L * (q.r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
-    fl.h_out = pinned_get(s, total, &fl.h_bytes);
-    int err = fl.h_out ? 0 : FPCC_ENOMEM;
-    fl.reqs.reserve(batch.size());
+    fl->h_out = (char*)pinned_get(s, total, &fl->h_bytes);
+    fl->h_up = (char*)pinned_get(s, (size_t)16 * 4 * batch.size() + 1024 * (groups.size() + 4), &fl->up_bytes);
+    int err = (fl->h_out && fl->h_up) ? 0 : FPCC_ENOMEM;
+    fl->reqs.reserve(batch.size());
     size_t off = 0;
     for (auto& kv : groups) {
       if (err) break;
       const size_t base = off;
       for (Req* q : kv.second) {
-        fl.reqs.push_back(*q);
-        fl.out_off.push_back(off);
+        fl->reqs.push_back(*q);
+        fl->out_off.push_back((int64_t)off);
         off += (size_t)q->L * (q->r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
       }
-      err = run_group(s, kv.first, kv.second, fl, base);
+      err = run_group(s, kv.first, kv.second, *fl, base);
     }
-    if (!err) {
-      cudaEventCreateWithFlags(&fl.done, cudaEventDisableTiming);
-      cudaEventRecord(fl.done, s->st);
-      s->batches++;
-      s->inflight.push_back(std::move(fl));
-    } else {
+    if (err) {
       cudaStreamSynchronize(s->st);
-      s->last_error = err;
-      if (fl.reqs.empty())
-        for (auto& q : batch) fl.reqs.push_back(q);
-      finish(s, fl, err);
+      fl->reqs.clear();
+      for (auto& q : batch) fl->reqs.push_back(q);
+      fl->err = err;
+    } else {
+      cudaEventCreateWithFlags(&fl->done, cudaEventDisableTiming);
+      cudaEventRecord(fl->done, s->st);
+      s->batches++;
     }
+    s->in_flight++;
+    {
+      std::lock_guard<std::mutex> lk(s->mu_c);
+      s->launched.push_back(fl);
+    }
+    s->cv_c.notify_one();
   }
 }
 
@@ -565,6 +649,7 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
   }
   s->st = (cudaStream_t)fpcc_get_stream(s->ctx);
   s->worker = std::thread(worker_main, s);
+  for (int i = 0; i < 4; i++) s->completers.emplace_back(completer_main, s);
   *out = reinterpret_cast<fpcc_server*>(s);
   return 0;
 }
@@ -578,11 +663,17 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
   }
   s->cv.notify_all();
   s->worker.join();
+  {
+    std::lock_guard<std::mutex> lk(s->mu_c);
+  }
+  s->cv_c.notify_all();
+  for (auto& t : s->completers) t.join();
   cudaSetDevice(s->device);
   cudaStreamSynchronize(s->st);
   for (auto& kv : s->slabs) if (kv.second.base) cudaFree(kv.second.base);
   for (void** p : {&s->d_tmp_x, &s->d_tmp_p, &s->d_idx, &s->d_y, &s->d_pl}) if (*p) cudaFree(*p);
   for (size_t i = 0; i < s->pinned_pool.size(); i += 2) cudaFreeHost(s->pinned_pool[i]);
+  for (char* a : s->arena) cudaFreeHost(a);
   fpcc_destroy(s->ctx);
   delete s;
   return 0;
@@ -592,8 +683,20 @@ extern "C" int fpcc_put_station_window(fpcc_server* h, int32_t sta, int32_t wind
   Server* s = reinterpret_cast<Server*>(h);
   if (!s || !x || N <= 0) return FPCC_EARG;
   std::lock_guard<std::mutex> lk(s->mu);
-  auto& w = s->windows[{sta, window}];
-  w.assign(x, x + N);
+  const size_t bytes = ((size_t)N * 4 + 255) & ~size_t(255);
+  if (bytes > s->arena_left) {
+    const size_t chunk = std::max(bytes, (size_t)64 << 20);
+    char* p = nullptr;
+    if (cudaMallocHost(&p, chunk) != cudaSuccess) return FPCC_ENOMEM;
+    s->arena.push_back(p);
+    s->arena_ptr = p;
+    s->arena_left = chunk;
+  }
+  float* dst = (float*)s->arena_ptr;
+  s->arena_ptr += bytes;
+  s->arena_left -= bytes;
+  memcpy(dst, x, (size_t)N * 4);
+  s->windows[{sta, window}] = {dst, N};
   return 0;
 }
 
@@ -609,8 +712,8 @@ extern "C" int64_t fpcc_submit(fpcc_server* h, const fpcc_request* req) {
     auto a = s->windows.find({req->sta1, req->window});
     auto b = s->windows.find({req->sta2, req->window});
     if (a == s->windows.end() || b == s->windows.end()) return FPCC_EARG;
-    N = (int)a->second.size();
-    if ((int)b->second.size() != N) return FPCC_EARG;
+    N = a->second.second;
+    if (b->second.second != N) return FPCC_EARG;
   }
   const int M = std::max(std::abs(req->Lag1), std::abs(req->Lag2));
   if (M >= N) return FPCC_EARG;

@@ -104,7 +104,7 @@ def test_server_mixed_methods_against_oracle_and_alone(F, orc):
 
 def test_server_eviction_under_small_budget(F, orc):
     x = _stations(8, 1, 3000, "serve/evict")
-    srv = F.Server(hbm_budget=600 << 10, max_batch=4)    # a few station products at a time
+    srv = F.Server(hbm_budget=200 << 10, max_batch=1)    # room for a few station products only
     for s in range(8):
         srv.put(s, 0, x[s, 0])
     reqs = [(0, i, j, 0, -200, 200, 0.0) for i in range(8) for j in range(8) if i < j]
