@@ -221,19 +221,26 @@ int find_row(Slab& sl, int64_t key) {
   return it->second;
 }
 
+void wait_one_retired(Server* s);
+
 // A free or least-recently-used unpinned row for `key` (grows the slab first).
+// When every row is held by batches in flight, waits for them to finish
+// (admission by memory): only rows of the batch being built can then remain.
 int claim_row(Server* s, Slab& sl, int64_t key, int rows_needed_now) {
   if ((int)sl.row_of.size() + rows_needed_now > sl.cap) grow(s, sl, std::max(sl.cap * 2, (int)sl.row_of.size() + rows_needed_now));
-  for (auto it = sl.lru.rbegin(); it != sl.lru.rend(); ++it) {
-    const int r = *it;
-    if (sl.pin[r]) continue;
-    if (sl.key_of[r] >= 0) sl.row_of.erase(sl.key_of[r]);
-    sl.key_of[r] = key;
-    sl.row_of[key] = r;
-    touch(sl, r);
-    return r;
+  for (;;) {
+    for (auto it = sl.lru.rbegin(); it != sl.lru.rend(); ++it) {
+      const int r = *it;
+      if (sl.pin[r]) continue;
+      if (sl.key_of[r] >= 0) sl.row_of.erase(sl.key_of[r]);
+      sl.key_of[r] = key;
+      sl.row_of[key] = r;
+      touch(sl, r);
+      return r;
+    }
+    if (s->in_flight == 0) return -1;
+    wait_one_retired(s);
   }
-  return -1;
 }
 
 void* dbuf(void** p, size_t* n, size_t need) {
@@ -544,6 +551,14 @@ void release_retired(Server* s) {
   }
 }
 
+void wait_one_retired(Server* s) {
+  {
+    std::unique_lock<std::mutex> lk(s->mu_c);
+    s->cv_c.wait_for(lk, std::chrono::milliseconds(1), [&] { return !s->retired.empty(); });
+  }
+  release_retired(s);
+}
+
 constexpr int kMaxInFlight = 3;
 constexpr auto kLingerStep = std::chrono::microseconds(25);
 constexpr auto kLingerMax = std::chrono::microseconds(400);
@@ -584,12 +599,7 @@ void worker_main(Server* s) {
       }
     }
     // bound the number of batches in flight
-    while (s->in_flight >= kMaxInFlight) {
-      std::unique_lock<std::mutex> lk(s->mu_c);
-      s->cv_c.wait_for(lk, std::chrono::milliseconds(1), [&] { return !s->retired.empty(); });
-      lk.unlock();
-      release_retired(s);
-    }
+    while (s->in_flight >= kMaxInFlight) wait_one_retired(s);
     InFlight* fl = new InFlight();
     std::map<GroupKey, std::vector<Req*>> groups;
     for (auto& q : batch) {
