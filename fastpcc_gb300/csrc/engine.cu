@@ -1,6 +1,10 @@
 // Host-side planning: radix schedules and padded correlation lengths.
 #include <math.h>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "engine.h"
 #include "menu.cuh"
 #include "large.cuh"
@@ -81,7 +85,25 @@ static double length_cost(int n) {
 
 bool nz_usable(int nz) { return nz > 0 && (nz % 2) == 0 && usable(nz) && usable(nz / 2); }
 
+static int choose_nz_uncached(int N, int M, int mode);
+
+// Memoised: the serving loop asks once per request.
 int choose_nz(int N, int M, int mode) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int>, int> memo;
+  const auto key = std::make_tuple(N, M, mode);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+  }
+  const int nz = choose_nz_uncached(N, M, mode);
+  std::lock_guard<std::mutex> lk(mu);
+  memo[key] = nz;
+  return nz;
+}
+
+static int choose_nz_uncached(int N, int M, int mode) {
   const int need = N + M;
   if (mode >= 2) {
     // explicit padded length
