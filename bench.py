@@ -149,8 +149,9 @@ def served_leg(F, x, pairs, n_win, L, rate_frac=0.5, poisson_max=60000):
         srv.put(row // n_win, row % n_win, x[row])
     P = pairs.shape[0]
     out = np.zeros((P, L), np.float32)
-    reqs = [F.Server.request(F.PCC2, int(a // n_win), int(b // n_win), int(a % n_win), -LAG, LAG, out[i])
-            for i, (a, b) in enumerate(pairs)]
+    reqs = F.Server.request_array(
+        [F.Server.request(F.PCC2, int(a // n_win), int(b // n_win), int(a % n_win), -LAG, LAG, out[i])
+         for i, (a, b) in enumerate(pairs)])
     t0 = time.perf_counter()
     srv.submit_many(reqs)
     srv.drain()
@@ -166,7 +167,7 @@ def served_leg(F, x, pairs, n_win, L, rate_frac=0.5, poisson_max=60000):
     n_p = min(P, poisson_max, int(rate * 3.0) + 1)
     srv.reset_stats()
     t0 = time.perf_counter()
-    srv.submit_many(reqs[:n_p], poisson_rate=rate, seed=7)
+    srv.submit_many(reqs, poisson_rate=rate, seed=7, count=n_p)
     srv.drain()
     t_p = time.perf_counter() - t0
     st_p = srv.stats()

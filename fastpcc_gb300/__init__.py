@@ -307,14 +307,20 @@ class Server:
         self._keep[rid] = out
         return rid
 
-    def submit_many(self, reqs, outs=None, poisson_rate=None, seed=1):
-        arr = (Request * len(reqs))(*reqs)
-        ids = np.zeros(len(reqs), np.int64)
+    @staticmethod
+    def request_array(reqs):
+        """A ctypes array of Request for submit_many (build once, submit many times)."""
+        return (Request * len(reqs))(*reqs)
+
+    def submit_many(self, reqs, outs=None, poisson_rate=None, seed=1, count=None):
+        arr = reqs if isinstance(reqs, C.Array) else self.request_array(reqs)
+        n = len(arr) if count is None else int(count)
+        ids = np.zeros(n, np.int64)
         idp = ids.ctypes.data_as(C.POINTER(C.c_int64))
         if poisson_rate:
-            rc = lib().fpcc_server_offer_poisson(self._h, arr, len(reqs), float(poisson_rate), seed, idp)
+            rc = lib().fpcc_server_offer_poisson(self._h, arr, n, float(poisson_rate), seed, idp)
         else:
-            rc = lib().fpcc_submit_many(self._h, arr, len(reqs), idp)
+            rc = lib().fpcc_submit_many(self._h, arr, n, idp)
         check(rc)
         return ids
 
