@@ -63,6 +63,7 @@ struct fpcc_ctx {
   DevBuf pin[8];
   cudaStream_t stream2 = nullptr;   // second stream of the pipelined drop-ins
   std::map<int, float2*> twiddles;   // device tables exp(-2 pi i t/n), per n
+  std::map<int, float2*> bluestein;  // per window length N: M-point filter spectra, forward then inverse
   std::mutex mu;
 };
 
@@ -160,6 +161,7 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
   for (auto& b : c->dev) if (b.p) cudaFree(b.p);
   for (auto& b : c->pin) if (b.p) cudaFreeHost(b.p);
   for (auto& kv : c->twiddles) cudaFree(kv.second);
+  for (auto& kv : c->bluestein) cudaFree(kv.second);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
   {
@@ -226,7 +228,7 @@ namespace {
 // Workspace slots of the context.
 enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_PAIRS = 5, S_ANA_A = 6,
             S_ANA_B = 7, S_RSTAT = 8, S_LARGE_T = 9, S_WP_X = 10, S_WP_BAND = 11, S_WP_RMAX = 12,
-            S_WP_Y = 13, S_WP_STAGE = 14 };
+            S_WP_Y = 13, S_WP_STAGE = 14, S_BLUE_O = 23 };
 
 constexpr size_t kLargeChunkBytes = size_t(512) << 20;   // four-step intermediate per chunk
 
@@ -313,13 +315,94 @@ int twiddle_table(fpcc_ctx* c, int n, const float2** out) {
   return 0;
 }
 
+// Generic passes of one M-point transform over rows (ping-pong between A and B,
+// starting from A); returns the buffer that holds the result.
+int passes(fpcc_ctx* c, float2* A, float2* B, int M, int nrows, int dir, float2** result) {
+  FftPlan p;
+  if (!make_plan(M, &p)) return fail(FPCC_EUNSUP, "length %d is not 2,3,5-smooth", M);
+  const float2* tw = nullptr;
+  int rc = twiddle_table(c, M, &tw);
+  if (rc) return rc;
+  float2* bufs[2] = {A, B};
+  int cur = 0, Ns = 1;
+  for (int i = 0; i < p.npass; i++) {
+    CK(launch_gpass(p.rad[i], dir, bufs[cur], false, M, bufs[cur ^ 1], M, M, Ns, nrows, tw, c->stream));
+    g_launches++;
+    cur ^= 1;
+    Ns *= p.rad[i];
+  }
+  *result = bufs[cur];
+  return 0;
+}
+
+int smooth_at_least(int n) {
+  for (int m = n;; m++) {
+    int a, b, cc;
+    if (factor235(m, &a, &b, &cc)) return m;
+  }
+}
+
+// Analytic signal for window lengths with a prime factor above 5, by Bluestein
+// transforms (DFT_N then masked IDFT_N) on M-point generic passes.
+int analytic_rows_bluestein(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, const float2** out,
+                            const float** rmax, const float** rsum) {
+  const int M = smooth_at_least(2 * N - 1);
+  float2* Bf = nullptr;
+  auto it = c->bluestein.find(N);
+  if (it == c->bluestein.end()) {
+    // filter spectra for both directions (computed once per N)
+    CK(cudaMalloc(&Bf, (size_t)2 * M * sizeof(float2)));
+    void* tmp;
+    int rc = dev_buf(c, S_ANA_B, (size_t)2 * M * sizeof(float2), &tmp);
+    if (rc) { cudaFree(Bf); return rc; }
+    for (int d = 0; d < 2; d++) {
+      const int dir = d ? +1 : -1;
+      CK(launch_blue_filter(Bf + (size_t)d * M, N, M, dir, c->stream));
+      float2* res = nullptr;
+      if ((rc = passes(c, Bf + (size_t)d * M, (float2*)tmp, M, 1, -1, &res))) { cudaFree(Bf); return rc; }
+      if (res != Bf + (size_t)d * M)
+        CK(cudaMemcpyAsync(Bf + (size_t)d * M, res, (size_t)M * sizeof(float2), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    c->bluestein[N] = Bf;
+  } else {
+    Bf = it->second;
+  }
+  void *A, *B, *O, *S;
+  int rc;
+  const size_t mb = (size_t)nrows * M * sizeof(float2);
+  if ((rc = dev_buf(c, S_ANA_A, mb, &A)) || (rc = dev_buf(c, S_ANA_B, mb, &B)) ||
+      (rc = dev_buf(c, S_BLUE_O, (size_t)nrows * N * sizeof(float2), &O)) ||
+      (rc = dev_buf(c, S_RSTAT, (size_t)2 * nrows * sizeof(float), &S)))
+    return rc;
+  for (int d = 0; d < 2; d++) {
+    const int dir = d ? +1 : -1;
+    const void* src = d ? (const void*)O : (const void*)d_x;
+    CK(launch_blue_pre(src, d == 0, d ? N : ldx, (float2*)A, M, N, M, dir, d, nrows, c->stream));
+    float2* r1 = nullptr;
+    if ((rc = passes(c, (float2*)A, (float2*)B, M, nrows, -1, &r1))) return rc;
+    CK(launch_blue_mul(r1, M, Bf + (size_t)d * M, M, nrows, c->stream));
+    float2* r2 = nullptr;
+    float2* other = (r1 == (float2*)A) ? (float2*)B : (float2*)A;
+    if ((rc = passes(c, r1, other, M, nrows, +1, &r2))) return rc;
+    CK(launch_blue_post(r2, M, (float2*)O, N, N, M, dir, nrows, c->stream));
+    g_launches += 3;
+  }
+  float* st = (float*)S;
+  CK(launch_rowstats((const float2*)O, N, N, nrows, st, st + nrows, c->stream));
+  g_launches++;
+  *out = (const float2*)O;
+  *rmax = st;
+  *rsum = st + nrows;
+  return 0;
+}
+
 // Analytic signal of nrows real rows (src/FFTapps.c:104-124): DFT_N, mask,
 // IDFT_N, by generic passes.  Leaves the rows (stride N) in *out and the row
 // statistics (max and sum of |a|^2) in *rmax / *rsum.
 int analytic_rows(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, const float2** out,
                   const float** rmax, const float** rsum) {
   FftPlan p;
-  if (!make_plan(N, &p)) return fail(FPCC_EUNSUP, "window length N=%d is not 2,3,5-smooth", N);
+  if (!make_plan(N, &p)) return analytic_rows_bluestein(c, d_x, ldx, nrows, N, out, rmax, rsum);
   const float2* tw = nullptr;
   int rc = twiddle_table(c, N, &tw);
   if (rc) return rc;

@@ -281,6 +281,67 @@ __global__ void __launch_bounds__(256) k_rowstats(const float2* a, int64_t ld, i
   }
 }
 
+// ------------------------------------------------------------ Bluestein helpers
+// chirp c[n] = exp(dir * pi * i * n^2 / N) with n^2 reduced mod 2N exactly.
+__device__ __forceinline__ float2 chirp(int64_t n, int N, int dir) {
+  const int64_t r = (n * n) % (2 * (int64_t)N);
+  double s, c;
+  sincospi((double)dir * (double)r / (double)N, &s, &c);
+  return make_float2((float)c, (float)s);
+}
+
+// a[j] = in[j] * c_dir[j] (j < N), 0 for N <= j < M.  in: real (real_in) or complex rows,
+// optionally multiplied first by the analytic mask (mask_n = N) with its 1/N.
+__global__ void k_blue_pre(const void* __restrict__ in, bool real_in, int64_t ldin, float2* __restrict__ a,
+                           int64_t lda, int N, int M, int dir, int mask) {
+  const int row = blockIdx.y;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x) {
+    float2 v = make_float2(0.f, 0.f);
+    if (j < N) {
+      if (real_in) v = make_float2(reinterpret_cast<const float*>(in)[(int64_t)row * ldin + j], 0.f);
+      else v = reinterpret_cast<const float2*>(in)[(int64_t)row * ldin + j];
+      if (mask) {
+        const float d = 1.0f / (float)N;
+        const int half = (N + 1) >> 1;
+        float f;
+        if (j == 0) f = d;
+        else if (j < half) f = 2.0f * d;
+        else if (!(N & 1) && j == (N >> 1)) f = d;
+        else f = 0.0f;
+        v = cscale(v, f);
+      }
+      v = cmul(v, chirp(j, N, dir));
+    }
+    a[(int64_t)row * lda + j] = v;
+  }
+}
+
+// a[k] *= B[k] (one filter spectrum for all rows)
+__global__ void k_blue_mul(float2* __restrict__ a, int64_t lda, const float2* __restrict__ B, int M) {
+  const int row = blockIdx.y;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x)
+    a[(int64_t)row * lda + k] = cmul(a[(int64_t)row * lda + k], B[k]);
+}
+
+// out[k] = c_dir[k] * a[k] / M, k < N
+__global__ void k_blue_post(const float2* __restrict__ a, int64_t lda, float2* __restrict__ out, int64_t ldo, int N,
+                            int M, int dir) {
+  const int row = blockIdx.y;
+  const float inv = 1.0f / (float)M;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x)
+    out[(int64_t)row * ldo + k] = cscale(cmul(a[(int64_t)row * lda + k], chirp(k, N, dir)), inv);
+}
+
+// filter b[j] = conj-chirp for |j| < N, placed circularly in M points
+__global__ void k_blue_filter(float2* __restrict__ b, int N, int M, int dir) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x) {
+    float2 v = make_float2(0.f, 0.f);
+    if (j < N) v = chirp(j, N, -dir);
+    else if (j > M - N) v = chirp(M - j, N, -dir);
+    b[j] = v;
+  }
+}
+
 template <typename K>
 cudaError_t launch_k(K kern, int grid, int T, size_t smem, cudaStream_t st, const void* args) {
   if (smem > 48 * 1024) {
@@ -386,6 +447,44 @@ cudaError_t launch_rowstats(const float2* a, int64_t ld, int n, int nrows, float
                             cudaStream_t st) {
   if (nrows <= 0) return cudaSuccess;
   k_rowstats<<<nrows, 256, 0, st>>>(a, ld, n, rmax, rsum);
+  return cudaGetLastError();
+}
+
+}  // namespace fpcc
+
+namespace fpcc {
+
+static dim3 rows_grid(int n, int nrows) {
+  int gx = (n + 255) / 256;
+  if (gx > 256) gx = 256;
+  return dim3(gx, nrows);
+}
+
+cudaError_t launch_blue_pre(const void* in, bool real_in, int64_t ldin, float2* a, int64_t lda, int N, int M,
+                            int dir, int mask, int nrows, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  if (nrows > 65535) return cudaErrorInvalidValue;
+  k_blue_pre<<<rows_grid(M, nrows), 256, 0, st>>>(in, real_in, ldin, a, lda, N, M, dir, mask);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_blue_mul(float2* a, int64_t lda, const float2* B, int M, int nrows, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  if (nrows > 65535) return cudaErrorInvalidValue;
+  k_blue_mul<<<rows_grid(M, nrows), 256, 0, st>>>(a, lda, B, M);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_blue_post(const float2* a, int64_t lda, float2* out, int64_t ldo, int N, int M, int dir,
+                             int nrows, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  if (nrows > 65535) return cudaErrorInvalidValue;
+  k_blue_post<<<rows_grid(N, nrows), 256, 0, st>>>(a, lda, out, ldo, N, M, dir);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_blue_filter(float2* b, int N, int M, int dir, cudaStream_t st) {
+  k_blue_filter<<<(M + 255) / 256 < 1024 ? (M + 255) / 256 : 1024, 256, 0, st>>>(b, N, M, dir);
   return cudaGetLastError();
 }
 

@@ -93,4 +93,14 @@ cudaError_t launch_analytic_mask(float2* a, int64_t ld, int n, int nrows, cudaSt
 cudaError_t launch_rowstats(const float2* a, int64_t ld, int n, int nrows, float* rmax, float* rsum,
                             cudaStream_t st);
 
+// Bluestein's chirp-z transform for window lengths with a prime factor above 5:
+// DFT_N(x)[k] = c[k] sum_j (x[j] c[j]) conj(c[k-j]),  c[n] = exp(dir pi i n^2 / N),
+// with the convolution done by M-point DFTs (M >= 2N-1, 2,3,5-smooth).
+cudaError_t launch_blue_pre(const void* in, bool real_in, int64_t ldin, float2* a, int64_t lda, int N, int M,
+                            int dir, int mask, int nrows, cudaStream_t st);
+cudaError_t launch_blue_mul(float2* a, int64_t lda, const float2* B, int M, int nrows, cudaStream_t st);
+cudaError_t launch_blue_post(const float2* a, int64_t lda, float2* out, int64_t ldo, int N, int M, int dir,
+                             int nrows, cudaStream_t st);
+cudaError_t launch_blue_filter(float2* b, int N, int M, int dir, cudaStream_t st);
+
 }  // namespace fpcc

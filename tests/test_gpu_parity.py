@@ -167,3 +167,13 @@ def test_wpcc_wavelet_config_size(F, orc):
     y64 = orc.wpcc(a, b, -4000, 4000, 4.0, 1000.0, V=5, wtype=-1)
     y = F.wpcc_set(a, b, -4000, 4000, 4.0, 1000.0, V=5, type=-1)
     assert relerr(y, y64) < TOL
+
+
+# ---- window lengths with prime factors above 5 (Bluestein analytic signal) -----
+@pytest.mark.parametrize("N,l1,l2", [(997, -100, 100), (1007, -50, 300), (4099, -400, 400), (37123, -3000, 2500)])
+def test_non_smooth_window_lengths(F, orc, N, l1, l2):
+    a, b = synth.plain_pair(N=N, n_windows=2, delay=min(150, N // 20), tag=f"gpu/blue/{N}")
+    assert relerr(F.pcc2_set(a, b, l1, l2), orc.pcc2(a, b, l1, l2)) < TOL
+    lo, hi = min(l1, l2), max(l1, l2)
+    assert relerr(F.pcc1_set(a, b, lo, hi), orc.pcc1(a, b, lo, hi)) < TOL
+    assert relerr(F.ccgn_set(a, b, l1, l2), orc.gncc(a, b, l1, l2)) < TOL
