@@ -16,6 +16,7 @@
 #include "direct.cuh"
 #include "engine.h"
 #include "kernels.cuh"
+#include "jit.h"
 #include "large.cuh"
 #include "menu.cuh"
 #include "wavelet.h"
@@ -482,6 +483,15 @@ extern "C" int fpcc_station_stage(fpcc_ctx* c, int method, const float* d_x, int
     }
     return large_station(c, method == FPCC_GNCC ? COL_REAL : COL_SIGN, d_x, sizeof(float), ldx, nrows, N, Nz, 0,
                          nullptr, rule == FPCC_SIGN_GE ? 1 : 0, FPCC_F32, 1, d_out, ldo);
+  }
+  if (method == FPCC_PCC2) {
+    // one fused kernel per station window, specialised at run time for (N, Nz)
+    const cudaError_t e = launch_station_fused(d_x, ldx, nrows, N, Nz, rule, fmt, d_out, ldo, c->stream);
+    if (e == cudaSuccess) {
+      g_launches++;
+      return 0;
+    }
+    if (e != cudaErrorNotSupported) return cuda_fail(e, "fused station kernel");
   }
   SpecArgs a{};
   a.nrows = nrows; a.N = N; a.Nz = Nz; a.fmt = fmt; a.out = d_out; a.ldo = ldo;

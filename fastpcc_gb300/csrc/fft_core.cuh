@@ -14,9 +14,17 @@
 // w^r are formed by repeated complex multiplication (error about R ulps).
 #pragma once
 
+#ifdef __CUDACC_RTC__
+// run-time compilation (NVRTC): builtin vector types; fixed-width integers by hand
+typedef unsigned long long uint64_t;
+typedef long long int64_t;
+typedef unsigned int uint32_t;
+#include <cuda_fp16.h>
+#else
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
+#endif
 
 namespace fpcc {
 

@@ -46,12 +46,32 @@ def up_to_date() -> bool:
     return os.path.exists(OUT) and os.path.getmtime(OUT) >= _newest_input()
 
 
+def cuda_home(cc: str) -> str:
+    return os.path.dirname(os.path.dirname(os.path.realpath(cc)))
+
+
+def write_jit_source() -> None:
+    """The fused station kernel's source as a C++ string for run-time compilation."""
+    parts = []
+    for name in ("fft_core.cuh", "fused.cuh"):
+        text = open(os.path.join(CSRC, name)).read()
+        text = "\n".join(l for l in text.splitlines()
+                         if l.strip() not in ("#pragma once", '#include "fft_core.cuh"'))
+        parts.append(text)
+    body = "\n".join(parts)
+    assert ")FPCCJIT\"" not in body
+    with open(os.path.join(OBJDIR, "jit_source.inc"), "w") as f:
+        f.write('static const char* kJitSource = R"FPCCJIT(' + body + '\n)FPCCJIT";\n')
+
+
 def build(force: bool = False, verbose: bool = False, extra=None) -> str:
     if not force and up_to_date():
         return OUT
     os.makedirs(OBJDIR, exist_ok=True)
     cc = nvcc()
-    flags = NVCC_FLAGS + ARCH + list(extra or [])
+    write_jit_source()
+    home = cuda_home(cc)
+    flags = NVCC_FLAGS + ARCH + ["-I" + OBJDIR, f'-DFPCC_CUDA_INCLUDE="{home}/include"'] + list(extra or [])
 
     def one(src):
         obj = os.path.join(OBJDIR, os.path.splitext(os.path.basename(src))[0] + ".o")
@@ -69,7 +89,7 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(one, srcs))
     tmp = OUT + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lnvrtc"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
