@@ -134,6 +134,7 @@ Entry build(int dev, int N, int Nz) {
   const int nmax = N > Nz ? N : Nz;
   int T = ((ceil_div(nmax, 16) + 31) / 32) * 32;
   if (T < 128) T = 128;
+  if (T > 1024) T = 1024;
   std::vector<int> rn, rz;
   for (; T <= 1024; T += 32) {
     rn = schedule(N, T);
