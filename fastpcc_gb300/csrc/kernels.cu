@@ -115,6 +115,14 @@ __device__ __forceinline__ float2 zbin(const void* X1, const void* X2, int p, in
   }
 }
 
+// Block size of the pair kernel for a half length H: enough threads that every
+// pass stages at most 16-24 complex values per thread.
+__host__ __device__ constexpr int pair_threads(int H) {
+  return H / 10 < 128 ? 128 : (H / 10 > 1024 ? 1024 : ((H / 10 + 31) / 32) * 32);
+}
+
+// Pair kernel: one block per pair; blocks are issued in pair order, so blocks
+// running together work on neighbouring pairs, which share station spectra in L2.
 template <int T, typename RAD, int FMT, bool HERM>
 __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
   constexpr int H = rad_len(RAD{});
@@ -129,60 +137,63 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
   build_twiddles(zlo, zhi, NZ);
   __syncthreads();
   const TwTab twZ{zlo, zhi};
-  const int p = blockIdx.x;
-  const int2 pr = a.pairs[p];
   constexpr int esz = (FMT == SPEC_F16) ? 4 : 8;
-  const char* X1 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.x * a.ldspec * esz;
-  const char* X2 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.y * a.ldspec * esz;
-
-  // F[k] = (H[k] + H[k+h]) + i w^k (H[k] - H[k+h]), H = Hermitian part of Z,
-  // w = exp(2 pi i / Nz); the group {k, h-k} reads Z at k, h-k, h+k, Nz-k.
-  for (int k = threadIdx.x; k <= (H >> 1); k += T) {
-    const int k2 = H - k;
-    const float2 z0 = zbin<FMT, HERM>(X1, X2, k, NZ);
-    const float2 z1 = zbin<FMT, HERM>(X1, X2, k2, NZ);
-    const float2 z2 = zbin<FMT, HERM>(X1, X2, H + k, NZ);
-    const float2 z3 = zbin<FMT, HERM>(X1, X2, (k == 0) ? 0 : NZ - k, NZ);
-    const float2 Hk = cscale(cadd(z0, cconj(z3)), 0.5f);
-    const float2 Hkh = cscale(cadd(z2, cconj(z1)), 0.5f);
-    float2 w = twiddle(twZ, k);
-    w.y = -w.y;
-    const float2 e = cadd(Hk, Hkh);
-    const float2 o = cmul(w, csub(Hk, Hkh));
-    s[PADI(k)] = make_float2(e.x - o.y, e.y + o.x);
-    if (k2 != k && k2 < H) {
-      // H[k2] = conj(H[k+h]), H[k2+h] = conj(H[k])
-      float2 w2 = twiddle(twZ, k2);
-      w2.y = -w2.y;
-      const float2 e2 = cconj(cadd(Hkh, Hk));
-      const float2 o2 = cmul(w2, cconj(csub(Hkh, Hk)));
-      s[PADI(k2)] = make_float2(e2.x - o2.y, e2.y + o2.x);
-    }
-  }
-  __syncthreads();
-  ct_fft<+1, T, 1>(s, 1, 0, TwTab{hlo, hhi}, RAD{});
-
-  float* y = a.y + (int64_t)p * a.ldy;
   const int N = a.N;
-  const double* E1 = (a.norm == 1) ? a.energy + (int64_t)pr.x * a.ldE : nullptr;
-  const double* E2 = (a.norm == 1) ? a.energy + (int64_t)pr.y * a.ldE : nullptr;
-  for (int l = threadIdx.x; l < a.L; l += T) {
-    const int lag = a.lag0 + l;
-    const int idx = lag < 0 ? lag + NZ : lag;
-    const float2 zz = s[PADI(idx >> 1)];
-    float v = ((idx & 1) ? zz.y : zz.x) * a.scale;
-    if (a.norm == 1) {
-      // overlap x1[n11,n12), x2[n21,n22) (src/FFTapps.c:896-902)
-      int n11 = 0, n21 = 0, n12 = N, n22 = N;
-      if (lag > 0) { n21 = lag; n12 -= lag; }
-      else { n11 = -lag; n22 += lag; }
-      const double e1 = E1[n12] - E1[n11];
-      const double e2 = E2[n22] - E2[n21];
-      v = (float)((double)v / sqrt(e1 * e2));
-    } else if (a.norm == 2) {
-      v = (float)((double)v / (double)(N - abs(lag)));
+  {
+    const int p = blockIdx.x;
+    const int2 pr = a.pairs[p];
+    const char* X1 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.x * a.ldspec * esz;
+    const char* X2 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.y * a.ldspec * esz;
+
+    // F[k] = (H[k] + H[k+h]) + i w^k (H[k] - H[k+h]), H = Hermitian part of Z,
+    // w = exp(2 pi i / Nz); the group {k, h-k} reads Z at k, h-k, h+k, Nz-k.
+#pragma unroll 1
+    for (int k = threadIdx.x; k <= (H >> 1); k += T) {
+      const int k2 = H - k;
+      const float2 z0 = zbin<FMT, HERM>(X1, X2, k, NZ);
+      const float2 z1 = zbin<FMT, HERM>(X1, X2, k2, NZ);
+      const float2 z2 = zbin<FMT, HERM>(X1, X2, H + k, NZ);
+      const float2 z3 = zbin<FMT, HERM>(X1, X2, (k == 0) ? 0 : NZ - k, NZ);
+      const float2 Hk = cscale(cadd(z0, cconj(z3)), 0.5f);
+      const float2 Hkh = cscale(cadd(z2, cconj(z1)), 0.5f);
+      float2 w = twiddle(twZ, k);
+      w.y = -w.y;
+      const float2 e = cadd(Hk, Hkh);
+      const float2 o = cmul(w, csub(Hk, Hkh));
+      s[PADI(k)] = make_float2(e.x - o.y, e.y + o.x);
+      if (k2 != k && k2 < H) {
+        // H[k2] = conj(H[k+h]), H[k2+h] = conj(H[k])
+        float2 w2 = twiddle(twZ, k2);
+        w2.y = -w2.y;
+        const float2 e2 = cconj(cadd(Hkh, Hk));
+        const float2 o2 = cmul(w2, cconj(csub(Hkh, Hk)));
+        s[PADI(k2)] = make_float2(e2.x - o2.y, e2.y + o2.x);
+      }
     }
-    y[l] = v;
+    __syncthreads();
+    ct_fft<+1, T, 1>(s, 1, 0, TwTab{hlo, hhi}, RAD{});
+
+    float* y = a.y + (int64_t)p * a.ldy;
+    const double* E1 = (a.norm == 1) ? a.energy + (int64_t)pr.x * a.ldE : nullptr;
+    const double* E2 = (a.norm == 1) ? a.energy + (int64_t)pr.y * a.ldE : nullptr;
+    for (int l = threadIdx.x; l < a.L; l += T) {
+      const int lag = a.lag0 + l;
+      const int idx = lag < 0 ? lag + NZ : lag;
+      const float2 zz = s[PADI(idx >> 1)];
+      float v = ((idx & 1) ? zz.y : zz.x) * a.scale;
+      if (a.norm == 1) {
+        // overlap x1[n11,n12), x2[n21,n22) (src/FFTapps.c:896-902)
+        int n11 = 0, n21 = 0, n12 = N, n22 = N;
+        if (lag > 0) { n21 = lag; n12 -= lag; }
+        else { n11 = -lag; n22 += lag; }
+        const double e1 = E1[n12] - E1[n11];
+        const double e2 = E2[n22] - E2[n21];
+        v = (float)((double)v / sqrt(e1 * e2));
+      } else if (a.norm == 2) {
+        v = (float)((double)v / (double)(N - abs(lag)));
+      }
+      y[l] = v;
+    }
   }
 }
 
@@ -379,12 +390,34 @@ cudaError_t launch_spec(const SpecArgs& a, cudaStream_t st) {
   }
 }
 
+template <typename K>
+static cudaError_t launch_persistent(K kern, int npairs, int T, size_t smem, cudaStream_t st, const void* args) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem);
+  if (sms <= 0) sms = 1;
+  if (per_sm <= 0) per_sm = 1;
+  // one block per pair (a persistent loop keeps the transform's index
+  // arithmetic live across pairs and spills)
+  int grid = npairs;
+  (void)sms;
+  void* argv[] = {const_cast<void*>(args)};
+  return cudaLaunchKernel((const void*)kern, dim3(grid), dim3(T), argv, smem, st);
+}
+
 template <int FMT, bool HERM>
 static cudaError_t launch_pairs_t(const PairArgs& a, cudaStream_t st) {
   const size_t smem = pair_smem_bytes(a.Nz);
   switch (a.Nz / 2) {
-#define FPCC_PAIR_CASE(SZ, T, ...) \
-  case SZ: return launch_k(k_pairs<T, Radices<__VA_ARGS__>, FMT, HERM>, a.npairs, T, smem, st, &a);
+#define FPCC_PAIR_CASE(SZ, T, ...)                                                                   \
+  case SZ:                                                                                         \
+    return launch_persistent(k_pairs<pair_threads(SZ), Radices<__VA_ARGS__>, FMT, HERM>, a.npairs, \
+                             pair_threads(SZ), smem, st, &a);
     FPCC_SIZE_MENU(FPCC_PAIR_CASE)
 #undef FPCC_PAIR_CASE
     default: return cudaErrorInvalidValue;
