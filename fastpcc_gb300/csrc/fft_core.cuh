@@ -231,6 +231,15 @@ __device__ __forceinline__ float2 twiddle(const TwTab& tw, int t) {
 // radices already applied.  Each of the T threads stages B = ceil(nvec*N/R / T)
 // butterflies in registers (B is bounded by BMAX, a compile-time value that the
 // caller derives from its nvec bound).
+// Powers w^1..w^(R-1) of a twiddle, formed as a shallow product tree
+// (w^(2a) = (w^a)^2, w^(2a+1) = w^(2a) w) so the multiplications overlap.
+template <int R>
+__device__ __forceinline__ void twiddle_powers(float2 w1, float2* w) {
+  w[1] = w1;
+#pragma unroll
+  for (int r = 2; r < R; r++) w[r] = (r & 1) ? cmul(w[r - 1], w1) : cmul(w[r >> 1], w[r >> 1]);
+}
+
 template <int R, int DIR, int N, int Ns, int T, int BMAX>
 __device__ __forceinline__ void ct_pass(float2* s, int nvec, int vstride, const TwTab& tw) {
   constexpr int m = N / R;
@@ -244,8 +253,15 @@ __device__ __forceinline__ void ct_pass(float2* s, int nvec, int vstride, const 
       const int vec = g / m;
       const int j = g - vec * m;
       const float2* sv = s + vec * vstride;
+      if constexpr (m % 32 == 0) {
+        // PADI(j + r m) = PADI(j) + r m + r m / 32: constant offsets
+        const float2* sj = sv + PADI(j);
 #pragma unroll
-      for (int r = 0; r < R; r++) v[b][r] = sv[PADI(j + r * m)];
+        for (int r = 0; r < R; r++) v[b][r] = sj[r * m + ((r * m) >> 5)];
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; r++) v[b][r] = sv[PADI(j + r * m)];
+      }
     }
   }
   __syncthreads();
@@ -259,18 +275,22 @@ __device__ __forceinline__ void ct_pass(float2* s, int nvec, int vstride, const 
       if (Ns > 1 && k != 0) {
         float2 w1 = twiddle(tw, k * tstride);
         if (DIR > 0) w1.y = -w1.y;
-        float2 w = w1;
+        float2 w[R];
+        twiddle_powers<R>(w1, w);
 #pragma unroll
-        for (int r = 1; r < R; r++) {
-          v[b][r] = cmul(v[b][r], w);
-          if (r + 1 < R) w = cmul(w, w1);
-        }
+        for (int r = 1; r < R; r++) v[b][r] = cmul(v[b][r], w[r]);
       }
       dft<R, DIR>(v[b]);
       const int base = (j - k) * R + k;
       float2* sv = s + vec * vstride;
+      if constexpr (Ns % 32 == 0) {
+        float2* sb = sv + PADI(base);
 #pragma unroll
-      for (int r = 0; r < R; r++) sv[PADI(base + r * Ns)] = v[b][dft_perm<R>(r)];
+        for (int r = 0; r < R; r++) sb[r * Ns + ((r * Ns) >> 5)] = v[b][dft_perm<R>(r)];
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; r++) sv[PADI(base + r * Ns)] = v[b][dft_perm<R>(r)];
+      }
     }
   }
   __syncthreads();

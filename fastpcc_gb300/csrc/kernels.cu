@@ -390,34 +390,14 @@ cudaError_t launch_spec(const SpecArgs& a, cudaStream_t st) {
   }
 }
 
-template <typename K>
-static cudaError_t launch_persistent(K kern, int npairs, int T, size_t smem, cudaStream_t st, const void* args) {
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, smem);
-  if (sms <= 0) sms = 1;
-  if (per_sm <= 0) per_sm = 1;
-  // one block per pair (a persistent loop keeps the transform's index
-  // arithmetic live across pairs and spills)
-  int grid = npairs;
-  (void)sms;
-  void* argv[] = {const_cast<void*>(args)};
-  return cudaLaunchKernel((const void*)kern, dim3(grid), dim3(T), argv, smem, st);
-}
-
 template <int FMT, bool HERM>
 static cudaError_t launch_pairs_t(const PairArgs& a, cudaStream_t st) {
   const size_t smem = pair_smem_bytes(a.Nz);
   switch (a.Nz / 2) {
 #define FPCC_PAIR_CASE(SZ, T, ...)                                                                   \
   case SZ:                                                                                         \
-    return launch_persistent(k_pairs<pair_threads(SZ), Radices<__VA_ARGS__>, FMT, HERM>, a.npairs, \
-                             pair_threads(SZ), smem, st, &a);
+    return launch_k(k_pairs<pair_threads(SZ), Radices<__VA_ARGS__>, FMT, HERM>, a.npairs, pair_threads(SZ), \
+                    smem, st, &a);
     FPCC_SIZE_MENU(FPCC_PAIR_CASE)
 #undef FPCC_PAIR_CASE
     default: return cudaErrorInvalidValue;
