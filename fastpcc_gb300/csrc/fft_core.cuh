@@ -296,14 +296,73 @@ __device__ __forceinline__ void ct_pass(float2* s, int nvec, int vstride, const 
   __syncthreads();
 }
 
-template <int... Rs>
-struct Radices {};
-
 template <int R, int... Rest>
 constexpr int prod_radices() {
   if constexpr (sizeof...(Rest) == 0) return R;
   else return R * prod_radices<Rest...>();
 }
+
+// Out-of-place Stockham pass (ping-pong): butterflies go from src to dst one
+// at a time, so a thread holds only R values and each pass needs one barrier.
+template <int R, int DIR, int N, int Ns, int T>
+__device__ __forceinline__ void pp_pass(const float2* __restrict__ src, float2* __restrict__ dst, const TwTab& tw) {
+  constexpr int m = N / R;
+  constexpr int tstride = N / (Ns * R);
+#pragma unroll 1
+  for (int j = threadIdx.x; j < m; j += T) {
+    float2 v[R];
+    if constexpr (m % 32 == 0) {
+      const float2* sj = src + PADI(j);
+#pragma unroll
+      for (int r = 0; r < R; r++) v[r] = sj[r * m + ((r * m) >> 5)];
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; r++) v[r] = src[PADI(j + r * m)];
+    }
+    const int k = (Ns == 1) ? 0 : j % Ns;
+    if (Ns > 1 && k != 0) {
+      float2 w1 = twiddle(tw, k * tstride);
+      if (DIR > 0) w1.y = -w1.y;
+      float2 w[R];
+      twiddle_powers<R>(w1, w);
+#pragma unroll
+      for (int r = 1; r < R; r++) v[r] = cmul(v[r], w[r]);
+    }
+    dft<R, DIR>(v);
+    const int base = (j - k) * R + k;
+    if constexpr (Ns % 32 == 0) {
+      float2* sb = dst + PADI(base);
+#pragma unroll
+      for (int r = 0; r < R; r++) sb[r * Ns + ((r * Ns) >> 5)] = v[dft_perm<R>(r)];
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; r++) dst[PADI(base + r * Ns)] = v[dft_perm<R>(r)];
+    }
+  }
+  __syncthreads();
+}
+
+template <int DIR, int N, int Ns, int T, int R, int... Rest>
+__device__ __forceinline__ void pp_passes(float2* a, float2* b, const TwTab& tw) {
+  pp_pass<R, DIR, N, Ns, T>(a, b, tw);
+  if constexpr (sizeof...(Rest) > 0) pp_passes<DIR, N, Ns * R, T, Rest...>(b, a, tw);
+}
+
+template <int... Rs>
+struct Radices;
+
+// Transform of one vector held in a (padded); the result ends in a when the
+// number of passes is even, else in b.  The caller synchronises before the call.
+template <int DIR, int T, int... Rs>
+__device__ __forceinline__ float2* pp_fft(float2* a, float2* b, const TwTab& tw, Radices<Rs...>) {
+  constexpr int N = prod_radices<Rs...>();
+  pp_passes<DIR, N, 1, T, Rs...>(a, b, tw);
+  return (sizeof...(Rs) % 2 == 0) ? a : b;
+}
+
+template <int... Rs>
+struct Radices {};
+
 
 // Staging bound of a pass: ceil(NV*N/R / T) butterflies per thread.
 template <int N, int R, int T, int NV>

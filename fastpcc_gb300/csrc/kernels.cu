@@ -123,13 +123,20 @@ __host__ __device__ constexpr int pair_threads(int H) {
 
 // Pair kernel: one block per pair; blocks are issued in pair order, so blocks
 // running together work on neighbouring pairs, which share station spectra in L2.
+// Two transform buffers (ping-pong passes) when they fit one block's shared memory.
+__host__ __device__ constexpr bool pair_pingpong(int H) {
+  return (2LL * (H + (H >> 5) + 1) + 128 + (H + 127) / 128 + 128 + (2 * H + 127) / 128) * 8 <= 227LL * 1024;
+}
+
 template <int T, typename RAD, int FMT, bool HERM>
 __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
   constexpr int H = rad_len(RAD{});
   constexpr int NZ = 2 * H;
+  constexpr bool PP = pair_pingpong(H);
   extern __shared__ float4 smem_raw[];
   float2* s = reinterpret_cast<float2*>(smem_raw);
-  float2* hlo = s + padded_len(H);
+  float2* s2 = s + (PP ? padded_len(H) : 0);
+  float2* hlo = s2 + padded_len(H);
   float2* hhi = hlo + 128;
   float2* zlo = hhi + tw_hi_len(H);
   float2* zhi = zlo + 128;
@@ -171,7 +178,12 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
       }
     }
     __syncthreads();
-    ct_fft<+1, T, 1>(s, 1, 0, TwTab{hlo, hhi}, RAD{});
+    const float2* res = s;
+    if constexpr (PP) {
+      res = pp_fft<+1, T>(s, s2, TwTab{hlo, hhi}, RAD{});
+    } else {
+      ct_fft<+1, T, 1>(s, 1, 0, TwTab{hlo, hhi}, RAD{});
+    }
 
     float* y = a.y + (int64_t)p * a.ldy;
     const double* E1 = (a.norm == 1) ? a.energy + (int64_t)pr.x * a.ldE : nullptr;
@@ -179,7 +191,7 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
     for (int l = threadIdx.x; l < a.L; l += T) {
       const int lag = a.lag0 + l;
       const int idx = lag < 0 ? lag + NZ : lag;
-      const float2 zz = s[PADI(idx >> 1)];
+      const float2 zz = res[PADI(idx >> 1)];
       float v = ((idx & 1) ? zz.y : zz.x) * a.scale;
       if (a.norm == 1) {
         // overlap x1[n11,n12), x2[n21,n22) (src/FFTapps.c:896-902)
@@ -375,7 +387,8 @@ size_t spec_smem_bytes(int Nz) {
 
 size_t pair_smem_bytes(int Nz) {
   const int h = Nz / 2;
-  return ((size_t)padded_len(h) + 128 + tw_hi_len(h) + 128 + tw_hi_len(Nz)) * sizeof(float2);
+  const size_t bufs = pair_pingpong(h) ? 2 : 1;
+  return (bufs * padded_len(h) + 128 + tw_hi_len(h) + 128 + tw_hi_len(Nz)) * sizeof(float2);
 }
 
 cudaError_t launch_spec(const SpecArgs& a, cudaStream_t st) {
