@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
 
     // F[k] = (H[k] + H[k+h]) + i w^k (H[k] - H[k+h]), H = Hermitian part of Z,
     // w = exp(2 pi i / Nz); the group {k, h-k} reads Z at k, h-k, h+k, Nz-k.
+    // 2H is formed (the 1/2 goes into the output scale) and w^(h-k) = -conj(w^k).
 #pragma unroll 1
     for (int k = threadIdx.x; k <= (H >> 1); k += T) {
       const int k2 = H - k;
@@ -161,19 +162,19 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
       const float2 z1 = zbin<FMT, HERM>(X1, X2, k2, NZ);
       const float2 z2 = zbin<FMT, HERM>(X1, X2, H + k, NZ);
       const float2 z3 = zbin<FMT, HERM>(X1, X2, (k == 0) ? 0 : NZ - k, NZ);
-      const float2 Hk = cscale(cadd(z0, cconj(z3)), 0.5f);
-      const float2 Hkh = cscale(cadd(z2, cconj(z1)), 0.5f);
+      const float2 Hk = cadd(z0, cconj(z3));
+      const float2 Hkh = cadd(z2, cconj(z1));
       float2 w = twiddle(twZ, k);
       w.y = -w.y;
       const float2 e = cadd(Hk, Hkh);
-      const float2 o = cmul(w, csub(Hk, Hkh));
+      const float2 d = csub(Hk, Hkh);
+      const float2 o = cmul(w, d);
       s[PADI(k)] = make_float2(e.x - o.y, e.y + o.x);
       if (k2 != k && k2 < H) {
-        // H[k2] = conj(H[k+h]), H[k2+h] = conj(H[k])
-        float2 w2 = twiddle(twZ, k2);
-        w2.y = -w2.y;
-        const float2 e2 = cconj(cadd(Hkh, Hk));
-        const float2 o2 = cmul(w2, cconj(csub(Hkh, Hk)));
+        // H[k2] = conj(H[k+h]), H[k2+h] = conj(H[k]); w^k2 = -conj(w^k)
+        const float2 w2 = make_float2(-w.x, w.y);
+        const float2 e2 = cconj(e);
+        const float2 o2 = cmul(w2, make_float2(-d.x, d.y));
         s[PADI(k2)] = make_float2(e2.x - o2.y, e2.y + o2.x);
       }
     }
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
       const int lag = a.lag0 + l;
       const int idx = lag < 0 ? lag + NZ : lag;
       const float2 zz = res[PADI(idx >> 1)];
-      float v = ((idx & 1) ? zz.y : zz.x) * a.scale;
+      float v = ((idx & 1) ? zz.y : zz.x) * (0.5f * a.scale);
       if (a.norm == 1) {
         // overlap x1[n11,n12), x2[n21,n22) (src/FFTapps.c:896-902)
         int n11 = 0, n21 = 0, n12 = N, n22 = N;
