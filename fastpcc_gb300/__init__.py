@@ -90,6 +90,7 @@ def lib():
             L.fpcc_wpcc_plan_create.argtypes = [vp, C.POINTER(vp), u, i, i, d, d, u, i, d, i, i]
             L.fpcc_wpcc_plan_info.argtypes = [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]
             L.fpcc_wpcc_plan_destroy.argtypes = [vp]
+            L.fpcc_wpcc_plan_set_band.argtypes = [vp, i, i]
             L.fpcc_wpcc_station_stage.argtypes = [vp, vp, vp, i64, i, vp, i]
             L.fpcc_wpcc_pair_stage.argtypes = [vp, vp, vp, i, vp, i, vp, i64]
             L.fpcc_server_create.argtypes = [C.POINTER(vp), i, C.c_size_t, i]
@@ -342,3 +343,38 @@ class Server:
 
     def reset_stats(self):
         check(lib().fpcc_server_reset_stats(self._h))
+
+
+class WpccPlan:
+    """Device-resident wavelet PCC plan (fpcc_wpcc_plan_* of the C ABI)."""
+
+    def __init__(self, ctx, N, Lag1, Lag2, pmin, pmax, V=2, type=-3, op1=0.0, rule=AMP_D_REG, nz_mode=NZ_FAST):
+        self._h = C.c_void_p()
+        self.ctx = ctx
+        check(lib().fpcc_wpcc_plan_create(ctx.handle, C.byref(self._h), N, Lag1, Lag2, float(pmin), float(pmax),
+                                          V, type, float(op1), rule, nz_mode))
+        nz, S, L = C.c_int(), C.c_int(), C.c_int()
+        check(lib().fpcc_wpcc_plan_info(self._h, C.byref(nz), C.byref(S), C.byref(L)))
+        self.Nz, self.S, self.L, self.N = nz.value, S.value, L.value, N
+
+    def set_band(self, s_lo, s_hi):
+        check(lib().fpcc_wpcc_plan_set_band(self._h, s_lo, s_hi))
+
+    def station_stage(self, d_x, ldx, nrows, d_P, fmt=F32):
+        check(lib().fpcc_wpcc_station_stage(self.ctx.handle, self._h, C.c_void_p(d_x), ldx, nrows,
+                                            C.c_void_p(d_P), fmt))
+
+    def pair_stage(self, d_P, d_pairs, npairs, d_y, ldy, fmt=F32):
+        check(lib().fpcc_wpcc_pair_stage(self.ctx.handle, self._h, C.c_void_p(d_P), fmt, C.c_void_p(d_pairs),
+                                         npairs, C.c_void_p(d_y), ldy))
+
+    def close(self):
+        if self._h:
+            lib().fpcc_wpcc_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

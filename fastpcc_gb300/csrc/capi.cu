@@ -923,6 +923,21 @@ extern "C" int fpcc_wpcc_plan_create(fpcc_ctx* c, fpcc_wpcc_plan** out, unsigned
   return 0;
 }
 
+extern "C" int fpcc_wpcc_plan_set_band(fpcc_wpcc_plan* p, int s_lo, int s_hi) {
+  if (!p) return fail(FPCC_EARG, "null plan");
+  const int S = p->dev.S;
+  std::vector<float> a(S, 0.0f);
+  for (int s = 0; s < S; s++)
+    if (s >= s_lo && s < s_hi) a[s] = (float)(1.0 / (p->su.wf.scale.empty() ? 1.0 : p->su.wf.scale[s]) / p->dev.Nz);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(p->device);
+  const cudaError_t e = cudaMemcpy(p->a, a.data(), S * sizeof(float), cudaMemcpyHostToDevice);
+  cudaSetDevice(cur);
+  if (e != cudaSuccess) return cuda_fail(e, "band weights");
+  return 0;
+}
+
 extern "C" int fpcc_wpcc_plan_info(const fpcc_wpcc_plan* p, int* Nz, int* S, int* L) {
   if (!p) return fail(FPCC_EARG, "null plan");
   if (Nz) *Nz = p->dev.Nz;

@@ -145,6 +145,9 @@ typedef struct fpcc_wpcc_plan fpcc_wpcc_plan;
 int fpcc_wpcc_plan_create(fpcc_ctx *ctx, fpcc_wpcc_plan **out, unsigned N, int Lag1, int Lag2, double pmin,
                           double pmax, unsigned V, int type, double op1, int rule, int nz_mode);
 int fpcc_wpcc_plan_info(const fpcc_wpcc_plan *p, int *Nz, int *S, int *L);
+/* Accumulate only scales s_lo <= s < s_hi (per-band diagnostics; the output
+ * scale keeps all scales).  fpcc_wpcc_plan_set_band(p, 0, S) restores the plan. */
+int fpcc_wpcc_plan_set_band(fpcc_wpcc_plan *p, int s_lo, int s_hi);
 int fpcc_wpcc_plan_destroy(fpcc_wpcc_plan *p);
 int fpcc_wpcc_station_stage(fpcc_ctx *ctx, const fpcc_wpcc_plan *p, const float *d_x, int64_t ldx, int nrows,
                             void *d_P, int fmt);

@@ -63,6 +63,7 @@ def lib():
             L.orc_cc1b_set.argtypes = [_f64p, _f32p, _f32p, u, u, i, i]
             L.orc_cc1b_num.argtypes = [_i64p, _f32p, _f32p, u, u, i, i]
             L.orc_wpcc_set.argtypes = [_f64p, _f32p, _f32p, u, u, i, i, d, d, u, i, d, i]
+            L.orc_wpcc_band.argtypes = [_f64p, _f32p, _f32p, u, u, i, i, d, d, u, i, d, i, u, u]
             L.orc_wpcc_setup.argtypes = [u, i, i, d, d, u, i, d, C.POINTER(u), C.POINTER(d),
                                          C.POINTER(d), C.POINTER(u)]
             L.orc_wpcc_setup.restype = u
@@ -185,6 +186,15 @@ def wpcc(x1, x2, Lag1, Lag2, pmin, pmax, V=2, wtype=-3, op1=0.0, rule=AMP_D_REG)
     x1, x2, Tr, N = _windows(x1, x2)
     y = np.empty((Tr, abs(Lag2 - Lag1 + 1)), np.float64)
     _check(lib().orc_wpcc_set(y, x1, x2, N, Tr, Lag1, Lag2, pmin, pmax, V, wtype, op1, rule), "orc_wpcc_set")
+    return y
+
+
+def wpcc_band(x1, x2, Lag1, Lag2, pmin, pmax, s_lo, s_hi, V=2, wtype=-3, op1=0.0, rule=AMP_D_REG):
+    """WPCC accumulating only scales s_lo <= s < s_hi (per-band error diagnostics)."""
+    x1, x2, Tr, N = _windows(x1, x2)
+    y = np.empty((Tr, abs(Lag2 - Lag1 + 1)), np.float64)
+    _check(lib().orc_wpcc_band(y, x1, x2, N, Tr, Lag1, Lag2, pmin, pmax, V, wtype, op1, rule, s_lo, s_hi),
+           "orc_wpcc_band")
     return y
 
 

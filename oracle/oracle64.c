@@ -356,9 +356,9 @@ unsigned orc_wpcc_setup(unsigned N, int Lag1, int Lag2, double pmin, double pmax
  * IDFT(X W_s), amplitude-normalised and transformed back, and the cross
  * spectrum sum_s conj(P1_s) P2_s / (scale_s Nz) is inverted (:1200-1220);
  * lags are scaled by C = 1/(K0 N), K0 = sum_s 1/scale_s (:1114-1120,1223-1224). */
-int orc_wpcc_set(double *y, const float *x1, const float *x2, unsigned N, unsigned Tr,
-                 int Lag1, int Lag2, double pmin, double pmax, unsigned V, int type,
-                 double op1, int rule) {
+int orc_wpcc_band(double *y, const float *x1, const float *x2, unsigned N, unsigned Tr,
+                  int Lag1, int Lag2, double pmin, double pmax, unsigned V, int type,
+                  double op1, int rule, unsigned s_lo, unsigned s_hi) {
     unsigned Nz, J; double s0, op1v;
     unsigned S = orc_wpcc_setup(N, Lag1, Lag2, pmin, pmax, V, type, op1, &Nz, &s0, &op1v, &J);
     if (S == 0) return -3;
@@ -403,7 +403,7 @@ int orc_wpcc_set(double *y, const float *x1, const float *x2, unsigned N, unsign
         for (unsigned n = 0; n < N; n++) { in1[Ls0 + n] = da2 * a1[n]; in2[Ls0 + n] = da2 * a2[n]; }
         fft64_c2c(in1, Nz, -1);
         fft64_c2c(in2, Nz, -1);
-        for (unsigned s = 0; s < S; s++) {
+        for (unsigned s = s_lo; s < S && s < s_hi; s++) {
             const double complex *f = fw + (size_t)s * Nz;
             for (unsigned n = 0; n < Nz; n++) { w1[n] = in1[n] * f[n]; w2[n] = in2[n] * f[n]; }
             fft64_c2c(w1, Nz, +1); orc_ampnorm(w1, Nz, rule); fft64_c2c(w1, Nz, -1);
@@ -422,4 +422,10 @@ int orc_wpcc_set(double *y, const float *x1, const float *x2, unsigned N, unsign
     }
     free(fw); free(taps); free(scale); free(Ls); free(center);
     return 0;
+}
+
+int orc_wpcc_set(double *y, const float *x1, const float *x2, unsigned N, unsigned Tr,
+                 int Lag1, int Lag2, double pmin, double pmax, unsigned V, int type,
+                 double op1, int rule) {
+    return orc_wpcc_band(y, x1, x2, N, Tr, Lag1, Lag2, pmin, pmax, V, type, op1, rule, 0, ~0u);
 }

@@ -85,6 +85,12 @@ int orc_wpcc_set(double *y, const float *x1, const float *x2, unsigned N, unsign
                  int Lag1, int Lag2, double pmin, double pmax, unsigned V, int type,
                  double op1, int rule);
 
+/* The same restricted to scales s_lo <= s < s_hi (per-band diagnostics; the
+ * output scale C still uses all scales). */
+int orc_wpcc_band(double *y, const float *x1, const float *x2, unsigned N, unsigned Tr,
+                  int Lag1, int Lag2, double pmin, double pmax, unsigned V, int type,
+                  double op1, int rule, unsigned s_lo, unsigned s_hi);
+
 #ifdef __cplusplus
 }
 #endif

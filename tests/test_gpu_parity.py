@@ -177,3 +177,29 @@ def test_non_smooth_window_lengths(F, orc, N, l1, l2):
     lo, hi = min(l1, l2), max(l1, l2)
     assert relerr(F.pcc1_set(a, b, lo, hi), orc.pcc1(a, b, lo, hi)) < TOL
     assert relerr(F.ccgn_set(a, b, l1, l2), orc.gncc(a, b, l1, l2)) < TOL
+
+
+def test_wpcc_error_per_octave_band(F, orc):
+    """Wavelet config shape (20 Hz, 0.02-5 Hz, Morlet, V=5): error of each octave's
+    partial sum against the oracle's, relative to that band's own peak."""
+    import torch
+    x1, x2, _ = synth.wavelet_pairs(n_pairs=1, n_windows=1, N=16384, tag="gpu/wpcc-bands")
+    a, b = x1[0], x2[0]
+    l1, l2, pmin, pmax, V = -1000, 1000, 4.0, 256.0, 5
+    ctx = F.Context(0)
+    plan = F.WpccPlan(ctx, a.shape[1], l1, l2, pmin, pmax, V=V, type=-1)
+    xs = torch.from_numpy(np.concatenate([a, b])).cuda()
+    P = torch.empty((2, plan.S, plan.Nz, 2), dtype=torch.float32, device="cuda")
+    plan.station_stage(xs.data_ptr(), a.shape[1], 2, P.data_ptr())
+    pairs = torch.tensor([[0, 1]], dtype=torch.int32, device="cuda")
+    y = torch.empty((1, plan.L), dtype=torch.float32, device="cuda")
+    errs = []
+    for lo in range(0, plan.S, V):
+        plan.set_band(lo, lo + V)
+        plan.pair_stage(P.data_ptr(), pairs.data_ptr(), 1, y.data_ptr(), plan.L)
+        ctx.sync()
+        y64 = orc.wpcc_band(a, b, l1, l2, pmin, pmax, lo, lo + V, V=V, wtype=-1)
+        errs.append(relerr(y.cpu().numpy(), y64))
+    plan.close()
+    ctx.close()
+    assert max(errs) < TOL, errs
