@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--fmt", default="f32", choices=["f32", "f16"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served (request loop) leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the uneven-batch and request-stream legs")
+    ap.add_argument("--mixed-only", action="store_true", help="run only the uneven-batch and request-stream legs")
     return ap.parse_args()
 
 
@@ -183,6 +185,164 @@ def served_leg(F, x, pairs, n_win, L, rate_frac=0.5, poisson_max=60000):
     }
 
 
+# mixed workloads: method shares of the uneven batch and of the request stream
+MIX_BATCH = {0: 0.40, 2: 0.30, 1: 0.20, 4: 0.10}                        # PCC2, 1-bit, GNCC, PCC1
+MIX_STREAM = {0: 0.38, 2: 0.285, 1: 0.19, 4: 0.095, 6: 0.05}            # ... and 5 % wavelet PCC
+WAVELET = dict(pmin=4.0, pmax=1000.0, V=5, type=-1)                      # Morlet, 40 scales
+METHOD_NAME = {0: "pcc2", 1: "gncc", 2: "cc1b", 3: "cc1b_popcount", 4: "pcc1", 6: "wpcc"}
+
+
+def _plain_call(F, m, a, b, l1, l2):
+    """One request through the plain drop-in of its method (own launch sequence)."""
+    if m == F.WPCC:
+        return F.wpcc_set(a, b, l1, l2, WAVELET["pmin"], WAVELET["pmax"], V=WAVELET["V"], type=WAVELET["type"])[0]
+    return F.correlate(m, a, b, l1, l2, plain=True)[0]
+
+
+def _oracle_call(O, m, a, b, l1, l2):
+    a, b = a[None], b[None]
+    if m == 0:
+        return O.pcc2(a, b, l1, l2)[0]
+    if m == 1:
+        return O.gncc(a, b, l1, l2)[0]
+    if m == 2:
+        return O.cc1b(a, b, l1, l2)[0]
+    if m == 4:
+        return O.pcc1(a, b, l1, l2)[0]
+    return O.wpcc(a, b, l1, l2, WAVELET["pmin"], WAVELET["pmax"], V=WAVELET["V"], wtype=WAVELET["type"])[0]
+
+
+def _serve_requests(F, srv, reqs, sta_of, outs=None):
+    """A Request array over reqs = [(method, s1, s2, window, Lag1, Lag2)] and its outputs."""
+    if outs is None:
+        outs = [np.zeros(abs(l2 - l1) + 1, np.float32) for (_, _, _, _, l1, l2) in reqs]
+    arr = F.Server.request_array([F.Server.request(m, sta_of(s1, w), sta_of(s2, w), w, l1, l2, o)
+                                  for (m, s1, s2, w, l1, l2), o in zip(reqs, outs)])
+    return arr, outs
+
+
+def _errors(O, F, reqs, outs, win, n_max, per_method=2):
+    """Max relative error per method over a few requests with short windows."""
+    err = {}
+    for (m, s1, s2, w, l1, l2), o in zip(reqs, outs):
+        N = win[w].shape[1]
+        name = METHOD_NAME[m]
+        if N > n_max or len(err.get(name, [])) >= per_method:
+            continue
+        y64 = _oracle_call(O, m, win[w][s1], win[w][s2], l1, l2)
+        err.setdefault(name, []).append(float(O.relerr(o[None], y64[None]).max()))
+    return {k: max(v) for k, v in err.items()}
+
+
+def uneven_batch_leg(F, n_pairs=500, fmt=1):
+    """500 pairs with window lengths log-uniform in 2^12-2^17 (5 % of samples in
+    gaps), lags +-(1-10 %) of the length, methods 40/30/20/10 % PCC2 / 1-bit /
+    GNCC / PCC1: the whole batch through the server (products computed on
+    demand, pair stages packed per method and padded length) against the plain
+    per-pair drop-in."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(41)
+    lengths = np.round(2.0 ** rng.uniform(12, 17, n_pairs)).astype(int)
+    from fastpcc_gb300 import synth
+    win = synth.uneven_windows(lengths, 2, gap_frac=0.05, tag="uneven-batch")
+    methods = rng.choice(list(MIX_BATCH), size=n_pairs, p=list(MIX_BATCH.values()))
+    reqs = []
+    for i in range(n_pairs):
+        M = max(1, int(rng.uniform(0.01, 0.10) * lengths[i]))
+        reqs.append((int(methods[i]), 0, 1, i, -M, M))
+    # plain: every pair through its method's plain drop-in
+    _plain_call(F, 0, win[0][0][None], win[0][1][None], -10, 10)
+    t0 = time.perf_counter()
+    for (m, s1, s2, w, l1, l2) in reqs:
+        _plain_call(F, m, win[w][s1][None], win[w][s2][None], l1, l2)
+    t_plain = time.perf_counter() - t0
+    srv = F.Server(hbm_budget=150 << 30, max_batch=8192, fmt=fmt)
+    for w in range(n_pairs):
+        srv.put(0, w, win[w][0])
+        srv.put(1, w, win[w][1])
+    arr, outs = _serve_requests(F, srv, reqs, lambda s, w: s)
+    t0 = time.perf_counter()
+    srv.submit_many(arr)
+    srv.drain()
+    t_cold = time.perf_counter() - t0
+    st = srv.stats()
+    srv.reset_stats()
+    t0 = time.perf_counter()
+    srv.submit_many(arr)
+    srv.drain()
+    t_warm = time.perf_counter() - t0
+    srv.close()
+    err = _errors(O, F, reqs, outs, win, n_max=1 << 14)
+    return {"workload": f"{n_pairs} pairs, window lengths log-uniform 2^12-2^17, 5 % gaps, lags +-(1-10 %), "
+                        "methods 40/30/20/10 % PCC2/1-bit/GNCC/PCC1",
+            "plain": {"value": n_pairs / t_plain, "unit": UNIT},
+            "batched": {"value": n_pairs / t_cold, "unit": UNIT, "batches": st["batches"],
+                        "what": "station products computed on demand, pair stages packed"},
+            "batched_resident": {"value": n_pairs / t_warm, "unit": UNIT, "what": "second pass, products resident"},
+            "speedup_vs_plain": t_plain / t_cold, "spectra": "f16" if fmt else "f32",
+            "max_rel_err": err, "err_sample": "2 requests per method with N <= 2^14 against the FP64 oracle"}
+
+
+def serving_leg(F, n_sta=200, n_win=8, n_req=4000, fmt=1, rates=(1e3, 1e4, 1e5, 1e6)):
+    """Request stream over a 200-station pool: window lengths lognormal (median
+    2^15, sigma 1) clipped to 2^12-2^18, lags +-(1-10 %), methods 38/28.5/19/9.5/5 %
+    PCC2 / 1-bit / GNCC / PCC1 / wavelet PCC; Poisson arrivals swept over the
+    offered rates, products cached under a 150 GB budget; the plain per-request
+    drop-in timed on a sample of the same requests."""
+    from oracle import oracle as O
+    from fastpcc_gb300 import synth
+    rng = np.random.default_rng(43)
+    lengths = np.clip(np.round(np.exp(rng.normal(np.log(2.0 ** 15), 1.0, n_win))), 2 ** 12, 2 ** 18).astype(int)
+    win = synth.uneven_windows(lengths, n_sta, tag="serving")
+    reqs = synth.mixed_requests(n_req, n_sta, lengths, MIX_STREAM, seed=6)
+    n_plain = 150
+    _plain_call(F, 0, win[0][0][None], win[0][1][None], -10, 10)
+    t0 = time.perf_counter()
+    for (m, s1, s2, w, l1, l2) in reqs[:n_plain]:
+        _plain_call(F, m, win[w][s1][None], win[w][s2][None], l1, l2)
+    t_plain = time.perf_counter() - t0
+    srv = F.Server(hbm_budget=150 << 30, max_batch=8192, fmt=fmt, wavelet=WAVELET)
+    for w in range(n_win):
+        for k in range(n_sta):
+            srv.put(k, w, win[w][k])
+    arr, outs = _serve_requests(F, srv, reqs, lambda s, w: s)
+    t0 = time.perf_counter()
+    srv.submit_many(arr)
+    srv.drain()
+    t_cold = time.perf_counter() - t0
+    srv.reset_stats()
+    t0 = time.perf_counter()
+    srv.submit_many(arr)
+    srv.drain()
+    t_warm = time.perf_counter() - t0
+    st_w = srv.stats()
+    sweep = []
+    for r in rates:
+        cnt = int(min(n_req, max(500, r * 1.0)))
+        srv.reset_stats()
+        t0 = time.perf_counter()
+        srv.submit_many(arr, poisson_rate=r, seed=int(r), count=cnt)
+        srv.drain()
+        dt = time.perf_counter() - t0
+        st = srv.stats()
+        sweep.append({"offered": r, "requests": cnt, "achieved": cnt / dt, "p50_ms": st["p50_ms"],
+                      "p99_ms": st["p99_ms"], "max_ms": st["max_ms"], "batches": st["batches"]})
+    hbm = srv.stats()["hbm_used"]
+    srv.close()
+    err = _errors(O, F, reqs, outs, win, n_max=20000)
+    plain = n_plain / t_plain
+    return {"workload": f"{n_req} requests, {n_sta} stations x {n_win} windows, lengths {sorted(lengths.tolist())}, "
+                        "lags +-(1-10 %), methods 38/28.5/19/9.5/5 % PCC2/1-bit/GNCC/PCC1/WPCC",
+            "plain": {"value": plain, "unit": UNIT, "sample": f"first {n_plain} requests"},
+            "served_saturation": {"value": n_req / t_warm, "unit": UNIT, "p50_ms": st_w["p50_ms"],
+                                  "p99_ms": st_w["p99_ms"], "batches": st_w["batches"],
+                                  "what": "all requests at once, products resident"},
+            "served_cold": {"value": n_req / t_cold, "unit": UNIT, "what": "products computed on demand"},
+            "speedup_vs_plain": (n_req / t_warm) / plain, "poisson": sweep, "hbm_used_bytes": hbm,
+            "spectra": "f16" if fmt else "f32", "max_rel_err": err,
+            "err_sample": "2 requests per method with N <= 20000 against the FP64 oracle"}
+
+
 def cpu_baseline(x, pairs, budget_s=12.0):
     """The oracle's PCC2 on host cores over a bounded sample of the workload."""
     from oracle import oracle as O
@@ -252,6 +412,11 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     F.build()
+    if args.mixed_only:
+        fmt = F.F16 if args.fmt == "f16" else F.F32
+        print(json.dumps({"uneven_batch": uneven_batch_leg(F, fmt=fmt), "serving": serving_leg(F, fmt=fmt)}),
+              flush=True)
+        return
     n_sta, n_win = args.stations, args.windows
     from fastpcc_gb300 import synth
     # weak scaling: rank r correlates its own block of windows
@@ -330,6 +495,9 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / t_pair / 1e9
     traffic = profiled_traffic()
+    if traffic is not None:
+        # the profile is of the default workload with F32 spectra
+        traffic = traffic * P / float(N_STA * (N_STA - 1) // 2 * N_WIN) if fmt == F.F32 else None
 
     # --- parity spot check against the oracle ---
     err = None
@@ -373,6 +541,10 @@ def run_ours(args):
     if rank == 0 and not args.no_served:
         served = served_leg(F, x, pairs, n_win, L)
 
+    mixed = None
+    if rank == 0 and not args.no_mixed:
+        mixed = {"uneven_batch": uneven_batch_leg(F), "serving": serving_leg(F)}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(x, pairs)
@@ -385,13 +557,14 @@ def run_ours(args):
             "data": "synthetic (seeded noise + shared band-passed component, per-station delays)",
             "config": {"workload": f"all-pairs PCC2: {n_sta} stations x {n_win} windows x {N_SAMP} samples, "
                                    f"{P} pair-windows per step, lags +-{LAG}",
-                       "Nz": Nz, "spectra": args.fmt, "l2": "inputs 221 MB and outputs 1.55 GB exceed L2; no flush",
+                       "Nz": Nz, "spectra": args.fmt, "l2": f"inputs {x.nbytes / 1e6:.0f} MB and outputs {P * L * 4 / 1e9:.2f} GB exceed L2; no flush",
                        "parallelism": f"replicas x{world}"},
             "max_rel_err": err,
             "latency_ms": {"p50": statistics.median(step_ms), "p99": float(np.percentile(step_ms, 99)),
-                           "what": "batched step (3072 station windows + 96768 correlations)"},
+                           "what": f"batched step ({x.shape[0]} station windows + {P} correlations)"},
             "plain": plain,
             "served": served,
+            "mixed": mixed,
             "gpu_launches": int(launches),
             "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -38,9 +38,16 @@ class Request(C.Structure):
                 ("Lag1", C.c_int), ("Lag2", C.c_int), ("v", C.c_float), ("y", C.c_void_p), ("num", C.c_void_p)]
 
 
+class PairDesc(C.Structure):
+    """fpcc_pair_desc: one correlation of a packed pair stage (device addresses)."""
+    _fields_ = [("a", C.c_void_p), ("b", C.c_void_p), ("ea", C.c_void_p), ("eb", C.c_void_p), ("y", C.c_void_p),
+                ("N", C.c_int32), ("lag0", C.c_int32), ("L", C.c_int32), ("scale", C.c_float)]
+
+
 class ServerStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("batches", C.c_int64), ("station_rows", C.c_int64),
-                ("hbm_used", C.c_int64), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double)]
+                ("hbm_used", C.c_int64), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
+                ("pair_stages", C.c_int64)]
 
 
 class FpccError(RuntimeError):
@@ -93,7 +100,11 @@ def lib():
             L.fpcc_wpcc_plan_set_band.argtypes = [vp, i, i]
             L.fpcc_wpcc_station_stage.argtypes = [vp, vp, vp, i64, i, vp, i]
             L.fpcc_wpcc_pair_stage.argtypes = [vp, vp, vp, i, vp, i, vp, i64]
+            L.fpcc_wpcc_plan_set_lags.argtypes = [vp, i, i]
+            L.fpcc_pair_stage_packed.argtypes = [vp, i, i, i, vp, i, i, f, i]
             L.fpcc_server_create.argtypes = [C.POINTER(vp), i, C.c_size_t, i]
+            L.fpcc_server_set_format.argtypes = [vp, i]
+            L.fpcc_server_set_wavelet.argtypes = [vp, d, d, u, i, d, i]
             L.fpcc_server_destroy.argtypes = [vp]
             L.fpcc_put_station_window.argtypes = [vp, C.c_int32, C.c_int32, vp, i]
             L.fpcc_submit.argtypes = [vp, C.POINTER(Request)]
@@ -187,7 +198,7 @@ def wpcc_set(x1, x2, Lag1, Lag2, pmin, pmax, V=2, type=-3, op1=0.0, rule=AMP_D_R
     """Wavelet PCC (reference tspcc2_set, src/FFTapps.c:1076): pmin/pmax in samples,
     V voices per octave, type -1 Morlet / -2 complete Morlet / -3 complex Mexican hat."""
     x1, x2, Tr, N = _windows(x1, x2)
-    y = np.zeros((Tr, abs(Lag2 - Lag1 + 1)), np.float32)
+    y = np.zeros((Tr, lag_count(Lag1, Lag2)), np.float32)
     check(lib().fpcc_wpcc_host(_rows(y), _rows(x1), _rows(x2), N, Tr, Lag1, Lag2, float(pmin), float(pmax),
                                V, type, float(op1), rule, nz_mode))
     return y
@@ -253,6 +264,11 @@ class Context:
                                     npairs, N, Nz, Lag1, Lag2, float(v), C.c_void_p(d_E or 0), ldE,
                                     C.c_void_p(d_y or 0), ldy, C.c_void_p(d_num or 0)))
 
+    def pair_stage_packed(self, method, fmt, Nz, d_desc, npairs, maxL, v=0.0, numerators=False):
+        """d_desc: device array of npairs PairDesc (lengths and lags per correlation)."""
+        check(lib().fpcc_pair_stage_packed(self._h, method, fmt, Nz, C.c_void_p(d_desc), npairs, maxL, float(v),
+                                           1 if numerators else 0))
+
     def allpairs_host(self, method, x, pairs, Lag1, Lag2, y, v=0.0, nz_mode=NZ_FAST, fmt=F32):
         """x: (nsta, N) float32 host array (pinned or pageable); pairs (npairs, 2) int32;
         y: (npairs, L) float32 host output."""
@@ -270,10 +286,25 @@ class Server:
     Outputs are written into numpy arrays owned by the caller; keep them alive
     until the request completes (``wait``/``drain``)."""
 
-    def __init__(self, device: int = 0, hbm_budget: int = 150 << 30, max_batch: int = 4096):
+    def __init__(self, device: int = 0, hbm_budget: int = 150 << 30, max_batch: int = 4096, fmt: int = F32,
+                 wavelet: dict = None):
+        """fmt: storage of cached phase spectra / phase signals (F32 or F16).
+        wavelet: family of WPCC requests, keys pmin, pmax, V, type, op1, rule
+        (as WpccPlan)."""
         self._h = C.c_void_p()
         check(lib().fpcc_server_create(C.byref(self._h), device, hbm_budget, max_batch))
         self._keep = {}
+        try:
+            if fmt != F32:
+                check(lib().fpcc_server_set_format(self._h, fmt))
+            if wavelet is not None:
+                w = dict(V=2, type=-3, op1=0.0, rule=AMP_D_REG)
+                w.update(wavelet)
+                check(lib().fpcc_server_set_wavelet(self._h, float(w["pmin"]), float(w["pmax"]), int(w["V"]),
+                                                    int(w["type"]), float(w["op1"]), int(w["rule"])))
+        except Exception:
+            self.close()
+            raise
 
     def close(self):
         if self._h:
@@ -359,6 +390,10 @@ class WpccPlan:
 
     def set_band(self, s_lo, s_hi):
         check(lib().fpcc_wpcc_plan_set_band(self._h, s_lo, s_hi))
+
+    def set_lags(self, Lag1, Lag2):
+        check(lib().fpcc_wpcc_plan_set_lags(self._h, Lag1, Lag2))
+        self.L = lag_count(Lag1, Lag2)
 
     def station_stage(self, d_x, ldx, nrows, d_P, fmt=F32):
         check(lib().fpcc_wpcc_station_stage(self.ctx.handle, self._h, C.c_void_p(d_x), ldx, nrows,

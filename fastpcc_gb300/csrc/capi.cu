@@ -602,6 +602,51 @@ extern "C" int fpcc_pair_stage(fpcc_ctx* c, int method, const void* d_station, i
   return fail(FPCC_EUNSUP, "method %d has no pair stage", method);
 }
 
+extern "C" int fpcc_pair_stage_packed(fpcc_ctx* c, int method, int fmt, int Nz, const fpcc_pair_desc* d_desc,
+                                      int npairs, int maxL, float v, int numerators) {
+  if (!c) return fail(FPCC_EARG, "null context");
+  if (npairs <= 0) return 0;
+  if (!d_desc || maxL <= 0) return fail(FPCC_EARG, "packed pair stage needs descriptors and maxL > 0");
+  if (npairs > 0x7fffffff / 2) return fail(FPCC_EARG, "too many pairs");
+  if (is_fft_method(method)) {
+    if ((Nz & 1) || !pair_supported(Nz))
+      return fail(FPCC_EUNSUP, "packed pair stage: Nz=%d is not an in-block length", Nz);
+    if (method != FPCC_PCC2 && fmt != FPCC_F32) return fail(FPCC_EUNSUP, "GNCC and 1-bit spectra are F32");
+    PairArgs a{};
+    a.fmt = fmt;
+    a.npairs = npairs;
+    a.Nz = Nz;
+    a.norm = method == FPCC_PCC2 ? 0 : (method == FPCC_GNCC ? 1 : 2);
+    a.desc = d_desc;
+    CK(launch_pairs(a, c->stream));
+    g_launches++;
+    return 0;
+  }
+  if (method == FPCC_PCC1 || method == FPCC_PCCV) {
+    PccvArgs a{};
+    a.half = (fmt == FPCC_F16);
+    a.npairs = npairs;
+    a.L = maxL;
+    a.v = (method == FPCC_PCC1) ? 1.0f : v;
+    a.norm_gpu = 1;
+    a.desc = d_desc;
+    CK(launch_pccv(a, c->stream));
+    g_launches++;
+    return 0;
+  }
+  if (method == FPCC_CC1B_POPCOUNT) {
+    Cc1bArgs a{};
+    a.npairs = npairs;
+    a.L = maxL;
+    a.desc = d_desc;
+    a.desc_num = numerators ? 1 : 0;
+    CK(launch_cc1b_popcount(a, c->stream));
+    g_launches++;
+    return 0;
+  }
+  return fail(FPCC_EUNSUP, "method %d has no packed pair stage", method);
+}
+
 // ============================================================== host entry points
 namespace {
 
@@ -935,6 +980,24 @@ extern "C" int fpcc_wpcc_plan_set_band(fpcc_wpcc_plan* p, int s_lo, int s_hi) {
   const cudaError_t e = cudaMemcpy(p->a, a.data(), S * sizeof(float), cudaMemcpyHostToDevice);
   cudaSetDevice(cur);
   if (e != cudaSuccess) return cuda_fail(e, "band weights");
+  return 0;
+}
+
+extern "C" int fpcc_wpcc_plan_set_lags(fpcc_wpcc_plan* p, int Lag1, int Lag2) {
+  if (!p) return fail(FPCC_EARG, "null plan");
+  const int N = p->dev.N;
+  int rc = check_lags(N, Lag1, Lag2);
+  if (rc) return rc;
+  const int M = abs(Lag1) > abs(Lag2) ? abs(Lag1) : abs(Lag2);
+  bool capped = false;
+  for (unsigned s = 0; s < p->su.wf.S; s++) capped |= (p->su.wf.Ls[s] >= p->su.Nz0);
+  // exact for any length holding the data, the lags and the longest wavelet; a
+  // family whose lengths hit the cap is the reference's only for lags giving
+  // the same cap 2^ceil(log2(N+M))
+  const unsigned cap = 1u << (unsigned)std::ceil(std::log2((double)(N + M)));
+  if (capped ? cap != p->su.Nz0 : N + M + (int)p->su.Ls0 > p->dev.Nz)
+    return fail(FPCC_EARG, "lags up to %d do not fit the plan's length Nz=%d", M, p->dev.Nz);
+  lag_window(Lag1, Lag2, &p->dev.lag0, &p->dev.L);
   return 0;
 }
 

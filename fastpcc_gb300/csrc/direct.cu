@@ -55,17 +55,38 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
   __shared__ float2 s1[kTile];
   __shared__ float2 s2[kTile + kLagBlock];
   const int p = blockIdx.x;
-  const int2 pr = a.pairs[p];
-  const int N = a.N;
   const int lblk = blockIdx.y * kLagBlock;       // first lag index of the block
   const int l = lblk + threadIdx.x;
-  const int lagb = a.Lag1 + lblk;                 // lag of thread 0
+  int N, Lag1, L;
+  const void* R1;
+  const void* R2;
+  float* y;
+  if (a.desc) {
+    const fpcc_pair_desc& d = a.desc[p];
+    N = d.N;
+    Lag1 = d.lag0;
+    L = d.L;
+    R1 = d.a;
+    R2 = d.b;
+    y = reinterpret_cast<float*>(d.y);
+    if (lblk >= L) return;                       // whole block beyond this pair's lags
+  } else {
+    const int2 pr = a.pairs[p];
+    N = a.N;
+    Lag1 = a.Lag1;
+    L = a.L;
+    const int64_t esz = HALF ? 4 : 8;
+    R1 = reinterpret_cast<const char*>(a.phase) + (int64_t)pr.x * a.ldp * esz;
+    R2 = reinterpret_cast<const char*>(a.phase) + (int64_t)pr.y * a.ldp * esz;
+    y = a.y + (int64_t)p * a.ldy;
+  }
+  const int lagb = Lag1 + lblk;                   // lag of thread 0
   const float V = 0.5f * a.v;
   double acc = 0.0;
-  const float2* P1f = reinterpret_cast<const float2*>(a.phase) + (int64_t)pr.x * a.ldp;
-  const float2* P2f = reinterpret_cast<const float2*>(a.phase) + (int64_t)pr.y * a.ldp;
-  const __half2* P1h = reinterpret_cast<const __half2*>(a.phase) + (int64_t)pr.x * a.ldp;
-  const __half2* P2h = reinterpret_cast<const __half2*>(a.phase) + (int64_t)pr.y * a.ldp;
+  const float2* P1f = reinterpret_cast<const float2*>(R1);
+  const float2* P2f = reinterpret_cast<const float2*>(R2);
+  const __half2* P1h = reinterpret_cast<const __half2*>(R1);
+  const __half2* P2h = reinterpret_cast<const __half2*>(R2);
   // samples n of station 1 that overlap any lag of the block
   int nlo = -(lagb + kLagBlock - 1);
   if (nlo < 0) nlo = 0;
@@ -102,9 +123,8 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
     acc += (double)part;
     __syncthreads();
   }
-  if (l < a.L) {
-    const int lag = a.Lag1 + l;
-    float* y = a.y + (int64_t)p * a.ldy;
+  if (l < L) {
+    const int lag = Lag1 + l;
     if (lag < -N || lag > N) { y[l] = 0.0f; return; }
     const double cnt = (double)(N - abs(lag));
     const double D = a.norm_gpu ? 2.0 * cnt : exp2((double)V) * cnt;
@@ -145,12 +165,26 @@ __device__ __forceinline__ uint32_t bits_at(const uint32_t* r, int nw, int b) {
 __global__ void __launch_bounds__(256) k_cc1b_popcount(Cc1bArgs a) {
   const int p = blockIdx.x;
   const int l = blockIdx.y * blockDim.x + threadIdx.x;
-  if (l >= a.L) return;
-  const int2 pr = a.pairs[p];
-  const int N = a.N, nw = (N + 31) >> 5;
-  const uint32_t* B1 = a.bits + (int64_t)pr.x * a.ldb;
-  const uint32_t* B2 = a.bits + (int64_t)pr.y * a.ldb;
-  const int lag = a.lag0 + l;
+  int N, lag0;
+  const uint32_t* B1;
+  const uint32_t* B2;
+  if (a.desc) {
+    const fpcc_pair_desc& d = a.desc[p];
+    if (l >= d.L) return;
+    N = d.N;
+    lag0 = d.lag0;
+    B1 = reinterpret_cast<const uint32_t*>(d.a);
+    B2 = reinterpret_cast<const uint32_t*>(d.b);
+  } else {
+    if (l >= a.L) return;
+    const int2 pr = a.pairs[p];
+    N = a.N;
+    lag0 = a.lag0;
+    B1 = a.bits + (int64_t)pr.x * a.ldb;
+    B2 = a.bits + (int64_t)pr.y * a.ldb;
+  }
+  const int nw = (N + 31) >> 5;
+  const int lag = lag0 + l;
   const int n1 = lag < 0 ? -lag : 0;
   const int n2 = lag < 0 ? N : N - lag;
   const int cnt = n2 - n1;
@@ -164,6 +198,11 @@ __global__ void __launch_bounds__(256) k_cc1b_popcount(Cc1bArgs a) {
     mism += __popc(d);
   }
   const long long num = (long long)cnt - 2LL * mism;
+  if (a.desc) {
+    if (a.desc_num) reinterpret_cast<long long*>(a.desc[p].y)[l] = num;
+    else reinterpret_cast<float*>(a.desc[p].y)[l] = (float)((double)num / (double)cnt);
+    return;
+  }
   if (a.num) a.num[(int64_t)p * a.ldy + l] = num;
   if (a.y) a.y[(int64_t)p * a.ldy + l] = (float)((double)num / (double)cnt);
 }

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/fastpcc_gb300.h"
+
 namespace fpcc {
 
 struct PccvArgs {
@@ -20,6 +22,7 @@ struct PccvArgs {
   int norm_gpu;        // 1: divide by 2(N-|lag|); 0: by 2^(v/2)(N-|lag|)
   float* y;
   int64_t ldy;
+  const fpcc_pair_desc* desc;   // packed mode: per-pair rows, N, lags, output (N, Lag1, L above: maxima)
 };
 
 struct Cc1bArgs {
@@ -33,6 +36,8 @@ struct Cc1bArgs {
   float* y;              // optional normalised output (num / overlap)
   long long* num;        // optional exact numerators
   int64_t ldy;
+  const fpcc_pair_desc* desc;   // packed mode (L above: the maximum); desc.y is int64 when desc_num
+  int desc_num;
 };
 
 cudaError_t launch_energy_prefix(const float* x, int64_t ldx, int nrows, int N, double* E, int64_t ldE,

@@ -145,12 +145,18 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
   __syncthreads();
   const TwTab twZ{zlo, zhi};
   constexpr int esz = (FMT == SPEC_F16) ? 4 : 8;
-  const int N = a.N;
   {
     const int p = blockIdx.x;
-    const int2 pr = a.pairs[p];
-    const char* X1 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.x * a.ldspec * esz;
-    const char* X2 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.y * a.ldspec * esz;
+    const char* X1;
+    const char* X2;
+    if (a.desc) {
+      X1 = reinterpret_cast<const char*>(a.desc[p].a);
+      X2 = reinterpret_cast<const char*>(a.desc[p].b);
+    } else {
+      const int2 pr = a.pairs[p];
+      X1 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.x * a.ldspec * esz;
+      X2 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.y * a.ldspec * esz;
+    }
 
     // F[k] = (H[k] + H[k+h]) + i w^k (H[k] - H[k+h]), H = Hermitian part of Z,
     // w = exp(2 pi i / Nz); the group {k, h-k} reads Z at k, h-k, h+k, Nz-k.
@@ -186,14 +192,37 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
       ct_fft<+1, T, 1>(s, 1, 0, TwTab{hlo, hhi}, RAD{});
     }
 
-    float* y = a.y + (int64_t)p * a.ldy;
-    const double* E1 = (a.norm == 1) ? a.energy + (int64_t)pr.x * a.ldE : nullptr;
-    const double* E2 = (a.norm == 1) ? a.energy + (int64_t)pr.y * a.ldE : nullptr;
-    for (int l = threadIdx.x; l < a.L; l += T) {
-      const int lag = a.lag0 + l;
+    float* y;
+    const double* E1 = nullptr;
+    const double* E2 = nullptr;
+    int N, lag0, L;
+    float scale;
+    if (a.desc) {
+      const PairDesc& d = a.desc[p];
+      y = reinterpret_cast<float*>(d.y);
+      if (a.norm == 1) { E1 = d.ea; E2 = d.eb; }
+      N = d.N;
+      lag0 = d.lag0;
+      L = d.L;
+      scale = d.scale != 0.0f ? d.scale
+                              : (a.norm == 0 ? 1.0f / ((float)NZ * (float)N) : (float)(1.0 / (double)NZ));
+    } else {
+      const int2 pr = a.pairs[p];
+      y = a.y + (int64_t)p * a.ldy;
+      if (a.norm == 1) {
+        E1 = a.energy + (int64_t)pr.x * a.ldE;
+        E2 = a.energy + (int64_t)pr.y * a.ldE;
+      }
+      N = a.N;
+      lag0 = a.lag0;
+      L = a.L;
+      scale = a.scale;
+    }
+    for (int l = threadIdx.x; l < L; l += T) {
+      const int lag = lag0 + l;
       const int idx = lag < 0 ? lag + NZ : lag;
       const float2 zz = res[PADI(idx >> 1)];
-      float v = ((idx & 1) ? zz.y : zz.x) * (0.5f * a.scale);
+      float v = ((idx & 1) ? zz.y : zz.x) * (0.5f * scale);
       if (a.norm == 1) {
         // overlap x1[n11,n12), x2[n21,n22) (src/FFTapps.c:896-902)
         int n11 = 0, n21 = 0, n12 = N, n22 = N;

@@ -4,9 +4,13 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/fastpcc_gb300.h"
 #include "fft_core.cuh"
 
 namespace fpcc {
+
+// One correlation of a packed launch (lengths and lags per entry).
+using PairDesc = fpcc_pair_desc;
 
 // Amplitude-normalisation rules of the reference.
 enum AmpRule : int {
@@ -57,6 +61,7 @@ struct PairArgs {
   const double* energy;  // per station row: N+1 prefix sums of x^2
   int64_t ldE;
   int N;
+  const PairDesc* desc;  // packed mode: per-pair rows, N, lags, output (the fields above unused)
 };
 
 // Per-row phase signal store for the direct-sum methods.

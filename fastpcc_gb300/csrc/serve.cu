@@ -3,9 +3,11 @@
 //
 // Requests (method, station pair, window, lag window) arrive from any host
 // thread.  A worker thread repeatedly takes everything pending (up to max_batch
-// requests), groups it by (method, window length, padded length, lag window,
-// power), computes the station products the group lacks — uploading raw windows
-// first — and launches one pair stage per group.  While a batch's kernels and
+// requests), groups it — by (method, padded length, power) where the pair
+// kernel takes per-correlation descriptors (window lengths and lag windows then
+// differ freely inside one launch), else by (method, window length, padded
+// length, lag window) — computes the station products the group lacks
+// (uploading raw windows first) and launches one pair stage per group.  While a batch's kernels and
 // output copy run, the worker is already forming the next batch: requests that
 // arrive meanwhile join it.  Completion is detected from CUDA events; the
 // worker copies each result into the caller's buffer and records its latency.
@@ -32,8 +34,11 @@
 
 #include "../../include/fastpcc_gb300.h"
 #include "engine.h"
+#include "kernels.cuh"
 #include "large.cuh"
 #include "serve.h"
+#include "wavelet.h"
+#include "wpcc.h"
 
 namespace fpcc {
 namespace {
@@ -72,14 +77,18 @@ struct Slab {
   std::list<int> lru;              // front = most recent
   std::vector<std::list<int>::iterator> pos;
   std::unordered_map<int64_t, int> row_of;
+  uint64_t last_use = 0;           // server tick of the last lookup or claim
 };
 
 struct Product {  // identifies a product class
   int kind;       // 0 raw window, 1 phase spectrum, 2 real half spectrum, 3 sign half spectrum (GE),
-                  // 4 sign half spectrum (GT), 5 energies, 6 phase signal, 7 bits GE, 8 bits GT
+                  // 4 sign half spectrum (GT), 5 energies, 6 phase signal, 7 bits GE, 8 bits GT,
+                  // 9 wavelet per-scale phase spectra (S x Nz)
   int N, Nz, fmt;
+  int aux = 0;    // kind 9: the wavelet length cap of the family
+  int S = 0;      // kind 9: scales
   bool operator<(const Product& o) const {
-    return std::tie(kind, N, Nz, fmt) < std::tie(o.kind, o.N, o.Nz, o.fmt);
+    return std::tie(kind, N, Nz, fmt, aux) < std::tie(o.kind, o.N, o.Nz, o.fmt, o.aux);
   }
 };
 
@@ -88,6 +97,7 @@ struct Req {
   fpcc_request r;
   Clock::time_point t_submit;
   int N = 0, Nz = 0, lag0 = 0, L = 0;
+  int aux = 0;    // WPCC: wavelet length cap
 };
 
 struct InFlight {
@@ -113,10 +123,21 @@ cudaError_t upload(InFlight& fl, void* dst, const void* src, size_t bytes, cudaS
 
 }  // namespace
 
+struct WaveletCfg {
+  bool set = false;
+  double pmin = 0, pmax = 0, op1 = 0;
+  unsigned V = 0;
+  int type = -1, rule = FPCC_AMP_D_REG, S = 0;
+};
+
 struct Server {
   int device = 0;
   size_t budget = 0, used = 0;
   int max_batch = 4096;
+  int fmt = FPCC_F32;                  // storage of phase spectra and phase signals
+  WaveletCfg wav;
+  std::map<std::pair<int, int>, std::pair<int, int>> wsetup;   // (N, M) -> (Nz, length cap)   [mu]
+  std::map<std::tuple<int, int, int>, fpcc_wpcc_plan*> wplans;  // (N, Nz, cap)   [worker]
   cudaStream_t st = nullptr;
   fpcc_ctx* ctx = nullptr;
   // host copies of registered windows
@@ -146,15 +167,18 @@ struct Server {
   void* d_idx = nullptr; size_t n_idx = 0;
   void* d_y = nullptr; size_t n_y = 0;
   void* d_pl = nullptr; size_t n_pl = 0;
+  void* d_desc = nullptr; size_t n_desc = 0;
   std::vector<void*> pinned_pool;
   // stats
   std::vector<double> lat_ms;
-  int64_t completed = 0, batches = 0, station_rows = 0;
+  int64_t completed = 0, batches = 0, station_rows = 0, pair_stages = 0;
   double busy_s = 0;
   int last_error = 0;
 };
 
 namespace {
+
+std::atomic<uint64_t> g_tick{0};   // recency clock of slab use
 
 int64_t wkey(int sta, int win) { return ((int64_t)sta << 32) | (uint32_t)win; }
 
@@ -165,22 +189,50 @@ size_t product_row_bytes(const Product& p) {
     case 2: case 3: case 4: return (size_t)(p.Nz / 2 + 1) * 8;
     case 5: return (size_t)(p.N + 1) * 8;
     case 6: return (size_t)p.N * (p.fmt ? 4 : 8);
+    case 9: return (size_t)p.S * p.Nz * (p.fmt ? 4 : 8);
     default: return (size_t)((p.N + 31) / 32) * 4;
   }
 }
 
 int64_t round16(int64_t b) { return (b + 15) & ~int64_t(15); }
 
+// Frees the least recently used slab (other than `keep`) none of whose rows a
+// batch in flight holds; its products are recomputed when next needed.
+bool release_idle_slab(Server* s, const Slab* keep) {
+  Slab* victim = nullptr;
+  for (auto& kv : s->slabs) {
+    Slab& c = kv.second;
+    if (&c == keep || !c.base) continue;
+    bool busy = false;
+    for (int r = 0; r < c.cap && !busy; r++) busy = c.pin[r] != 0;
+    if (busy) continue;
+    if (!victim || c.last_use < victim->last_use) victim = &c;
+  }
+  if (!victim) return false;
+  cudaStreamSynchronize(s->st);
+  cudaFree(victim->base);
+  s->used -= (size_t)victim->cap * victim->row_bytes;
+  victim->base = nullptr;
+  victim->cap = 0;
+  victim->key_of.clear();
+  victim->pin.clear();
+  victim->lru.clear();
+  victim->pos.clear();
+  victim->row_of.clear();
+  return true;
+}
+
 bool grow(Server* s, Slab& sl, int need_rows) {
   if (sl.cap >= need_rows) return true;
-  int ncap = std::max(need_rows, std::max(64, sl.cap * 2));
-  size_t add = (size_t)(ncap - sl.cap) * sl.row_bytes;
-  if (s->used + add > s->budget) {
-    // a tight budget: grow only to what is needed now, else recycle rows
-    ncap = need_rows;
-    add = (size_t)(ncap - sl.cap) * sl.row_bytes;
-    if (s->used + add > s->budget) return false;
+  // start at 64 rows, or fewer for rows of tens of MB (wavelet spectra), then double
+  const int64_t init = std::max<int64_t>(1, std::min<int64_t>(64, ((int64_t)256 << 20) / sl.row_bytes));
+  int ncap = std::max(need_rows, std::max((int)init, sl.cap * 2));
+  // over budget: grow only to what is needed now, then release idle slabs
+  while (s->used + (size_t)(ncap - sl.cap) * sl.row_bytes > s->budget) {
+    if (ncap > need_rows) { ncap = need_rows; continue; }
+    if (!release_idle_slab(s, &sl)) return false;
   }
+  const size_t add = (size_t)(ncap - sl.cap) * sl.row_bytes;
   void* nb = nullptr;
   if (cudaMalloc(&nb, (size_t)ncap * sl.row_bytes) != cudaSuccess) return false;
   if (sl.base) {
@@ -215,6 +267,7 @@ void touch(Slab& sl, int r) {
 
 // Row holding `key`, or -1.
 int find_row(Slab& sl, int64_t key) {
+  if (sl.base) sl.last_use = ++g_tick;
   auto it = sl.row_of.find(key);
   if (it == sl.row_of.end()) return -1;
   touch(sl, it->second);
@@ -227,6 +280,7 @@ void wait_one_retired(Server* s);
 // When every row is held by batches in flight, waits for them to finish
 // (admission by memory): only rows of the batch being built can then remain.
 int claim_row(Server* s, Slab& sl, int64_t key, int rows_needed_now) {
+  sl.last_use = ++g_tick;
   if ((int)sl.row_of.size() + rows_needed_now > sl.cap) grow(s, sl, std::max(sl.cap * 2, (int)sl.row_of.size() + rows_needed_now));
   for (;;) {
     for (auto it = sl.lru.rbegin(); it != sl.lru.rend(); ++it) {
@@ -262,10 +316,36 @@ namespace {
 struct GroupKey {
   int method, N, Nz, lag0, L, fmt;
   float v;
+  int aux;      // WPCC: wavelet length cap
   bool operator<(const GroupKey& o) const {
-    return std::tie(method, N, Nz, lag0, L, fmt, v) < std::tie(o.method, o.N, o.Nz, o.lag0, o.L, o.fmt, o.v);
+    return std::tie(method, N, Nz, lag0, L, fmt, v, aux) <
+           std::tie(o.method, o.N, o.Nz, o.lag0, o.L, o.fmt, o.v, o.aux);
   }
 };
+
+// Pair kernels that take per-correlation descriptors: every request of the
+// method (and padded length class) shares one launch.
+bool packable(int method, int Nz) {
+  if (method == FPCC_PCC1 || method == FPCC_PCCV || method == FPCC_CC1B_POPCOUNT) return true;
+  if (method == FPCC_PCC2 || method == FPCC_GNCC || method == FPCC_CC1B) return pair_supported(Nz);
+  return false;
+}
+
+int product_fmt(const Server* s, int method) {
+  return (method == FPCC_PCC2 || method == FPCC_PCC1 || method == FPCC_PCCV || method == FPCC_WPCC) ? s->fmt
+                                                                                                     : FPCC_F32;
+}
+
+void method_kinds(int m, int* kind1, int* kind2) {
+  switch (m) {
+    case FPCC_PCC2: *kind1 = *kind2 = 1; break;
+    case FPCC_GNCC: *kind1 = *kind2 = 2; break;
+    case FPCC_CC1B: *kind1 = 3; *kind2 = 4; break;
+    case FPCC_CC1B_POPCOUNT: *kind1 = 7; *kind2 = 8; break;
+    case FPCC_WPCC: *kind1 = *kind2 = 9; break;
+    default: *kind1 = *kind2 = 6; break;
+  }
+}
 
 // Ensure raw windows of the listed (sta, win) are on the device; returns rows.
 int ensure_raw(Server* s, int N, const std::vector<int64_t>& keys, std::vector<int>& rows, InFlight& fl) {
@@ -369,13 +449,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
     k2[i] = wkey(reqs[i]->r.sta2, reqs[i]->r.window);
   }
   int kind1, kind2;
-  switch (m) {
-    case FPCC_PCC2: kind1 = kind2 = 1; break;
-    case FPCC_GNCC: kind1 = kind2 = 2; break;
-    case FPCC_CC1B: kind1 = 3; kind2 = 4; break;
-    case FPCC_CC1B_POPCOUNT: kind1 = 7; kind2 = 8; break;
-    default: kind1 = kind2 = 6; break;
-  }
+  method_kinds(m, &kind1, &kind2);
   const int Nz = (m == FPCC_PCC1 || m == FPCC_PCCV || m == FPCC_CC1B_POPCOUNT) ? 0 : g.Nz;
   Product p1{kind1, g.N, Nz, g.fmt}, p2{kind2, g.N, Nz, g.fmt};
   std::vector<int> r1, r2;
@@ -463,6 +537,160 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
                          g.lag0 + g.L - 1, g.v, E, ldE, (float*)dy, g.L, nullptr);
   }
   if (rc) return rc;
+  cudaMemcpyAsync((char*)fl.h_out + out_base, dy, ybytes, cudaMemcpyDeviceToHost, s->st);
+  return 0;
+}
+
+// A group whose pair kernel takes descriptors: window lengths and lag windows
+// vary per request; products are ensured per window length, then every
+// correlation of the group runs in one launch reading its rows in place.
+int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base) {
+  const int n = (int)reqs.size();
+  const int m = g.method;
+  int kind1, kind2;
+  method_kinds(m, &kind1, &kind2);
+  const bool fft = (m == FPCC_PCC2 || m == FPCC_GNCC || m == FPCC_CC1B);
+  const int Nz = fft ? g.Nz : 0;
+  std::map<int, std::vector<int>> byN;
+  for (int i = 0; i < n; i++) byN[reqs[i]->N].push_back(i);
+  std::vector<int> r1(n), r2(n), e1(n), e2(n);
+  int rc;
+  for (auto& kv : byN) {
+    const int N = kv.first;
+    const std::vector<int>& ix = kv.second;
+    const int k = (int)ix.size();
+    std::vector<int64_t> all(2 * k);
+    for (int j = 0; j < k; j++) {
+      all[j] = wkey(reqs[ix[j]]->r.sta1, reqs[ix[j]]->r.window);
+      all[k + j] = wkey(reqs[ix[j]]->r.sta2, reqs[ix[j]]->r.window);
+    }
+    std::vector<int> rr;
+    if (kind1 == kind2) {
+      if ((rc = ensure_products(s, Product{kind1, N, Nz, g.fmt}, all, rr, fl))) return rc;
+      for (int j = 0; j < k; j++) { r1[ix[j]] = rr[j]; r2[ix[j]] = rr[k + j]; }
+    } else {
+      std::vector<int64_t> k1(all.begin(), all.begin() + k), k2(all.begin() + k, all.end());
+      std::vector<int> rb;
+      if ((rc = ensure_products(s, Product{kind1, N, Nz, g.fmt}, k1, rr, fl)) ||
+          (rc = ensure_products(s, Product{kind2, N, Nz, g.fmt}, k2, rb, fl)))
+        return rc;
+      for (int j = 0; j < k; j++) { r1[ix[j]] = rr[j]; r2[ix[j]] = rb[j]; }
+    }
+    if (m == FPCC_GNCC) {
+      if ((rc = ensure_products(s, Product{5, N, 0, 0}, all, rr, fl))) return rc;
+      for (int j = 0; j < k; j++) { e1[ix[j]] = rr[j]; e2[ix[j]] = rr[k + j]; }
+    }
+  }
+  // every product is in place (slabs no longer move): descriptors with row addresses
+  const size_t osz = (m == FPCC_CC1B_POPCOUNT) ? 8 : 4;
+  size_t total = 0;
+  for (int i = 0; i < n; i++) total += (size_t)reqs[i]->L * osz;
+  char* dy = (char*)dbuf(&s->d_y, &s->n_y, total);
+  void* dd = dbuf(&s->d_desc, &s->n_desc, (size_t)n * sizeof(fpcc_pair_desc));
+  if (!dy || !dd) return FPCC_ENOMEM;
+  std::vector<fpcc_pair_desc> d(n);
+  size_t off = 0;
+  int maxL = 0;
+  for (int i = 0; i < n; i++) {
+    const Req& q = *reqs[i];
+    Slab& sa = slab_of(s, Product{kind1, q.N, Nz, g.fmt});
+    Slab& sb = slab_of(s, Product{kind2, q.N, Nz, g.fmt});
+    fpcc_pair_desc& e = d[i];
+    memset(&e, 0, sizeof(e));
+    e.a = (const char*)sa.base + (int64_t)r1[i] * sa.row_bytes;
+    e.b = (const char*)sb.base + (int64_t)r2[i] * sb.row_bytes;
+    if (m == FPCC_GNCC) {
+      Slab& se = slab_of(s, Product{5, q.N, 0, 0});
+      e.ea = (const double*)((const char*)se.base + (int64_t)e1[i] * se.row_bytes);
+      e.eb = (const double*)((const char*)se.base + (int64_t)e2[i] * se.row_bytes);
+    }
+    e.y = dy + off;
+    off += (size_t)q.L * osz;
+    e.N = q.N;
+    e.lag0 = q.lag0;
+    e.L = q.L;
+    // the scales of the per-group pair stage (src/FFTapps.c:832, :340, :357)
+    e.scale = (m == FPCC_PCC2) ? 1.0f / ((float)Nz * (float)q.N) : (fft ? (float)(1.0 / (double)Nz) : 0.0f);
+    maxL = std::max(maxL, q.L);
+  }
+  if (upload(fl, dd, d.data(), d.size() * sizeof(fpcc_pair_desc), s->st) != cudaSuccess) return FPCC_ECUDA;
+  rc = fpcc_pair_stage_packed(s->ctx, m, g.fmt, Nz, (const fpcc_pair_desc*)dd, n, maxL, g.v,
+                              m == FPCC_CC1B_POPCOUNT);
+  if (rc) return rc;
+  cudaMemcpyAsync((char*)fl.h_out + out_base, dy, total, cudaMemcpyDeviceToHost, s->st);
+  return 0;
+}
+
+// Wavelet PCC plan of a window length, padded length and family cap (built once).
+fpcc_wpcc_plan* wpcc_plan_for(Server* s, int N, int Nz, int cap, int Lag1, int Lag2) {
+  auto key = std::make_tuple(N, Nz, cap);
+  auto it = s->wplans.find(key);
+  if (it != s->wplans.end()) return it->second;
+  fpcc_wpcc_plan* p = nullptr;
+  if (fpcc_wpcc_plan_create(s->ctx, &p, (unsigned)N, Lag1, Lag2, s->wav.pmin, s->wav.pmax, s->wav.V, s->wav.type,
+                            s->wav.op1, s->wav.rule, FPCC_NZ_FAST) != 0)
+    return nullptr;
+  int nz = 0;
+  fpcc_wpcc_plan_info(p, &nz, nullptr, nullptr);
+  if (nz != Nz) {   // the request's length came from the same rule; a mismatch is a bug
+    fpcc_wpcc_plan_destroy(p);
+    return nullptr;
+  }
+  s->wplans[key] = p;
+  return p;
+}
+
+// A WPCC group (one window length, padded length and lag window): per-scale
+// phase spectra of each station window are computed into their slab rows
+// directly, then one pair stage runs over the group.
+int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base) {
+  const int n = (int)reqs.size();
+  const int lag1 = reqs[0]->r.Lag1, lag2 = reqs[0]->r.Lag2;
+  fpcc_wpcc_plan* p = wpcc_plan_for(s, g.N, g.Nz, g.aux, lag1, lag2);
+  if (!p) return FPCC_EUNSUP;
+  int rc;
+  if ((rc = fpcc_wpcc_plan_set_lags(p, g.lag0, g.lag0 + g.L - 1))) return rc;
+  const Product pk{9, g.N, g.Nz, g.fmt, g.aux, s->wav.S};
+  Slab& sl = slab_of(s, pk);
+  std::vector<int64_t> keys(2 * n);
+  for (int i = 0; i < n; i++) {
+    keys[i] = wkey(reqs[i]->r.sta1, reqs[i]->r.window);
+    keys[n + i] = wkey(reqs[i]->r.sta2, reqs[i]->r.window);
+  }
+  std::vector<int> rows(2 * n);
+  std::vector<int64_t> miss_keys;
+  std::vector<int> miss_rows;
+  for (int i = 0; i < 2 * n; i++) {
+    int r = find_row(sl, keys[i]);
+    if (r < 0) {
+      r = claim_row(s, sl, keys[i], 2 * n - i);
+      if (r < 0) return FPCC_ENOMEM;
+      miss_keys.push_back(keys[i]);
+      miss_rows.push_back(r);
+    }
+    rows[i] = r;
+    sl.pin[r]++;
+    fl.pinned_rows.push_back({&sl, r});
+  }
+  if (!miss_keys.empty()) {
+    std::vector<int> raw_rows;
+    if ((rc = ensure_raw(s, g.N, miss_keys, raw_rows, fl))) return rc;
+    Slab& raw = slab_of(s, Product{0, g.N, 0, 0});
+    for (size_t i = 0; i < miss_keys.size(); i++) {
+      const float* x = (const float*)((const char*)raw.base + (int64_t)raw_rows[i] * raw.row_bytes);
+      void* dst = (char*)sl.base + (int64_t)miss_rows[i] * sl.row_bytes;
+      if ((rc = fpcc_wpcc_station_stage(s->ctx, p, x, g.N, 1, dst, g.fmt))) return rc;
+    }
+    s->station_rows += (int64_t)miss_keys.size();
+  }
+  std::vector<int32_t> pairs(2 * n);
+  for (int i = 0; i < n; i++) { pairs[2 * i] = rows[i]; pairs[2 * i + 1] = rows[n + i]; }
+  const size_t ybytes = (size_t)n * g.L * 4;
+  void* dpl = dbuf(&s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
+  void* dy = dbuf(&s->d_y, &s->n_y, ybytes);
+  if (!dpl || !dy) return FPCC_ENOMEM;
+  if (upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st) != cudaSuccess) return FPCC_ECUDA;
+  if ((rc = fpcc_wpcc_pair_stage(s->ctx, p, sl.base, g.fmt, (const int32_t*)dpl, n, (float*)dy, g.L))) return rc;
   cudaMemcpyAsync((char*)fl.h_out + out_base, dy, ybytes, cudaMemcpyDeviceToHost, s->st);
   return 0;
 }
@@ -603,13 +831,19 @@ void worker_main(Server* s) {
     InFlight* fl = new InFlight();
     std::map<GroupKey, std::vector<Req*>> groups;
     for (auto& q : batch) {
-      GroupKey g{q.r.method, q.N, q.Nz, q.lag0, q.L, 0, q.r.method == FPCC_PCCV ? q.r.v : 0.f};
+      const int m = q.r.method;
+      const float v = m == FPCC_PCCV ? q.r.v : 0.f;
+      const int f = product_fmt(s, m);
+      // packed groups carry N = -1 (lengths and lags per request)
+      GroupKey g = packable(m, q.Nz) ? GroupKey{m, -1, q.Nz, 0, 0, f, v, 0}
+                                     : GroupKey{m, q.N, q.Nz, q.lag0, q.L, f, v, q.aux};
       groups[g].push_back(&q);
     }
     size_t total = 0;
     for (auto& q : batch) total += (size_t)q.L * (q.r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
     fl->h_out = (char*)pinned_get(s, total, &fl->h_bytes);
-    fl->h_up = (char*)pinned_get(s, (size_t)16 * 4 * batch.size() + 1024 * (groups.size() + 4), &fl->up_bytes);
+    fl->h_up = (char*)pinned_get(s, (size_t)(16 * 4 + sizeof(fpcc_pair_desc)) * batch.size() + 1024 * (groups.size() + 4),
+                                 &fl->up_bytes);
     int err = (fl->h_out && fl->h_up) ? 0 : FPCC_ENOMEM;
     fl->reqs.reserve(batch.size());
     size_t off = 0;
@@ -621,7 +855,11 @@ void worker_main(Server* s) {
         fl->out_off.push_back((int64_t)off);
         off += (size_t)q->L * (q->r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
       }
-      err = run_group(s, kv.first, kv.second, *fl, base);
+      const GroupKey& g = kv.first;
+      if (g.method == FPCC_WPCC) err = run_group_wpcc(s, g, kv.second, *fl, base);
+      else if (g.N < 0) err = run_group_packed(s, g, kv.second, *fl, base);
+      else err = run_group(s, g, kv.second, *fl, base);
+      s->pair_stages++;
     }
     if (err) {
       cudaStreamSynchronize(s->st);
@@ -681,11 +919,42 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
   cudaSetDevice(s->device);
   cudaStreamSynchronize(s->st);
   for (auto& kv : s->slabs) if (kv.second.base) cudaFree(kv.second.base);
-  for (void** p : {&s->d_tmp_x, &s->d_tmp_p, &s->d_idx, &s->d_y, &s->d_pl}) if (*p) cudaFree(*p);
+  for (void** p : {&s->d_tmp_x, &s->d_tmp_p, &s->d_idx, &s->d_y, &s->d_pl, &s->d_desc}) if (*p) cudaFree(*p);
+  for (auto& kv : s->wplans) fpcc_wpcc_plan_destroy(kv.second);
   for (size_t i = 0; i < s->pinned_pool.size(); i += 2) cudaFreeHost(s->pinned_pool[i]);
   for (char* a : s->arena) cudaFreeHost(a);
   fpcc_destroy(s->ctx);
   delete s;
+  return 0;
+}
+
+extern "C" int fpcc_server_set_format(fpcc_server* h, int fmt) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s || (fmt != FPCC_F32 && fmt != FPCC_F16)) return FPCC_EARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->next_id) return FPCC_EARG;   // before the first request
+  s->fmt = fmt;
+  return 0;
+}
+
+extern "C" int fpcc_server_set_wavelet(fpcc_server* h, double pmin, double pmax, unsigned V, int type, double op1,
+                                       int rule) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s) return FPCC_EARG;
+  // the scale count is fixed by pmin, pmax, V and type; probe it on a long window
+  WpccSetup su;
+  if (wpcc_setup(1u << 20, 0, 0, pmin, pmax, V, type, op1, &su) != 0) return FPCC_EARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->next_id) return FPCC_EARG;
+  s->wav.set = true;
+  s->wav.pmin = pmin;
+  s->wav.pmax = pmax;
+  s->wav.V = V;
+  s->wav.type = type;
+  s->wav.op1 = op1;
+  s->wav.rule = rule;
+  s->wav.S = (int)su.wf.S;
+  s->wsetup.clear();
   return 0;
 }
 
@@ -737,6 +1006,30 @@ extern "C" int64_t fpcc_submit(fpcc_server* h, const fpcc_request* req) {
   } else if (m == FPCC_PCC1 || m == FPCC_PCCV || m == FPCC_CC1B_POPCOUNT) {
     q.Nz = 0;
     if ((m == FPCC_PCC1 || m == FPCC_PCCV) && req->Lag1 > req->Lag2) return FPCC_EARG;
+  } else if (m == FPCC_WPCC) {
+    std::pair<int, int> nz{0, 0};
+    bool known = false;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      if (!s->wav.set) return FPCC_EARG;
+      auto it = s->wsetup.find({N, M});
+      if (it != s->wsetup.end()) { nz = it->second; known = true; }
+    }
+    if (!known) {
+      WpccSetup su;
+      if (wpcc_setup((unsigned)N, req->Lag1, req->Lag2, s->wav.pmin, s->wav.pmax, s->wav.V, s->wav.type,
+                     s->wav.op1, &su) != 0)
+        return FPCC_EARG;
+      nz.first = wpcc_choose_nz(su, (unsigned)N, FPCC_NZ_FAST);
+      bool capped = false;
+      for (unsigned k = 0; k < su.wf.S; k++) capped |= (su.wf.Ls[k] >= su.Nz0);
+      nz.second = capped ? (int)su.Nz0 : 0;   // the family depends on the cap only when a length hit it
+      if (nz.first <= 0) return FPCC_EUNSUP;
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->wsetup[{N, M}] = nz;
+    }
+    q.Nz = nz.first;
+    q.aux = nz.second;
   } else {
     return FPCC_EUNSUP;
   }
@@ -798,6 +1091,7 @@ extern "C" int fpcc_server_get_stats(fpcc_server* h, fpcc_server_stats* o) {
   o->p50_ms = pct(0.50);
   o->p99_ms = pct(0.99);
   o->max_ms = v.empty() ? 0.0 : v.back();
+  o->pair_stages = s->pair_stages;
   return 0;
 }
 
@@ -808,6 +1102,7 @@ extern "C" int fpcc_server_reset_stats(fpcc_server* h) {
   s->lat_ms.clear();
   s->batches = 0;
   s->station_rows = 0;
+  s->pair_stages = 0;
   return 0;
 }
 

@@ -94,3 +94,41 @@ def gaps(x: np.ndarray, frac=0.05, lo=50, hi=2000, seed_tag="gaps") -> np.ndarra
         x[s:s + g] = 0
         zeroed += g
     return x
+
+
+def uneven_windows(lengths, n_stations, fs=10.0, band=(0.05, 2.0), snr=0.3, max_delay=1500, gap_frac=0.0,
+                   tag="uneven"):
+    """One window per entry of ``lengths`` shared by all stations: a list of
+    float32 arrays (n_stations, lengths[w]); with ``gap_frac`` > 0 each trace has
+    that fraction of its samples zeroed in gaps of 50-2000 samples."""
+    rng = np.random.Generator(np.random.PCG64(_seed(tag, "delays")))
+    delays = rng.integers(-max_delay, max_delay + 1, size=n_stations)
+    out = []
+    for w, N in enumerate(lengths):
+        N = int(N)
+        d = np.clip(delays, -(N // 4), N // 4)
+        x = stations(f"{tag}/{w}", n_stations, 1, N, d, fs, band, snr)[:, 0]
+        if gap_frac > 0:
+            for k in range(n_stations):
+                x[k] = gaps(x[k], frac=gap_frac, seed_tag=f"{tag}/gaps/{w}/{k}")
+        out.append(x)
+    return out
+
+
+def mixed_requests(n_req, n_stations, lengths, mix, seed, lag_lo=0.01, lag_hi=0.10):
+    """Requests (method, station 1, station 2, window, Lag1, Lag2): a random
+    station pair, a window drawn uniformly, symmetric lags of half-width
+    U[lag_lo, lag_hi] x the window length, and the method drawn from ``mix``
+    ({method: probability})."""
+    rng = np.random.Generator(np.random.PCG64(_seed("mixed-requests", seed)))
+    methods = list(mix)
+    p = np.asarray([mix[m] for m in methods], np.float64)
+    p /= p.sum()
+    out = []
+    for _ in range(n_req):
+        w = int(rng.integers(0, len(lengths)))
+        N = int(lengths[w])
+        s1, s2 = rng.choice(n_stations, 2, replace=False)
+        M = max(1, min(N - 1, int(rng.uniform(lag_lo, lag_hi) * N)))
+        out.append((int(methods[rng.choice(len(methods), p=p)]), int(s1), int(s2), w, -M, M))
+    return out

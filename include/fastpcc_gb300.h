@@ -109,6 +109,23 @@ int fpcc_pair_stage(fpcc_ctx *ctx, int method, const void *d_station, int64_t ld
                     const int32_t *d_pairs, int npairs, int N, int Nz, int Lag1, int Lag2, float v,
                     const double *d_E, int64_t ldE, float *d_y, int64_t ldy, int64_t *d_num);
 
+/* Packed pair stage: correlations of different window lengths and lag windows
+ * in one launch.  Each descriptor names its own product rows (anywhere in device
+ * memory), window length, lags and output row; only the padded length Nz (FFT
+ * methods; must satisfy Nz >= N + max|lag| for every entry and be at most
+ * 2 * fpcc_max_block_len()), the storage format and the power v are shared.
+ * d_desc is a device array of npairs descriptors; maxL >= every entry's L.
+ * scale: 0 selects the method's own (PCC2 1/(Nz N), GNCC and 1-bit 1/Nz). */
+typedef struct {
+  const void *a, *b;          /* station-1 / station-2 product rows                    */
+  const double *ea, *eb;      /* GNCC: energy prefix sums of the two windows (N+1)     */
+  void *y;                    /* output row: L floats (L int64 for popcount numerators) */
+  int32_t N, lag0, L;         /* window length, first lag, number of lags              */
+  float scale;
+} fpcc_pair_desc;
+int fpcc_pair_stage_packed(fpcc_ctx *ctx, int method, int fmt, int Nz, const fpcc_pair_desc *d_desc,
+                           int npairs, int maxL, float v, int numerators);
+
 /* ---- host-buffer entry points (row-pointer arrays like the reference's *_set)
  * x1, x2: Tr rows of N floats (station 1 / station 2 windows); y: Tr rows of L.
  * The "batched" calls run each stage once over all windows; the plain drop-ins
@@ -148,6 +165,9 @@ int fpcc_wpcc_plan_info(const fpcc_wpcc_plan *p, int *Nz, int *S, int *L);
 /* Accumulate only scales s_lo <= s < s_hi (per-band diagnostics; the output
  * scale keeps all scales).  fpcc_wpcc_plan_set_band(p, 0, S) restores the plan. */
 int fpcc_wpcc_plan_set_band(fpcc_wpcc_plan *p, int s_lo, int s_hi);
+/* Change the plan's lag window (station products stay valid); lags must fit the
+ * plan's padded length. */
+int fpcc_wpcc_plan_set_lags(fpcc_wpcc_plan *p, int Lag1, int Lag2);
 int fpcc_wpcc_plan_destroy(fpcc_wpcc_plan *p);
 int fpcc_wpcc_station_stage(fpcc_ctx *ctx, const fpcc_wpcc_plan *p, const float *d_x, int64_t ldx, int nrows,
                             void *d_P, int fmt);
@@ -168,7 +188,7 @@ int fpcc_wpcc_host(float **y, float **x1, float **x2, unsigned N, unsigned Tr, i
  * computed on first use and recycled least-recently-used. */
 typedef struct fpcc_server fpcc_server;
 typedef struct {
-  int method;            /* FPCC_PCC2, GNCC, CC1B, CC1B_POPCOUNT, PCC1, PCCV          */
+  int method;            /* FPCC_PCC2, GNCC, CC1B, CC1B_POPCOUNT, PCC1, PCCV, WPCC    */
   int32_t sta1, sta2;    /* station ids (station 1 = virtual source)                  */
   int32_t window;        /* window id, registered for both stations                   */
   int Lag1, Lag2;
@@ -179,8 +199,16 @@ typedef struct {
 typedef struct {
   int64_t completed, batches, station_rows, hbm_used;
   double p50_ms, p99_ms, max_ms;   /* submit -> result latency of completed requests */
+  int64_t pair_stages;             /* pair-stage launches (one per group of a batch)  */
 } fpcc_server_stats;
 int fpcc_server_create(fpcc_server **out, int device, size_t hbm_budget_bytes, int max_batch);
+/* Storage format (FPCC_F32 / FPCC_F16) of the phase spectra and phase signals
+ * the server caches (PCC2, PCC1, PCCV, WPCC); before the first request. */
+int fpcc_server_set_format(fpcc_server *s, int fmt);
+/* Wavelet family of FPCC_WPCC requests (arguments of fpcc_wpcc_plan_create);
+ * before the first request.  WPCC requests fail with FPCC_EARG without it. */
+int fpcc_server_set_wavelet(fpcc_server *s, double pmin, double pmax, unsigned V, int type, double op1,
+                            int rule);
 int fpcc_server_destroy(fpcc_server *s);
 int fpcc_put_station_window(fpcc_server *s, int32_t sta, int32_t window, const float *x, int N);
 /* Returns a request id (>= 0) or a negative FPCC_E* code. */

@@ -75,6 +75,18 @@ def _run(F, srv, reqs):
     return outs
 
 
+def _run_many(F, srv, reqs):
+    """All requests in one submit_many call (arrivals faster than a batch)."""
+    outs, rs = [], []
+    for (m, s1, s2, w, l1, l2, v) in reqs:
+        out = np.zeros(abs(l2 - l1) + 1, np.int64 if m == F.CC1B_POPCOUNT else np.float32)
+        outs.append(out)
+        rs.append(srv.request(m, s1, s2, w, l1, l2, out, v))
+    srv.submit_many(rs)
+    srv.drain()
+    return outs
+
+
 def test_server_mixed_methods_against_oracle_and_alone(F, orc):
     xa = _stations(6, 2, 3000, "serve/a")
     xb = _stations(4, 2, 4800, "serve/b")
@@ -138,3 +150,131 @@ def test_server_concurrent_submitters(F, orc):
     srv.close()
     for (m, s1, s2, w, l1, l2, v), out in zip(jobs, outs):
         assert relerr(out, orc.pcc2(x[s1, w][None], x[s2, w][None], l1, l2)[0]) < TOL
+
+
+def _uneven(seed, n_req, lengths, methods):
+    """Requests over windows of uneven lengths (one length per window id) with
+    lag windows of 1-10 % of the length, drawn per request."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for _ in range(n_req):
+        w = int(rng.integers(0, len(lengths)))
+        N = lengths[w]
+        m = int(rng.choice(methods))
+        s1, s2 = rng.choice(5, 2, replace=False)
+        M = max(1, int(rng.uniform(0.01, 0.10) * N))
+        l1, l2 = (-M, M) if rng.random() < 0.7 else (-M, int(rng.integers(-M, M + 1)))
+        if m == 4 and l1 > l2:
+            l1, l2 = l2, l1
+        reqs.append((m, int(s1), int(s2), w, l1, l2, 0.0))
+    return reqs
+
+
+def _uneven_windows(lengths, tag):
+    xs = {}
+    for w, N in enumerate(lengths):
+        x = _stations(5, 1, N, f"{tag}/{N}")[:, 0]
+        gap = np.random.default_rng(N).integers(0, N - 60)
+        x[:, gap:gap + 50] = 0.0
+        xs[w] = x
+    return xs
+
+
+def test_server_uneven_lengths_share_launches(F, orc):
+    # window lengths with large prime factors (Bluestein analytic signals), one per window id
+    lengths = [1499, 2003, 2500, 3001, 3457, 4096, 4801]
+    xs = _uneven_windows(lengths, "serve/uneven")
+    reqs = _uneven(5, 120, lengths, [0, 0, 1, 2, 3, 4])
+    srv = F.Server(hbm_budget=2 << 30, max_batch=4096)
+    for w, x in xs.items():
+        for s in range(5):
+            srv.put(s, w, x[s])
+    outs = _run_many(F, srv, reqs)
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(reqs)
+    for (m, s1, s2, w, l1, l2, v), out in zip(reqs, outs):
+        a, b = xs[w][s1], xs[w][s2]
+        if m == F.CC1B_POPCOUNT:
+            assert np.array_equal(out, orc.cc1b_num(a[None], b[None], l1, l2)[0])
+        else:
+            assert relerr(out, _oracle(orc, m, a, b, l1, l2, v)) < TOL, (m, len(a), l1, l2)
+    # pair stages are packed per (method, padded length) instead of per request
+    n_groups = len({(m, F.choose_nz(lengths[w], l1, l2) if m in (0, 1, 2) else 0)
+                    for (m, s1, s2, w, l1, l2, v) in reqs})
+    assert st["batches"] <= 4
+    assert st["pair_stages"] <= n_groups * st["batches"] and n_groups < len(reqs) // 3
+    for i in range(0, len(reqs), 17):
+        alone = F.Server(hbm_budget=1 << 30)
+        for w, x in xs.items():
+            for s in range(5):
+                alone.put(s, w, x[s])
+        (o,) = _run(F, alone, [reqs[i]])
+        alone.close()
+        assert np.array_equal(o, outs[i]), reqs[i]
+
+
+def test_server_f16_storage(F, orc):
+    lengths = [2048, 3000, 3557]
+    xs = _uneven_windows(lengths, "serve/f16")
+    reqs = _uneven(9, 40, lengths, [0, 4])
+    srv = F.Server(hbm_budget=1 << 30, fmt=F.F16)
+    for w, x in xs.items():
+        for s in range(5):
+            srv.put(s, w, x[s])
+    outs = _run(F, srv, reqs)
+    srv.close()
+    for (m, s1, s2, w, l1, l2, v), out in zip(reqs, outs):
+        a, b = xs[w][s1], xs[w][s2]
+        # FP16 storage of unit-modulus phase spectra / phase signals, FP32 arithmetic
+        assert relerr(out, _oracle(orc, m, a, b, l1, l2, v)) < 3e-4, (m, len(a), l1, l2)
+
+
+def test_server_wpcc_requests(F, orc):
+    wav = dict(pmin=4.0, pmax=100.0, V=3, type=-1)
+    lengths = [3000, 4096]
+    xs = _uneven_windows(lengths, "serve/wpcc")
+    reqs = [(6, 0, 1, 0, -200, 200, 0.0), (6, 2, 3, 0, -200, 200, 0.0), (6, 1, 4, 1, -350, 100, 0.0),
+            (0, 0, 1, 0, -200, 200, 0.0), (6, 0, 1, 0, -60, 60, 0.0), (6, 3, 2, 1, -350, 100, 0.0)]
+    srv = F.Server(hbm_budget=2 << 30, wavelet=wav)
+    for w, x in xs.items():
+        for s in range(5):
+            srv.put(s, w, x[s])
+    outs = _run(F, srv, reqs)
+    srv.close()
+    for (m, s1, s2, w, l1, l2, v), out in zip(reqs, outs):
+        a, b = xs[w][s1], xs[w][s2]
+        if m == 6:
+            y64 = orc.wpcc(a[None], b[None], l1, l2, wav["pmin"], wav["pmax"], V=wav["V"], wtype=wav["type"])[0]
+            assert relerr(out, y64) < TOL, (l1, l2)
+            # the same as the host-buffer WPCC call at the same padded length
+            yh = F.wpcc_set(a, b, l1, l2, wav["pmin"], wav["pmax"], V=wav["V"], type=wav["type"])[0]
+            assert relerr(out, yh) < 1e-6
+        else:
+            assert relerr(out, orc.pcc2(a[None], b[None], l1, l2)[0]) < TOL
+    with pytest.raises(F.FpccError):
+        plain = F.Server(hbm_budget=1 << 30)
+        plain.put(0, 0, xs[0][0])
+        plain.put(1, 0, xs[0][1])
+        try:
+            plain.submit(6, 0, 1, 0, -10, 10, np.zeros(21, np.float32))
+        finally:
+            plain.close()
+
+
+def test_server_releases_idle_product_classes(F, orc):
+    # each window length is its own product class; the budget holds about one
+    # class at a time, so classes are released and rebuilt as requests move on
+    lengths = [2000, 2400, 2800]
+    xs = _uneven_windows(lengths, "serve/release")
+    reqs = [(0, i, j, w, -100, 100, 0.0) for w in (0, 1, 2, 0) for i in range(5) for j in range(5) if i < j]
+    srv = F.Server(hbm_budget=600 << 10, max_batch=10)
+    for w, x in xs.items():
+        for s in range(5):
+            srv.put(s, w, x[s])
+    outs = _run(F, srv, reqs)
+    st = srv.stats()
+    srv.close()
+    assert st["station_rows"] > 15
+    for (m, s1, s2, w, l1, l2, v), out in zip(reqs, outs):
+        assert relerr(out, orc.pcc2(xs[w][s1][None], xs[w][s2][None], l1, l2)[0]) < TOL
