@@ -27,6 +27,7 @@ AMP_F_REG, AMP_D_REG, AMP_PURE, AMP_THRESH, AMP_SUMTHR = 0, 1, 2, 3, 4
 F32, F16 = 0, 1
 SIGN_GE, SIGN_GT = 0, 1
 NZ_REFERENCE, NZ_FAST = 0, 1
+ANALYTIC_F32, ANALYTIC_AUTO, ANALYTIC_F64 = 0, 1, 2
 
 _lock = threading.Lock()
 _lib = None
@@ -85,6 +86,8 @@ def lib():
             L.fpcc_station_row_elems.argtypes = [i, i, i]
             L.fpcc_station_row_elems.restype = i64
             L.fpcc_station_stage.argtypes = [vp, i, vp, i64, i, i, i, i, i, vp, i64]
+            L.fpcc_station_stage_ex.argtypes = [vp, i, vp, i64, i, i, i, i, i, vp, i64, vp, i]
+            L.fpcc_set_analytic_precision.argtypes = [vp, i]
             L.fpcc_energy_stage.argtypes = [vp, vp, i64, i, i, vp, i64]
             L.fpcc_pair_stage.argtypes = [vp, i, vp, i64, i, vp, i, i, i, i, i, f, vp, i64, vp, i64, vp]
             L.fpcc_host_batched.argtypes = [i, fpp, fpp, fpp, u, u, i, i, f, i, i]
@@ -250,6 +253,10 @@ class Context:
 
     def sync(self):
         check(lib().fpcc_sync(self._h))
+
+    def set_analytic_precision(self, mode):
+        """ANALYTIC_F32, ANALYTIC_AUTO (FP64 for windows with zero runs) or ANALYTIC_F64."""
+        check(lib().fpcc_set_analytic_precision(self._h, mode))
 
     def station_stage(self, method, d_x, ldx, nrows, N, Nz, fmt, rule, d_out, ldo):
         check(lib().fpcc_station_stage(self._h, method, C.c_void_p(d_x), ldx, nrows, N, Nz, fmt, rule,

@@ -10,6 +10,7 @@
 #include <semaphore.h>
 #include <cmath>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/fastpcc_gb300.h"
@@ -21,6 +22,7 @@
 #include "menu.cuh"
 #include "wavelet.h"
 #include "wpcc.h"
+#include "precise.cuh"
 
 using namespace fpcc;
 
@@ -60,11 +62,14 @@ struct fpcc_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  DevBuf dev[24];
+  DevBuf dev[32];
   DevBuf pin[8];
   cudaStream_t stream2 = nullptr;   // second stream of the pipelined drop-ins
   std::map<int, float2*> twiddles;   // device tables exp(-2 pi i t/n), per n
   std::map<int, float2*> bluestein;  // per window length N: M-point filter spectra, forward then inverse
+  std::map<int, double2*> twiddles64;   // FP64 tables exp(-2 pi i t/n)
+  std::map<int, double2*> bluestein64;  // FP64 filter spectra per N, forward then inverse
+  int precision = FPCC_ANALYTIC_AUTO;   // when analytic signals are computed in FP64
   std::mutex mu;
 };
 
@@ -163,6 +168,8 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
   for (auto& b : c->pin) if (b.p) cudaFreeHost(b.p);
   for (auto& kv : c->twiddles) cudaFree(kv.second);
   for (auto& kv : c->bluestein) cudaFree(kv.second);
+  for (auto& kv : c->twiddles64) cudaFree(kv.second);
+  for (auto& kv : c->bluestein64) cudaFree(kv.second);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
   {
@@ -170,6 +177,13 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
     if (c == g_default) g_default = nullptr;
   }
   delete c;
+  return 0;
+}
+
+extern "C" int fpcc_set_analytic_precision(fpcc_ctx* c, int mode) {
+  if (!c) return fail(FPCC_EARG, "null context");
+  if (mode < FPCC_ANALYTIC_F32 || mode > FPCC_ANALYTIC_F64) return fail(FPCC_EARG, "unknown precision mode %d", mode);
+  c->precision = mode;
   return 0;
 }
 
@@ -229,7 +243,8 @@ namespace {
 // Workspace slots of the context.
 enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_PAIRS = 5, S_ANA_A = 6,
             S_ANA_B = 7, S_RSTAT = 8, S_LARGE_T = 9, S_WP_X = 10, S_WP_BAND = 11, S_WP_RMAX = 12,
-            S_WP_Y = 13, S_WP_STAGE = 14, S_BLUE_O = 23 };
+            S_WP_Y = 13, S_WP_STAGE = 14, S_BLUE_O = 23, S_P64_D = 24, S_P64_A = 25, S_P64_B = 26,
+            S_P64_CNT = 27 };
 
 constexpr size_t kLargeChunkBytes = size_t(512) << 20;   // four-step intermediate per chunk
 
@@ -285,13 +300,14 @@ int large_pairs(fpcc_ctx* c, const PairArgs& q, int herm) {
     a.nrows = (int)((q.npairs - p0) < chunk ? (q.npairs - p0) : chunk);
     a.cmode = COL_PAIR;
     a.spec = q.spec; a.ldspec = q.ldspec; a.fmt = q.fmt; a.herm = herm;
-    a.pairs = q.pairs + p0;
+    if (q.desc) a.desc = q.desc + p0;
+    else a.pairs = q.pairs + p0;
     a.Nz = q.Nz;
     a.T = (float2*)T;
     a.rmode = ROW_LAGS;
     a.lag0 = q.lag0; a.L = q.L; a.scale = q.scale; a.norm = q.norm;
     a.energy = q.energy; a.ldE = q.ldE; a.N = q.N;
-    a.y = q.y + (size_t)p0 * q.ldy; a.ldy = q.ldy;
+    if (!q.desc) { a.y = q.y + (size_t)p0 * q.ldy; a.ldy = q.ldy; }
     CK(launch_large(a, c->stream));
     g_launches += 2;
   }
@@ -341,6 +357,155 @@ int smooth_at_least(int n) {
     int a, b, cc;
     if (factor235(m, &a, &b, &cc)) return m;
   }
+}
+
+// ---------------------------------------------------------------- FP64 analytic signals
+// Rows with at least FPCC_F64_ZERO_SAMPLES zero samples get FP64 analytic
+// signals in the automatic mode (runs of zeros are where FP32 transforms lose
+// the phase).
+constexpr int kZeroSamples = FPCC_F64_ZERO_SAMPLES;
+
+int twiddle64(fpcc_ctx* c, int n, const double2** out) {
+  auto it = c->twiddles64.find(n);
+  if (it != c->twiddles64.end()) { *out = it->second; return 0; }
+  std::vector<double2> h(n);
+  for (int t = 0; t < n; t++) {
+    const double a = -2.0 * M_PI * (double)t / (double)n;
+    h[t] = make_double2(cos(a), sin(a));
+  }
+  double2* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, (size_t)n * sizeof(double2));
+  if (e != cudaSuccess) return fail(FPCC_ENOMEM, "FP64 twiddle table: %s", cudaGetErrorString(e));
+  e = cudaMemcpy(d, h.data(), (size_t)n * sizeof(double2), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(d); return cuda_fail(e, "FP64 twiddle upload"); }
+  c->twiddles64[n] = d;
+  *out = d;
+  return 0;
+}
+
+// Radix-4/2/3/5 schedule of n (empty when n has another prime factor).
+std::vector<int> radices64(int n) {
+  std::vector<int> r;
+  while (n % 4 == 0) { r.push_back(4); n /= 4; }
+  if (n % 2 == 0) { r.push_back(2); n /= 2; }
+  while (n % 3 == 0) { r.push_back(3); n /= 3; }
+  while (n % 5 == 0) { r.push_back(5); n /= 5; }
+  if (n != 1) r.clear();
+  return r;
+}
+
+// n-point FP64 transforms of nrows rows held in A (ping-pong with B); *res gets the result.
+int passes64(fpcc_ctx* c, double2* A, double2* B, int n, int nrows, int dir, double2** res) {
+  const std::vector<int> rad = radices64(n);
+  if (rad.empty() && n != 1) return fail(FPCC_EUNSUP, "length %d is not 2,3,5-smooth", n);
+  const double2* tw = nullptr;
+  int rc = twiddle64(c, n, &tw);
+  if (rc) return rc;
+  double2* bufs[2] = {A, B};
+  int cur = 0, Ns = 1;
+  for (int R : rad) {
+    CK(launch_pass64(R, dir, bufs[cur], bufs[cur ^ 1], n, Ns, nrows, tw, c->stream));
+    g_launches++;
+    cur ^= 1;
+    Ns *= R;
+  }
+  *res = bufs[cur];
+  return 0;
+}
+
+// DFT_N (dir) of nrows FP64 rows of stride N in D, in place, by Bluestein
+// transforms of length M on the buffers A and B.
+int bluestein64(fpcc_ctx* c, double2* D, double2* A, double2* B, int N, int M, int nrows, int dir) {
+  double2* F = nullptr;
+  auto it = c->bluestein64.find(N);
+  if (it == c->bluestein64.end()) {
+    CK(cudaMalloc(&F, (size_t)2 * M * sizeof(double2)));
+    for (int d = 0; d < 2; d++) {
+      double2* f = F + (size_t)d * M;
+      CK(launch_blue_filter64(f, N, M, d ? +1 : -1, c->stream));
+      double2* r = nullptr;
+      int rc = passes64(c, f, B, M, 1, -1, &r);
+      if (rc) { cudaFree(F); return rc; }
+      if (r != f) CK(cudaMemcpyAsync(f, r, (size_t)M * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    c->bluestein64[N] = F;
+  } else {
+    F = it->second;
+  }
+  CK(launch_blue_pre64(D, N, A, N, M, dir, nrows, c->stream));
+  double2* r1 = nullptr;
+  int rc = passes64(c, A, B, M, nrows, -1, &r1);
+  if (rc) return rc;
+  CK(launch_blue_mul64(r1, F + (size_t)(dir > 0 ? 1 : 0) * M, M, nrows, c->stream));
+  double2* r2 = nullptr;
+  if ((rc = passes64(c, r1, r1 == A ? B : A, M, nrows, +1, &r2))) return rc;
+  CK(launch_blue_post64(r2, M, D, N, N, dir, nrows, c->stream));
+  g_launches += 3;
+  return 0;
+}
+
+// Rows whose analytic signals are to be computed in FP64 under the context's mode.
+int precise_rows(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, std::vector<int>* rows) {
+  rows->clear();
+  if (c->precision == FPCC_ANALYTIC_F32 || nrows <= 0) return 0;
+  if (c->precision == FPCC_ANALYTIC_F64) {
+    for (int r = 0; r < nrows; r++) rows->push_back(r);
+    return 0;
+  }
+  void* cnt;
+  int rc = dev_buf(c, S_P64_CNT, (size_t)nrows * sizeof(int), &cnt);
+  if (rc) return rc;
+  CK(launch_zero_count(d_x, ldx, N, nrows, (int*)cnt, c->stream));
+  g_launches++;
+  std::vector<int> h(nrows);
+  CK(cudaMemcpyAsync(h.data(), cnt, (size_t)nrows * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int r = 0; r < nrows; r++)
+    if (h[r] >= kZeroSamples) rows->push_back(r);
+  return 0;
+}
+
+// Overwrites the listed rows of the FP32 analytic signals `an` (stride ldan)
+// with FP64 analytic signals of the same rows of x, rounded to float2.
+int refine_analytic(fpcc_ctx* c, const float* d_x, int64_t ldx, int N, const std::vector<int>& rows, float2* an,
+                    int64_t ldan) {
+  if (rows.empty()) return 0;
+  const bool smooth = !radices64(N).empty();
+  const int M = smooth ? N : smooth_at_least(2 * N - 1);
+  const size_t per_row = (size_t)N * sizeof(double2) + (smooth ? (size_t)N : (size_t)2 * M) * sizeof(double2);
+  int chunk = (int)std::max<size_t>(1, ((size_t)512 << 20) / per_row);
+  if (chunk > 65535) chunk = 65535;
+  if (chunk > (int)rows.size()) chunk = (int)rows.size();
+  void *D, *A, *B, *ridx;
+  int rc;
+  if ((rc = dev_buf(c, S_P64_D, (size_t)chunk * N * sizeof(double2), &D)) ||
+      (rc = dev_buf(c, S_P64_A, (size_t)chunk * M * sizeof(double2), &A)) ||
+      (rc = dev_buf(c, S_P64_B, (size_t)chunk * M * sizeof(double2), &B)) ||
+      (rc = dev_buf(c, S_P64_CNT, rows.size() * sizeof(int), &ridx)))
+    return rc;
+  CK(cudaMemcpyAsync(ridx, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  for (size_t r0 = 0; r0 < rows.size(); r0 += chunk) {
+    const int n = (int)std::min<size_t>(chunk, rows.size() - r0);
+    const int* ri = (const int*)ridx + r0;
+    double2* d = (double2*)D;
+    if (smooth) {
+      CK(launch_gather64(d_x, ldx, ri, n, N, N, (double2*)A, c->stream));
+      double2* r1 = nullptr;
+      if ((rc = passes64(c, (double2*)A, (double2*)B, N, n, -1, &r1))) return rc;
+      CK(launch_mask64(r1, N, n, c->stream));
+      double2* r2 = nullptr;
+      if ((rc = passes64(c, r1, r1 == (double2*)A ? (double2*)B : (double2*)A, N, n, +1, &r2))) return rc;
+      d = r2;
+    } else {
+      CK(launch_gather64(d_x, ldx, ri, n, N, N, d, c->stream));
+      if ((rc = bluestein64(c, d, (double2*)A, (double2*)B, N, M, n, -1))) return rc;
+      CK(launch_mask64(d, N, n, c->stream));
+      if ((rc = bluestein64(c, d, (double2*)A, (double2*)B, N, M, n, +1))) return rc;
+    }
+    CK(launch_store64(d, N, ri, n, N, an, ldan, c->stream));
+    g_launches += 3;
+  }
+  return 0;
 }
 
 // Analytic signal for window lengths with a prime factor above 5, by Bluestein
@@ -444,10 +609,28 @@ int analytic_rows(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, 
   return 0;
 }
 
+// FP64 analytic signals for the listed rows of `an` (stride N), then the row
+// statistics of all rows again.
+int refine_rows_stats(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, const std::vector<int>& rows,
+                      const float2* an, const float* rmax, const float* rsum) {
+  if (rows.empty()) return 0;
+  int rc = refine_analytic(c, d_x, ldx, N, rows, const_cast<float2*>(an), N);
+  if (rc) return rc;
+  CK(launch_rowstats(an, N, N, nrows, const_cast<float*>(rmax), const_cast<float*>(rsum), c->stream));
+  g_launches++;
+  return 0;
+}
+
 }  // namespace
 
 extern "C" int fpcc_station_stage(fpcc_ctx* c, int method, const float* d_x, int64_t ldx, int nrows, int N,
                                   int Nz, int fmt, int rule, void* d_out, int64_t ldo) {
+  return fpcc_station_stage_ex(c, method, d_x, ldx, nrows, N, Nz, fmt, rule, d_out, ldo, nullptr, -1);
+}
+
+extern "C" int fpcc_station_stage_ex(fpcc_ctx* c, int method, const float* d_x, int64_t ldx, int nrows, int N,
+                                     int Nz, int fmt, int rule, void* d_out, int64_t ldo, const int32_t* h_f64_rows,
+                                     int n_f64_rows) {
   if (!c) return fail(FPCC_EARG, "null context");
   if (nrows <= 0) return 0;
   if (N <= 0) return fail(FPCC_EARG, "N must be positive");
@@ -458,9 +641,22 @@ extern "C" int fpcc_station_stage(fpcc_ctx* c, int method, const float* d_x, int
     g_launches++;
     return 0;
   }
+  std::vector<int> p64;   // rows whose analytic signals are computed in FP64
+  const bool phase_method = (method == FPCC_PCC1 || method == FPCC_PCCV || method == FPCC_PCC2);
+  if (phase_method) {
+    if (n_f64_rows >= 0) {
+      for (int i = 0; i < n_f64_rows; i++) {
+        if (!h_f64_rows || h_f64_rows[i] < 0 || h_f64_rows[i] >= nrows) return fail(FPCC_EARG, "bad FP64 row list");
+        p64.push_back(h_f64_rows[i]);
+      }
+    } else if ((rc = precise_rows(c, d_x, ldx, nrows, N, &p64))) {
+      return rc;
+    }
+  }
   if (method == FPCC_PCC1 || method == FPCC_PCCV) {
     const float2 *an; const float *rmax, *rsum;
     if ((rc = analytic_rows(c, d_x, ldx, nrows, N, &an, &rmax, &rsum))) return rc;
+    if ((rc = refine_rows_stats(c, d_x, ldx, nrows, N, p64, an, rmax, rsum))) return rc;
     PhaseArgs a{};
     a.in = an; a.ldin = N; a.nrows = nrows; a.N = N; a.rule = rule;
     a.rowstat = (rule == FPCC_AMP_SUMTHR) ? rsum : rmax;
@@ -478,13 +674,14 @@ extern "C" int fpcc_station_stage(fpcc_ctx* c, int method, const float* d_x, int
     if (method == FPCC_PCC2) {
       const float2 *an; const float *rmax, *rsum;
       if ((rc = analytic_rows(c, d_x, ldx, nrows, N, &an, &rmax, &rsum))) return rc;
+      if ((rc = refine_rows_stats(c, d_x, ldx, nrows, N, p64, an, rmax, rsum))) return rc;
       return large_station(c, COL_PHASE, an, sizeof(float2), N, nrows, N, Nz, rule,
                            (rule == FPCC_AMP_SUMTHR) ? rsum : rmax, 0, fmt, 0, d_out, ldo);
     }
     return large_station(c, method == FPCC_GNCC ? COL_REAL : COL_SIGN, d_x, sizeof(float), ldx, nrows, N, Nz, 0,
                          nullptr, rule == FPCC_SIGN_GE ? 1 : 0, FPCC_F32, 1, d_out, ldo);
   }
-  if (method == FPCC_PCC2) {
+  if (method == FPCC_PCC2 && p64.empty()) {
     // one fused kernel per station window, specialised at run time for (N, Nz)
     const cudaError_t e = launch_station_fused(d_x, ldx, nrows, N, Nz, rule, fmt, d_out, ldo, c->stream);
     if (e == cudaSuccess) {
@@ -498,6 +695,7 @@ extern "C" int fpcc_station_stage(fpcc_ctx* c, int method, const float* d_x, int
   if (method == FPCC_PCC2) {
     const float2 *an; const float *rmax, *rsum;
     if ((rc = analytic_rows(c, d_x, ldx, nrows, N, &an, &rmax, &rsum))) return rc;
+    if ((rc = refine_rows_stats(c, d_x, ldx, nrows, N, p64, an, rmax, rsum))) return rc;
     a.in = an; a.ldin = N; a.mode = SPEC_PHASE; a.rule = rule;
     a.rowstat = (rule == FPCC_AMP_SUMTHR) ? rsum : rmax;
   } else {
@@ -609,8 +807,7 @@ extern "C" int fpcc_pair_stage_packed(fpcc_ctx* c, int method, int fmt, int Nz, 
   if (!d_desc || maxL <= 0) return fail(FPCC_EARG, "packed pair stage needs descriptors and maxL > 0");
   if (npairs > 0x7fffffff / 2) return fail(FPCC_EARG, "too many pairs");
   if (is_fft_method(method)) {
-    if ((Nz & 1) || !pair_supported(Nz))
-      return fail(FPCC_EUNSUP, "packed pair stage: Nz=%d is not an in-block length", Nz);
+    if (Nz & 1) return fail(FPCC_EARG, "packed pair stage: Nz=%d must be even", Nz);
     if (method != FPCC_PCC2 && fmt != FPCC_F32) return fail(FPCC_EUNSUP, "GNCC and 1-bit spectra are F32");
     PairArgs a{};
     a.fmt = fmt;
@@ -618,6 +815,7 @@ extern "C" int fpcc_pair_stage_packed(fpcc_ctx* c, int method, int fmt, int Nz, 
     a.Nz = Nz;
     a.norm = method == FPCC_PCC2 ? 0 : (method == FPCC_GNCC ? 1 : 2);
     a.desc = d_desc;
+    if (!pair_supported(Nz)) return large_pairs(c, a, method == FPCC_PCC2 ? 0 : 1);
     CK(launch_pairs(a, c->stream));
     g_launches++;
     return 0;

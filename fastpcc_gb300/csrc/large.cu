@@ -47,13 +47,22 @@ __device__ __forceinline__ float2 ld_bin(const void* base, int fmt, int64_t i) {
 __device__ __forceinline__ float2 pair_bin(const LargeArgs& a, int row, int p) {
   const int Nz = a.Nz;
   if (a.herm == 2) return ld_bin(a.spec, a.fmt, (int64_t)row * a.ldspec + p);
-  const int2 pr = a.pairs[row];
-  const int64_t b1 = (int64_t)pr.x * a.ldspec, b2 = (int64_t)pr.y * a.ldspec;
+  const void* X1;
+  const void* X2;
+  if (a.desc) {
+    X1 = a.desc[row].a;
+    X2 = a.desc[row].b;
+  } else {
+    const int2 pr = a.pairs[row];
+    const int64_t esz = (a.fmt == SPEC_F16) ? 4 : 8;
+    X1 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.x * a.ldspec * esz;
+    X2 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.y * a.ldspec * esz;
+  }
   if (a.herm == 1 && p > (Nz >> 1)) {
     const int q = Nz - p;
-    return cconj(cconjmul(ld_bin(a.spec, a.fmt, b1 + q), ld_bin(a.spec, a.fmt, b2 + q)));
+    return cconj(cconjmul(ld_bin(X1, a.fmt, q), ld_bin(X2, a.fmt, q)));
   }
-  return cconjmul(ld_bin(a.spec, a.fmt, b1 + p), ld_bin(a.spec, a.fmt, b2 + p));
+  return cconjmul(ld_bin(X1, a.fmt, p), ld_bin(X2, a.fmt, p));
 }
 
 __device__ __forceinline__ float2 col_load(const LargeArgs& a, int row, int j, float eps) {
@@ -175,18 +184,40 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
     } else {
       // y_full[2k] = Re z[k], y_full[2k+1] = Im z[k]; lag = idx or idx - Nz
       const int Nz = 2 * n;
-      const int N = a.N;
+      int N, lag0, L;
+      float scale;
+      float* yrow;
+      const double* E1 = nullptr;
+      const double* E2 = nullptr;
+      if (a.desc) {
+        const PairDesc& d = a.desc[row];
+        N = d.N;
+        lag0 = d.lag0;
+        L = d.L;
+        scale = d.scale != 0.0f ? d.scale
+                                : (a.norm == 0 ? 1.0f / ((float)Nz * (float)N) : (float)(1.0 / (double)Nz));
+        yrow = reinterpret_cast<float*>(d.y);
+        if (a.norm == 1) { E1 = d.ea; E2 = d.eb; }
+      } else {
+        N = a.N;
+        lag0 = a.lag0;
+        L = a.L;
+        scale = a.scale;
+        yrow = a.y + (int64_t)row * a.ldy;
+        if (a.norm == 1) {
+          const int2 pr = a.pairs[row];
+          E1 = a.energy + (int64_t)pr.x * a.ldE;
+          E2 = a.energy + (int64_t)pr.y * a.ldE;
+        }
+      }
 #pragma unroll
       for (int q = 0; q < 2; q++) {
         const int idx = 2 * k + q;
         const int lag = (idx <= (Nz >> 1)) ? idx : idx - Nz;
-        const int l = lag - a.lag0;
-        if (l < 0 || l >= a.L) continue;
-        float val = (q ? v.y : v.x) * a.scale;
+        const int l = lag - lag0;
+        if (l < 0 || l >= L) continue;
+        float val = (q ? v.y : v.x) * scale;
         if (a.norm == 1) {
-          const int2 pr = a.pairs[row];
-          const double* E1 = a.energy + (int64_t)pr.x * a.ldE;
-          const double* E2 = a.energy + (int64_t)pr.y * a.ldE;
           int n11 = 0, n21 = 0, n12 = N, n22 = N;
           if (lag > 0) { n21 = lag; n12 -= lag; }
           else { n11 = -lag; n22 += lag; }
@@ -194,7 +225,7 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
         } else if (a.norm == 2) {
           val = (float)((double)val / (double)(N - abs(lag)));
         }
-        a.y[(int64_t)row * a.ldy + l] = val;
+        yrow[l] = val;
       }
     }
   }

@@ -76,6 +76,8 @@ struct LargeArgs {
   int64_t ldE;
   float* y;
   int64_t ldy;
+  // packed pair stage: per-row product rows, N, lags, energies and output (COL_PAIR / ROW_LAGS)
+  const PairDesc* desc;
 };
 
 // True when n has a supported four-step decomposition; writes n1, n2.

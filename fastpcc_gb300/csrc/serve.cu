@@ -143,7 +143,12 @@ struct Server {
   // host copies of registered windows
   std::mutex mu;
   std::condition_variable cv, cv_done;
-  std::map<std::pair<int, int>, std::pair<float*, int>> windows;   // (sta, win) -> pinned samples, N
+  struct Window {
+    float* x;      // pinned samples
+    int N;
+    int zeros;     // zero samples (such windows get FP64 analytic signals)
+  };
+  std::map<std::pair<int, int>, Window> windows;
   std::vector<char*> arena;                                       // pinned chunks holding the windows
   size_t arena_left = 0;
   char* arena_ptr = nullptr;
@@ -327,7 +332,9 @@ struct GroupKey {
 // method (and padded length class) shares one launch.
 bool packable(int method, int Nz) {
   if (method == FPCC_PCC1 || method == FPCC_PCCV || method == FPCC_CC1B_POPCOUNT) return true;
-  if (method == FPCC_PCC2 || method == FPCC_GNCC || method == FPCC_CC1B) return pair_supported(Nz);
+  int n1, n2;
+  if (method == FPCC_PCC2 || method == FPCC_GNCC || method == FPCC_CC1B)
+    return pair_supported(Nz) || large_supported(Nz / 2, &n1, &n2);
   return false;
 }
 
@@ -369,7 +376,7 @@ int ensure_raw(Server* s, int N, const std::vector<int64_t>& keys, std::vector<i
       std::lock_guard<std::mutex> lk(s->mu);
       auto it = s->windows.find({(int)(keys[i] >> 32), (int)(uint32_t)keys[i]});
       if (it == s->windows.end()) return FPCC_EARG;
-      w = it->second.first;
+      w = it->second.x;
     }
     if (cudaMemcpyAsync((char*)sl.base + (int64_t)rows[i] * sl.row_bytes, w, (size_t)N * 4, cudaMemcpyHostToDevice,
                         s->st) != cudaSuccess)
@@ -430,7 +437,17 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   if (pk.kind == 5) {
     rc = fpcc_energy_stage(s->ctx, (const float*)dx, ldx, n, pk.N, (double*)dp, sl.row_bytes / 8);
   } else {
-    rc = fpcc_station_stage(s->ctx, method, (const float*)dx, ldx, n, pk.N, pk.Nz, pk.fmt, rule, dp, ldo);
+    // FP64 analytic signals for windows with zero runs (known from the host copies)
+    std::vector<int32_t> f64;
+    if (method == FPCC_PCC2 || method == FPCC_PCC1) {
+      std::lock_guard<std::mutex> lk(s->mu);
+      for (int i = 0; i < n; i++) {
+        auto it = s->windows.find({(int)(miss_keys[i] >> 32), (int)(uint32_t)miss_keys[i]});
+        if (it != s->windows.end() && it->second.zeros >= FPCC_F64_ZERO_SAMPLES) f64.push_back(i);
+      }
+    }
+    rc = fpcc_station_stage_ex(s->ctx, method, (const float*)dx, ldx, n, pk.N, pk.Nz, pk.fmt, rule, dp, ldo,
+                               f64.data(), (int)f64.size());
   }
   if (rc) return rc;
   if (copy_rows(dp, sl.row_bytes, nullptr, sl.base, sl.row_bytes, (const int*)di + n, n, sl.row_bytes, s->st) !=
@@ -975,7 +992,9 @@ extern "C" int fpcc_put_station_window(fpcc_server* h, int32_t sta, int32_t wind
   s->arena_ptr += bytes;
   s->arena_left -= bytes;
   memcpy(dst, x, (size_t)N * 4);
-  s->windows[{sta, window}] = {dst, N};
+  int zeros = 0;
+  for (int n = 0; n < N; n++) zeros += (x[n] == 0.0f);
+  s->windows[{sta, window}] = Server::Window{dst, N, zeros};
   return 0;
 }
 
@@ -991,8 +1010,8 @@ extern "C" int64_t fpcc_submit(fpcc_server* h, const fpcc_request* req) {
     auto a = s->windows.find({req->sta1, req->window});
     auto b = s->windows.find({req->sta2, req->window});
     if (a == s->windows.end() || b == s->windows.end()) return FPCC_EARG;
-    N = a->second.second;
-    if (b->second.second != N) return FPCC_EARG;
+    N = a->second.N;
+    if (b->second.N != N) return FPCC_EARG;
   }
   const int M = std::max(std::abs(req->Lag1), std::abs(req->Lag2));
   if (M >= N) return FPCC_EARG;

@@ -64,6 +64,15 @@ enum fpcc_format { FPCC_F32 = 0, FPCC_F16 = 1 };
  * (src/FFTapps.c:1037,1042). */
 enum fpcc_sign_rule { FPCC_SIGN_GE = 0, FPCC_SIGN_GT = 1 };
 
+/* Precision of the analytic signals of the phase methods (PCC2, PCC1, PCCV).
+ * FP32 transforms leave an absolute error of about 1e-7 x rms on every sample,
+ * which loses the phase where the analytic signal is small — inside runs of
+ * zero samples (data gaps, zero padding).  AUTO (the default) computes the
+ * analytic signals of windows with at least FPCC_F64_ZERO_SAMPLES zero samples
+ * in FP64. */
+enum fpcc_analytic_precision { FPCC_ANALYTIC_F32 = 0, FPCC_ANALYTIC_AUTO = 1, FPCC_ANALYTIC_F64 = 2 };
+#define FPCC_F64_ZERO_SAMPLES 4
+
 /* Padded correlation length rules. */
 enum fpcc_nz_mode { FPCC_NZ_REFERENCE = 0, FPCC_NZ_FAST = 1 };
 
@@ -72,6 +81,8 @@ typedef struct fpcc_ctx fpcc_ctx;
 /* ---- context ------------------------------------------------------------ */
 int fpcc_create(fpcc_ctx **out, int device);
 int fpcc_destroy(fpcc_ctx *ctx);
+/* fpcc_analytic_precision mode of the context's station stages (default AUTO). */
+int fpcc_set_analytic_precision(fpcc_ctx *ctx, int mode);
 /* Run subsequent work on this CUDA stream (cudaStream_t; NULL = the context's own). */
 int fpcc_set_stream(fpcc_ctx *ctx, void *stream);
 void *fpcc_get_stream(fpcc_ctx *ctx);
@@ -99,6 +110,12 @@ int64_t fpcc_station_row_elems(int method, int N, int Nz);
  */
 int fpcc_station_stage(fpcc_ctx *ctx, int method, const float *d_x, int64_t ldx, int nrows, int N,
                        int Nz, int fmt, int rule, void *d_out, int64_t ldo);
+/* As fpcc_station_stage, with the rows whose analytic signals are computed in
+ * FP64 named by the caller (host array of n_f64_rows row indices); n_f64_rows < 0
+ * applies the context's fpcc_analytic_precision mode instead. */
+int fpcc_station_stage_ex(fpcc_ctx *ctx, int method, const float *d_x, int64_t ldx, int nrows, int N,
+                          int Nz, int fmt, int rule, void *d_out, int64_t ldo, const int32_t *h_f64_rows,
+                          int n_f64_rows);
 /* FP64 prefix sums E[n] = sum_{m<n} x[m]^2, N+1 per row (GNCC normalisation). */
 int fpcc_energy_stage(fpcc_ctx *ctx, const float *d_x, int64_t ldx, int nrows, int N, double *d_E,
                       int64_t ldE);
@@ -112,8 +129,9 @@ int fpcc_pair_stage(fpcc_ctx *ctx, int method, const void *d_station, int64_t ld
 /* Packed pair stage: correlations of different window lengths and lag windows
  * in one launch.  Each descriptor names its own product rows (anywhere in device
  * memory), window length, lags and output row; only the padded length Nz (FFT
- * methods; must satisfy Nz >= N + max|lag| for every entry and be at most
- * 2 * fpcc_max_block_len()), the storage format and the power v are shared.
+ * methods; must satisfy Nz >= N + max|lag| for every entry; lengths above
+ * 2 * fpcc_max_block_len() run as four-step transforms), the storage format and
+ * the power v are shared.
  * d_desc is a device array of npairs descriptors; maxL >= every entry's L.
  * scale: 0 selects the method's own (PCC2 1/(Nz N), GNCC and 1-bit 1/Nz). */
 typedef struct {

@@ -203,3 +203,18 @@ def test_wpcc_error_per_octave_band(F, orc):
     plan.close()
     ctx.close()
     assert max(errs) < TOL, errs
+
+
+@pytest.mark.parametrize("N,M", [(2500, 200), (4099, 300), (18000, 1500), (40000, 2000)])
+def test_phase_methods_on_gapped_windows(F, orc, N, M):
+    # 5 % of the samples zeroed in gaps of 50-2000 samples: the analytic signals
+    # of such windows are computed in FP64 (FP32 transforms lose their phase
+    # inside the gaps and drift by a few 1e-4)
+    a, b = synth.plain_pair(N=N, n_windows=2, delay=-M // 3, tag=f"gpu/gaps/{N}")
+    a = np.stack([synth.gaps(a[k], seed_tag=f"a{k}") for k in range(2)])
+    b = np.stack([synth.gaps(b[k], seed_tag=f"b{k}") for k in range(2)])
+    y64 = orc.pcc2(a, b, -M, M)
+    assert relerr(F.pcc2_set(a, b, -M, M), y64) < TOL
+    assert relerr(F.pcc2_set(a, b, -M, M, plain=True), y64) < TOL
+    if N <= 18000:
+        assert relerr(F.pcc1_set(a, b, -M // 4, M // 4), orc.pcc1(a, b, -M // 4, M // 4)) < TOL
