@@ -62,3 +62,21 @@ def test_no_cuda_calls_without_gpu(libpath):
     L.fpcc_last_error.restype = ctypes.c_char_p
     assert L.fpcc_create(ctypes.byref(h), 0) != 0
     assert L.fpcc_last_error()
+
+
+def test_reference_cli_links_against_library(libpath):
+    """The reference CLI (src/PCC_fullpair_1b.c and FFTapps.c built with -DCUDAON)
+    links with libfastpcc_gb300.so in place of ccs_cuda.o and no undefined symbol
+    (needs the reference sources, present only where they are mounted)."""
+    src = "/root/reference/src"
+    if not os.path.isdir(src):
+        pytest.skip("reference sources not present")
+    r = subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-B", "cli_gb300"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    exe = os.path.join(ROOT, "oracle", "_ref", "PCC_fullpair_1b_gb300")
+    out = subprocess.run(["nm", "-D", "--undefined-only", exe], capture_output=True, text=True, check=True).stdout
+    undefined = {l.split()[-1] for l in out.splitlines()}
+    assert {"pcc_highlevel", "pcc1_highlevel", "cuda_tspcc2_set_freq"} <= undefined   # resolved by the library
+    ldd = subprocess.run(["ldd", exe], capture_output=True, text=True).stdout
+    assert "libfastpcc_gb300.so" in ldd and "not found" not in ldd

@@ -218,3 +218,21 @@ def test_phase_methods_on_gapped_windows(F, orc, N, M):
     assert relerr(F.pcc2_set(a, b, -M, M, plain=True), y64) < TOL
     if N <= 18000:
         assert relerr(F.pcc1_set(a, b, -M // 4, M // 4), orc.pcc1(a, b, -M // 4, M // 4)) < TOL
+
+
+def test_example_records_against_reference_cli(F, orc):
+    """Three days of the reference's GEOSCOPE example records (N = 21600, lags
+    +-3000): every method against the reference CLI's own outputs and the oracle."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_cli_geoscope.npz"))
+    x1, x2, l1, l2 = g["x1"], g["x2"], int(g["Lag1"]), int(g["Lag2"])
+    got = {"pcc2": F.pcc2_set(x1, x2, l1, l2), "pcc1": F.pcc1_set(x1, x2, l1, l2),
+           "ccgn": F.ccgn_set(x1, x2, l1, l2), "cc1b": F.cc1b_set(x1, x2, l1, l2),
+           "wpcc2": F.wpcc_set(x1, x2, l1, l2, float(g["pmin"]), float(g["pmax"]), V=2, type=-3)}
+    ref64 = {"pcc2": orc.pcc2(x1, x2, l1, l2), "pcc1": orc.pcc1(x1, x2, l1, l2), "ccgn": orc.gncc(x1, x2, l1, l2),
+             "cc1b": orc.cc1b(x1, x2, l1, l2),
+             "wpcc2": orc.wpcc(x1, x2, l1, l2, float(g["pmin"]), float(g["pmax"]), V=2, wtype=-3)}
+    for k, y in got.items():
+        assert relerr(y, ref64[k]) < TOL, k
+        assert relerr(y, g[k]) < TOL, k
+    assert np.array_equal(F.cc1b_numerators(x1, x2, l1, l2), orc.cc1b_num(x1, x2, l1, l2))

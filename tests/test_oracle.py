@@ -39,6 +39,20 @@ def test_oracle_matches_reference_golden_wpcc(orc):
         assert orc.relerr(g[key], y).max() < TOL_REF, key
 
 
+def test_oracle_matches_reference_cli_on_example_records(orc):
+    """The reference CLI's own outputs on three days of its GEOSCOPE example
+    records (N = 21600, lags +-3000); its phase methods run in float, hence the
+    looser bound for PCC2 / PCC1."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_cli_geoscope.npz"))
+    x1, x2, l1, l2 = g["x1"], g["x2"], int(g["Lag1"]), int(g["Lag2"])
+    assert orc.relerr(g["pcc2"], orc.pcc2(x1, x2, l1, l2)).max() < 2e-5
+    assert orc.relerr(g["pcc1"], orc.pcc1(x1, x2, l1, l2)).max() < 2e-5
+    assert orc.relerr(g["ccgn"], orc.gncc(x1, x2, l1, l2)).max() < TOL_REF
+    assert orc.relerr(g["cc1b"], orc.cc1b(x1, x2, l1, l2)).max() < TOL_REF
+    y = orc.wpcc(x1, x2, l1, l2, float(g["pmin"]), float(g["pmax"]), V=2, wtype=-3)
+    assert orc.relerr(g["wpcc2"], y).max() < TOL_REF
+
+
 @pytest.mark.parametrize("N", [64, 97, 1000, 1024, 18000 // 8, 4099])
 def test_analytic_signal_matches_numpy(orc, N):
     x = np.random.default_rng(N).standard_normal(N).astype(np.float32)
