@@ -234,7 +234,18 @@ def _errors(O, F, reqs, outs, win, n_max, per_method=2):
     return {k: max(v) for k, v in err.items()}
 
 
-def uneven_batch_leg(F, n_pairs=500, fmt=1):
+def autotune(F, max_nz=1 << 20):
+    """Measured padded-length table on this GPU (fpcc_autotune), outside any timed region."""
+    ctx = F.Context(0)
+    t0 = time.perf_counter()
+    path = os.path.join(ROOT, "gpurun_out", "autotune.json") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) \
+        else None
+    table = ctx.autotune(min_nz=512, max_nz=max_nz, reuse=8.0, path=path)
+    ctx.close()
+    return {"lengths_timed": len(table) if table else None, "seconds": time.perf_counter() - t0}
+
+
+def uneven_batch_leg(F, n_pairs=500, fmt=1, nz_mode=1):
     """500 pairs with window lengths log-uniform in 2^12-2^17 (5 % of samples in
     gaps), lags +-(1-10 %) of the length, methods 40/30/20/10 % PCC2 / 1-bit /
     GNCC / PCC1: the whole batch through the server (products computed on
@@ -256,7 +267,7 @@ def uneven_batch_leg(F, n_pairs=500, fmt=1):
     for (m, s1, s2, w, l1, l2) in reqs:
         _plain_call(F, m, win[w][s1][None], win[w][s2][None], l1, l2)
     t_plain = time.perf_counter() - t0
-    srv = F.Server(hbm_budget=150 << 30, max_batch=8192, fmt=fmt)
+    srv = F.Server(hbm_budget=150 << 30, max_batch=8192, fmt=fmt, nz_mode=nz_mode)
     for w in range(n_pairs):
         srv.put(0, w, win[w][0])
         srv.put(1, w, win[w][1])
@@ -283,7 +294,7 @@ def uneven_batch_leg(F, n_pairs=500, fmt=1):
             "max_rel_err": err, "err_sample": "2 requests per method with N <= 2^14 against the FP64 oracle"}
 
 
-def serving_leg(F, n_sta=200, n_win=8, n_req=4000, fmt=1, rates=(1e3, 1e4, 1e5, 1e6)):
+def serving_leg(F, n_sta=200, n_win=8, n_req=4000, fmt=1, rates=(1e3, 1e4, 1e5, 1e6), nz_mode=1):
     """Request stream over a 200-station pool: window lengths lognormal (median
     2^15, sigma 1) clipped to 2^12-2^18, lags +-(1-10 %), methods 38/28.5/19/9.5/5 %
     PCC2 / 1-bit / GNCC / PCC1 / wavelet PCC; Poisson arrivals swept over the
@@ -301,7 +312,7 @@ def serving_leg(F, n_sta=200, n_win=8, n_req=4000, fmt=1, rates=(1e3, 1e4, 1e5, 
     for (m, s1, s2, w, l1, l2) in reqs[:n_plain]:
         _plain_call(F, m, win[w][s1][None], win[w][s2][None], l1, l2)
     t_plain = time.perf_counter() - t0
-    srv = F.Server(hbm_budget=150 << 30, max_batch=8192, fmt=fmt, wavelet=WAVELET)
+    srv = F.Server(hbm_budget=150 << 30, max_batch=8192, fmt=fmt, wavelet=WAVELET, nz_mode=nz_mode)
     for w in range(n_win):
         for k in range(n_sta):
             srv.put(k, w, win[w][k])
@@ -414,8 +425,11 @@ def run_ours(args):
     F.build()
     if args.mixed_only:
         fmt = F.F16 if args.fmt == "f16" else F.F32
-        print(json.dumps({"uneven_batch": uneven_batch_leg(F, fmt=fmt), "serving": serving_leg(F, fmt=fmt)}),
-              flush=True)
+        tune = autotune(F)
+        print(json.dumps({"autotune": tune,
+                          "uneven_batch": uneven_batch_leg(F, fmt=fmt, nz_mode=F.NZ_TUNED),
+                          "uneven_batch_fast_nz": uneven_batch_leg(F, fmt=fmt, nz_mode=F.NZ_FAST),
+                          "serving": serving_leg(F, fmt=fmt, nz_mode=F.NZ_TUNED)}), flush=True)
         return
     n_sta, n_win = args.stations, args.windows
     from fastpcc_gb300 import synth
@@ -543,7 +557,8 @@ def run_ours(args):
 
     mixed = None
     if rank == 0 and not args.no_mixed:
-        mixed = {"uneven_batch": uneven_batch_leg(F), "serving": serving_leg(F)}
+        mixed = {"autotune": autotune(F), "uneven_batch": uneven_batch_leg(F, nz_mode=F.NZ_TUNED),
+                 "serving": serving_leg(F, nz_mode=F.NZ_TUNED)}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

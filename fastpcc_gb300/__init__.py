@@ -26,7 +26,7 @@ PCC2, GNCC, CC1B, CC1B_POPCOUNT, PCC1, PCCV, WPCC = 0, 1, 2, 3, 4, 5, 6
 AMP_F_REG, AMP_D_REG, AMP_PURE, AMP_THRESH, AMP_SUMTHR = 0, 1, 2, 3, 4
 F32, F16 = 0, 1
 SIGN_GE, SIGN_GT = 0, 1
-NZ_REFERENCE, NZ_FAST = 0, 1
+NZ_TUNED, NZ_REFERENCE, NZ_FAST = -1, 0, 1
 ANALYTIC_F32, ANALYTIC_AUTO, ANALYTIC_F64 = 0, 1, 2
 
 _lock = threading.Lock()
@@ -107,6 +107,9 @@ def lib():
             L.fpcc_pair_stage_packed.argtypes = [vp, i, i, i, vp, i, i, f, i]
             L.fpcc_server_create.argtypes = [C.POINTER(vp), i, C.c_size_t, i]
             L.fpcc_server_set_format.argtypes = [vp, i]
+            L.fpcc_server_set_nz_mode.argtypes = [vp, i]
+            L.fpcc_autotune.argtypes = [vp, i, i, C.c_double, C.c_char_p]
+            L.fpcc_autotune_load.argtypes = [C.c_char_p]
             L.fpcc_server_set_wavelet.argtypes = [vp, d, d, u, i, d, i]
             L.fpcc_server_destroy.argtypes = [vp]
             L.fpcc_put_station_window.argtypes = [vp, C.c_int32, C.c_int32, vp, i]
@@ -139,6 +142,15 @@ def choose_nz(N: int, Lag1: int, Lag2: int, mode: int = NZ_FAST) -> int:
     if nz <= 0:
         raise FpccError(-4, f"no supported correlation length for N={N}, lags [{Lag1},{Lag2}]")
     return nz
+
+
+def load_tuning(path: str) -> dict:
+    """Loads an autotuner table into the library (fpcc_autotune_load) and returns it."""
+    import json
+    check(lib().fpcc_autotune_load(path.encode()))
+    with open(path) as f:
+        d = json.load(f)
+    return {int(k): tuple(v) for k, v in d["lengths"].items()}
 
 
 def lag_count(Lag1: int, Lag2: int) -> int:
@@ -271,6 +283,12 @@ class Context:
                                     npairs, N, Nz, Lag1, Lag2, float(v), C.c_void_p(d_E or 0), ldE,
                                     C.c_void_p(d_y or 0), ldy, C.c_void_p(d_num or 0)))
 
+    def autotune(self, min_nz=512, max_nz=1 << 19, reuse=8.0, path=None) -> dict:
+        """Times every usable padded length on this GPU (fpcc_autotune); the table
+        then drives NZ_TUNED.  Returns {Nz: (pair ns per correlation, station ns per window)}."""
+        check(lib().fpcc_autotune(self._h, min_nz, max_nz, float(reuse), path.encode() if path else None))
+        return load_tuning(path) if path else {}
+
     def pair_stage_packed(self, method, fmt, Nz, d_desc, npairs, maxL, v=0.0, numerators=False):
         """d_desc: device array of npairs PairDesc (lengths and lags per correlation)."""
         check(lib().fpcc_pair_stage_packed(self._h, method, fmt, Nz, C.c_void_p(d_desc), npairs, maxL, float(v),
@@ -294,7 +312,7 @@ class Server:
     until the request completes (``wait``/``drain``)."""
 
     def __init__(self, device: int = 0, hbm_budget: int = 150 << 30, max_batch: int = 4096, fmt: int = F32,
-                 wavelet: dict = None):
+                 wavelet: dict = None, nz_mode: int = NZ_FAST):
         """fmt: storage of cached phase spectra / phase signals (F32 or F16).
         wavelet: family of WPCC requests, keys pmin, pmax, V, type, op1, rule
         (as WpccPlan)."""
@@ -304,6 +322,8 @@ class Server:
         try:
             if fmt != F32:
                 check(lib().fpcc_server_set_format(self._h, fmt))
+            if nz_mode != NZ_FAST:
+                check(lib().fpcc_server_set_nz_mode(self._h, nz_mode))
             if wavelet is not None:
                 w = dict(V=2, type=-3, op1=0.0, rule=AMP_D_REG)
                 w.update(wavelet)

@@ -352,11 +352,30 @@ int passes(fpcc_ctx* c, float2* A, float2* B, int M, int nrows, int dir, float2*
   return 0;
 }
 
+// Transform length of Bluestein's method for windows of n/2 samples: the
+// cheapest length >= n (by the pass cost model) that the generic passes run
+// (2,3,5-smooth within the pass limit), searched up to 2n.
 int smooth_at_least(int n) {
-  for (int m = n;; m++) {
-    int a, b, cc;
-    if (factor235(m, &a, &b, &cc)) return m;
+  static std::mutex mu;
+  static std::map<int, int> memo;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = memo.find(n);
+    if (it != memo.end()) return it->second;
   }
+  int best = -1;
+  double bc = 1e300;
+  for (int m = n; m <= 2 * n + 64; m++) {
+    int a, b, cc;
+    if (!factor235(m, &a, &b, &cc)) continue;
+    FftPlan p;
+    if (!make_plan(m, &p)) continue;
+    const double c = plan_cost(m);
+    if (c < bc) { bc = c; best = m; }
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  memo[n] = best;
+  return best;
 }
 
 // ---------------------------------------------------------------- FP64 analytic signals

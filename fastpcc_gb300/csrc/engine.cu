@@ -4,6 +4,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <vector>
 
 #include "engine.h"
 #include "menu.cuh"
@@ -88,23 +89,82 @@ bool nz_usable(int nz) { return nz > 0 && (nz % 2) == 0 && usable(nz) && usable(
 static int choose_nz_uncached(int N, int M, int mode);
 
 // Memoised: the serving loop asks once per request.
+static std::mutex g_memo_mu;
+static std::map<std::tuple<int, int, int>, int> g_memo;
+
+// Measured costs per padded length (autotuner): pair stage per correlation and
+// station stage per window, in ns; a length's cost is pair + station / reuse.
+static std::mutex g_tune_mu;
+static std::map<int, std::pair<double, double>> g_tuned;
+static double g_reuse = 8.0;
+
+void tuned_set(int nz, double pair_ns, double station_ns) {
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[nz] = {pair_ns, station_ns};
+  }
+  std::lock_guard<std::mutex> lk(g_memo_mu);
+  g_memo.clear();
+}
+
+void tuned_set_reuse(double reuse) {
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_reuse = reuse > 0 ? reuse : 8.0;
+  }
+  std::lock_guard<std::mutex> lk(g_memo_mu);
+  g_memo.clear();
+}
+
+std::vector<std::tuple<int, double, double>> tuned_table(double* reuse) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::vector<std::tuple<int, double, double>> v;
+  for (auto& kv : g_tuned) v.emplace_back(kv.first, kv.second.first, kv.second.second);
+  if (reuse) *reuse = g_reuse;
+  return v;
+}
+
+static bool tuned_cost(int nz, double* cost) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find(nz);
+  if (it == g_tuned.end()) return false;
+  *cost = it->second.first + it->second.second / g_reuse;
+  return true;
+}
+
+std::vector<int> usable_lengths(int lo, int hi) {
+  std::vector<int> v;
+  for (int nz = lo + (lo & 1); nz <= hi; nz += 2) {
+    int a2, b3, c5;
+    if (factor235(nz, &a2, &b3, &c5) && nz_usable(nz)) v.push_back(nz);
+  }
+  return v;
+}
+
 int choose_nz(int N, int M, int mode) {
-  static std::mutex mu;
-  static std::map<std::tuple<int, int, int>, int> memo;
   const auto key = std::make_tuple(N, M, mode);
   {
-    std::lock_guard<std::mutex> lk(mu);
-    auto it = memo.find(key);
-    if (it != memo.end()) return it->second;
+    std::lock_guard<std::mutex> lk(g_memo_mu);
+    auto it = g_memo.find(key);
+    if (it != g_memo.end()) return it->second;
   }
-  const int nz = choose_nz_uncached(N, M, mode);
-  std::lock_guard<std::mutex> lk(mu);
-  memo[key] = nz;
+  int nz = choose_nz_uncached(N, M, mode);
+  if (nz <= 0 && mode == FPCC_NZ_TUNED_MODE) nz = choose_nz_uncached(N, M, 1);
+  std::lock_guard<std::mutex> lk(g_memo_mu);
+  g_memo[key] = nz;
   return nz;
 }
 
 static int choose_nz_uncached(int N, int M, int mode) {
   const int need = N + M;
+  if (mode == FPCC_NZ_TUNED_MODE) {
+    // the measured cheapest length among those the autotuner timed
+    int best = -1;
+    double bc = 1e300, c;
+    for (int nz = need + (need & 1); nz <= 2 * need + 64 && nz <= (1 << 21); nz += 2)
+      if (tuned_cost(nz, &c) && c < bc) { bc = c; best = nz; }
+    return best;
+  }
   if (mode >= 2) {
     // explicit padded length
     return (mode >= need && nz_usable(mode)) ? mode : -1;

@@ -3,6 +3,9 @@
 
 #include <stdint.h>
 
+#include <tuple>
+#include <vector>
+
 #include "fft_core.cuh"
 
 namespace fpcc {
@@ -25,7 +28,19 @@ bool make_plan_raw(int n, FftPlan* p, const int* forced, int nforced);
 //           one block, by a per-pass cost model (results are identical for any
 //           length >= N+M: the correlation is linear).
 //   mode >= 2: that explicit length, if usable and >= N+M.
+//   mode FPCC_NZ_TUNED_MODE (-1): the measured cheapest length from the autotuner's
+//           table (mode 1 when the table holds no length >= N+M).
+constexpr int FPCC_NZ_TUNED_MODE = -1;
 int choose_nz(int N, int M, int mode);
+
+// Autotuner table: measured pair-stage ns per correlation and station-stage ns
+// per window for a padded length; reuse = correlations per station window
+// assumed when weighing the two.
+void tuned_set(int nz, double pair_ns, double station_ns);
+void tuned_set_reuse(double reuse);
+std::vector<std::tuple<int, double, double>> tuned_table(double* reuse);
+// Even 2,3,5-smooth lengths in [lo, hi] usable as padded lengths.
+std::vector<int> usable_lengths(int lo, int hi);
 // Nz and Nz/2 both run in one block or as four-step transforms.
 bool nz_usable(int nz);
 

@@ -135,6 +135,7 @@ struct Server {
   size_t budget = 0, used = 0;
   int max_batch = 4096;
   int fmt = FPCC_F32;                  // storage of phase spectra and phase signals
+  int nz_mode = FPCC_NZ_FAST;          // padded-length rule of FFT requests
   WaveletCfg wav;
   std::map<std::pair<int, int>, std::pair<int, int>> wsetup;   // (N, M) -> (Nz, length cap)   [mu]
   std::map<std::tuple<int, int, int>, fpcc_wpcc_plan*> wplans;  // (N, Nz, cap)   [worker]
@@ -286,8 +287,10 @@ void wait_one_retired(Server* s);
 // (admission by memory): only rows of the batch being built can then remain.
 int claim_row(Server* s, Slab& sl, int64_t key, int rows_needed_now) {
   sl.last_use = ++g_tick;
-  if ((int)sl.row_of.size() + rows_needed_now > sl.cap) grow(s, sl, std::max(sl.cap * 2, (int)sl.row_of.size() + rows_needed_now));
   for (;;) {
+    // room first (growing may release idle product classes), then the least recently used free row
+    if ((int)sl.row_of.size() + rows_needed_now > sl.cap)
+      grow(s, sl, std::max(sl.cap * 2, (int)sl.row_of.size() + rows_needed_now));
     for (auto it = sl.lru.rbegin(); it != sl.lru.rend(); ++it) {
       const int r = *it;
       if (sl.pin[r]) continue;
@@ -954,6 +957,15 @@ extern "C" int fpcc_server_set_format(fpcc_server* h, int fmt) {
   return 0;
 }
 
+extern "C" int fpcc_server_set_nz_mode(fpcc_server* h, int mode) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s || mode < FPCC_NZ_TUNED || mode > FPCC_NZ_FAST) return FPCC_EARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->next_id) return FPCC_EARG;
+  s->nz_mode = mode;
+  return 0;
+}
+
 extern "C" int fpcc_server_set_wavelet(fpcc_server* h, double pmin, double pmax, unsigned V, int type, double op1,
                                        int rule) {
   Server* s = reinterpret_cast<Server*>(h);
@@ -1020,7 +1032,7 @@ extern "C" int64_t fpcc_submit(fpcc_server* h, const fpcc_request* req) {
   q.L = std::abs(req->Lag2 - req->Lag1) + 1;
   const int m = req->method;
   if (m == FPCC_PCC2 || m == FPCC_GNCC || m == FPCC_CC1B) {
-    q.Nz = choose_nz(N, M, FPCC_NZ_FAST);
+    q.Nz = choose_nz(N, M, s->nz_mode);
     if (q.Nz <= 0) return FPCC_EUNSUP;
   } else if (m == FPCC_PCC1 || m == FPCC_PCCV || m == FPCC_CC1B_POPCOUNT) {
     q.Nz = 0;

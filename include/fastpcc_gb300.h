@@ -74,7 +74,7 @@ enum fpcc_analytic_precision { FPCC_ANALYTIC_F32 = 0, FPCC_ANALYTIC_AUTO = 1, FP
 #define FPCC_F64_ZERO_SAMPLES 4
 
 /* Padded correlation length rules. */
-enum fpcc_nz_mode { FPCC_NZ_REFERENCE = 0, FPCC_NZ_FAST = 1 };
+enum fpcc_nz_mode { FPCC_NZ_TUNED = -1, FPCC_NZ_REFERENCE = 0, FPCC_NZ_FAST = 1 };
 
 typedef struct fpcc_ctx fpcc_ctx;
 
@@ -95,6 +95,14 @@ int64_t fpcc_launch_count(void);
 /* ---- planning ----------------------------------------------------------- */
 /* Padded correlation length for N samples and the lag window (mode: fpcc_nz_mode). */
 int fpcc_choose_nz(int N, int Lag1, int Lag2, int mode);
+/* Autotuner: times the pair stage (per correlation) and the station stage (per
+ * window) of every usable padded length in [min_nz, max_nz] on the context's
+ * GPU and keeps the table that FPCC_NZ_TUNED chooses from (cost = pair +
+ * station / reuse, reuse = correlations per station window); writes it as JSON
+ * to json_path when given.  FPCC_NZ_TUNED falls back to FPCC_NZ_FAST for
+ * lengths the table does not cover. */
+int fpcc_autotune(fpcc_ctx *ctx, int min_nz, int max_nz, double reuse, const char *json_path);
+int fpcc_autotune_load(const char *json_path);
 /* Largest length an in-block transform of this build supports. */
 int fpcc_max_block_len(void);
 /* Elements per row of the station product of a method (for sizing buffers). */
@@ -223,6 +231,9 @@ int fpcc_server_create(fpcc_server **out, int device, size_t hbm_budget_bytes, i
 /* Storage format (FPCC_F32 / FPCC_F16) of the phase spectra and phase signals
  * the server caches (PCC2, PCC1, PCCV, WPCC); before the first request. */
 int fpcc_server_set_format(fpcc_server *s, int fmt);
+/* Padded-length rule of FFT requests (fpcc_nz_mode; default FPCC_NZ_FAST);
+ * before the first request. */
+int fpcc_server_set_nz_mode(fpcc_server *s, int mode);
 /* Wavelet family of FPCC_WPCC requests (arguments of fpcc_wpcc_plan_create);
  * before the first request.  WPCC requests fail with FPCC_EARG without it. */
 int fpcc_server_set_wavelet(fpcc_server *s, double pmin, double pmax, unsigned V, int type, double op1,
