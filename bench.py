@@ -354,6 +354,123 @@ def serving_leg(F, n_sta=200, n_win=8, n_req=4000, fmt=1, rates=(1e3, 1e4, 1e5, 
             "err_sample": "2 requests per method with N <= 20000 against the FP64 oracle"}
 
 
+def _time_ms(torch, stream, fn, reps=3):
+    """Average CUDA-event time of fn() on `stream` after one untimed call."""
+    fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def method_legs(F, torch, ctx, stream, dev, x, d_x, pairs, Nz, peak):
+    """Pair-stage (and station-stage) kernels of every method on the all-pairs
+    workload, timed with CUDA events, against their rooflines: HBM bytes for the
+    FFT methods, sqrt throughput for PCC1, bit operations for the popcount form."""
+    N, L, rows, P = N_SAMP, 2 * LAG + 1, x.shape[0], pairs.shape[0]
+    d_pairs = torch.from_numpy(pairs).to(dev)
+    d_y = torch.empty((P, L), dtype=torch.float32, device=dev)
+    out = {}
+
+    def hbm(name, ms, alg_bytes, units):
+        out[name] = {"kernel_ms": ms, "alg_bytes": alg_bytes, "achieved_GBs": alg_bytes / ms / 1e6,
+                     "frac_of_measured_hbm": alg_bytes / ms / 1e6 / peak, "correlations": units}
+
+    # PCC2 station stage (fused analytic + normalisation + DFT_Nz), F32 and F16 spectra
+    for fmt, esz, tag in ((F.F32, 8, "f32"), (F.F16, 4, "f16")):
+        spec = torch.empty((rows, Nz * esz // 4), dtype=torch.float32, device=dev)
+        ms = _time_ms(torch, stream, lambda: ctx.station_stage(F.PCC2, d_x.data_ptr(), N, rows, N, Nz, fmt,
+                                                               F.AMP_F_REG, spec.data_ptr(), Nz))
+        out[f"pcc2_station_{tag}"] = {"kernel_ms": ms, "alg_bytes": rows * (4 * N + esz * Nz),
+                                      "achieved_GBs": rows * (4 * N + esz * Nz) / ms / 1e6, "windows": rows}
+        if fmt == F.F16:
+            ms = _time_ms(torch, stream, lambda: ctx.pair_stage(F.PCC2, spec.data_ptr(), Nz, fmt, d_pairs.data_ptr(),
+                                                                P, N, Nz, -LAG, LAG, d_y=d_y.data_ptr(), ldy=L))
+            hbm("pcc2_pairs_f16", ms, P * (2 * Nz * esz + 4 * L), P)
+        del spec
+    # GNCC: half spectra + FP64 energy prefix sums
+    H = Nz // 2 + 1
+    half = torch.empty((rows, 2 * H), dtype=torch.float32, device=dev)
+    E = torch.empty((rows, N + 1), dtype=torch.float64, device=dev)
+    ctx.station_stage(F.GNCC, d_x.data_ptr(), N, rows, N, Nz, F.F32, 0, half.data_ptr(), H)
+    ctx.energy_stage(d_x.data_ptr(), N, rows, N, E.data_ptr(), N + 1)
+    ms = _time_ms(torch, stream, lambda: ctx.pair_stage(F.GNCC, half.data_ptr(), H, F.F32, d_pairs.data_ptr(), P, N,
+                                                        Nz, -LAG, LAG, d_E=E.data_ptr(), ldE=N + 1,
+                                                        d_y=d_y.data_ptr(), ldy=L))
+    hbm("gncc_pairs", ms, P * (2 * H * 8 + 2 * L * 8 + 4 * L), P)
+    del E
+    # 1-bit, DFT form: station 1 signs x >= 0, station 2 signs x > 0 (rows offset by `rows`)
+    half2 = torch.empty((2 * rows, 2 * H), dtype=torch.float32, device=dev)
+    ctx.station_stage(F.CC1B, d_x.data_ptr(), N, rows, N, Nz, F.F32, F.SIGN_GE, half2.data_ptr(), H)
+    ctx.station_stage(F.CC1B, d_x.data_ptr(), N, rows, N, Nz, F.F32, F.SIGN_GT, half2[rows:].data_ptr(), H)
+    p2 = pairs.copy()
+    p2[:, 1] += rows
+    d_p2 = torch.from_numpy(p2).to(dev)
+    ms = _time_ms(torch, stream, lambda: ctx.pair_stage(F.CC1B, half2.data_ptr(), H, F.F32, d_p2.data_ptr(), P, N, Nz,
+                                                        -LAG, LAG, d_y=d_y.data_ptr(), ldy=L))
+    hbm("cc1b_pairs_dft", ms, P * (2 * H * 8 + 4 * L), P)
+    del half, half2
+    # 1-bit, exact popcount form: XOR + popcount of 32-bit words over every overlap
+    nw = (N + 31) // 32
+    bits = torch.empty((2 * rows, nw), dtype=torch.int32, device=dev)
+    ctx.station_stage(F.CC1B_POPCOUNT, d_x.data_ptr(), N, rows, N, 0, F.F32, F.SIGN_GE, bits.data_ptr(), nw)
+    ctx.station_stage(F.CC1B_POPCOUNT, d_x.data_ptr(), N, rows, N, 0, F.F32, F.SIGN_GT, bits[rows:].data_ptr(), nw)
+    ms = _time_ms(torch, stream, lambda: ctx.pair_stage(F.CC1B_POPCOUNT, bits.data_ptr(), nw, F.F32, d_p2.data_ptr(),
+                                                        P, N, 0, -LAG, LAG, d_y=d_y.data_ptr(), ldy=L))
+    words = P * sum((N - abs(l) + 31) // 32 for l in range(-LAG, LAG + 1))
+    out["cc1b_pairs_popcount"] = {"kernel_ms": ms, "word_ops": words, "Gword_ops_per_s": words / ms / 1e6,
+                                  "correlations": P}
+    del bits
+    # PCC1 by direct lag sums, one window (2016 pairs): two square roots per term
+    ph = torch.empty((rows, 2 * N), dtype=torch.float32, device=dev)
+    ctx.station_stage(F.PCC1, d_x.data_ptr(), N, rows, N, 0, F.F32, F.AMP_F_REG, ph.data_ptr(), N)
+    P1 = N_STA * (N_STA - 1) // 2
+    ms = _time_ms(torch, stream, lambda: ctx.pair_stage(F.PCC1, ph.data_ptr(), N, F.F32, d_pairs.data_ptr(), P1, N,
+                                                        0, -LAG, LAG, d_y=d_y.data_ptr(), ldy=L), reps=1)
+    terms = P1 * sum(N - abs(l) for l in range(-LAG, LAG + 1))
+    clk = 2.07e9
+    sfu_peak = 152 * 16 * clk / 2.0    # 16 special-function results per SM per clock, 2 per term
+    out["pcc1_pairs"] = {"kernel_ms": ms, "terms": terms, "Gterms_per_s": terms / ms / 1e6,
+                         "frac_of_sfu_peak": terms / ms * 1e3 / sfu_peak, "correlations": P1,
+                         "sfu_peak_assumed": "152 SMs x 16 sqrt/clk x 2.07 GHz, 2 sqrt per term"}
+    del ph, d_y
+    return out
+
+
+def wpcc_leg(F, torch, ctx, stream, dev, peak, n_pairs=16, n_win=24, N=65536, lag=4000):
+    """Wavelet PCC on its configuration (16 station pairs x 24 windows x 65536
+    samples at 20 Hz, Morlet, 40 scales over 0.02-5 Hz, lags +-4000): station
+    and pair stages timed, pair stage against the HBM roofline."""
+    from fastpcc_gb300 import synth
+    a, b, _ = synth.wavelet_pairs(n_pairs=n_pairs, n_windows=n_win, N=N, tag="bench/wpcc")
+    x = np.ascontiguousarray(np.concatenate([a.reshape(-1, N), b.reshape(-1, N)]))
+    P = n_pairs * n_win
+    plan = F.WpccPlan(ctx, N, -lag, lag, WAVELET["pmin"], WAVELET["pmax"], V=WAVELET["V"], type=WAVELET["type"])
+    S, Nz, L = plan.S, plan.Nz, plan.L
+    d_x = torch.from_numpy(x).to(dev)
+    d_P = torch.empty((2 * P, S * Nz * 2), dtype=torch.float32, device=dev)
+    pairs = np.stack([np.arange(P), P + np.arange(P)], 1).astype(np.int32)
+    d_pairs = torch.from_numpy(pairs).to(dev)
+    d_y = torch.empty((P, L), dtype=torch.float32, device=dev)
+    ms_st = _time_ms(torch, stream, lambda: plan.station_stage(d_x.data_ptr(), N, 2 * P, d_P.data_ptr()), reps=1)
+    ms = _time_ms(torch, stream, lambda: plan.pair_stage(d_P.data_ptr(), d_pairs.data_ptr(), P, d_y.data_ptr(), L))
+    alg = P * (2 * S * Nz * 8 + 4 * L)
+    from oracle import oracle as O
+    k = 0
+    y64 = O.wpcc(x[k][None], x[P + k][None], -lag, lag, WAVELET["pmin"], WAVELET["pmax"], V=WAVELET["V"],
+                 wtype=WAVELET["type"])
+    err = float(O.relerr(d_y[k:k + 1].cpu().numpy(), y64).max())
+    plan.close()
+    return {"workload": f"{n_pairs} pairs x {n_win} windows x {N} samples, S={S}, Nz={Nz}, lags +-{lag}",
+            "station_ms": ms_st, "station_windows": 2 * P, "pair_kernel_ms": ms, "correlations": P,
+            "correlations_per_s_device": P / ((ms + ms_st) / 1e3), "alg_bytes": alg,
+            "achieved_GBs": alg / ms / 1e6, "frac_of_measured_hbm": alg / ms / 1e6 / peak, "max_rel_err": err}
+
+
 def cpu_baseline(x, pairs, budget_s=12.0):
     """The oracle's PCC2 on host cores over a bounded sample of the workload."""
     from oracle import oracle as O
@@ -555,6 +672,11 @@ def run_ours(args):
     if rank == 0 and not args.no_served:
         served = served_leg(F, x, pairs, n_win, L)
 
+    methods = None
+    if rank == 0 and not args.no_mixed:
+        methods = method_legs(F, torch, ctx, stream, dev, x, d_x, pairs, Nz, peak)
+        methods["wpcc_config"] = wpcc_leg(F, torch, ctx, stream, dev, peak)
+
     mixed = None
     if rank == 0 and not args.no_mixed:
         mixed = {"autotune": autotune(F), "uneven_batch": uneven_batch_leg(F, nz_mode=F.NZ_TUNED),
@@ -579,6 +701,7 @@ def run_ours(args):
                            "what": f"batched step ({x.shape[0]} station windows + {P} correlations)"},
             "plain": plain,
             "served": served,
+            "methods": methods,
             "mixed": mixed,
             "gpu_launches": int(launches),
             "e2e": e2e,
