@@ -41,7 +41,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--stations", type=int, default=N_STA)
     ap.add_argument("--windows", type=int, default=N_WIN)
-    ap.add_argument("--fmt", default="f32", choices=["f32", "f16"])
+    ap.add_argument("--fmt", default="f32", choices=["f32", "f16", "i16"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served (request loop) leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the uneven-batch and request-stream legs")
@@ -245,7 +245,7 @@ def autotune(F, max_nz=1 << 20):
     return {"lengths_timed": len(table) if table else None, "seconds": time.perf_counter() - t0}
 
 
-def uneven_batch_leg(F, n_pairs=500, fmt=1, nz_mode=1):
+def uneven_batch_leg(F, n_pairs=500, fmt=2, nz_mode=1):
     """500 pairs with window lengths log-uniform in 2^12-2^17 (5 % of samples in
     gaps), lags +-(1-10 %) of the length, methods 40/30/20/10 % PCC2 / 1-bit /
     GNCC / PCC1: the whole batch through the server (products computed on
@@ -290,11 +290,11 @@ def uneven_batch_leg(F, n_pairs=500, fmt=1, nz_mode=1):
             "batched": {"value": n_pairs / t_cold, "unit": UNIT, "batches": st["batches"],
                         "what": "station products computed on demand, pair stages packed"},
             "batched_resident": {"value": n_pairs / t_warm, "unit": UNIT, "what": "second pass, products resident"},
-            "speedup_vs_plain": t_plain / t_cold, "spectra": "f16" if fmt else "f32",
+            "speedup_vs_plain": t_plain / t_cold, "spectra": ("f32", "f16", "i16")[fmt],
             "max_rel_err": err, "err_sample": "2 requests per method with N <= 2^14 against the FP64 oracle"}
 
 
-def serving_leg(F, n_sta=200, n_win=8, n_req=4000, fmt=1, rates=(1e3, 1e4, 1e5, 1e6), nz_mode=1):
+def serving_leg(F, n_sta=200, n_win=8, n_req=4000, fmt=2, rates=(1e3, 1e4, 1e5, 1e6), nz_mode=1):
     """Request stream over a 200-station pool: window lengths lognormal (median
     2^15, sigma 1) clipped to 2^12-2^18, lags +-(1-10 %), methods 38/28.5/19/9.5/5 %
     PCC2 / 1-bit / GNCC / PCC1 / wavelet PCC; Poisson arrivals swept over the
@@ -350,7 +350,7 @@ def serving_leg(F, n_sta=200, n_win=8, n_req=4000, fmt=1, rates=(1e3, 1e4, 1e5, 
                                   "what": "all requests at once, products resident"},
             "served_cold": {"value": n_req / t_cold, "unit": UNIT, "what": "products computed on demand"},
             "speedup_vs_plain": (n_req / t_warm) / plain, "poisson": sweep, "hbm_used_bytes": hbm,
-            "spectra": "f16" if fmt else "f32", "max_rel_err": err,
+            "spectra": ("f32", "f16", "i16")[fmt], "max_rel_err": err,
             "err_sample": "2 requests per method with N <= 20000 against the FP64 oracle"}
 
 
@@ -381,16 +381,22 @@ def method_legs(F, torch, ctx, stream, dev, x, d_x, pairs, Nz, peak):
                      "frac_of_measured_hbm": alg_bytes / ms / 1e6 / peak, "correlations": units}
 
     # PCC2 station stage (fused analytic + normalisation + DFT_Nz), F32 and F16 spectra
-    for fmt, esz, tag in ((F.F32, 8, "f32"), (F.F16, 4, "f16")):
-        spec = torch.empty((rows, Nz * esz // 4), dtype=torch.float32, device=dev)
+    for fmt, esz, tag in ((F.F32, 8, "f32"), (F.F16, 4, "f16"), (F.I16, 4, "i16")):
+        lds = Nz + 4 if fmt == F.I16 else Nz
+        spec = torch.empty((rows, lds * esz // 4), dtype=torch.float32, device=dev)
         ms = _time_ms(torch, stream, lambda: ctx.station_stage(F.PCC2, d_x.data_ptr(), N, rows, N, Nz, fmt,
-                                                               F.AMP_F_REG, spec.data_ptr(), Nz))
-        out[f"pcc2_station_{tag}"] = {"kernel_ms": ms, "alg_bytes": rows * (4 * N + esz * Nz),
-                                      "achieved_GBs": rows * (4 * N + esz * Nz) / ms / 1e6, "windows": rows}
-        if fmt == F.F16:
-            ms = _time_ms(torch, stream, lambda: ctx.pair_stage(F.PCC2, spec.data_ptr(), Nz, fmt, d_pairs.data_ptr(),
+                                                               F.AMP_F_REG, spec.data_ptr(), lds))
+        out[f"pcc2_station_{tag}"] = {"kernel_ms": ms, "alg_bytes": rows * (4 * N + esz * lds),
+                                      "achieved_GBs": rows * (4 * N + esz * lds) / ms / 1e6, "windows": rows}
+        if fmt != F.F32:
+            ms = _time_ms(torch, stream, lambda: ctx.pair_stage(F.PCC2, spec.data_ptr(), lds, fmt, d_pairs.data_ptr(),
                                                                 P, N, Nz, -LAG, LAG, d_y=d_y.data_ptr(), ldy=L))
-            hbm("pcc2_pairs_f16", ms, P * (2 * Nz * esz + 4 * L), P)
+            hbm(f"pcc2_pairs_{tag}", ms, P * (2 * lds * esz + 4 * L), P)
+            from oracle import oracle as O
+            sel = np.random.default_rng(4).choice(P, 6, replace=False)
+            y64 = O.pcc2(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)
+            out[f"pcc2_pairs_{tag}"]["max_rel_err"] = float(
+                O.relerr(d_y[torch.from_numpy(sel).to(dev)].cpu().numpy(), y64).max())
         del spec
     # GNCC: half spectra + FP64 energy prefix sums
     H = Nz // 2 + 1
@@ -541,7 +547,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     F.build()
     if args.mixed_only:
-        fmt = F.F16 if args.fmt == "f16" else F.F32
+        fmt = {"f32": F.F32, "f16": F.F16, "i16": F.I16}[args.fmt]
         tune = autotune(F)
         print(json.dumps({"autotune": tune,
                           "uneven_batch": uneven_batch_leg(F, fmt=fmt, nz_mode=F.NZ_TUNED),
@@ -556,9 +562,9 @@ def run_ours(args):
     pairs = all_pairs_index(n_sta, n_win)
     P = pairs.shape[0]
     L = 2 * LAG + 1
-    fmt = F.F16 if args.fmt == "f16" else F.F32
+    fmt = {"f32": F.F32, "f16": F.F16, "i16": F.I16}[args.fmt]
     Nz = F.choose_nz(N_SAMP, -LAG, LAG, F.NZ_FAST)
-    esz = 4 if fmt == F.F16 else 8
+    esz = 8 if fmt == F.F32 else 4
 
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
@@ -566,13 +572,14 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
     d_x = torch.from_numpy(x).to(dev)
     d_pairs = torch.from_numpy(pairs).to(dev)
-    d_spec = torch.empty((x.shape[0], Nz * esz // 4), dtype=torch.float32, device=dev)
+    lds = Nz + 4 if fmt == F.I16 else Nz     # int16 rows carry a 16-byte scale header
+    d_spec = torch.empty((x.shape[0], lds * esz // 4), dtype=torch.float32, device=dev)
     d_y = torch.empty((P, L), dtype=torch.float32, device=dev)
 
     def step():
         ctx.station_stage(F.PCC2, d_x.data_ptr(), N_SAMP, x.shape[0], N_SAMP, Nz, fmt, F.AMP_F_REG,
-                          d_spec.data_ptr(), Nz)
-        ctx.pair_stage(F.PCC2, d_spec.data_ptr(), Nz, fmt, d_pairs.data_ptr(), P, N_SAMP, Nz, -LAG, LAG,
+                          d_spec.data_ptr(), lds)
+        ctx.pair_stage(F.PCC2, d_spec.data_ptr(), lds, fmt, d_pairs.data_ptr(), P, N_SAMP, Nz, -LAG, LAG,
                        d_y=d_y.data_ptr(), ldy=L)
 
     def barrier():
@@ -611,13 +618,13 @@ def run_ours(args):
 
     # --- roofline: the pair kernel alone, timed on its stream ---
     ctx.station_stage(F.PCC2, d_x.data_ptr(), N_SAMP, x.shape[0], N_SAMP, Nz, fmt, F.AMP_F_REG,
-                      d_spec.data_ptr(), Nz)
+                      d_spec.data_ptr(), lds)
     reps = max(3, args.steps)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize(dev)
     e0.record(stream)
     for _ in range(reps):
-        ctx.pair_stage(F.PCC2, d_spec.data_ptr(), Nz, fmt, d_pairs.data_ptr(), P, N_SAMP, Nz, -LAG, LAG,
+        ctx.pair_stage(F.PCC2, d_spec.data_ptr(), lds, fmt, d_pairs.data_ptr(), P, N_SAMP, Nz, -LAG, LAG,
                        d_y=d_y.data_ptr(), ldy=L)
     e1.record(stream)
     torch.cuda.synchronize(dev)
@@ -690,7 +697,7 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if fmt == F.F32 else "f32 (f16 spectra)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if fmt == F.F32 else f"f32 ({args.fmt} spectra)",
             "data": "synthetic (seeded noise + shared band-passed component, per-station delays)",
             "config": {"workload": f"all-pairs PCC2: {n_sta} stations x {n_win} windows x {N_SAMP} samples, "
                                    f"{P} pair-windows per step, lags +-{LAG}",

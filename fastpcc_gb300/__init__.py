@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(HERE, "libfastpcc_gb300.so")
 PCC2, GNCC, CC1B, CC1B_POPCOUNT, PCC1, PCCV, WPCC = 0, 1, 2, 3, 4, 5, 6
 # amplitude-normalisation rules (enum fpcc_amp_rule)
 AMP_F_REG, AMP_D_REG, AMP_PURE, AMP_THRESH, AMP_SUMTHR = 0, 1, 2, 3, 4
-F32, F16 = 0, 1
+F32, F16, I16 = 0, 1, 2
 SIGN_GE, SIGN_GT = 0, 1
 NZ_TUNED, NZ_REFERENCE, NZ_FAST = -1, 0, 1
 ANALYTIC_F32, ANALYTIC_AUTO, ANALYTIC_F64 = 0, 1, 2
@@ -85,6 +85,8 @@ def lib():
             L.fpcc_max_block_len.restype = i
             L.fpcc_station_row_elems.argtypes = [i, i, i]
             L.fpcc_station_row_elems.restype = i64
+            L.fpcc_station_row_bytes.argtypes = [i, i, i, i]
+            L.fpcc_station_row_bytes.restype = i64
             L.fpcc_station_stage.argtypes = [vp, i, vp, i64, i, i, i, i, i, vp, i64]
             L.fpcc_station_stage_ex.argtypes = [vp, i, vp, i64, i, i, i, i, i, vp, i64, vp, i]
             L.fpcc_set_analytic_precision.argtypes = [vp, i]

@@ -225,6 +225,18 @@ extern "C" int fpcc_choose_nz(int N, int Lag1, int Lag2, int mode) {
 
 extern "C" int fpcc_max_block_len(void) { return kMenu[kMenuLen - 1]; }
 
+extern "C" int64_t fpcc_station_row_bytes(int method, int N, int Nz, int fmt) {
+  switch (method) {
+    case FPCC_PCC2: return fmt == FPCC_I16 ? 16 + 4 * (int64_t)Nz : (int64_t)Nz * (fmt == FPCC_F16 ? 4 : 8);
+    case FPCC_PCC1:
+    case FPCC_PCCV: return (int64_t)N * (fmt == FPCC_F32 ? 8 : 4);
+    case FPCC_GNCC:
+    case FPCC_CC1B: return ((int64_t)Nz / 2 + 1) * 8;
+    case FPCC_CC1B_POPCOUNT: return ((int64_t)N + 31) / 32 * 4;
+    default: return -1;
+  }
+}
+
 extern "C" int64_t fpcc_station_row_elems(int method, int N, int Nz) {
   switch (method) {
     case FPCC_PCC2: return Nz;
@@ -244,7 +256,7 @@ namespace {
 enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_PAIRS = 5, S_ANA_A = 6,
             S_ANA_B = 7, S_RSTAT = 8, S_LARGE_T = 9, S_WP_X = 10, S_WP_BAND = 11, S_WP_RMAX = 12,
             S_WP_Y = 13, S_WP_STAGE = 14, S_BLUE_O = 23, S_P64_D = 24, S_P64_A = 25, S_P64_B = 26,
-            S_P64_CNT = 27 };
+            S_P64_CNT = 27, S_I16_Q = 28 };
 
 constexpr size_t kLargeChunkBytes = size_t(512) << 20;   // four-step intermediate per chunk
 
@@ -261,7 +273,10 @@ int large_station(fpcc_ctx* c, int cmode, const void* in, size_t in_esz, int64_t
   void* T = nullptr;
   int rc = dev_buf(c, S_LARGE_T, (size_t)chunk * Nz * sizeof(float2), &T);
   if (rc) return rc;
-  const size_t out_esz = (fmt == FPCC_F16) ? 4 : 8;
+  // int16 rows: F32 spectra of the chunk first, then the block-scaled rows
+  void* Q = nullptr;
+  if (fmt == FPCC_I16 && (rc = dev_buf(c, S_I16_Q, (size_t)chunk * Nz * sizeof(float2), &Q))) return rc;
+  const size_t out_esz = (fmt == FPCC_F32) ? 8 : 4;
   for (int r0 = 0; r0 < nrows; r0 += (int)chunk) {
     LargeArgs a{};
     a.n = Nz; a.n1 = n1; a.n2 = n2; a.dir = -1;
@@ -273,10 +288,19 @@ int large_station(fpcc_ctx* c, int cmode, const void* in, size_t in_esz, int64_t
     a.sign_ge = sign_ge; a.in_scale = 1.0f;
     a.T = (float2*)T;
     a.rmode = ROW_SPEC;
-    a.out = (char*)out + (size_t)r0 * ldo * out_esz;
-    a.ldo = ldo; a.out_fmt = fmt; a.out_half = half;
+    if (fmt == FPCC_I16) {
+      a.out = Q; a.ldo = Nz; a.out_fmt = FPCC_F32; a.out_half = half;
+    } else {
+      a.out = (char*)out + (size_t)r0 * ldo * out_esz;
+      a.ldo = ldo; a.out_fmt = fmt; a.out_half = half;
+    }
     CK(launch_large(a, c->stream));
     g_launches += 2;
+    if (fmt == FPCC_I16) {
+      CK(launch_quantize_i16((const float2*)Q, Nz, half ? Nz / 2 + 1 : Nz, a.nrows, (char*)out + (size_t)r0 * ldo * 4,
+                             ldo, c->stream));
+      g_launches++;
+    }
   }
   return 0;
 }
@@ -689,6 +713,8 @@ extern "C" int fpcc_station_stage_ex(fpcc_ctx* c, int method, const float* d_x, 
   if (Nz < N || (Nz & 1)) return fail(FPCC_EARG, "Nz=%d must be even and >= N=%d", Nz, N);
   if ((method == FPCC_GNCC || method == FPCC_CC1B) && fmt != FPCC_F32)
     return fail(FPCC_EUNSUP, "real-trace spectra are stored in F32");
+  if (fmt == FPCC_I16 && ldo < (int64_t)Nz + 4)
+    return fail(FPCC_EARG, "int16 spectrum rows need ldo >= Nz + 4 (16-byte header)");
   if (!spec_supported(Nz)) {
     if (method == FPCC_PCC2) {
       const float2 *an; const float *rmax, *rsum;
@@ -784,7 +810,7 @@ extern "C" int fpcc_pair_stage(fpcc_ctx* c, int method, const void* d_station, i
     PccvArgs a{};
     a.phase = d_station;
     a.ldp = lds;
-    a.half = (fmt == FPCC_F16);
+    a.half = fmt;
     a.pairs = reinterpret_cast<const int2*>(d_pairs);
     a.npairs = npairs;
     a.N = N;
@@ -841,7 +867,7 @@ extern "C" int fpcc_pair_stage_packed(fpcc_ctx* c, int method, int fmt, int Nz, 
   }
   if (method == FPCC_PCC1 || method == FPCC_PCCV) {
     PccvArgs a{};
-    a.half = (fmt == FPCC_F16);
+    a.half = fmt;
     a.npairs = npairs;
     a.L = maxL;
     a.v = (method == FPCC_PCC1) ? 1.0f : v;
@@ -884,9 +910,11 @@ int make_layout(int method, int N, int Lag1, int Lag2, int nz_mode, int fmt, Lay
   if (o->Nz <= 0) return fail(FPCC_EUNSUP, "no padded length for N=%d", N);
   if (method == FPCC_GNCC || method == FPCC_CC1B) fmt = FPCC_F32;
   o->fmt = fmt;
-  o->lds = fpcc_station_row_elems(method, N, o->Nz);
-  if (o->lds < 0) return fail(FPCC_EUNSUP, "method %d not available here", method);
-  o->esz = (method == FPCC_CC1B_POPCOUNT) ? 4 : (fmt == FPCC_F16 ? 4 : 8);
+  if (fmt < FPCC_F32 || fmt > FPCC_I16) return fail(FPCC_EARG, "unknown storage format %d", fmt);
+  o->esz = (method == FPCC_CC1B_POPCOUNT) ? 4 : (fmt == FPCC_F32 ? 8 : 4);
+  const int64_t rb = fpcc_station_row_bytes(method, N, o->Nz, fmt);
+  if (rb < 0) return fail(FPCC_EUNSUP, "method %d not available here", method);
+  o->lds = rb / (int64_t)o->esz;
   o->two_rules = (method == FPCC_CC1B || method == FPCC_CC1B_POPCOUNT);
   return 0;
 }
@@ -1242,6 +1270,7 @@ extern "C" int fpcc_wpcc_plan_destroy(fpcc_wpcc_plan* p) {
 extern "C" int fpcc_wpcc_station_stage(fpcc_ctx* c, const fpcc_wpcc_plan* p, const float* d_x, int64_t ldx,
                                        int nrows, void* d_P, int fmt) {
   if (!c || !p) return fail(FPCC_EARG, "null argument");
+  if (fmt != FPCC_F32 && fmt != FPCC_F16) return fail(FPCC_EUNSUP, "wavelet spectra are stored in F32 or F16");
   if (nrows <= 0) return 0;
   return wpcc_station_run(c, p, d_x, ldx, nrows, d_P, fmt);
 }
@@ -1249,6 +1278,7 @@ extern "C" int fpcc_wpcc_station_stage(fpcc_ctx* c, const fpcc_wpcc_plan* p, con
 extern "C" int fpcc_wpcc_pair_stage(fpcc_ctx* c, const fpcc_wpcc_plan* p, const void* d_P, int fmt,
                                     const int32_t* d_pairs, int npairs, float* d_y, int64_t ldy) {
   if (!c || !p) return fail(FPCC_EARG, "null argument");
+  if (fmt != FPCC_F32 && fmt != FPCC_F16) return fail(FPCC_EUNSUP, "wavelet spectra are stored in F32 or F16");
   if (npairs <= 0) return 0;
   return wpcc_pairs_run(c, p, d_P, fmt, d_pairs, npairs, d_y, ldy);
 }

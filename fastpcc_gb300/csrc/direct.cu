@@ -50,7 +50,28 @@ __global__ void __launch_bounds__(256) k_energy_prefix(const float* __restrict__
 constexpr int kLagBlock = 256;
 constexpr int kTile = 512;
 
-template <int MODE, bool HALF>   // MODE 1: v = 1, 2: v = 2, 0: general power
+// Square root by the hardware approximation (relative error about 1 ulp); the
+// terms are summed in FP32 tiles and FP64 across tiles, far below the 1e-4 bound.
+__device__ __forceinline__ float sqrt_fast(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Phase sample n of a row in storage format FMT (0 float2, 1 half2, 2 int16 of scale 1/32767).
+template <int FMT>
+__device__ __forceinline__ float2 phase_at(const void* row, int n) {
+  if constexpr (FMT == 1) {
+    return __half22float2(reinterpret_cast<const __half2*>(row)[n]);
+  } else if constexpr (FMT == 2) {
+    const short2 q = reinterpret_cast<const short2*>(row)[n];
+    return make_float2((float)q.x * (1.0f / 32767.0f), (float)q.y * (1.0f / 32767.0f));
+  } else {
+    return reinterpret_cast<const float2*>(row)[n];
+  }
+}
+
+template <int MODE, int FMT>   // MODE 1: v = 1, 2: v = 2, 0: general power
 __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
   __shared__ float2 s1[kTile];
   __shared__ float2 s2[kTile + kLagBlock];
@@ -75,7 +96,7 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
     N = a.N;
     Lag1 = a.Lag1;
     L = a.L;
-    const int64_t esz = HALF ? 4 : 8;
+    const int64_t esz = FMT ? 4 : 8;
     R1 = reinterpret_cast<const char*>(a.phase) + (int64_t)pr.x * a.ldp * esz;
     R2 = reinterpret_cast<const char*>(a.phase) + (int64_t)pr.y * a.ldp * esz;
     y = a.y + (int64_t)p * a.ldy;
@@ -83,10 +104,6 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
   const int lagb = Lag1 + lblk;                   // lag of thread 0
   const float V = 0.5f * a.v;
   double acc = 0.0;
-  const float2* P1f = reinterpret_cast<const float2*>(R1);
-  const float2* P2f = reinterpret_cast<const float2*>(R2);
-  const __half2* P1h = reinterpret_cast<const __half2*>(R1);
-  const __half2* P2h = reinterpret_cast<const __half2*>(R2);
   // samples n of station 1 that overlap any lag of the block
   int nlo = -(lagb + kLagBlock - 1);
   if (nlo < 0) nlo = 0;
@@ -96,13 +113,13 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
     for (int i = threadIdx.x; i < kTile; i += kLagBlock) {
       const int n = n0 + i;
       float2 v = make_float2(0.f, 0.f);
-      if (n < N) v = HALF ? __half22float2(P1h[n]) : P1f[n];
+      if (n < N) v = phase_at<FMT>(R1, n);
       s1[i] = v;
     }
     for (int i = threadIdx.x; i < kTile + kLagBlock; i += kLagBlock) {
       const int n = n0 + lagb + i;
       float2 v = make_float2(0.f, 0.f);
-      if (n >= 0 && n < N) v = HALF ? __half22float2(P2h[n]) : P2f[n];
+      if (n >= 0 && n < N) v = phase_at<FMT>(R2, n);
       s2[i] = v;
     }
     __syncthreads();
@@ -116,7 +133,7 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
       const float dx = u.x - w.x, dy = u.y - w.y;
       const float s2v = sx * sx + sy * sy;
       const float d2v = dx * dx + dy * dy;
-      if (MODE == 1) part += sqrtf(s2v) - sqrtf(d2v);
+      if (MODE == 1) part += sqrt_fast(s2v) - sqrt_fast(d2v);
       else if (MODE == 2) part += s2v - d2v;
       else part += powf(s2v, V) - powf(d2v, V);
     }
@@ -221,16 +238,18 @@ cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st) {
   if ((a.L + kLagBlock - 1) / kLagBlock > 65535) return cudaErrorInvalidValue;
   dim3 grid(a.npairs, (a.L + kLagBlock - 1) / kLagBlock);
   const int mode = (a.v == 1.0f) ? 1 : (a.v == 2.0f ? 2 : 0);
-  if (a.half) {
-    if (mode == 1) k_pccv<1, true><<<grid, kLagBlock, 0, st>>>(a);
-    else if (mode == 2) k_pccv<2, true><<<grid, kLagBlock, 0, st>>>(a);
-    else k_pccv<0, true><<<grid, kLagBlock, 0, st>>>(a);
-  } else {
-    if (mode == 1) k_pccv<1, false><<<grid, kLagBlock, 0, st>>>(a);
-    else if (mode == 2) k_pccv<2, false><<<grid, kLagBlock, 0, st>>>(a);
-    else k_pccv<0, false><<<grid, kLagBlock, 0, st>>>(a);
+#define FPCC_PCCV_FMT(F)                                                  \
+  if (a.half == F) {                                                      \
+    if (mode == 1) k_pccv<1, F><<<grid, kLagBlock, 0, st>>>(a);           \
+    else if (mode == 2) k_pccv<2, F><<<grid, kLagBlock, 0, st>>>(a);      \
+    else k_pccv<0, F><<<grid, kLagBlock, 0, st>>>(a);                     \
+    return cudaGetLastError();                                            \
   }
-  return cudaGetLastError();
+  FPCC_PCCV_FMT(0)
+  FPCC_PCCV_FMT(1)
+  FPCC_PCCV_FMT(2)
+#undef FPCC_PCCV_FMT
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_sign_bits(const float* x, int64_t ldx, int nrows, int N, uint32_t* bits, int64_t ldb,

@@ -12,7 +12,7 @@ namespace fpcc {
 struct PccvArgs {
   const void* phase;   // phase signals, N complex per row (float2 or half2)
   int64_t ldp;
-  int half;            // 1: half2 storage
+  int half;            // storage: 0 float2, 1 half2, 2 int16 of scale 1/32767
   const int2* pairs;   // (row of station 1, row of station 2)
   int npairs;
   int N;

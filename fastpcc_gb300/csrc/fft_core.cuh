@@ -414,4 +414,40 @@ __device__ __forceinline__ float block_max(float v, float* scratch) {
   return v;
 }
 
+// Block-scaled int16 storage: a row starts with a 16-byte header holding the
+// row's float scale, then short2 values; value = q * scale, with the scale set
+// so that the largest component maps to 32767.  Relative to FP16 (11-bit
+// significands) it keeps about 15 bits for components near the row maximum and
+// more absolute precision for the typical component of a flat spectrum.
+constexpr int kI16Header = 16;
+constexpr float kI16Max = 32767.0f;
+
+__device__ __forceinline__ float i16_row_scale(const void* row) { return *reinterpret_cast<const float*>(row); }
+__device__ __forceinline__ const short2* i16_row_bins(const void* row) {
+  return reinterpret_cast<const short2*>(reinterpret_cast<const char*>(row) + kI16Header);
+}
+__device__ __forceinline__ short i16_quant(float v, float inv) {
+  const float q = fminf(fmaxf(rintf(v * inv), -kI16Max), kI16Max);
+  return (short)q;
+}
+
+// Quantise the n values s[PADI(0..n)] of a block into the int16 row `row`
+// (header + bins); every thread of the block calls it.  scratch: >= 32 floats.
+template <int T>
+__device__ __forceinline__ void store_i16_row(const float2* s, int n, void* row, float* scratch) {
+  float m = 0.0f;
+  for (int k = threadIdx.x; k < n; k += T) {
+    const float2 v = s[PADI(k)];
+    m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+  }
+  m = block_max(m, scratch);
+  const float inv = (m > 0.0f) ? kI16Max / m : 0.0f;
+  if (threadIdx.x < 4) reinterpret_cast<float*>(row)[threadIdx.x] = (threadIdx.x == 0) ? m / kI16Max : 0.0f;
+  short2* o = reinterpret_cast<short2*>(reinterpret_cast<char*>(row) + kI16Header);
+  for (int k = threadIdx.x; k < n; k += T) {
+    const float2 v = s[PADI(k)];
+    o[k] = make_short2(i16_quant(v.x, inv), i16_quant(v.y, inv));
+  }
+}
+
 }  // namespace fpcc

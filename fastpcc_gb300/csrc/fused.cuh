@@ -16,7 +16,7 @@ struct FusedArgs {
   long long ldx;
   int nrows;
   int rule;            // amplitude rule (0 F_REG, 1 D_REG, 2 PURE, 3 THRESH, 4 SUMTHR)
-  int fmt;             // 0 float2, 1 half2 spectra
+  int fmt;             // 0 float2, 1 half2, 2 block-scaled int16 spectra (header + short2)
   void* out;           // rows of Nz bins
   long long ldo;
 };
@@ -102,7 +102,9 @@ __global__ void __launch_bounds__(T, 1) k_station_fused(FusedArgs a) {
   for (int n = N + threadIdx.x; n < NZ; n += T) s[PADI(n)] = make_float2(0.0f, 0.0f);
   __syncthreads();
   ct_fft<-1, T, 1>(s, 1, 0, TwTab{zlo, zhi}, RADZ{});
-  if (a.fmt == 1) {
+  if (a.fmt == 2) {
+    store_i16_row<T>(s, NZ, reinterpret_cast<char*>(a.out) + (long long)row * a.ldo * 4, red);
+  } else if (a.fmt == 1) {
     __half2* o = reinterpret_cast<__half2*>(a.out) + (long long)row * a.ldo;
     for (int k = threadIdx.x; k < NZ; k += T) o[k] = __float22half2_rn(s[PADI(k)]);
   } else {

@@ -45,13 +45,25 @@ __device__ __forceinline__ float amp_factor(int rule, float m2, float eps) {
   return (m2 > eps) ? rsqrtf(m2) : 0.0f;   // src/ccs_cuda.cu:201-208, 223-230
 }
 
+// Bin i of a spectrum row; for block-scaled int16 rows the bins follow the
+// header and come back unscaled (the pair's scale product goes into the output).
 template <int FMT>
 __device__ __forceinline__ float2 load_bin(const void* base, int i) {
   if constexpr (FMT == SPEC_F16) {
     return __half22float2(reinterpret_cast<const __half2*>(base)[i]);
+  } else if constexpr (FMT == SPEC_I16) {
+    const short2 q = i16_row_bins(base)[i];
+    return make_float2((float)q.x, (float)q.y);
   } else {
     return reinterpret_cast<const float2*>(base)[i];
   }
+}
+
+// v / sqrt(e1 e2) for the overlap energies e1, e2 (exact FP64 differences of the
+// prefix sums): FP32 reciprocal square roots in the normal range, FP64 outside it.
+__device__ __forceinline__ float gncc_norm(float v, double e1, double e2) {
+  if (e1 >= 1e-30 && e2 >= 1e-30 && e1 <= 1e30 && e2 <= 1e30) return v * (rsqrtf((float)e1) * rsqrtf((float)e2));
+  return (float)((double)v / sqrt(e1 * e2));
 }
 
 template <int... Rs>
@@ -92,7 +104,10 @@ __global__ void __launch_bounds__(T, 1) k_spec(SpecArgs a) {
   __syncthreads();
   ct_fft<-1, T, 1>(s, 1, 0, TwTab{lo, hi}, RAD{});
   const int nout = (a.mode == SPEC_PHASE) ? NZ : (NZ / 2 + 1);
-  if (a.fmt == SPEC_F16) {
+  if (a.fmt == SPEC_I16) {
+    __shared__ float scratch[32];
+    store_i16_row<T>(s, nout, reinterpret_cast<char*>(a.out) + (int64_t)row * a.ldo * 4, scratch);
+  } else if (a.fmt == SPEC_F16) {
     __half2* o = reinterpret_cast<__half2*>(a.out) + (int64_t)row * a.ldo;
     for (int k = threadIdx.x; k < nout; k += T) o[k] = __float22half2_rn(s[PADI(k)]);
   } else {
@@ -144,7 +159,7 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
   build_twiddles(zlo, zhi, NZ);
   __syncthreads();
   const TwTab twZ{zlo, zhi};
-  constexpr int esz = (FMT == SPEC_F16) ? 4 : 8;
+  constexpr int esz = (FMT == SPEC_F32) ? 8 : 4;
   {
     const int p = blockIdx.x;
     const char* X1;
@@ -206,6 +221,7 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
       L = d.L;
       scale = d.scale != 0.0f ? d.scale
                               : (a.norm == 0 ? 1.0f / ((float)NZ * (float)N) : (float)(1.0 / (double)NZ));
+      if constexpr (FMT == SPEC_I16) scale *= i16_row_scale(d.a) * i16_row_scale(d.b);
     } else {
       const int2 pr = a.pairs[p];
       y = a.y + (int64_t)p * a.ldy;
@@ -217,6 +233,10 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
       lag0 = a.lag0;
       L = a.L;
       scale = a.scale;
+      if constexpr (FMT == SPEC_I16) {
+        const char* sp = reinterpret_cast<const char*>(a.spec);
+        scale *= i16_row_scale(sp + (int64_t)pr.x * a.ldspec * 4) * i16_row_scale(sp + (int64_t)pr.y * a.ldspec * 4);
+      }
     }
     for (int l = threadIdx.x; l < L; l += T) {
       const int lag = lag0 + l;
@@ -228,11 +248,9 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
         int n11 = 0, n21 = 0, n12 = N, n22 = N;
         if (lag > 0) { n21 = lag; n12 -= lag; }
         else { n11 = -lag; n22 += lag; }
-        const double e1 = E1[n12] - E1[n11];
-        const double e2 = E2[n22] - E2[n21];
-        v = (float)((double)v / sqrt(e1 * e2));
+        v = gncc_norm(v, E1[n12] - E1[n11], E2[n22] - E2[n21]);
       } else if (a.norm == 2) {
-        v = (float)((double)v / (double)(N - abs(lag)));
+        v = v / (float)(N - abs(lag));
       }
       y[l] = v;
     }
@@ -247,8 +265,27 @@ __global__ void __launch_bounds__(256) k_phase_store(PhaseArgs a) {
   const float eps = amp_eps(a.rule, a.rowstat[row]);
   const float2 v = a.in[(int64_t)row * a.ldin + n];
   const float2 p = cscale(v, amp_factor(a.rule, v.x * v.x + v.y * v.y, eps));
-  if (a.fmt == 1) reinterpret_cast<__half2*>(a.out)[(int64_t)row * a.ldo + n] = __float22half2_rn(p);
+  if (a.fmt == SPEC_I16)   // |p| <= 1: fixed scale 1/32767
+    reinterpret_cast<short2*>(a.out)[(int64_t)row * a.ldo + n] = make_short2(i16_quant(p.x, kI16Max),
+                                                                              i16_quant(p.y, kI16Max));
+  else if (a.fmt == SPEC_F16) reinterpret_cast<__half2*>(a.out)[(int64_t)row * a.ldo + n] = __float22half2_rn(p);
   else reinterpret_cast<float2*>(a.out)[(int64_t)row * a.ldo + n] = p;
+}
+
+// ------------------------------------------------------------ int16 rows
+// One block per row: the row maximum, then the block-scaled int16 row.
+__global__ void __launch_bounds__(256) k_quantize_i16(const float2* __restrict__ in, int64_t ldin, int n,
+                                                      char* __restrict__ out, int64_t ldo_bytes) {
+  __shared__ float scratch[32];
+  const float2* r = in + (int64_t)blockIdx.x * ldin;
+  float m = 0.0f;
+  for (int k = threadIdx.x; k < n; k += 256) m = fmaxf(m, fmaxf(fabsf(r[k].x), fabsf(r[k].y)));
+  m = block_max(m, scratch);
+  const float inv = (m > 0.0f) ? kI16Max / m : 0.0f;
+  char* row = out + (int64_t)blockIdx.x * ldo_bytes;
+  if (threadIdx.x < 4) reinterpret_cast<float*>(row)[threadIdx.x] = (threadIdx.x == 0) ? m / kI16Max : 0.0f;
+  short2* o = reinterpret_cast<short2*>(row + kI16Header);
+  for (int k = threadIdx.x; k < n; k += 256) o[k] = make_short2(i16_quant(r[k].x, inv), i16_quant(r[k].y, inv));
 }
 
 // ------------------------------------------------------------ generic passes
@@ -450,8 +487,16 @@ static cudaError_t launch_pairs_t(const PairArgs& a, cudaStream_t st) {
 cudaError_t launch_pairs(const PairArgs& a, cudaStream_t st) {
   if (a.npairs <= 0) return cudaSuccess;
   const bool herm = (a.norm != 0);
+  if (a.fmt == SPEC_I16) return herm ? cudaErrorInvalidValue : launch_pairs_t<SPEC_I16, false>(a, st);
   if (a.fmt == SPEC_F16) return herm ? launch_pairs_t<SPEC_F16, true>(a, st) : launch_pairs_t<SPEC_F16, false>(a, st);
   return herm ? launch_pairs_t<SPEC_F32, true>(a, st) : launch_pairs_t<SPEC_F32, false>(a, st);
+}
+
+cudaError_t launch_quantize_i16(const float2* in, int64_t ldin, int n, int nrows, void* out, int64_t ldo,
+                                cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  k_quantize_i16<<<nrows, 256, 0, st>>>(in, ldin, n, reinterpret_cast<char*>(out), ldo * 4);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_phase_store(const PhaseArgs& a, cudaStream_t st) {

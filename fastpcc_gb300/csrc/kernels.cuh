@@ -21,7 +21,7 @@ enum AmpRule : int {
   AMP_SUMTHR = 4   // cuda_AmpNormf2 on the sum (src/ccs_cuda.cu:493-511): x/|x| above 1e-6 sum|x|^2
 };
 
-enum SpecFmt : int { SPEC_F32 = 0, SPEC_F16 = 1 };
+enum SpecFmt : int { SPEC_F32 = 0, SPEC_F16 = 1, SPEC_I16 = 2 };
 
 // Station spectrum stage input modes.
 enum SpecMode : int {
@@ -85,6 +85,10 @@ size_t pair_smem_bytes(int Nz);
 cudaError_t launch_spec(const SpecArgs& a, cudaStream_t st);
 cudaError_t launch_pairs(const PairArgs& a, cudaStream_t st);
 cudaError_t launch_phase_store(const PhaseArgs& a, cudaStream_t st);
+// Block-scaled int16 rows (header + n short2, row stride ldo four-byte elements)
+// from float2 rows of stride ldin.
+cudaError_t launch_quantize_i16(const float2* in, int64_t ldin, int n, int nrows, void* out, int64_t ldo,
+                                cudaStream_t st);
 
 // Generic transforms for any 2,3,5-smooth length: one kernel per radix pass,
 // reading `in` and writing `out` (rows of n complex, row stride ld).  The first

@@ -37,8 +37,13 @@ __device__ __forceinline__ float factor_of(int rule, float m2, float eps) {
   return (m2 > eps) ? rsqrtf(m2) : 0.0f;
 }
 
+// Bin i of a spectrum row (int16 rows: after the header, unscaled).
 __device__ __forceinline__ float2 ld_bin(const void* base, int fmt, int64_t i) {
   if (fmt == SPEC_F16) return __half22float2(reinterpret_cast<const __half2*>(base)[i]);
+  if (fmt == SPEC_I16) {
+    const short2 q = i16_row_bins(base)[i];
+    return make_float2((float)q.x, (float)q.y);
+  }
   return reinterpret_cast<const float2*>(base)[i];
 }
 
@@ -54,7 +59,7 @@ __device__ __forceinline__ float2 pair_bin(const LargeArgs& a, int row, int p) {
     X2 = a.desc[row].b;
   } else {
     const int2 pr = a.pairs[row];
-    const int64_t esz = (a.fmt == SPEC_F16) ? 4 : 8;
+    const int64_t esz = (a.fmt == SPEC_F32) ? 8 : 4;
     X1 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.x * a.ldspec * esz;
     X2 = reinterpret_cast<const char*>(a.spec) + (int64_t)pr.y * a.ldspec * esz;
   }
@@ -196,6 +201,7 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
         L = d.L;
         scale = d.scale != 0.0f ? d.scale
                                 : (a.norm == 0 ? 1.0f / ((float)Nz * (float)N) : (float)(1.0 / (double)Nz));
+        if (a.fmt == SPEC_I16) scale *= i16_row_scale(d.a) * i16_row_scale(d.b);
         yrow = reinterpret_cast<float*>(d.y);
         if (a.norm == 1) { E1 = d.ea; E2 = d.eb; }
       } else {
@@ -204,8 +210,12 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
         L = a.L;
         scale = a.scale;
         yrow = a.y + (int64_t)row * a.ldy;
+        const int2 pr = a.pairs[row];
+        if (a.fmt == SPEC_I16) {
+          const char* sp = reinterpret_cast<const char*>(a.spec);
+          scale *= i16_row_scale(sp + (int64_t)pr.x * a.ldspec * 4) * i16_row_scale(sp + (int64_t)pr.y * a.ldspec * 4);
+        }
         if (a.norm == 1) {
-          const int2 pr = a.pairs[row];
           E1 = a.energy + (int64_t)pr.x * a.ldE;
           E2 = a.energy + (int64_t)pr.y * a.ldE;
         }
@@ -221,9 +231,11 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
           int n11 = 0, n21 = 0, n12 = N, n22 = N;
           if (lag > 0) { n21 = lag; n12 -= lag; }
           else { n11 = -lag; n22 += lag; }
-          val = (float)((double)val / sqrt((E1[n12] - E1[n11]) * (E2[n22] - E2[n21])));
+          const double e1 = E1[n12] - E1[n11], e2 = E2[n22] - E2[n21];
+          if (e1 >= 1e-30 && e2 >= 1e-30 && e1 <= 1e30 && e2 <= 1e30) val *= rsqrtf((float)e1) * rsqrtf((float)e2);
+          else val = (float)((double)val / sqrt(e1 * e2));
         } else if (a.norm == 2) {
-          val = (float)((double)val / (double)(N - abs(lag)));
+          val = val / (float)(N - abs(lag));
         }
         yrow[l] = val;
       }

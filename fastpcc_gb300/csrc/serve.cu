@@ -191,7 +191,7 @@ int64_t wkey(int sta, int win) { return ((int64_t)sta << 32) | (uint32_t)win; }
 size_t product_row_bytes(const Product& p) {
   switch (p.kind) {
     case 0: return (size_t)p.N * 4;
-    case 1: return (size_t)p.Nz * (p.fmt ? 4 : 8);
+    case 1: return p.fmt == FPCC_I16 ? 16 + (size_t)p.Nz * 4 : (size_t)p.Nz * (p.fmt ? 4 : 8);
     case 2: case 3: case 4: return (size_t)(p.Nz / 2 + 1) * 8;
     case 5: return (size_t)(p.N + 1) * 8;
     case 6: return (size_t)p.N * (p.fmt ? 4 : 8);
@@ -342,8 +342,8 @@ bool packable(int method, int Nz) {
 }
 
 int product_fmt(const Server* s, int method) {
-  return (method == FPCC_PCC2 || method == FPCC_PCC1 || method == FPCC_PCCV || method == FPCC_WPCC) ? s->fmt
-                                                                                                     : FPCC_F32;
+  if (method == FPCC_WPCC) return s->fmt == FPCC_I16 ? FPCC_F32 : s->fmt;   // wavelet spectra: F32 or F16
+  return (method == FPCC_PCC2 || method == FPCC_PCC1 || method == FPCC_PCCV) ? s->fmt : FPCC_F32;
 }
 
 void method_kinds(int m, int* kind1, int* kind2) {
@@ -950,7 +950,7 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
 
 extern "C" int fpcc_server_set_format(fpcc_server* h, int fmt) {
   Server* s = reinterpret_cast<Server*>(h);
-  if (!s || (fmt != FPCC_F32 && fmt != FPCC_F16)) return FPCC_EARG;
+  if (!s || (fmt != FPCC_F32 && fmt != FPCC_F16 && fmt != FPCC_I16)) return FPCC_EARG;
   std::lock_guard<std::mutex> lk(s->mu);
   if (s->next_id) return FPCC_EARG;   // before the first request
   s->fmt = fmt;

@@ -57,8 +57,14 @@ enum fpcc_amp_rule {
   FPCC_AMP_SUMTHR = 4  /* x/|x| above 1e-6 sum|x|^2, src/ccs_cuda.cu:493-511        */
 };
 
-/* Storage formats of cached station products. */
-enum fpcc_format { FPCC_F32 = 0, FPCC_F16 = 1 };
+/* Storage formats of cached station products (phase spectra, phase signals).
+ * FPCC_I16: block-scaled int16 — phase-spectrum rows start with a 16-byte
+ * header holding the row's float scale (value = q * scale, the largest
+ * component at 32767), then Nz short2 bins, so a row spans Nz + 4 four-byte
+ * elements; phase-signal rows hold N short2 values of scale 1/32767 (|phase| <= 1)
+ * and no header.  4 bytes per complex value like F16, with about 8 times less
+ * rounding error on the correlations. */
+enum fpcc_format { FPCC_F32 = 0, FPCC_F16 = 1, FPCC_I16 = 2 };
 
 /* 1-bit sign rules: the reference maps x1 >= 0 -> +1 but x2 > 0 -> +1
  * (src/FFTapps.c:1037,1042). */
@@ -107,6 +113,8 @@ int fpcc_autotune_load(const char *json_path);
 int fpcc_max_block_len(void);
 /* Elements per row of the station product of a method (for sizing buffers). */
 int64_t fpcc_station_row_elems(int method, int N, int Nz);
+/* Bytes per row of the station product of a method in a storage format. */
+int64_t fpcc_station_row_bytes(int method, int N, int Nz, int fmt);
 
 /* ---- device-resident stages (all pointers are device memory) -------------
  * Station stage: one output row per input row.

@@ -85,6 +85,20 @@ def test_pcc2_fp16_storage(F, orc):
     assert relerr(F.pcc2_set(a, b, -450, 450, fmt=F.F16), y64) < 3e-4
 
 
+@pytest.mark.parametrize("N,l1,l2,nz", [(1000, -100, 100, 1), (4500, -450, 450, 1), (18000, -2000, 2000, 1),
+                                         (36000, -3000, 3000, 1 << 17)])
+def test_int16_storage_within_1e4(F, orc, N, l1, l2, nz):
+    """Block-scaled int16 phase spectra (PCC2) and fixed-scale int16 phase
+    signals (PCC1): 4 bytes per complex value, within 1e-4 of the FP64 oracle
+    (in-block, run-time specialised and four-step station paths)."""
+    a, b = _data(N, 2, -N // 30, "i16")
+    y64 = orc.pcc2(a, b, l1, l2)
+    assert relerr(F.pcc2_set(a, b, l1, l2, fmt=F.I16, nz_mode=nz), y64) < TOL
+    assert relerr(F.pcc2_set(a, b, l1, l2, fmt=F.I16, nz_mode=nz, plain=True), y64) < TOL
+    if N <= 4500:
+        assert relerr(F.pcc1_set(a, b, l1, l2, fmt=F.I16), orc.pcc1(a, b, l1, l2)) < TOL
+
+
 def test_pcc2_reference_padding_rule(F, orc):
     a, b = _data(3000, 2, 60, "nzref")
     y64 = orc.pcc2(a, b, -500, 500)

@@ -280,3 +280,20 @@ def test_server_releases_idle_product_classes(F, orc):
     assert st["station_rows"] > 15
     for (m, s1, s2, w, l1, l2, v), out in zip(reqs, outs):
         assert relerr(out, orc.pcc2(xs[w][s1][None], xs[w][s2][None], l1, l2)[0]) < TOL
+
+
+def test_server_int16_storage(F, orc):
+    lengths = [2048, 3000, 3557, 30011]
+    xs = _uneven_windows(lengths, "serve/i16")
+    reqs = _uneven(11, 40, lengths, [0, 4])
+    srv = F.Server(hbm_budget=1 << 30, fmt=F.I16)
+    for w, x in xs.items():
+        for s in range(5):
+            srv.put(s, w, x[s])
+    outs = _run(F, srv, reqs)
+    srv.close()
+    for (m, s1, s2, w, l1, l2, v), out in zip(reqs, outs):
+        a, b = xs[w][s1], xs[w][s2]
+        if m == 4 and len(a) > 5000:
+            continue   # the FP64 direct-sum oracle is slow at this length
+        assert relerr(out, _oracle(orc, m, a, b, l1, l2, v)) < TOL, (m, len(a), l1, l2)
