@@ -652,14 +652,27 @@ int analytic_rows(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, 
   return 0;
 }
 
-// FP64 analytic signals for the listed rows of `an` (stride N), then the row
-// statistics of all rows again.
-int refine_rows_stats(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, const std::vector<int>& rows,
-                      const float2* an, const float* rmax, const float* rsum) {
-  if (rows.empty()) return 0;
-  int rc = refine_analytic(c, d_x, ldx, N, rows, const_cast<float2*>(an), N);
-  if (rc) return rc;
-  CK(launch_rowstats(an, N, N, nrows, const_cast<float*>(rmax), const_cast<float*>(rsum), c->stream));
+// Analytic signals of nrows rows with the listed rows in FP64: when every row is
+// listed the FP32 transforms are skipped altogether.
+int analytic_rows_p64(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, const std::vector<int>& rows,
+                      const float2** out, const float** rmax, const float** rsum) {
+  if ((int)rows.size() != nrows || nrows == 0) {
+    int rc = analytic_rows(c, d_x, ldx, nrows, N, out, rmax, rsum);
+    if (rc || rows.empty()) return rc;
+    rc = refine_analytic(c, d_x, ldx, N, rows, const_cast<float2*>(*out), N);
+    if (rc) return rc;
+  } else {
+    void *A, *S;
+    int rc;
+    if ((rc = dev_buf(c, S_ANA_A, (size_t)nrows * N * sizeof(float2), &A)) ||
+        (rc = dev_buf(c, S_RSTAT, (size_t)2 * nrows * sizeof(float), &S)))
+      return rc;
+    if ((rc = refine_analytic(c, d_x, ldx, N, rows, (float2*)A, N))) return rc;
+    *out = (const float2*)A;
+    *rmax = (const float*)S;
+    *rsum = (const float*)S + nrows;
+  }
+  CK(launch_rowstats(*out, N, N, nrows, const_cast<float*>(*rmax), const_cast<float*>(*rsum), c->stream));
   g_launches++;
   return 0;
 }
@@ -695,11 +708,12 @@ extern "C" int fpcc_station_stage_ex(fpcc_ctx* c, int method, const float* d_x, 
     } else if ((rc = precise_rows(c, d_x, ldx, nrows, N, &p64))) {
       return rc;
     }
+    std::sort(p64.begin(), p64.end());
+    p64.erase(std::unique(p64.begin(), p64.end()), p64.end());
   }
   if (method == FPCC_PCC1 || method == FPCC_PCCV) {
     const float2 *an; const float *rmax, *rsum;
-    if ((rc = analytic_rows(c, d_x, ldx, nrows, N, &an, &rmax, &rsum))) return rc;
-    if ((rc = refine_rows_stats(c, d_x, ldx, nrows, N, p64, an, rmax, rsum))) return rc;
+    if ((rc = analytic_rows_p64(c, d_x, ldx, nrows, N, p64, &an, &rmax, &rsum))) return rc;
     PhaseArgs a{};
     a.in = an; a.ldin = N; a.nrows = nrows; a.N = N; a.rule = rule;
     a.rowstat = (rule == FPCC_AMP_SUMTHR) ? rsum : rmax;
@@ -718,8 +732,7 @@ extern "C" int fpcc_station_stage_ex(fpcc_ctx* c, int method, const float* d_x, 
   if (!spec_supported(Nz)) {
     if (method == FPCC_PCC2) {
       const float2 *an; const float *rmax, *rsum;
-      if ((rc = analytic_rows(c, d_x, ldx, nrows, N, &an, &rmax, &rsum))) return rc;
-      if ((rc = refine_rows_stats(c, d_x, ldx, nrows, N, p64, an, rmax, rsum))) return rc;
+      if ((rc = analytic_rows_p64(c, d_x, ldx, nrows, N, p64, &an, &rmax, &rsum))) return rc;
       return large_station(c, COL_PHASE, an, sizeof(float2), N, nrows, N, Nz, rule,
                            (rule == FPCC_AMP_SUMTHR) ? rsum : rmax, 0, fmt, 0, d_out, ldo);
     }
@@ -739,8 +752,7 @@ extern "C" int fpcc_station_stage_ex(fpcc_ctx* c, int method, const float* d_x, 
   a.nrows = nrows; a.N = N; a.Nz = Nz; a.fmt = fmt; a.out = d_out; a.ldo = ldo;
   if (method == FPCC_PCC2) {
     const float2 *an; const float *rmax, *rsum;
-    if ((rc = analytic_rows(c, d_x, ldx, nrows, N, &an, &rmax, &rsum))) return rc;
-    if ((rc = refine_rows_stats(c, d_x, ldx, nrows, N, p64, an, rmax, rsum))) return rc;
+    if ((rc = analytic_rows_p64(c, d_x, ldx, nrows, N, p64, &an, &rmax, &rsum))) return rc;
     a.in = an; a.ldin = N; a.mode = SPEC_PHASE; a.rule = rule;
     a.rowstat = (rule == FPCC_AMP_SUMTHR) ? rsum : rmax;
   } else {

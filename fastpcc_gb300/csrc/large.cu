@@ -210,14 +210,17 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
         L = a.L;
         scale = a.scale;
         yrow = a.y + (int64_t)row * a.ldy;
-        const int2 pr = a.pairs[row];
-        if (a.fmt == SPEC_I16) {
-          const char* sp = reinterpret_cast<const char*>(a.spec);
-          scale *= i16_row_scale(sp + (int64_t)pr.x * a.ldspec * 4) * i16_row_scale(sp + (int64_t)pr.y * a.ldspec * 4);
-        }
-        if (a.norm == 1) {
-          E1 = a.energy + (int64_t)pr.x * a.ldE;
-          E2 = a.energy + (int64_t)pr.y * a.ldE;
+        // station rows of the pair: only with a pair list (precomputed cross-spectrum rows have none)
+        if (a.herm != 2 && (a.fmt == SPEC_I16 || a.norm == 1)) {
+          const int2 pr = a.pairs[row];
+          if (a.fmt == SPEC_I16) {
+            const char* sp = reinterpret_cast<const char*>(a.spec);
+            scale *= i16_row_scale(sp + (int64_t)pr.x * a.ldspec * 4) * i16_row_scale(sp + (int64_t)pr.y * a.ldspec * 4);
+          }
+          if (a.norm == 1) {
+            E1 = a.energy + (int64_t)pr.x * a.ldE;
+            E2 = a.energy + (int64_t)pr.y * a.ldE;
+          }
         }
       }
 #pragma unroll
