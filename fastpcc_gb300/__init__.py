@@ -107,6 +107,9 @@ def lib():
             L.fpcc_wpcc_pair_stage.argtypes = [vp, vp, vp, i, vp, i, vp, i64]
             L.fpcc_wpcc_plan_set_lags.argtypes = [vp, i, i]
             L.fpcc_pair_stage_packed.argtypes = [vp, i, i, i, vp, i, i, f, i]
+            L.fpcc_clip_rows.argtypes = [vp, vp, i64, i, i]
+            L.fpcc_whiten_rows.argtypes = [vp, vp, i64, i, i, d, d, d]
+            L.fpcc_prep_last_error.restype = C.c_char_p
             L.fpcc_server_create.argtypes = [C.POINTER(vp), i, C.c_size_t, i]
             L.fpcc_server_set_format.argtypes = [vp, i]
             L.fpcc_server_set_nz_mode.argtypes = [vp, i]

@@ -36,14 +36,15 @@ def sources():
 
 def _newest_input() -> float:
     t = 0.0
-    for d in (CSRC, os.path.join(os.path.dirname(HERE), "include")):
+    for d in (CSRC, os.path.join(HERE, "cli"), os.path.join(os.path.dirname(HERE), "include")):
         for f in os.listdir(d):
             t = max(t, os.path.getmtime(os.path.join(d, f)))
     return max(t, os.path.getmtime(__file__))
 
 
 def up_to_date() -> bool:
-    return os.path.exists(OUT) and os.path.getmtime(OUT) >= _newest_input()
+    return (os.path.exists(OUT) and os.path.exists(CLI_OUT) and
+            min(os.path.getmtime(OUT), os.path.getmtime(CLI_OUT)) >= _newest_input())
 
 
 def cuda_home(cc: str) -> str:
@@ -94,7 +95,24 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, OUT)
+    build_cli(cc)
     return OUT
+
+
+CLI_SRC = os.path.join(HERE, "cli", "fpcc_fullpair.cpp")
+CLI_OUT = os.path.join(HERE, "bin", "fpcc_fullpair")
+
+
+def build_cli(cc: str) -> str:
+    """The command-line program (host C++), linked against the library in place."""
+    os.makedirs(os.path.dirname(CLI_OUT), exist_ok=True)
+    cmd = [cc, "-O2", "-std=c++17", CLI_SRC, "-o", CLI_OUT + ".tmp", "-L" + HERE, "-lfastpcc_gb300", "-lcudart",
+           "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN/..", "-Xcompiler", "-pthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"building the CLI failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(CLI_OUT + ".tmp", CLI_OUT)
+    return CLI_OUT
 
 
 if __name__ == "__main__":

@@ -160,6 +160,20 @@ typedef struct {
 int fpcc_pair_stage_packed(fpcc_ctx *ctx, int method, int fmt, int Nz, const fpcc_pair_desc *d_desc,
                            int npairs, int maxL, float v, int numerators);
 
+/* ---- preprocessing of station windows (device memory, in place) -----------
+ * The reference CLI's optional steps before correlating (src/PCC_fullpair_1b.c).
+ * fpcc_clip_rows: clip each of nrows rows (N samples, stride ldx) at
+ *   4 median(|x|) / 0.6745 (clipping :881-891 with qabsmedian :1179-1214).
+ * fpcc_whiten_rows: smooth spectral whitening of a station's windows between
+ *   f1 and f2 Hz at sampling interval dt (AveWhite :1065-1177): FP64 transforms
+ *   of length 2^ceil(log2 N), the amplitude spectrum averaged over the nrows
+ *   windows, the band-limited inverse filter (gain capped at 1000x its minimum,
+ *   11-tap smoothing), applied to every window.  Messages: fpcc_prep_last_error(). */
+int fpcc_clip_rows(fpcc_ctx *ctx, float *d_x, int64_t ldx, int nrows, int N);
+int fpcc_whiten_rows(fpcc_ctx *ctx, float *d_x, int64_t ldx, int nrows, int N, double f1, double f2,
+                     double dt);
+const char *fpcc_prep_last_error(void);
+
 /* ---- host-buffer entry points (row-pointer arrays like the reference's *_set)
  * x1, x2: Tr rows of N floats (station 1 / station 2 windows); y: Tr rows of L.
  * The "batched" calls run each stage once over all windows; the plain drop-ins
