@@ -163,7 +163,9 @@ void whitening_filter(std::vector<double>& H, int N, int Nz, double f1, double f
     s += win[m];
   }
   for (int m = 0; m < 11; m++) win[m] /= s;
-  // convolution HS[n-5] = sum_m win[m] H[n-m], mirrored at DC and at Nyquist
+  // convolution HS[n-5] = sum_m win[m] H[n-m], mirrored at DC and at Nyquist.
+  // The reference's loops skip n = 10, leaving HS[5] as its fresh allocation
+  // holds it (zeros for the large buffers of long windows); it is zero here.
   HS.assign(Nh, 0.0);
   for (int k = 5; k < 10; k++) {
     double a = 0;
