@@ -23,6 +23,7 @@
 #include "wavelet.h"
 #include "wpcc.h"
 #include "precise.cuh"
+#include "multi.cuh"
 
 using namespace fpcc;
 
@@ -69,6 +70,11 @@ struct fpcc_ctx {
   std::map<int, float2*> bluestein;  // per window length N: M-point filter spectra, forward then inverse
   std::map<int, double2*> twiddles64;   // FP64 tables exp(-2 pi i t/n)
   std::map<int, double2*> bluestein64;  // FP64 filter spectra per N, forward then inverse
+  // filter spectra of the packed path per (N, M, fp64): forward then inverse, M values each,
+  // held in blocks of one batched computation
+  std::map<std::tuple<int, int, int>, void*> multi_filters;
+  std::vector<void*> multi_blocks;
+  size_t multi_filter_bytes = 0;
   int precision = FPCC_ANALYTIC_AUTO;   // when analytic signals are computed in FP64
   std::mutex mu;
 };
@@ -170,6 +176,7 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
   for (auto& kv : c->bluestein) cudaFree(kv.second);
   for (auto& kv : c->twiddles64) cudaFree(kv.second);
   for (auto& kv : c->bluestein64) cudaFree(kv.second);
+  for (void* b : c->multi_blocks) cudaFree(b);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
   {
@@ -256,7 +263,7 @@ namespace {
 enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_PAIRS = 5, S_ANA_A = 6,
             S_ANA_B = 7, S_RSTAT = 8, S_LARGE_T = 9, S_WP_X = 10, S_WP_BAND = 11, S_WP_RMAX = 12,
             S_WP_Y = 13, S_WP_STAGE = 14, S_BLUE_O = 23, S_P64_D = 24, S_P64_A = 25, S_P64_B = 26,
-            S_P64_CNT = 27, S_I16_Q = 28 };
+            S_P64_CNT = 27, S_I16_Q = 28, S_MULTI_A = 29, S_MULTI_B = 30, S_MULTI_AN = 31 };
 
 constexpr size_t kLargeChunkBytes = size_t(512) << 20;   // four-step intermediate per chunk
 
@@ -677,7 +684,226 @@ int analytic_rows_p64(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int
   return 0;
 }
 
+// ---------------------------------------------------------------- packed analytic signals
+// Bluestein length class of a window length: the smallest 2^a, 3 2^a or 5 2^a
+// >= 2N - 1 (about three classes per octave, so windows of nearby lengths share
+// their transforms).
+int bluestein_class_len(int N) {
+  const int need = 2 * N - 1;
+  int best = -1;
+  for (int base : {1, 3, 5})
+    for (long long m = base; m <= (1LL << 26); m *= 2)
+      if (m >= need) {
+        if (best < 0 || m < best) best = (int)m;
+        break;
+      }
+  return best;
+}
+
+constexpr size_t kMultiFilterCache = (size_t)1 << 30;   // bytes of cached filter spectra per context
+
+// Filter spectra (forward, inverse) of every window length in Ns for transforms
+// of M points in precision T; returns device pointers per entry of Ns.  New
+// lengths are computed together (their filters as rows of one batched
+// transform) and cached in blocks; the cache is emptied first when it would
+// grow past kMultiFilterCache.
+template <typename T>
+int multi_filters(fpcc_ctx* c, const std::vector<int>& Ns, int M, std::vector<const void*>& fwd,
+                  std::vector<const void*>& inv) {
+  const int f64 = sizeof(T) == 16;
+  std::vector<int> missing;
+  for (int N : Ns)
+    if (!c->multi_filters.count(std::make_tuple(N, M, f64)) &&
+        std::find(missing.begin(), missing.end(), N) == missing.end())
+      missing.push_back(N);
+  const size_t need = missing.size() * (size_t)2 * M * sizeof(T);
+  if (need && c->multi_filter_bytes + need > kMultiFilterCache && c->multi_filter_bytes) {
+    CK(cudaStreamSynchronize(c->stream));
+    for (void* b : c->multi_blocks) cudaFree(b);
+    c->multi_blocks.clear();
+    c->multi_filters.clear();
+    c->multi_filter_bytes = 0;
+    missing.clear();
+    for (int N : Ns)
+      if (std::find(missing.begin(), missing.end(), N) == missing.end()) missing.push_back(N);
+  }
+  for (size_t i0 = 0; i0 < missing.size(); i0 += 64) {
+    const int n = (int)std::min<size_t>(64, missing.size() - i0);
+    const std::vector<int> lens(missing.begin() + i0, missing.begin() + i0 + n);
+    void *B, *A, *dN;
+    int rc;
+    if ((rc = dev_buf(c, S_MULTI_B, (size_t)2 * n * M * sizeof(T), &B)) ||
+        (rc = dev_buf(c, S_MULTI_A, (size_t)2 * n * M * sizeof(T), &A)) ||
+        (rc = dev_buf(c, S_P64_CNT, (size_t)n * sizeof(int), &dN)))
+      return rc;
+    CK(cudaMemcpyAsync(dN, lens.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    // rows [0, n): forward filters; rows [n, 2n): inverse filters
+    CK(launch_multi_filter<T>((const int*)dN, n, (T*)B, M, -1, c->stream));
+    CK(launch_multi_filter<T>((const int*)dN, n, (T*)B + (size_t)n * M, M, +1, c->stream));
+    g_launches += 2;
+    void* res = nullptr;
+    if constexpr (sizeof(T) == 16) {
+      double2* r = nullptr;
+      if ((rc = passes64(c, (double2*)B, (double2*)A, M, 2 * n, -1, &r))) return rc;
+      res = r;
+    } else {
+      float2* r = nullptr;
+      if ((rc = passes(c, (float2*)B, (float2*)A, M, 2 * n, -1, &r))) return rc;
+      res = r;
+    }
+    void* block = nullptr;
+    CK(cudaMalloc(&block, (size_t)2 * n * M * sizeof(T)));
+    c->multi_blocks.push_back(block);
+    c->multi_filter_bytes += (size_t)2 * n * M * sizeof(T);
+    for (int j = 0; j < n; j++) {
+      char* dst = (char*)block + (size_t)2 * j * M * sizeof(T);
+      CK(cudaMemcpyAsync(dst, (const char*)res + (size_t)j * M * sizeof(T), (size_t)M * sizeof(T),
+                         cudaMemcpyDeviceToDevice, c->stream));
+      CK(cudaMemcpyAsync(dst + (size_t)M * sizeof(T), (const char*)res + (size_t)(n + j) * M * sizeof(T),
+                         (size_t)M * sizeof(T), cudaMemcpyDeviceToDevice, c->stream));
+      c->multi_filters[std::make_tuple(lens[j], M, f64)] = dst;
+    }
+  }
+  fwd.resize(Ns.size());
+  inv.resize(Ns.size());
+  for (size_t i = 0; i < Ns.size(); i++) {
+    char* p = (char*)c->multi_filters.at(std::make_tuple(Ns[i], M, f64));
+    fwd[i] = p;
+    inv[i] = p + (size_t)M * sizeof(T);
+  }
+  return 0;
+}
+
+// Analytic signals of `rows` (all of length class M, precision T) into their
+// out pointers, in chunks that keep each transform buffer under 512 MB.
+template <typename T>
+int multi_group(fpcc_ctx* c, std::vector<MultiRow>& rows, int M) {
+  std::vector<int> Ns(rows.size());
+  for (size_t i = 0; i < rows.size(); i++) Ns[i] = rows[i].N;
+  std::vector<const void*> fwd, inv;
+  int rc = multi_filters<T>(c, Ns, M, fwd, inv);
+  if (rc) return rc;
+  for (size_t i = 0; i < rows.size(); i++) { rows[i].ffwd = fwd[i]; rows[i].finv = inv[i]; }
+  const int chunk = (int)std::max<size_t>(1, std::min<size_t>(4096, ((size_t)512 << 20) / ((size_t)M * sizeof(T))));
+  for (size_t r0 = 0; r0 < rows.size(); r0 += chunk) {
+    const int n = (int)std::min<size_t>(chunk, rows.size() - r0);
+    void *A, *B, *d;
+    if ((rc = dev_buf(c, S_MULTI_A, (size_t)n * M * sizeof(T), &A)) ||
+        (rc = dev_buf(c, S_MULTI_B, (size_t)n * M * sizeof(T), &B)) ||
+        (rc = dev_buf(c, S_P64_CNT, (size_t)n * sizeof(MultiRow), &d)))
+      return rc;
+    CK(cudaMemcpyAsync(d, rows.data() + r0, (size_t)n * sizeof(MultiRow), cudaMemcpyHostToDevice, c->stream));
+    const MultiRow* dr = (const MultiRow*)d;
+    T* bufs[2] = {(T*)A, (T*)B};
+    int cur = 0;
+    auto tr = [&](int dir) -> int {
+      T* res = nullptr;
+      int rc2;
+      if constexpr (sizeof(T) == 16) rc2 = passes64(c, (double2*)bufs[cur], (double2*)bufs[cur ^ 1], M, n, dir, (double2**)&res);
+      else rc2 = passes(c, (float2*)bufs[cur], (float2*)bufs[cur ^ 1], M, n, dir, (float2**)&res);
+      if (rc2) return rc2;
+      if (res != bufs[cur]) cur ^= 1;
+      return 0;
+    };
+    CK(launch_multi_pre<T>(dr, n, bufs[cur], M, c->stream));
+    if ((rc = tr(-1))) return rc;
+    CK(launch_multi_mul<T>(dr, n, bufs[cur], M, 0, c->stream));
+    if ((rc = tr(+1))) return rc;
+    CK(launch_multi_mask<T>(dr, n, bufs[cur], M, c->stream));
+    if ((rc = tr(-1))) return rc;
+    CK(launch_multi_mul<T>(dr, n, bufs[cur], M, 1, c->stream));
+    if ((rc = tr(+1))) return rc;
+    CK(launch_multi_post<T>(dr, n, bufs[cur], M, c->stream));
+    g_launches += 5;
+  }
+  return 0;
+}
+
 }  // namespace
+
+extern "C" int fpcc_station_stage_multi(fpcc_ctx* c, int method, const fpcc_station_row* h_rows, int nrows,
+                                        int fmt, int rule, void* d_out, int64_t ldo) {
+  if (!c || (!h_rows && nrows > 0) || !d_out) return fail(FPCC_EARG, "null argument");
+  if (nrows <= 0) return 0;
+  if (method != FPCC_PCC2 && method != FPCC_PCC1 && method != FPCC_PCCV)
+    return fail(FPCC_EUNSUP, "the packed station stage serves the phase methods");
+  if (fmt < FPCC_F32 || fmt > FPCC_I16) return fail(FPCC_EARG, "unknown storage format %d", fmt);
+  for (int r = 1; r < nrows; r++)
+    if (h_rows[r].N < h_rows[r - 1].N || (h_rows[r].N == h_rows[r - 1].N && h_rows[r].Nz < h_rows[r - 1].Nz))
+      return fail(FPCC_EARG, "rows must be ordered by (N, Nz)");
+  for (int r = 0; r < nrows; r++) {
+    const auto& q = h_rows[r];
+    if (q.N <= 0 || !q.d_x) return fail(FPCC_EARG, "row %d: bad window", r);
+    if (method == FPCC_PCC2) {
+      if (q.Nz < q.N || (q.Nz & 1)) return fail(FPCC_EARG, "row %d: Nz=%d must be even and >= N", r, q.Nz);
+      if (fpcc_station_row_bytes(method, q.N, q.Nz, fmt) > ldo * (fmt == FPCC_F32 ? 8 : 4))
+        return fail(FPCC_EARG, "row %d does not fit ldo", r);
+    } else if (q.N > ldo) {
+      return fail(FPCC_EARG, "row %d does not fit ldo", r);
+    }
+  }
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  // analytic signals, packed: row r at offset off[r] (float2)
+  std::vector<int64_t> off(nrows + 1, 0);
+  for (int r = 0; r < nrows; r++) off[r + 1] = off[r] + h_rows[r].N;
+  void *an, *st;
+  int rc;
+  if ((rc = dev_buf(c, S_MULTI_AN, (size_t)off[nrows] * sizeof(float2), &an)) ||
+      (rc = dev_buf(c, S_RSTAT, (size_t)2 * nrows * sizeof(float), &st)))
+    return rc;
+  std::map<std::pair<int, int>, std::vector<MultiRow>> groups;   // (M, fp64)
+  std::vector<MultiRow> all(nrows);
+  for (int r = 0; r < nrows; r++) {
+    MultiRow m{};
+    m.x = h_rows[r].d_x;
+    m.out = (float2*)an + off[r];
+    m.N = h_rows[r].N;
+    all[r] = m;
+    groups[{bluestein_class_len(m.N), h_rows[r].f64 ? 1 : 0}].push_back(m);
+  }
+  for (auto& kv : groups) {
+    const int M = kv.first.first;
+    rc = kv.first.second ? multi_group<double2>(c, kv.second, M) : multi_group<float2>(c, kv.second, M);
+    if (rc) return rc;
+  }
+  void* dall;
+  if ((rc = dev_buf(c, S_P64_CNT, (size_t)nrows * sizeof(MultiRow), &dall))) return rc;
+  CK(cudaMemcpyAsync(dall, all.data(), (size_t)nrows * sizeof(MultiRow), cudaMemcpyHostToDevice, c->stream));
+  float* rmax = (float*)st;
+  float* rsum = rmax + nrows;
+  CK(launch_multi_rowstats((const MultiRow*)dall, nrows, rmax, rsum, c->stream));
+  g_launches++;
+  // normalisation, zero padding and DFT_Nz (or the phase signal) per (N, Nz) run of rows
+  const size_t oesz = fmt == FPCC_F32 ? 8 : 4;
+  for (int r0 = 0; r0 < nrows;) {
+    int r1 = r0 + 1;
+    while (r1 < nrows && h_rows[r1].N == h_rows[r0].N && h_rows[r1].Nz == h_rows[r0].Nz) r1++;
+    const int N = h_rows[r0].N, Nz = h_rows[r0].Nz, n = r1 - r0;
+    const float2* in = (const float2*)an + off[r0];
+    const float* rs = ((rule == FPCC_AMP_SUMTHR) ? rsum : rmax) + r0;
+    void* out = (char*)d_out + (size_t)r0 * ldo * oesz;
+    if (method == FPCC_PCC2) {
+      if (spec_supported(Nz)) {
+        SpecArgs a{};
+        a.in = in; a.ldin = N; a.nrows = n; a.N = N; a.Nz = Nz; a.mode = SPEC_PHASE; a.rule = rule;
+        a.rowstat = rs; a.fmt = fmt; a.out = out; a.ldo = ldo;
+        CK(launch_spec(a, c->stream));
+        g_launches++;
+      } else if ((rc = large_station(c, COL_PHASE, in, sizeof(float2), N, n, N, Nz, rule, rs, 0, fmt, 0, out, ldo))) {
+        return rc;
+      }
+    } else {
+      PhaseArgs a{};
+      a.in = in; a.ldin = N; a.nrows = n; a.N = N; a.rule = rule; a.rowstat = rs;
+      a.fmt = fmt; a.out = out; a.ldo = ldo;
+      CK(launch_phase_store(a, c->stream));
+      g_launches++;
+    }
+    r0 = r1;
+  }
+  return 0;
+}
 
 extern "C" int fpcc_station_stage(fpcc_ctx* c, int method, const float* d_x, int64_t ldx, int nrows, int N,
                                   int Nz, int fmt, int rule, void* d_out, int64_t ldo) {

@@ -28,6 +28,7 @@
 #include <list>
 #include <map>
 #include <mutex>
+#include <set>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -65,6 +66,20 @@ cudaError_t copy_rows(const void* src, int64_t lds, const int* sidx, void* dst, 
   if (gx < 1) gx = 1;
   k_copy_rows<<<dim3(gx, n), 256, 0, st>>>((const char*)src, lds, sidx, (char*)dst, ldd, didx, row_bytes);
   return cudaGetLastError();
+}
+
+// Row copies with their own source, destination and length (16-byte aligned).
+struct RowCopy {
+  const char* src;
+  char* dst;
+  int64_t bytes;
+};
+
+__global__ void k_scatter_rows(const RowCopy* __restrict__ rc) {
+  const RowCopy r = rc[blockIdx.y];
+  const int64_t n16 = r.bytes / 16;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += (int64_t)gridDim.x * blockDim.x)
+    reinterpret_cast<int4*>(r.dst)[i] = reinterpret_cast<const int4*>(r.src)[i];
 }
 
 // A slab of equal rows with least-recently-used recycling.
@@ -561,6 +576,94 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
   return 0;
 }
 
+// Station products of the phase methods for windows of different lengths, in
+// shared launches (fpcc_station_stage_multi): every missing product of the group
+// whose window length is not 2,3,5-smooth, or whose window has zero samples
+// (FP64 analytic signal), is made here; the per-length path makes the rest.
+// Which path makes a product depends only on its window, so a result is the
+// same alone and in any mix.
+int prefetch_phase(Server* s, const GroupKey& g, int kind, std::vector<Req*>& reqs, InFlight& fl) {
+  const int Nz = (kind == 1) ? g.Nz : 0;
+  struct Miss {
+    int N;
+    int64_t key;
+    Slab* sl;
+    int row;
+    int f64;
+  };
+  std::vector<Miss> miss;
+  std::set<std::pair<int, int64_t>> seen;
+  for (Req* q : reqs) {
+    for (int side = 0; side < 2; side++) {
+      const int64_t key = wkey(side ? q->r.sta2 : q->r.sta1, q->r.window);
+      if (!seen.insert({q->N, key}).second) continue;
+      int zeros = 0;
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->windows.find({(int)(key >> 32), (int)(uint32_t)key});
+        if (it != s->windows.end()) zeros = it->second.zeros;
+      }
+      int a2, b3, c5;
+      const int f64 = zeros >= FPCC_F64_ZERO_SAMPLES;
+      if (factor235(q->N, &a2, &b3, &c5) && !f64) continue;
+      Slab& sl = slab_of(s, Product{kind, q->N, Nz, g.fmt});
+      if (find_row(sl, key) >= 0) continue;
+      const int r = claim_row(s, sl, key, 1);
+      if (r < 0) return FPCC_ENOMEM;
+      sl.pin[r]++;
+      fl.pinned_rows.push_back({&sl, r});
+      miss.push_back({q->N, key, &sl, r, f64});
+    }
+  }
+  if (miss.empty()) return 0;
+  std::stable_sort(miss.begin(), miss.end(), [](const Miss& a, const Miss& b) { return a.N < b.N; });
+  const int n = (int)miss.size();
+  std::vector<int> rawrow(n);
+  int rc;
+  for (int i0 = 0; i0 < n;) {
+    int i1 = i0;
+    std::vector<int64_t> keys;
+    while (i1 < n && miss[i1].N == miss[i0].N) keys.push_back(miss[i1++].key);
+    std::vector<int> rr;
+    if ((rc = ensure_raw(s, miss[i0].N, keys, rr, fl))) return rc;
+    for (int i = i0; i < i1; i++) rawrow[i] = rr[i - i0];
+    i0 = i1;
+  }
+  // all rows claimed: addresses are stable from here on
+  const int64_t esz = g.fmt == FPCC_F32 ? 8 : 4;
+  int64_t ldo = 0;
+  for (auto& m : miss) ldo = std::max<int64_t>(ldo, m.sl->row_bytes / esz);
+  std::vector<fpcc_station_row> rows(n);
+  for (int i = 0; i < n; i++) {
+    Slab& raw = slab_of(s, Product{0, miss[i].N, 0, 0});
+    rows[i].d_x = (const float*)((const char*)raw.base + (int64_t)rawrow[i] * raw.row_bytes);
+    rows[i].N = miss[i].N;
+    rows[i].Nz = Nz;
+    rows[i].f64 = miss[i].f64;
+    rows[i].pad = 0;
+  }
+  void* tmp = dbuf(&s->d_tmp_p, &s->n_tmp_p, (size_t)n * ldo * esz);
+  void* dc = dbuf(&s->d_idx, &s->n_idx, (size_t)n * sizeof(RowCopy) + 64);
+  if (!tmp || !dc) return FPCC_ENOMEM;
+  const int method = (kind == 1) ? FPCC_PCC2 : FPCC_PCC1;
+  if ((rc = fpcc_station_stage_multi(s->ctx, method, rows.data(), n, g.fmt, FPCC_AMP_F_REG, tmp, ldo))) return rc;
+  std::vector<RowCopy> cp(n);
+  for (int i = 0; i < n; i++)
+    cp[i] = RowCopy{(const char*)tmp + (size_t)i * ldo * esz,
+                    (char*)miss[i].sl->base + (int64_t)miss[i].row * miss[i].sl->row_bytes, miss[i].sl->row_bytes};
+  if (upload(fl, dc, cp.data(), cp.size() * sizeof(RowCopy), s->st) != cudaSuccess) return FPCC_ECUDA;
+  for (int i0 = 0; i0 < n; i0 += 65535) {
+    const int k = std::min(65535, n - i0);
+    int64_t mx = 0;
+    for (int i = i0; i < i0 + k; i++) mx = std::max(mx, cp[i].bytes);
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(64, (mx / 16 + 255) / 256));
+    k_scatter_rows<<<dim3(gx, k), 256, 0, s->st>>>((const RowCopy*)dc + i0);
+    if (cudaGetLastError() != cudaSuccess) return FPCC_ECUDA;
+  }
+  s->station_rows += n;
+  return 0;
+}
+
 // A group whose pair kernel takes descriptors: window lengths and lag windows
 // vary per request; products are ensured per window length, then every
 // correlation of the group runs in one launch reading its rows in place.
@@ -575,6 +678,8 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
   for (int i = 0; i < n; i++) byN[reqs[i]->N].push_back(i);
   std::vector<int> r1(n), r2(n), e1(n), e2(n);
   int rc;
+  if (m == FPCC_PCC2 && (rc = prefetch_phase(s, g, 1, reqs, fl))) return rc;
+  if ((m == FPCC_PCC1 || m == FPCC_PCCV) && (rc = prefetch_phase(s, g, 6, reqs, fl))) return rc;
   for (auto& kv : byN) {
     const int N = kv.first;
     const std::vector<int>& ix = kv.second;

@@ -132,6 +132,20 @@ int fpcc_station_stage(fpcc_ctx *ctx, int method, const float *d_x, int64_t ldx,
 int fpcc_station_stage_ex(fpcc_ctx *ctx, int method, const float *d_x, int64_t ldx, int nrows, int N,
                           int Nz, int fmt, int rule, void *d_out, int64_t ldo, const int32_t *h_f64_rows,
                           int n_f64_rows);
+/* Station stage of the phase methods (PCC2, PCC1, PCCV) for windows of
+ * different lengths: row r reads h_rows[r].d_x (N samples) and writes d_out +
+ * r * ldo (ldo in elements of the format: 8 bytes for F32, 4 otherwise).  The
+ * analytic signals of all rows run as Bluestein transforms grouped by length
+ * class (2^a, 3 2^a or 5 2^a >= 2N - 1; FP64 for rows with f64 set), so the
+ * windows share their launches; rows must be ordered by (N, Nz). */
+typedef struct {
+  const float *d_x;   /* the window's samples (device)                */
+  int32_t N, Nz;      /* window length, padded length (PCC2)          */
+  int32_t f64;        /* 1: FP64 analytic signal (windows with gaps)  */
+  int32_t pad;
+} fpcc_station_row;
+int fpcc_station_stage_multi(fpcc_ctx *ctx, int method, const fpcc_station_row *h_rows, int nrows, int fmt,
+                             int rule, void *d_out, int64_t ldo);
 /* FP64 prefix sums E[n] = sum_{m<n} x[m]^2, N+1 per row (GNCC normalisation). */
 int fpcc_energy_stage(fpcc_ctx *ctx, const float *d_x, int64_t ldx, int nrows, int N, double *d_E,
                       int64_t ldE);
