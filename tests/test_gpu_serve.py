@@ -270,7 +270,7 @@ def test_server_releases_idle_product_classes(F, orc):
     lengths = [2000, 2400, 2800]
     xs = _uneven_windows(lengths, "serve/release")
     reqs = [(0, i, j, w, -100, 100, 0.0) for w in (0, 1, 2, 0) for i in range(5) for j in range(5) if i < j]
-    srv = F.Server(hbm_budget=600 << 10, max_batch=10)
+    srv = F.Server(hbm_budget=250 << 10, max_batch=10)   # one class: 5 spectra + 5 raw windows, ~150 KB
     for w, x in xs.items():
         for s in range(5):
             srv.put(s, w, x[s])
