@@ -66,6 +66,7 @@ struct fpcc_ctx {
   DevBuf dev[32];
   DevBuf pin[8];
   cudaStream_t stream2 = nullptr;   // second stream of the pipelined drop-ins
+  cudaEvent_t chunk_ev[8] = {};     // pair-stage chunks whose results stream2 downloads
   std::map<int, float2*> twiddles;   // device tables exp(-2 pi i t/n), per n
   std::map<int, float2*> bluestein;  // per window length N: M-point filter spectra, forward then inverse
   std::map<int, double2*> twiddles64;   // FP64 tables exp(-2 pi i t/n)
@@ -179,6 +180,8 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
   for (void* b : c->multi_blocks) cudaFree(b);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
+  for (cudaEvent_t e : c->chunk_ev)
+    if (e) cudaEventDestroy(e);
   {
     std::lock_guard<std::mutex> lk(g_default_mu);
     if (c == g_default) g_default = nullptr;
@@ -1162,8 +1165,14 @@ int make_layout(int method, int N, int Lag1, int Lag2, int nz_mode, int fmt, Lay
 // split >= 0 gives rows [0, split) the station-1 rule and the rest the station-2
 // rule; split < 0 computes both variants (rows [0,nsta) and [nsta,2 nsta)) and
 // expects each pair's station-2 index to point into the second half.
+// Station stage(s), then the pair stage.  With h_y (FP32 results wanted in host
+// memory) and enough pairs, the pair stage runs in chunks of consecutive pairs
+// and the second stream downloads each chunk's rows once its kernels are done,
+// so the download of one chunk overlaps the correlation of the next; every
+// kernel is queued before the first copy, so pageable host memory (whose
+// copies return only when done) does not hold back the launches.
 int run_device(fpcc_ctx* c, const Layout& Ly, const float* d_x, int nsta, const int32_t* d_pairs, int npairs,
-               float v, float* d_y, int64_t* d_num, int split) {
+               float v, float* d_y, int64_t* d_num, int split, float* h_y = nullptr) {
   void* d_st = nullptr;
   int rc;
   const int method = Ly.method;
@@ -1197,8 +1206,34 @@ int run_device(fpcc_ctx* c, const Layout& Ly, const float* d_x, int nsta, const 
     d_E = (double*)p;
     if ((rc = fpcc_energy_stage(c, d_x, Ly.N, nsta, Ly.N, d_E, Ly.N + 1))) return rc;
   }
-  return fpcc_pair_stage(c, method, d_st, Ly.lds, Ly.fmt, d_pairs, npairs, Ly.N, Ly.Nz, Ly.lag0,
-                         Ly.lag0 + Ly.L - 1, v, d_E, Ly.N + 1, d_y, Ly.L, d_num);
+  if (!h_y)
+    return fpcc_pair_stage(c, method, d_st, Ly.lds, Ly.fmt, d_pairs, npairs, Ly.N, Ly.Nz, Ly.lag0,
+                           Ly.lag0 + Ly.L - 1, v, d_E, Ly.N + 1, d_y, Ly.L, d_num);
+  const int nch = npairs >= 8192 ? 8 : 1;
+  if (nch > 1 && !c->stream2 && cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(FPCC_ECUDA, "stream creation failed");
+  for (int k = 0; k < nch; k++)
+    if (!c->chunk_ev[k] && cudaEventCreateWithFlags(&c->chunk_ev[k], cudaEventDisableTiming) != cudaSuccess)
+      return fail(FPCC_ECUDA, "event creation failed");
+  const int per = (npairs + nch - 1) / nch;
+  for (int k = 0; k < nch; k++) {
+    const int i0 = k * per, n = std::min(per, npairs - i0);
+    if (n <= 0) break;
+    if ((rc = fpcc_pair_stage(c, method, d_st, Ly.lds, Ly.fmt, d_pairs + 2 * (size_t)i0, n, Ly.N, Ly.Nz, Ly.lag0,
+                              Ly.lag0 + Ly.L - 1, v, d_E, Ly.N + 1, d_y + (size_t)i0 * Ly.L, Ly.L, nullptr)))
+      return rc;
+    CK(cudaEventRecord(c->chunk_ev[k], c->stream));
+  }
+  cudaStream_t dl = nch > 1 ? c->stream2 : c->stream;
+  for (int k = 0; k < nch; k++) {
+    const int i0 = k * per, n = std::min(per, npairs - i0);
+    if (n <= 0) break;
+    CK(cudaStreamWaitEvent(dl, c->chunk_ev[k], 0));
+    CK(cudaMemcpyAsync(h_y + (size_t)i0 * Ly.L, d_y + (size_t)i0 * Ly.L, (size_t)n * Ly.L * sizeof(float),
+                       cudaMemcpyDeviceToHost, dl));
+  }
+  CK(cudaStreamSynchronize(dl));
+  return 0;
 }
 
 int host_windows(int method, float** y, int64_t** num, float** x1, float** x2, unsigned N, unsigned Tr, int Lag1,
@@ -1286,9 +1321,9 @@ extern "C" int fpcc_allpairs_host(fpcc_ctx* c, int method, const float* h_x, int
   } else {
     CK(cudaMemcpyAsync(d_p, h_pairs, pbytes, cudaMemcpyHostToDevice, c->stream));
   }
-  if ((rc = run_device(c, Ly, (const float*)d_x, nsta, (const int32_t*)d_p, npairs, v, (float*)d_y, nullptr, -1)))
+  if ((rc = run_device(c, Ly, (const float*)d_x, nsta, (const int32_t*)d_p, npairs, v, (float*)d_y, nullptr, -1,
+                       h_y)))
     return rc;
-  CK(cudaMemcpyAsync(h_y, d_y, ybytes, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return 0;
 }
