@@ -63,10 +63,15 @@ struct fpcc_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  DevBuf dev[32];
+  DevBuf dev[40];
   DevBuf pin[8];
   cudaStream_t stream2 = nullptr;   // second stream of the pipelined drop-ins
   cudaEvent_t chunk_ev[8] = {};     // pair-stage chunks whose results stream2 downloads
+  // the context's device buffers and caches come from a pool of its own, allocated
+  // and freed in the order of `stream` (no device synchronisation when a buffer
+  // grows); ord_ev orders them against the second stream when it exists
+  cudaMemPool_t pool = nullptr;
+  cudaEvent_t ord_ev = nullptr;
   std::map<int, float2*> twiddles;   // device tables exp(-2 pi i t/n), per n
   std::map<int, float2*> bluestein;  // per window length N: M-point filter spectra, forward then inverse
   std::map<int, double2*> twiddles64;   // FP64 tables exp(-2 pi i t/n)
@@ -82,18 +87,50 @@ struct fpcc_ctx {
 
 namespace {
 
+// Stream-ordered allocation from the context's pool; when the second stream
+// exists it waits for the allocation before it can touch the memory.
+cudaError_t ctx_alloc(fpcc_ctx* c, void** p, size_t bytes) {
+  cudaError_t e = cudaMallocFromPoolAsync(p, bytes, c->pool, c->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return e;
+  }
+  if (c->stream2) {
+    cudaEventRecord(c->ord_ev, c->stream);
+    cudaStreamWaitEvent(c->stream2, c->ord_ev, 0);
+  }
+  return cudaSuccess;
+}
+
+// Stream-ordered free: after the work queued on `stream` (and on the second
+// stream, when it exists) that may still read the memory.
+void ctx_free(fpcc_ctx* c, void* p) {
+  if (!p) return;
+  if (c->stream2) {
+    cudaEventRecord(c->ord_ev, c->stream2);
+    cudaStreamWaitEvent(c->stream, c->ord_ev, 0);
+  }
+  cudaFreeAsync(p, c->stream);
+}
+
 int dev_buf(fpcc_ctx* c, int slot, size_t bytes, void** out) {
   DevBuf& b = c->dev[slot];
   if (b.n < bytes) {
-    if (b.p) {
-      cudaStreamSynchronize(c->stream);
-      cudaFree(b.p);
-    }
+    // a buffer that has to grow grows by half again at least, so that a run of
+    // slowly increasing sizes (windows sorted by length) reallocates rarely
+    const size_t nb = b.p ? std::max(bytes, b.n + b.n / 2) : bytes;
+    ctx_free(c, b.p);
     b.p = nullptr;
     b.n = 0;
-    cudaError_t e = cudaMalloc(&b.p, bytes);
-    if (e != cudaSuccess) return fail(FPCC_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
-    b.n = bytes;
+    cudaError_t e = ctx_alloc(c, &b.p, nb);
+    if (e != cudaSuccess && nb > bytes) {
+      e = ctx_alloc(c, &b.p, bytes);
+      if (e == cudaSuccess) b.n = bytes;
+    } else if (e == cudaSuccess) {
+      b.n = nb;
+    }
+    if (e != cudaSuccess) return fail(FPCC_ENOMEM, "device allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
   }
   *out = b.p;
   return 0;
@@ -163,6 +200,19 @@ extern "C" int fpcc_create(fpcc_ctx** out, int device) {
     return cuda_fail(e, "cudaStreamCreate");
   }
   c->own_stream = true;
+  cudaMemPoolProps pp = {};
+  pp.allocType = cudaMemAllocationTypePinned;
+  pp.location.type = cudaMemLocationTypeDevice;
+  pp.location.id = device;
+  uint64_t keep = UINT64_MAX;   // freed blocks stay mapped for the context's later buffers
+  if ((e = cudaMemPoolCreate(&c->pool, &pp)) != cudaSuccess ||
+      (e = cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c->ord_ev, cudaEventDisableTiming)) != cudaSuccess) {
+    if (c->pool) cudaMemPoolDestroy(c->pool);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return cuda_fail(e, "memory pool");
+  }
   *out = c;
   return 0;
 }
@@ -170,14 +220,17 @@ extern "C" int fpcc_create(fpcc_ctx** out, int device) {
 extern "C" int fpcc_destroy(fpcc_ctx* c) {
   if (!c) return 0;
   cudaSetDevice(c->device);
+  for (auto& b : c->dev) ctx_free(c, b.p);
+  for (auto& kv : c->twiddles) ctx_free(c, kv.second);
+  for (auto& kv : c->bluestein) ctx_free(c, kv.second);
+  for (auto& kv : c->twiddles64) ctx_free(c, kv.second);
+  for (auto& kv : c->bluestein64) ctx_free(c, kv.second);
+  for (void* b : c->multi_blocks) ctx_free(c, b);
   cudaStreamSynchronize(c->stream);
-  for (auto& b : c->dev) if (b.p) cudaFree(b.p);
+  if (c->stream2) cudaStreamSynchronize(c->stream2);
   for (auto& b : c->pin) if (b.p) cudaFreeHost(b.p);
-  for (auto& kv : c->twiddles) cudaFree(kv.second);
-  for (auto& kv : c->bluestein) cudaFree(kv.second);
-  for (auto& kv : c->twiddles64) cudaFree(kv.second);
-  for (auto& kv : c->bluestein64) cudaFree(kv.second);
-  for (void* b : c->multi_blocks) cudaFree(b);
+  cudaMemPoolDestroy(c->pool);
+  cudaEventDestroy(c->ord_ev);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
   for (cudaEvent_t e : c->chunk_ev)
@@ -206,10 +259,9 @@ extern "C" int fpcc_set_stream(fpcc_ctx* c, void* stream) {
     }
     return 0;
   }
-  if (c->own_stream) {
-    cudaStreamSynchronize(c->stream);
-    cudaStreamDestroy(c->stream);
-  }
+  // the context's buffers were allocated and freed in the old stream's order
+  cudaStreamSynchronize(c->stream);
+  if (c->own_stream) cudaStreamDestroy(c->stream);
   c->stream = (cudaStream_t)stream;
   c->own_stream = false;
   return 0;
@@ -266,7 +318,8 @@ namespace {
 enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_PAIRS = 5, S_ANA_A = 6,
             S_ANA_B = 7, S_RSTAT = 8, S_LARGE_T = 9, S_WP_X = 10, S_WP_BAND = 11, S_WP_RMAX = 12,
             S_WP_Y = 13, S_WP_STAGE = 14, S_BLUE_O = 23, S_P64_D = 24, S_P64_A = 25, S_P64_B = 26,
-            S_P64_CNT = 27, S_I16_Q = 28, S_MULTI_A = 29, S_MULTI_B = 30, S_MULTI_AN = 31 };
+            S_P64_CNT = 27, S_I16_Q = 28, S_MULTI_A = 29, S_MULTI_B = 30, S_MULTI_AN = 31, S_EPART = 32,
+            S_CONV_X = 33, S_CONV_Y = 34 };
 
 constexpr size_t kLargeChunkBytes = size_t(512) << 20;   // four-step intermediate per chunk
 
@@ -348,19 +401,35 @@ int large_pairs(fpcc_ctx* c, const PairArgs& q, int herm) {
   return 0;
 }
 
+// Twiddle table exp(-2 pi i t / n), t < n, computed on the device in FP64
+// (sincospi of the exact fraction -2t/n) and stored as float2 or double2, in
+// the context's stream order (no host loop, no synchronous upload).
+__global__ void k_twiddles(float2* f, double2* d, int n) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    double sn, cs;
+    sincospi(-2.0 * (double)t / (double)n, &sn, &cs);
+    if (f) f[t] = make_float2((float)cs, (float)sn);
+    if (d) d[t] = make_double2(cs, sn);
+  }
+}
+
+cudaError_t launch_twiddles(float2* f, double2* d, int n, cudaStream_t st) {
+  const int g = (int)std::min<int64_t>(1024, ((int64_t)n + 255) / 256);
+  k_twiddles<<<g > 0 ? g : 1, 256, 0, st>>>(f, d, n);
+  return cudaGetLastError();
+}
+
 int twiddle_table(fpcc_ctx* c, int n, const float2** out) {
   auto it = c->twiddles.find(n);
   if (it != c->twiddles.end()) { *out = it->second; return 0; }
-  std::vector<float2> h(n);
-  for (int t = 0; t < n; t++) {
-    const double a = -2.0 * M_PI * (double)t / (double)n;
-    h[t] = make_float2((float)cos(a), (float)sin(a));
-  }
   float2* d = nullptr;
-  cudaError_t e = cudaMalloc(&d, (size_t)n * sizeof(float2));
+  cudaError_t e = ctx_alloc(c, (void**)&d, (size_t)n * sizeof(float2));
   if (e != cudaSuccess) return fail(FPCC_ENOMEM, "twiddle table: %s", cudaGetErrorString(e));
-  e = cudaMemcpy(d, h.data(), (size_t)n * sizeof(float2), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) { cudaFree(d); return cuda_fail(e, "twiddle upload"); }
+  if ((e = launch_twiddles(d, nullptr, n, c->stream)) != cudaSuccess) {
+    ctx_free(c, d);
+    return cuda_fail(e, "twiddle table");
+  }
+  g_launches++;
   c->twiddles[n] = d;
   *out = d;
   return 0;
@@ -421,16 +490,14 @@ constexpr int kZeroSamples = FPCC_F64_ZERO_SAMPLES;
 int twiddle64(fpcc_ctx* c, int n, const double2** out) {
   auto it = c->twiddles64.find(n);
   if (it != c->twiddles64.end()) { *out = it->second; return 0; }
-  std::vector<double2> h(n);
-  for (int t = 0; t < n; t++) {
-    const double a = -2.0 * M_PI * (double)t / (double)n;
-    h[t] = make_double2(cos(a), sin(a));
-  }
   double2* d = nullptr;
-  cudaError_t e = cudaMalloc(&d, (size_t)n * sizeof(double2));
+  cudaError_t e = ctx_alloc(c, (void**)&d, (size_t)n * sizeof(double2));
   if (e != cudaSuccess) return fail(FPCC_ENOMEM, "FP64 twiddle table: %s", cudaGetErrorString(e));
-  e = cudaMemcpy(d, h.data(), (size_t)n * sizeof(double2), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) { cudaFree(d); return cuda_fail(e, "FP64 twiddle upload"); }
+  if ((e = launch_twiddles(nullptr, d, n, c->stream)) != cudaSuccess) {
+    ctx_free(c, d);
+    return cuda_fail(e, "FP64 twiddle table");
+  }
+  g_launches++;
   c->twiddles64[n] = d;
   *out = d;
   return 0;
@@ -472,13 +539,13 @@ int bluestein64(fpcc_ctx* c, double2* D, double2* A, double2* B, int N, int M, i
   double2* F = nullptr;
   auto it = c->bluestein64.find(N);
   if (it == c->bluestein64.end()) {
-    CK(cudaMalloc(&F, (size_t)2 * M * sizeof(double2)));
+    CK(ctx_alloc(c, (void**)&F, (size_t)2 * M * sizeof(double2)));
     for (int d = 0; d < 2; d++) {
       double2* f = F + (size_t)d * M;
       CK(launch_blue_filter64(f, N, M, d ? +1 : -1, c->stream));
       double2* r = nullptr;
       int rc = passes64(c, f, B, M, 1, -1, &r);
-      if (rc) { cudaFree(F); return rc; }
+      if (rc) { ctx_free(c, F); return rc; }
       if (r != f) CK(cudaMemcpyAsync(f, r, (size_t)M * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
     }
     c->bluestein64[N] = F;
@@ -570,15 +637,15 @@ int analytic_rows_bluestein(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrow
   auto it = c->bluestein.find(N);
   if (it == c->bluestein.end()) {
     // filter spectra for both directions (computed once per N)
-    CK(cudaMalloc(&Bf, (size_t)2 * M * sizeof(float2)));
+    CK(ctx_alloc(c, (void**)&Bf, (size_t)2 * M * sizeof(float2)));
     void* tmp;
     int rc = dev_buf(c, S_ANA_B, (size_t)2 * M * sizeof(float2), &tmp);
-    if (rc) { cudaFree(Bf); return rc; }
+    if (rc) { ctx_free(c, Bf); return rc; }
     for (int d = 0; d < 2; d++) {
       const int dir = d ? +1 : -1;
       CK(launch_blue_filter(Bf + (size_t)d * M, N, M, dir, c->stream));
       float2* res = nullptr;
-      if ((rc = passes(c, Bf + (size_t)d * M, (float2*)tmp, M, 1, -1, &res))) { cudaFree(Bf); return rc; }
+      if ((rc = passes(c, Bf + (size_t)d * M, (float2*)tmp, M, 1, -1, &res))) { ctx_free(c, Bf); return rc; }
       if (res != Bf + (size_t)d * M)
         CK(cudaMemcpyAsync(Bf + (size_t)d * M, res, (size_t)M * sizeof(float2), cudaMemcpyDeviceToDevice, c->stream));
     }
@@ -688,10 +755,10 @@ int analytic_rows_p64(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int
 }
 
 // ---------------------------------------------------------------- packed analytic signals
-// Bluestein length class of a window length: the smallest 2^a, 3 2^a or 5 2^a
-// >= 2N - 1 (about three classes per octave, so windows of nearby lengths share
-// their transforms).
-int bluestein_class_len(int N) {
+// Transform length class of a window length in the packed analytic-signal
+// stage: the smallest 2^a, 3 2^a or 5 2^a >= 2N - 1 (about three classes per
+// octave, so windows of nearby lengths share their transforms).
+int conv_class_len(int N) {
   const int need = 2 * N - 1;
   int best = -1;
   for (int base : {1, 3, 5})
@@ -703,26 +770,24 @@ int bluestein_class_len(int N) {
   return best;
 }
 
-constexpr size_t kMultiFilterCache = (size_t)1 << 30;   // bytes of cached filter spectra per context
+constexpr size_t kMultiFilterCache = (size_t)4 << 30;   // bytes of cached filter spectra per context
 
-// Filter spectra (forward, inverse) of every window length in Ns for transforms
-// of M points in precision T; returns device pointers per entry of Ns.  New
-// lengths are computed together (their filters as rows of one batched
-// transform) and cached in blocks; the cache is emptied first when it would
-// grow past kMultiFilterCache.
+// Kernel spectra H_N = FFT_M(kernel) / M of every window length in Ns, for
+// transforms of M points in precision T; returns a device pointer per entry of
+// Ns.  New lengths are computed together in FP64 (their kernels as rows of one
+// batched transform), rounded to T and cached in blocks; the cache is emptied
+// first when it would grow past kMultiFilterCache.
 template <typename T>
-int multi_filters(fpcc_ctx* c, const std::vector<int>& Ns, int M, std::vector<const void*>& fwd,
-                  std::vector<const void*>& inv) {
+int multi_filters(fpcc_ctx* c, const std::vector<int>& Ns, int M, std::vector<const void*>& filt) {
   const int f64 = sizeof(T) == 16;
   std::vector<int> missing;
   for (int N : Ns)
     if (!c->multi_filters.count(std::make_tuple(N, M, f64)) &&
         std::find(missing.begin(), missing.end(), N) == missing.end())
       missing.push_back(N);
-  const size_t need = missing.size() * (size_t)2 * M * sizeof(T);
+  const size_t need = missing.size() * (size_t)M * sizeof(T);
   if (need && c->multi_filter_bytes + need > kMultiFilterCache && c->multi_filter_bytes) {
-    CK(cudaStreamSynchronize(c->stream));
-    for (void* b : c->multi_blocks) cudaFree(b);
+    for (void* b : c->multi_blocks) ctx_free(c, b);   // in stream order: later work cannot read them
     c->multi_blocks.clear();
     c->multi_filters.clear();
     c->multi_filter_bytes = 0;
@@ -730,66 +795,50 @@ int multi_filters(fpcc_ctx* c, const std::vector<int>& Ns, int M, std::vector<co
     for (int N : Ns)
       if (std::find(missing.begin(), missing.end(), N) == missing.end()) missing.push_back(N);
   }
-  for (size_t i0 = 0; i0 < missing.size(); i0 += 64) {
-    const int n = (int)std::min<size_t>(64, missing.size() - i0);
+  // lengths per batch: at most 64, and FP64 work buffers of at most 256 MB each
+  const size_t per = std::max<size_t>(1, std::min<size_t>(64, ((size_t)256 << 20) / ((size_t)M * sizeof(double2))));
+  for (size_t i0 = 0; i0 < missing.size(); i0 += per) {
+    const int n = (int)std::min<size_t>(per, missing.size() - i0);
     const std::vector<int> lens(missing.begin() + i0, missing.begin() + i0 + n);
     void *B, *A, *dN;
     int rc;
-    if ((rc = dev_buf(c, S_MULTI_B, (size_t)2 * n * M * sizeof(T), &B)) ||
-        (rc = dev_buf(c, S_MULTI_A, (size_t)2 * n * M * sizeof(T), &A)) ||
+    if ((rc = dev_buf(c, S_MULTI_B, (size_t)n * M * sizeof(double2), &B)) ||
+        (rc = dev_buf(c, S_MULTI_A, (size_t)n * M * sizeof(double2), &A)) ||
         (rc = dev_buf(c, S_P64_CNT, (size_t)n * sizeof(int), &dN)))
       return rc;
     CK(cudaMemcpyAsync(dN, lens.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    // rows [0, n): forward filters; rows [n, 2n): inverse filters
-    CK(launch_multi_filter<T>((const int*)dN, n, (T*)B, M, -1, c->stream));
-    CK(launch_multi_filter<T>((const int*)dN, n, (T*)B + (size_t)n * M, M, +1, c->stream));
-    g_launches += 2;
-    void* res = nullptr;
-    if constexpr (sizeof(T) == 16) {
-      double2* r = nullptr;
-      if ((rc = passes64(c, (double2*)B, (double2*)A, M, 2 * n, -1, &r))) return rc;
-      res = r;
-    } else {
-      float2* r = nullptr;
-      if ((rc = passes(c, (float2*)B, (float2*)A, M, 2 * n, -1, &r))) return rc;
-      res = r;
-    }
+    CK(launch_multi_hkernel((const int*)dN, n, (double2*)B, M, c->stream));
+    double2* r = nullptr;
+    if ((rc = passes64(c, (double2*)B, (double2*)A, M, n, -1, &r))) return rc;
     void* block = nullptr;
-    CK(cudaMalloc(&block, (size_t)2 * n * M * sizeof(T)));
+    CK(ctx_alloc(c, &block, (size_t)n * M * sizeof(T)));
     c->multi_blocks.push_back(block);
-    c->multi_filter_bytes += (size_t)2 * n * M * sizeof(T);
-    for (int j = 0; j < n; j++) {
-      char* dst = (char*)block + (size_t)2 * j * M * sizeof(T);
-      CK(cudaMemcpyAsync(dst, (const char*)res + (size_t)j * M * sizeof(T), (size_t)M * sizeof(T),
-                         cudaMemcpyDeviceToDevice, c->stream));
-      CK(cudaMemcpyAsync(dst + (size_t)M * sizeof(T), (const char*)res + (size_t)(n + j) * M * sizeof(T),
-                         (size_t)M * sizeof(T), cudaMemcpyDeviceToDevice, c->stream));
-      c->multi_filters[std::make_tuple(lens[j], M, f64)] = dst;
-    }
+    c->multi_filter_bytes += (size_t)n * M * sizeof(T);
+    CK(launch_multi_convert<T>(r, (T*)block, (int64_t)n * M, c->stream));
+    g_launches += 2;
+    for (int j = 0; j < n; j++)
+      c->multi_filters[std::make_tuple(lens[j], M, f64)] = (char*)block + (size_t)j * M * sizeof(T);
   }
-  fwd.resize(Ns.size());
-  inv.resize(Ns.size());
-  for (size_t i = 0; i < Ns.size(); i++) {
-    char* p = (char*)c->multi_filters.at(std::make_tuple(Ns[i], M, f64));
-    fwd[i] = p;
-    inv[i] = p + (size_t)M * sizeof(T);
-  }
+  filt.resize(Ns.size());
+  for (size_t i = 0; i < Ns.size(); i++) filt[i] = c->multi_filters.at(std::make_tuple(Ns[i], M, f64));
   return 0;
 }
 
 // Analytic signals of `rows` (all of length class M, precision T) into their
-// out pointers, in chunks that keep each transform buffer under 512 MB.
+// out pointers, in chunks that keep each transform buffer under 512 MB: pairs of
+// windows share a forward transform, each window gets its own inverse one.
 template <typename T>
 int multi_group(fpcc_ctx* c, std::vector<MultiRow>& rows, int M) {
   std::vector<int> Ns(rows.size());
   for (size_t i = 0; i < rows.size(); i++) Ns[i] = rows[i].N;
-  std::vector<const void*> fwd, inv;
-  int rc = multi_filters<T>(c, Ns, M, fwd, inv);
+  std::vector<const void*> filt;
+  int rc = multi_filters<T>(c, Ns, M, filt);
   if (rc) return rc;
-  for (size_t i = 0; i < rows.size(); i++) { rows[i].ffwd = fwd[i]; rows[i].finv = inv[i]; }
+  for (size_t i = 0; i < rows.size(); i++) rows[i].filt = filt[i];
   const int chunk = (int)std::max<size_t>(1, std::min<size_t>(4096, ((size_t)512 << 20) / ((size_t)M * sizeof(T))));
   for (size_t r0 = 0; r0 < rows.size(); r0 += chunk) {
     const int n = (int)std::min<size_t>(chunk, rows.size() - r0);
+    const int np = (n + 1) / 2;
     void *A, *B, *d;
     if ((rc = dev_buf(c, S_MULTI_A, (size_t)n * M * sizeof(T), &A)) ||
         (rc = dev_buf(c, S_MULTI_B, (size_t)n * M * sizeof(T), &B)) ||
@@ -797,27 +846,19 @@ int multi_group(fpcc_ctx* c, std::vector<MultiRow>& rows, int M) {
       return rc;
     CK(cudaMemcpyAsync(d, rows.data() + r0, (size_t)n * sizeof(MultiRow), cudaMemcpyHostToDevice, c->stream));
     const MultiRow* dr = (const MultiRow*)d;
-    T* bufs[2] = {(T*)A, (T*)B};
-    int cur = 0;
-    auto tr = [&](int dir) -> int {
-      T* res = nullptr;
-      int rc2;
-      if constexpr (sizeof(T) == 16) rc2 = passes64(c, (double2*)bufs[cur], (double2*)bufs[cur ^ 1], M, n, dir, (double2**)&res);
-      else rc2 = passes(c, (float2*)bufs[cur], (float2*)bufs[cur ^ 1], M, n, dir, (float2**)&res);
-      if (rc2) return rc2;
-      if (res != bufs[cur]) cur ^= 1;
-      return 0;
+    auto tr = [&](T* in, T* other, int nr, int dir, T** res) -> int {
+      if constexpr (sizeof(T) == 16) return passes64(c, (double2*)in, (double2*)other, M, nr, dir, (double2**)res);
+      else return passes(c, (float2*)in, (float2*)other, M, nr, dir, (float2**)res);
     };
-    CK(launch_multi_pre<T>(dr, n, bufs[cur], M, c->stream));
-    if ((rc = tr(-1))) return rc;
-    CK(launch_multi_mul<T>(dr, n, bufs[cur], M, 0, c->stream));
-    if ((rc = tr(+1))) return rc;
-    CK(launch_multi_mask<T>(dr, n, bufs[cur], M, c->stream));
-    if ((rc = tr(-1))) return rc;
-    CK(launch_multi_mul<T>(dr, n, bufs[cur], M, 1, c->stream));
-    if ((rc = tr(+1))) return rc;
-    CK(launch_multi_post<T>(dr, n, bufs[cur], M, c->stream));
-    g_launches += 5;
+    T* z = nullptr;
+    CK(launch_multi_load2<T>(dr, n, (T*)A, M, c->stream));
+    if ((rc = tr((T*)A, (T*)B, np, -1, &z))) return rc;
+    T* y = (z == (T*)A) ? (T*)B : (T*)A;
+    CK(launch_multi_split<T>(dr, n, z, y, M, c->stream));
+    T* res = nullptr;
+    if ((rc = tr(y, z, n, +1, &res))) return rc;
+    CK(launch_multi_store<T>(dr, n, res, M, c->stream));
+    g_launches += 3;
   }
   return 0;
 }
@@ -863,7 +904,7 @@ extern "C" int fpcc_station_stage_multi(fpcc_ctx* c, int method, const fpcc_stat
     m.out = (float2*)an + off[r];
     m.N = h_rows[r].N;
     all[r] = m;
-    groups[{bluestein_class_len(m.N), h_rows[r].f64 ? 1 : 0}].push_back(m);
+    groups[{conv_class_len(m.N), h_rows[r].f64 ? 1 : 0}].push_back(m);
   }
   for (auto& kv : groups) {
     const int M = kv.first.first;
@@ -997,8 +1038,18 @@ extern "C" int fpcc_station_stage_ex(fpcc_ctx* c, int method, const float* d_x, 
 extern "C" int fpcc_energy_stage(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, double* d_E,
                                  int64_t ldE) {
   if (!c) return fail(FPCC_EARG, "null context");
-  CK(launch_energy_prefix(d_x, ldx, nrows, N, d_E, ldE, c->stream));
-  g_launches++;
+  if (nrows <= 0 || N <= 0) return 0;
+  if (!d_x || !d_E || ldE < (int64_t)N + 1 || ldx < N) return fail(FPCC_EARG, "bad energy stage arguments");
+  const int blk = std::min(nrows, 65535);   // rows per launch pair (grid y)
+  void* part;
+  int rc = dev_buf(c, S_EPART, (size_t)blk * energy_chunks(N) * sizeof(double), &part);
+  if (rc) return rc;
+  for (int r0 = 0; r0 < nrows; r0 += blk) {
+    const int n = std::min(blk, nrows - r0);
+    CK(launch_energy_prefix(d_x + (size_t)r0 * ldx, ldx, n, N, d_E + (size_t)r0 * ldE, ldE, (double*)part,
+                            c->stream));
+    g_launches += 2;
+  }
   return 0;
 }
 

@@ -12,34 +12,77 @@ namespace fpcc {
 namespace {
 
 // ---------------------------------------------------------------- energies
-__global__ void __launch_bounds__(256) k_energy_prefix(const float* __restrict__ x, int64_t ldx, int N,
-                                                       double* __restrict__ E, int64_t ldE) {
-  __shared__ double wsum[8];
-  __shared__ double carry_s;
-  const float* xr = x + (int64_t)blockIdx.x * ldx;
-  double* Er = E + (int64_t)blockIdx.x * ldE;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (threadIdx.x == 0) { Er[0] = 0.0; carry_s = 0.0; }
-  __syncthreads();
-  for (int t0 = 0; t0 < N; t0 += 256) {
-    const int n = t0 + threadIdx.x;
-    double v = 0.0;
-    if (n < N) { const double f = (double)__ldg(xr + n); v = f * f; }
-    // inclusive warp scan
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      double u = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += u;
-    }
-    if (lane == 31) wsum[w] = v;
-    __syncthreads();
-    double off = carry_s;
-    for (int i = 0; i < w; i++) off += wsum[i];
-    if (n < N) Er[n + 1] = off + v;
-    __syncthreads();
-    if (threadIdx.x == 255) carry_s = off + v;
-    __syncthreads();
+// FP64 prefix sums of x^2 over chunks of kEChunk samples, in two launches:
+// per-chunk totals, then each chunk's scan from the total of the chunks before
+// it.  Every x^2 is exact in FP64 (24-bit by 24-bit product), so only the
+// additions round.
+constexpr int kEChunk = 4096;
+constexpr int kEPer = kEChunk / 256;   // samples per thread
+
+__global__ void __launch_bounds__(256) k_energy_chunks(const float* __restrict__ x, int64_t ldx, int N, int nch,
+                                                       double* __restrict__ part) {
+  __shared__ double ws[8];
+  const int c = blockIdx.x;
+  const float* xr = x + (int64_t)blockIdx.y * ldx + (int64_t)c * kEChunk;
+  const int len = min(kEChunk, N - c * kEChunk);
+  double s = 0.0;
+  for (int i = threadIdx.x; i < len; i += 256) {
+    const double f = (double)__ldg(xr + i);
+    s += f * f;
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; w++) t += ws[w];
+    part[(int64_t)blockIdx.y * nch + c] = t;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_energy_scan(const float* __restrict__ x, int64_t ldx, int N, int nch,
+                                                     const double* __restrict__ part, double* __restrict__ E,
+                                                     int64_t ldE) {
+  __shared__ double ws[8];
+  __shared__ double base_s;
+  const int c = blockIdx.x, row = blockIdx.y;
+  const float* xr = x + (int64_t)row * ldx + (int64_t)c * kEChunk;
+  double* Er = E + (int64_t)row * ldE + (int64_t)c * kEChunk;
+  const int len = min(kEChunk, N - c * kEChunk);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int j = 0; j < c; j++) b += part[(int64_t)row * nch + j];
+    base_s = b;
+    if (c == 0) Er[0] = 0.0;
+  }
+  // each thread: kEPer consecutive samples, prefix in registers
+  double v[kEPer];
+  double t = 0.0;
+  const int i0 = threadIdx.x * kEPer;
+#pragma unroll
+  for (int j = 0; j < kEPer; j++) {
+    double f = 0.0;
+    if (i0 + j < len) f = (double)__ldg(xr + i0 + j);
+    t += f * f;
+    v[j] = t;
+  }
+  // exclusive scan of the thread totals
+  double incl = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) ws[w] = incl;
+  __syncthreads();
+  double off = base_s;
+  for (int k = 0; k < w; k++) off += ws[k];
+  off += incl - t;
+#pragma unroll
+  for (int j = 0; j < kEPer; j++)
+    if (i0 + j < len) Er[i0 + j + 1] = off + v[j];
 }
 
 // ---------------------------------------------------------------- PCC_v direct
@@ -226,10 +269,15 @@ __global__ void __launch_bounds__(256) k_cc1b_popcount(Cc1bArgs a) {
 
 }  // namespace
 
+int energy_chunks(int N) { return (N + kEChunk - 1) / kEChunk; }
+
 cudaError_t launch_energy_prefix(const float* x, int64_t ldx, int nrows, int N, double* E, int64_t ldE,
-                                 cudaStream_t st) {
-  if (nrows <= 0) return cudaSuccess;
-  k_energy_prefix<<<nrows, 256, 0, st>>>(x, ldx, N, E, ldE);
+                                 double* part, cudaStream_t st) {
+  if (nrows <= 0 || N <= 0) return cudaSuccess;
+  if (nrows > 65535) return cudaErrorInvalidValue;
+  const int nch = energy_chunks(N);
+  k_energy_chunks<<<dim3(nch, nrows), 256, 0, st>>>(x, ldx, N, nch, part);
+  k_energy_scan<<<dim3(nch, nrows), 256, 0, st>>>(x, ldx, N, nch, part, E, ldE);
   return cudaGetLastError();
 }
 

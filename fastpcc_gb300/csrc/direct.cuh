@@ -40,8 +40,11 @@ struct Cc1bArgs {
   int desc_num;
 };
 
+// FP64 prefix sums E[n] = sum_{m<n} x[m]^2 (N + 1 per row); `part` holds
+// nrows * energy_chunks(N) doubles of chunk totals.
+int energy_chunks(int N);
 cudaError_t launch_energy_prefix(const float* x, int64_t ldx, int nrows, int N, double* E, int64_t ldE,
-                                 cudaStream_t st);
+                                 double* part, cudaStream_t st);
 cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st);
 cudaError_t launch_sign_bits(const float* x, int64_t ldx, int nrows, int N, uint32_t* bits, int64_t ldb,
                              int pos_ge, const int8_t* sel, cudaStream_t st);

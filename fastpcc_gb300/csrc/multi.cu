@@ -1,6 +1,8 @@
 // Analytic signals of windows of different lengths in shared launches (see multi.cuh).
 #include "multi.cuh"
 
+#include <algorithm>
+
 namespace fpcc {
 namespace {
 
@@ -17,87 +19,91 @@ __device__ __forceinline__ T mul(T a, T b) {
   return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x, (T*)nullptr);
 }
 
-// exp(dir i pi n^2 / N), n^2 reduced mod 2N exactly
-__device__ __forceinline__ float2 chirp_of(long long n, int N, int dir, float2*) {
-  const long long q = (n * n) % (2LL * N);
-  float s, c;
-  sincospif((float)q / (float)N, &s, &c);
-  return make_float2(c, dir * s);
+template <typename T>
+__device__ __forceinline__ T cvt(double2 v) {
+  return mk(v.x, v.y, (T*)nullptr);
 }
-__device__ __forceinline__ double2 chirp_of(long long n, int N, int dir, double2*) {
-  const long long q = (n * n) % (2LL * N);
+
+// Im h(n), 0 < n < N, of h = IDFT_N(mask): for even N, (2/N) cot(pi n / N) at
+// odd n and 0 at even n; for odd N, (1/N) (cos(pi n/N) - (-1)^n) / sin(pi n/N),
+// written with half angles as cot(pi n / 2N) / N at odd n and -tan(pi n / 2N) / N
+// at even n (no cancellation; the angles lie in (0, pi/2)).
+__device__ __forceinline__ double hilbert_im(int n, int N) {
   double s, c;
-  sincospi((double)q / (double)N, &s, &c);
-  return make_double2(c, dir * s);
+  if (N & 1) {
+    sincospi((double)n / (2.0 * (double)N), &s, &c);
+    return (n & 1) ? c / (s * (double)N) : -s / (c * (double)N);
+  }
+  if (!(n & 1)) return 0.0;
+  sincospi((double)n / (double)N, &s, &c);
+  return 2.0 * c / (s * (double)N);
 }
 
 template <typename T>
-__global__ void k_multi_pre(const MultiRow* __restrict__ rows, T* A, int M) {
-  const MultiRow r = rows[blockIdx.y];
-  T* a = A + (int64_t)blockIdx.y * M;
+__global__ void k_multi_load2(const MultiRow* __restrict__ rows, int nrows, T* A, int M) {
+  const int j = blockIdx.y;
+  const MultiRow r0 = rows[2 * j];
+  const bool two = 2 * j + 1 < nrows;
+  const float* x1 = two ? rows[2 * j + 1].x : nullptr;
+  const int N1 = two ? rows[2 * j + 1].N : 0;
+  T* a = A + (int64_t)j * M;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-    T v = zero<T>();
-    if (m < r.N) {
-      const T c = chirp_of(m, r.N, -1, (T*)nullptr);
-      const float x = __ldg(r.x + m);
-      v = mk(x * c.x, x * c.y, (T*)nullptr);
-    }
-    a[m] = v;
+    const float u = (m < r0.N) ? __ldg(r0.x + m) : 0.0f;
+    const float v = (m < N1) ? __ldg(x1 + m) : 0.0f;
+    a[m] = mk(u, v, (T*)nullptr);
   }
 }
 
 template <typename T>
-__global__ void k_multi_mul(const MultiRow* __restrict__ rows, T* A, int M, int inv) {
-  const MultiRow r = rows[blockIdx.y];
-  const T* F = reinterpret_cast<const T*>(inv ? r.finv : r.ffwd);
-  T* a = A + (int64_t)blockIdx.y * M;
-  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) a[m] = mul(a[m], F[m]);
-}
-
-template <typename T>
-__global__ void k_multi_mask(const MultiRow* __restrict__ rows, T* A, int M) {
+__global__ void k_multi_split(const MultiRow* __restrict__ rows, int nrows, const T* __restrict__ Z, T* B, int M) {
   using S = decltype(T::x);
-  const int N = rows[blockIdx.y].N;
-  T* a = A + (int64_t)blockIdx.y * M;
-  const int half = (N + 1) >> 1;
-  const S d = (S)1 / (S)N;
+  const int j = blockIdx.y;
+  const bool two = 2 * j + 1 < nrows;
+  const T* z = Z + (int64_t)j * M;
+  const T* H0 = reinterpret_cast<const T*>(rows[2 * j].filt);
+  const T* H1 = two ? reinterpret_cast<const T*>(rows[2 * j + 1].filt) : nullptr;
+  T* b0 = B + (int64_t)(2 * j) * M;
+  T* b1 = B + (int64_t)(2 * j + 1) * M;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-    S f;
-    if (m == 0) f = d;
-    else if (m < half) f = 2 * d;
-    else if (!(N & 1) && m == (N >> 1)) f = d;
-    else f = 0;
-    const T v = a[m];
-    a[m] = (m < N) ? mk(v.x * f, v.y * f, (T*)nullptr) : zero<T>();
+    const T p = z[m];
+    const T q = z[m == 0 ? 0 : M - m];
+    // X0 = (Z[m] + conj Z[-m]) / 2,  X1 = (Z[m] - conj Z[-m]) / 2i
+    const T x0 = mk((p.x + q.x) * (S)0.5, (p.y - q.y) * (S)0.5, (T*)nullptr);
+    b0[m] = mul(x0, H0[m]);
+    if (two) {
+      const T x1 = mk((p.y + q.y) * (S)0.5, (q.x - p.x) * (S)0.5, (T*)nullptr);
+      b1[m] = mul(x1, H1[m]);
+    }
   }
 }
 
 template <typename T>
-__global__ void k_multi_post(const MultiRow* __restrict__ rows, const T* A, int M) {
+__global__ void k_multi_store(const MultiRow* __restrict__ rows, const T* A, int M) {
   const MultiRow r = rows[blockIdx.y];
   const T* a = A + (int64_t)blockIdx.y * M;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < r.N; k += gridDim.x * blockDim.x) {
-    const T v = mul(a[k], chirp_of(k, r.N, +1, (T*)nullptr));
+    const T v = a[k];
     r.out[k] = make_float2((float)v.x, (float)v.y);
   }
 }
 
-template <typename T>
-__global__ void k_multi_filter(const int* __restrict__ Ns, T* B, int M, int dir) {
+__global__ void k_multi_hkernel(const int* __restrict__ Ns, double2* B, int M) {
   const int N = Ns[blockIdx.y];
-  T* b = B + (int64_t)blockIdx.y * M;
+  double2* b = B + (int64_t)blockIdx.y * M;
   const double inv = 1.0 / (double)M;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-    int t = -1;
-    if (m < N) t = m;
-    else if (m > M - N) t = M - m;
-    T v = zero<T>();
-    if (t >= 0) {
-      const T c = chirp_of(t, N, dir, (T*)nullptr);
-      v = mk(c.x * inv, -c.y * inv, (T*)nullptr);
-    }
-    b[m] = v;
+    double re = 0.0, im = 0.0;
+    if (m == 0) re = inv;
+    else if (m < N) im = hilbert_im(m, N) * inv;
+    else if (m > M - N) im = hilbert_im(N - M + m, N) * inv;
+    b[m] = make_double2(re, im);
   }
+}
+
+template <typename T>
+__global__ void k_multi_convert(const double2* __restrict__ src, T* dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = cvt<T>(src[i]);
 }
 
 __global__ void __launch_bounds__(256) k_multi_rowstats(const MultiRow* __restrict__ rows, float* rmax,
@@ -135,38 +141,39 @@ dim3 grid2(int len, int nrows) {
 }  // namespace
 
 template <typename T>
-cudaError_t launch_multi_pre(const MultiRow* rows, int nrows, T* A, int M, cudaStream_t st) {
+cudaError_t launch_multi_load2(const MultiRow* rows, int nrows, T* A, int M, cudaStream_t st) {
   if (nrows <= 0) return cudaSuccess;
-  if (nrows > 65535) return cudaErrorInvalidValue;
-  k_multi_pre<T><<<grid2(M, nrows), 256, 0, st>>>(rows, A, M);
+  const int np = (nrows + 1) / 2;
+  if (np > 65535) return cudaErrorInvalidValue;
+  k_multi_load2<T><<<grid2(M, np), 256, 0, st>>>(rows, nrows, A, M);
   return cudaGetLastError();
 }
 template <typename T>
-cudaError_t launch_multi_mul(const MultiRow* rows, int nrows, T* A, int M, int inv, cudaStream_t st) {
+cudaError_t launch_multi_split(const MultiRow* rows, int nrows, const T* Z, T* B, int M, cudaStream_t st) {
   if (nrows <= 0) return cudaSuccess;
-  if (nrows > 65535) return cudaErrorInvalidValue;
-  k_multi_mul<T><<<grid2(M, nrows), 256, 0, st>>>(rows, A, M, inv);
+  const int np = (nrows + 1) / 2;
+  if (np > 65535) return cudaErrorInvalidValue;
+  k_multi_split<T><<<grid2(M, np), 256, 0, st>>>(rows, nrows, Z, B, M);
   return cudaGetLastError();
 }
 template <typename T>
-cudaError_t launch_multi_mask(const MultiRow* rows, int nrows, T* A, int M, cudaStream_t st) {
+cudaError_t launch_multi_store(const MultiRow* rows, int nrows, const T* A, int M, cudaStream_t st) {
   if (nrows <= 0) return cudaSuccess;
   if (nrows > 65535) return cudaErrorInvalidValue;
-  k_multi_mask<T><<<grid2(M, nrows), 256, 0, st>>>(rows, A, M);
+  k_multi_store<T><<<grid2(M / 2, nrows), 256, 0, st>>>(rows, A, M);
+  return cudaGetLastError();
+}
+cudaError_t launch_multi_hkernel(const int* Ns, int nrows, double2* B, int M, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  if (nrows > 65535) return cudaErrorInvalidValue;
+  k_multi_hkernel<<<grid2(M, nrows), 256, 0, st>>>(Ns, B, M);
   return cudaGetLastError();
 }
 template <typename T>
-cudaError_t launch_multi_post(const MultiRow* rows, int nrows, const T* A, int M, cudaStream_t st) {
-  if (nrows <= 0) return cudaSuccess;
-  if (nrows > 65535) return cudaErrorInvalidValue;
-  k_multi_post<T><<<grid2(M / 2, nrows), 256, 0, st>>>(rows, A, M);
-  return cudaGetLastError();
-}
-template <typename T>
-cudaError_t launch_multi_filter(const int* Ns, int nrows, T* B, int M, int dir, cudaStream_t st) {
-  if (nrows <= 0) return cudaSuccess;
-  if (nrows > 65535) return cudaErrorInvalidValue;
-  k_multi_filter<T><<<grid2(M, nrows), 256, 0, st>>>(Ns, B, M, dir);
+cudaError_t launch_multi_convert(const double2* src, T* dst, int64_t n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int g = (int)std::min<int64_t>(4096, (n + 255) / 256);
+  k_multi_convert<T><<<g, 256, 0, st>>>(src, dst, n);
   return cudaGetLastError();
 }
 cudaError_t launch_multi_rowstats(const MultiRow* rows, int nrows, float* rmax, float* rsum, cudaStream_t st) {
@@ -175,15 +182,13 @@ cudaError_t launch_multi_rowstats(const MultiRow* rows, int nrows, float* rmax, 
   return cudaGetLastError();
 }
 
-template cudaError_t launch_multi_pre<float2>(const MultiRow*, int, float2*, int, cudaStream_t);
-template cudaError_t launch_multi_pre<double2>(const MultiRow*, int, double2*, int, cudaStream_t);
-template cudaError_t launch_multi_mul<float2>(const MultiRow*, int, float2*, int, int, cudaStream_t);
-template cudaError_t launch_multi_mul<double2>(const MultiRow*, int, double2*, int, int, cudaStream_t);
-template cudaError_t launch_multi_mask<float2>(const MultiRow*, int, float2*, int, cudaStream_t);
-template cudaError_t launch_multi_mask<double2>(const MultiRow*, int, double2*, int, cudaStream_t);
-template cudaError_t launch_multi_post<float2>(const MultiRow*, int, const float2*, int, cudaStream_t);
-template cudaError_t launch_multi_post<double2>(const MultiRow*, int, const double2*, int, cudaStream_t);
-template cudaError_t launch_multi_filter<float2>(const int*, int, float2*, int, int, cudaStream_t);
-template cudaError_t launch_multi_filter<double2>(const int*, int, double2*, int, int, cudaStream_t);
+template cudaError_t launch_multi_load2<float2>(const MultiRow*, int, float2*, int, cudaStream_t);
+template cudaError_t launch_multi_load2<double2>(const MultiRow*, int, double2*, int, cudaStream_t);
+template cudaError_t launch_multi_split<float2>(const MultiRow*, int, const float2*, float2*, int, cudaStream_t);
+template cudaError_t launch_multi_split<double2>(const MultiRow*, int, const double2*, double2*, int, cudaStream_t);
+template cudaError_t launch_multi_store<float2>(const MultiRow*, int, const float2*, int, cudaStream_t);
+template cudaError_t launch_multi_store<double2>(const MultiRow*, int, const double2*, int, cudaStream_t);
+template cudaError_t launch_multi_convert<float2>(const double2*, float2*, int64_t, cudaStream_t);
+template cudaError_t launch_multi_convert<double2>(const double2*, double2*, int64_t, cudaStream_t);
 
 }  // namespace fpcc

@@ -1,15 +1,19 @@
 // Analytic signals of windows of different lengths in shared launches.
 //
-// Bluestein's method computes DFT_N as chirp * conv(chirp * x, conj chirp) with
-// the convolution done by transforms of any length M >= 2N - 1.  Windows whose
-// lengths fall in the same class of M therefore share every M-point pass;
-// only the chirp pre- and post-multiplications, the filter spectra and the
-// analytic mask depend on each window's own N, and these kernels take them per
-// row.  The analytic signal IDFT_N(mask * DFT_N(x)) runs as
-//   A = pre(x); A = IFFT_M(FFT_M(A) * F_fwd); A = mask(A)
-//   A = IFFT_M(FFT_M(A) * F_inv); out = post(A)
-// where the forward post-chirp and the inverse pre-chirp cancel (their product
-// is 1), so the middle step is a masked copy.  T is float2 or double2.
+// The analytic signal of an N-sample window, IDFT_N(mask * DFT_N(x)) with the
+// mask of src/FFTapps.c:104-124 (1/N at bin 0 and, for even N, at N/2; 2/N on
+// the bins in between; 0 above), is the circular convolution of x with
+// h = IDFT_N(mask): Re h = delta, and Im h has a closed form (the discrete
+// Hilbert kernel; see hilbert_im in multi.cu).  A circular convolution of length
+// N equals a circular convolution of any length M >= 2N - 1 with the kernel
+// laid out at offsets -(N-1)..(N-1), so windows whose lengths fall in the same
+// class of M (2^a, 3 2^a or 5 2^a) share every M-point pass; only the kernel
+// spectrum H_N = FFT_M(kernel) / M depends on each window's own N.  Two real
+// windows share one forward transform (as the real and imaginary parts of one
+// complex row); their spectra are separated by Hermitian symmetry and each
+// multiplied by its own H_N before one inverse transform per window:
+//   A = x_2j + i x_2j+1;  A = FFT_M(A);  B_r = X_r * H_{N_r};  B = IFFT_M(B);  out = B[0, N)
+// 1.5 M-point transforms per window.  T is float2 or double2.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -20,28 +24,29 @@ namespace fpcc {
 struct MultiRow {
   const float* x;        // the window's samples (real)
   float2* out;           // its analytic signal, N values
-  const void* ffwd;      // M-point filter spectra (T) of the window length, forward
-  const void* finv;      //   and inverse direction, including the 1/M of the inverse
+  const void* filt;      // H_N: M-point kernel spectrum (T) of the window length, including 1/M
   int N;
   int pad;
 };
 
-// A[r][m] = x_r[m] c_{N_r}(m, -1) for m < N_r, else 0 (rows of stride M).
+// A[j][m] = x_{2j}[m] + i x_{2j+1}[m] (zero beyond each window's N and for a
+// missing odd row), (nrows + 1) / 2 rows of stride M.
 template <typename T>
-cudaError_t launch_multi_pre(const MultiRow* rows, int nrows, T* A, int M, cudaStream_t st);
-// A[r][m] *= F_r[m], F_r the forward (inv = 0) or inverse (inv = 1) filter of row r.
+cudaError_t launch_multi_load2(const MultiRow* rows, int nrows, T* A, int M, cudaStream_t st);
+// From the transformed pairs in Z ((nrows + 1) / 2 rows): B[r][m] = X_r[m] H_r[m]
+// for every row r (nrows rows of stride M).
 template <typename T>
-cudaError_t launch_multi_mul(const MultiRow* rows, int nrows, T* A, int M, int inv, cudaStream_t st);
-// A[r][m] = mask_{N_r}(m) A[r][m] for m < N_r, else 0 (mask with the 1/N of the inverse).
+cudaError_t launch_multi_split(const MultiRow* rows, int nrows, const T* Z, T* B, int M, cudaStream_t st);
+// out_r[k] = A[r][k], k < N_r (rounded to float2).
 template <typename T>
-cudaError_t launch_multi_mask(const MultiRow* rows, int nrows, T* A, int M, cudaStream_t st);
-// out_r[k] = A[r][k] c_{N_r}(k, +1), k < N_r.
+cudaError_t launch_multi_store(const MultiRow* rows, int nrows, const T* A, int M, cudaStream_t st);
+// Kernel rows in FP64 before their forward transform: for window length Ns[r],
+// b[r][0] = 1/M, b[r][m] = i Im h(m) / M (0 < m < N), b[r][m] = i Im h(N - M + m) / M
+// (m > M - N), else 0.
+cudaError_t launch_multi_hkernel(const int* Ns, int nrows, double2* B, int M, cudaStream_t st);
+// dst[i] = src[i] rounded to T (n values).
 template <typename T>
-cudaError_t launch_multi_post(const MultiRow* rows, int nrows, const T* A, int M, cudaStream_t st);
-// Filter rows before their forward transform: b[r][m] = conj c_{N_r}(t, dir) / M at
-// t = m (m < N_r) and t = M - m (m > M - N_r), else 0.
-template <typename T>
-cudaError_t launch_multi_filter(const int* Ns, int nrows, T* B, int M, int dir, cudaStream_t st);
+cudaError_t launch_multi_convert(const double2* src, T* dst, int64_t n, cudaStream_t st);
 // Per row: max |a|^2 and sum |a|^2 over the row's N values.
 cudaError_t launch_multi_rowstats(const MultiRow* rows, int nrows, float* rmax, float* rsum, cudaStream_t st);
 

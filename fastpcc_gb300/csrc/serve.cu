@@ -156,6 +156,10 @@ struct Server {
   std::map<std::tuple<int, int, int>, fpcc_wpcc_plan*> wplans;  // (N, Nz, cap)   [worker]
   cudaStream_t st = nullptr;
   fpcc_ctx* ctx = nullptr;
+  // device memory of slabs and scratch: a pool of the server's own whose freed
+  // blocks stay mapped, allocated and freed in the order of the server's stream,
+  // so growing a slab or releasing one needs no device synchronisation
+  cudaMemPool_t pool = nullptr;
   // host copies of registered windows
   std::mutex mu;
   std::condition_variable cv, cv_done;
@@ -217,6 +221,19 @@ size_t product_row_bytes(const Product& p) {
 
 int64_t round16(int64_t b) { return (b + 15) & ~int64_t(15); }
 
+void* dalloc(Server* s, size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocFromPoolAsync(&p, bytes, s->pool, s->st) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+void dfree(Server* s, void* p) {
+  if (p) cudaFreeAsync(p, s->st);
+}
+
 // Frees the least recently used slab (other than `keep`) none of whose rows a
 // batch in flight holds; its products are recomputed when next needed.
 bool release_idle_slab(Server* s, const Slab* keep) {
@@ -230,8 +247,7 @@ bool release_idle_slab(Server* s, const Slab* keep) {
     if (!victim || c.last_use < victim->last_use) victim = &c;
   }
   if (!victim) return false;
-  cudaStreamSynchronize(s->st);
-  cudaFree(victim->base);
+  dfree(s, victim->base);
   s->used -= (size_t)victim->cap * victim->row_bytes;
   victim->base = nullptr;
   victim->cap = 0;
@@ -245,21 +261,21 @@ bool release_idle_slab(Server* s, const Slab* keep) {
 
 bool grow(Server* s, Slab& sl, int need_rows) {
   if (sl.cap >= need_rows) return true;
-  // start at 64 rows, or fewer for rows of tens of MB (wavelet spectra), then double
-  const int64_t init = std::max<int64_t>(1, std::min<int64_t>(64, ((int64_t)256 << 20) / sl.row_bytes));
-  int ncap = std::max(need_rows, std::max((int)init, sl.cap * 2));
+  // start at what is needed (at least 1 MB of rows, at most 64 rows), then double
+  const int64_t init = std::max<int64_t>(1, std::min<int64_t>(64, ((int64_t)1 << 20) / sl.row_bytes));
+  int ncap = std::max(need_rows, sl.cap ? sl.cap * 2 : (int)init);
   // over budget: grow only to what is needed now, then release idle slabs
   while (s->used + (size_t)(ncap - sl.cap) * sl.row_bytes > s->budget) {
     if (ncap > need_rows) { ncap = need_rows; continue; }
     if (!release_idle_slab(s, &sl)) return false;
   }
   const size_t add = (size_t)(ncap - sl.cap) * sl.row_bytes;
-  void* nb = nullptr;
-  if (cudaMalloc(&nb, (size_t)ncap * sl.row_bytes) != cudaSuccess) return false;
+  void* nb = dalloc(s, (size_t)ncap * sl.row_bytes);
+  if (!nb) return false;
   if (sl.base) {
+    // queued kernels that read the old rows run before the copy and the free
     cudaMemcpyAsync(nb, sl.base, (size_t)sl.cap * sl.row_bytes, cudaMemcpyDeviceToDevice, s->st);
-    cudaStreamSynchronize(s->st);
-    cudaFree(sl.base);
+    dfree(s, sl.base);
   }
   sl.base = nb;
   sl.key_of.resize(ncap, -1);
@@ -320,13 +336,15 @@ int claim_row(Server* s, Slab& sl, int64_t key, int rows_needed_now) {
   }
 }
 
-void* dbuf(void** p, size_t* n, size_t need) {
+// Scratch buffer of at least `need` bytes, grown by half again at least when
+// it grows; the old buffer is freed in stream order after the work queued on it.
+void* dbuf(Server* s, void** p, size_t* n, size_t need) {
   if (*n < need) {
-    if (*p) cudaFree(*p);
-    *p = nullptr;
+    const size_t nn = std::max(need, *n + *n / 2);
+    if (*p) dfree(s, *p);
     *n = 0;
-    if (cudaMalloc(p, need) != cudaSuccess) return nullptr;
-    *n = need;
+    if (!(*p = dalloc(s, nn))) return nullptr;
+    *n = nn;
   }
   return *p;
 }
@@ -430,9 +448,9 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   Slab& raw = slab_of(s, Product{0, pk.N, 0, 0});
   // gather raw rows contiguously, compute, scatter into the slab
   const int64_t N = pk.N;
-  void* dx = dbuf(&s->d_tmp_x, &s->n_tmp_x, (size_t)n * round16(N * 4));
-  void* dp = dbuf(&s->d_tmp_p, &s->n_tmp_p, (size_t)n * sl.row_bytes);
-  void* di = dbuf(&s->d_idx, &s->n_idx, (size_t)2 * n * sizeof(int) + 64);
+  void* dx = dbuf(s, &s->d_tmp_x, &s->n_tmp_x, (size_t)n * round16(N * 4));
+  void* dp = dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)n * sl.row_bytes);
+  void* di = dbuf(s, &s->d_idx, &s->n_idx, (size_t)2 * n * sizeof(int) + 64);
   if (!dx || !dp || !di) return FPCC_ENOMEM;
   std::vector<int> idx(2 * n);
   for (int i = 0; i < n; i++) { idx[i] = raw_rows[i]; idx[n + i] = miss_rows[i]; }
@@ -517,8 +535,8 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
   if (&s1 != &s2) {
     // stage the station-2 rows behind the station-1 rows in the temporary buffer
     const int64_t rb = s1.row_bytes;
-    void* merged = dbuf(&s->d_tmp_p, &s->n_tmp_p, (size_t)2 * n * rb);
-    void* di = dbuf(&s->d_idx, &s->n_idx, (size_t)2 * n * sizeof(int) + 64);
+    void* merged = dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)2 * n * rb);
+    void* di = dbuf(s, &s->d_idx, &s->n_idx, (size_t)2 * n * sizeof(int) + 64);
     if (!merged || !di) return FPCC_ENOMEM;
     std::vector<int> idx(2 * n);
     for (int i = 0; i < n; i++) { idx[i] = r1[i]; idx[n + i] = r2[i]; }
@@ -541,8 +559,8 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
     // the pair kernel reads energy rows by the pair's station rows, so stage both
     // spectra and energies in pair order
     const int64_t rb = s1.row_bytes, eb = se.row_bytes;
-    void* tmp = dbuf(&s->d_tmp_p, &s->n_tmp_p, (size_t)2 * n * (rb + eb));
-    void* di = dbuf(&s->d_idx, &s->n_idx, (size_t)4 * n * sizeof(int) + 64);
+    void* tmp = dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)2 * n * (rb + eb));
+    void* di = dbuf(s, &s->d_idx, &s->n_idx, (size_t)4 * n * sizeof(int) + 64);
     if (!tmp || !di) return FPCC_ENOMEM;
     std::vector<int> idx(4 * n);
     for (int i = 0; i < n; i++) { idx[i] = r1[i]; idx[n + i] = r2[i]; idx[2 * n + i] = e1[i]; idx[3 * n + i] = e2[i]; }
@@ -559,8 +577,8 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
   }
   // device pair list (its own buffer: the index buffer may still feed queued copies) and output
   const size_t ybytes = (size_t)n * g.L * (m == FPCC_CC1B_POPCOUNT ? 8 : 4);
-  void* dpl = dbuf(&s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
-  void* dy = dbuf(&s->d_y, &s->n_y, ybytes);
+  void* dpl = dbuf(s, &s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
+  void* dy = dbuf(s, &s->d_y, &s->n_y, ybytes);
   if (!dpl || !dy) return FPCC_ENOMEM;
   if (upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st) != cudaSuccess) return FPCC_ECUDA;
   const int64_t lds = slab_of(s, p1).row_bytes / ((m == FPCC_CC1B_POPCOUNT) ? 4 : (g.fmt ? 4 : 8));
@@ -642,8 +660,8 @@ int prefetch_phase(Server* s, const GroupKey& g, int kind, std::vector<Req*>& re
     rows[i].f64 = miss[i].f64;
     rows[i].pad = 0;
   }
-  void* tmp = dbuf(&s->d_tmp_p, &s->n_tmp_p, (size_t)n * ldo * esz);
-  void* dc = dbuf(&s->d_idx, &s->n_idx, (size_t)n * sizeof(RowCopy) + 64);
+  void* tmp = dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)n * ldo * esz);
+  void* dc = dbuf(s, &s->d_idx, &s->n_idx, (size_t)n * sizeof(RowCopy) + 64);
   if (!tmp || !dc) return FPCC_ENOMEM;
   const int method = (kind == 1) ? FPCC_PCC2 : FPCC_PCC1;
   if ((rc = fpcc_station_stage_multi(s->ctx, method, rows.data(), n, g.fmt, FPCC_AMP_F_REG, tmp, ldo))) return rc;
@@ -710,8 +728,8 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
   const size_t osz = (m == FPCC_CC1B_POPCOUNT) ? 8 : 4;
   size_t total = 0;
   for (int i = 0; i < n; i++) total += (size_t)reqs[i]->L * osz;
-  char* dy = (char*)dbuf(&s->d_y, &s->n_y, total);
-  void* dd = dbuf(&s->d_desc, &s->n_desc, (size_t)n * sizeof(fpcc_pair_desc));
+  char* dy = (char*)dbuf(s, &s->d_y, &s->n_y, total);
+  void* dd = dbuf(s, &s->d_desc, &s->n_desc, (size_t)n * sizeof(fpcc_pair_desc));
   if (!dy || !dd) return FPCC_ENOMEM;
   std::vector<fpcc_pair_desc> d(n);
   size_t off = 0;
@@ -811,8 +829,8 @@ int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlig
   std::vector<int32_t> pairs(2 * n);
   for (int i = 0; i < n; i++) { pairs[2 * i] = rows[i]; pairs[2 * i + 1] = rows[n + i]; }
   const size_t ybytes = (size_t)n * g.L * 4;
-  void* dpl = dbuf(&s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
-  void* dy = dbuf(&s->d_y, &s->n_y, ybytes);
+  void* dpl = dbuf(s, &s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
+  void* dy = dbuf(s, &s->d_y, &s->n_y, ybytes);
   if (!dpl || !dy) return FPCC_ENOMEM;
   if (upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st) != cudaSuccess) return FPCC_ECUDA;
   if ((rc = fpcc_wpcc_pair_stage(s->ctx, p, sl.base, g.fmt, (const int32_t*)dpl, n, (float*)dy, g.L))) return rc;
@@ -1021,6 +1039,19 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
     return FPCC_ECUDA;
   }
   s->st = (cudaStream_t)fpcc_get_stream(s->ctx);
+  cudaMemPoolProps pp = {};
+  pp.allocType = cudaMemAllocationTypePinned;
+  pp.location.type = cudaMemLocationTypeDevice;
+  pp.location.id = device;
+  // freed blocks are kept up to the budget and a quarter again (slabs and scratch)
+  uint64_t keep = (uint64_t)s->budget + (uint64_t)s->budget / 4;
+  if (cudaSetDevice(device) != cudaSuccess || cudaMemPoolCreate(&s->pool, &pp) != cudaSuccess ||
+      cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+    if (s->pool) cudaMemPoolDestroy(s->pool);
+    fpcc_destroy(s->ctx);
+    delete s;
+    return FPCC_ECUDA;
+  }
   s->worker = std::thread(worker_main, s);
   for (int i = 0; i < 4; i++) s->completers.emplace_back(completer_main, s);
   *out = reinterpret_cast<fpcc_server*>(s);
@@ -1042,9 +1073,10 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
   s->cv_c.notify_all();
   for (auto& t : s->completers) t.join();
   cudaSetDevice(s->device);
+  for (auto& kv : s->slabs) dfree(s, kv.second.base);
+  for (void** p : {&s->d_tmp_x, &s->d_tmp_p, &s->d_idx, &s->d_y, &s->d_pl, &s->d_desc}) dfree(s, *p);
   cudaStreamSynchronize(s->st);
-  for (auto& kv : s->slabs) if (kv.second.base) cudaFree(kv.second.base);
-  for (void** p : {&s->d_tmp_x, &s->d_tmp_p, &s->d_idx, &s->d_y, &s->d_pl, &s->d_desc}) if (*p) cudaFree(*p);
+  cudaMemPoolDestroy(s->pool);
   for (auto& kv : s->wplans) fpcc_wpcc_plan_destroy(kv.second);
   for (size_t i = 0; i < s->pinned_pool.size(); i += 2) cudaFreeHost(s->pinned_pool[i]);
   for (char* a : s->arena) cudaFreeHost(a);

@@ -135,9 +135,11 @@ int fpcc_station_stage_ex(fpcc_ctx *ctx, int method, const float *d_x, int64_t l
 /* Station stage of the phase methods (PCC2, PCC1, PCCV) for windows of
  * different lengths: row r reads h_rows[r].d_x (N samples) and writes d_out +
  * r * ldo (ldo in elements of the format: 8 bytes for F32, 4 otherwise).  The
- * analytic signals of all rows run as Bluestein transforms grouped by length
- * class (2^a, 3 2^a or 5 2^a >= 2N - 1; FP64 for rows with f64 set), so the
- * windows share their launches; rows must be ordered by (N, Nz). */
+ * analytic signal of each row is its circular convolution with the kernel
+ * IDFT_N(mask), computed with M-point transforms shared by every row of the same
+ * length class (M = 2^a, 3 2^a or 5 2^a >= 2N - 1; FP64 for rows with f64 set),
+ * two rows per forward transform, so the windows share their launches; rows
+ * must be ordered by (N, Nz). */
 typedef struct {
   const float *d_x;   /* the window's samples (device)                */
   int32_t N, Nz;      /* window length, padded length (PCC2)          */
