@@ -252,25 +252,44 @@ def uneven_batch_leg(F, n_pairs=500, fmt=2, nz_mode=1):
     demand, pair stages packed per method and padded length) against the plain
     per-pair drop-in."""
     from oracle import oracle as O
-    rng = np.random.default_rng(41)
-    lengths = np.round(2.0 ** rng.uniform(12, 17, n_pairs)).astype(int)
     from fastpcc_gb300 import synth
-    win = synth.uneven_windows(lengths, 2, gap_frac=0.05, tag="uneven-batch")
-    methods = rng.choice(list(MIX_BATCH), size=n_pairs, p=list(MIX_BATCH.values()))
-    reqs = []
-    for i in range(n_pairs):
-        M = max(1, int(rng.uniform(0.01, 0.10) * lengths[i]))
-        reqs.append((int(methods[i]), 0, 1, i, -M, M))
+
+    def case(n, seed, tag):
+        rng = np.random.default_rng(seed)
+        lengths = np.round(2.0 ** rng.uniform(12, 17, n)).astype(int)
+        win = synth.uneven_windows(lengths, 2, gap_frac=0.05, tag=tag)
+        methods = rng.choice(list(MIX_BATCH), size=n, p=list(MIX_BATCH.values()))
+        reqs = []
+        for i in range(n):
+            M = max(1, int(rng.uniform(0.01, 0.10) * lengths[i]))
+            reqs.append((int(methods[i]), 0, 1, i, -M, M))
+        return win, reqs
+
+    def server(win):
+        srv = F.Server(hbm_budget=150 << 30, max_batch=8192, fmt=fmt, nz_mode=nz_mode)
+        for w in range(len(win)):
+            srv.put(0, w, win[w][0])
+            srv.put(1, w, win[w][1])
+        return srv
+
+    # warm-up on another batch of the same distribution (other lengths), through
+    # both arms: loads every kernel once in this process; each timed arm below
+    # still starts with its own per-length caches empty (new lengths, new server)
+    wwin, wreqs = case(60, 141, "uneven-batch-warmup")
+    for (m, s1, s2, w, l1, l2) in wreqs:
+        _plain_call(F, m, wwin[w][s1][None], wwin[w][s2][None], l1, l2)
+    wsrv = server(wwin)
+    warr, _ = _serve_requests(F, wsrv, wreqs, lambda s, w: s)
+    wsrv.submit_many(warr)
+    wsrv.drain()
+    wsrv.close()
+    win, reqs = case(n_pairs, 41, "uneven-batch")
     # plain: every pair through its method's plain drop-in
-    _plain_call(F, 0, win[0][0][None], win[0][1][None], -10, 10)
     t0 = time.perf_counter()
     for (m, s1, s2, w, l1, l2) in reqs:
         _plain_call(F, m, win[w][s1][None], win[w][s2][None], l1, l2)
     t_plain = time.perf_counter() - t0
-    srv = F.Server(hbm_budget=150 << 30, max_batch=8192, fmt=fmt, nz_mode=nz_mode)
-    for w in range(n_pairs):
-        srv.put(0, w, win[w][0])
-        srv.put(1, w, win[w][1])
+    srv = server(win)
     arr, outs = _serve_requests(F, srv, reqs, lambda s, w: s)
     t0 = time.perf_counter()
     srv.submit_many(arr)
@@ -291,6 +310,7 @@ def uneven_batch_leg(F, n_pairs=500, fmt=2, nz_mode=1):
                         "what": "station products computed on demand, pair stages packed"},
             "batched_resident": {"value": n_pairs / t_warm, "unit": UNIT, "what": "second pass, products resident"},
             "speedup_vs_plain": t_plain / t_cold, "spectra": ("f32", "f16", "i16")[fmt],
+            "warmup": "60 pairs of another seed through both arms first (kernels loaded; no cached lengths)",
             "max_rel_err": err, "err_sample": "2 requests per method with N <= 2^14 against the FP64 oracle"}
 
 
@@ -307,7 +327,21 @@ def serving_leg(F, n_sta=200, n_win=8, n_req=4000, fmt=2, rates=(1e3, 1e4, 1e5, 
     win = synth.uneven_windows(lengths, n_sta, tag="serving")
     reqs = synth.mixed_requests(n_req, n_sta, lengths, MIX_STREAM, seed=6)
     n_plain = 150
-    _plain_call(F, 0, win[0][0][None], win[0][1][None], -10, 10)
+    # warm-up on a small pool of other lengths through both arms (kernels loaded;
+    # the timed server starts with no products and no cached lengths)
+    wl = np.array([5003, 12007, 30011])
+    wwin = synth.uneven_windows(wl, 8, tag="serving-warmup")
+    wreqs = synth.mixed_requests(60, 8, wl, MIX_STREAM, seed=61)
+    for (m, s1, s2, w, l1, l2) in wreqs:
+        _plain_call(F, m, wwin[w][s1][None], wwin[w][s2][None], l1, l2)
+    wsrv = F.Server(hbm_budget=8 << 30, max_batch=8192, fmt=fmt, wavelet=WAVELET, nz_mode=nz_mode)
+    for w in range(len(wl)):
+        for k in range(8):
+            wsrv.put(k, w, wwin[w][k])
+    warr, _ = _serve_requests(F, wsrv, wreqs, lambda s, w: s)
+    wsrv.submit_many(warr)
+    wsrv.drain()
+    wsrv.close()
     t0 = time.perf_counter()
     for (m, s1, s2, w, l1, l2) in reqs[:n_plain]:
         _plain_call(F, m, win[w][s1][None], win[w][s2][None], l1, l2)
@@ -350,6 +384,7 @@ def serving_leg(F, n_sta=200, n_win=8, n_req=4000, fmt=2, rates=(1e3, 1e4, 1e5, 
                                   "what": "all requests at once, products resident"},
             "served_cold": {"value": n_req / t_cold, "unit": UNIT, "what": "products computed on demand"},
             "speedup_vs_plain": (n_req / t_warm) / plain, "poisson": sweep, "hbm_used_bytes": hbm,
+            "warmup": "60 requests over 8 stations x 3 other lengths through both arms first",
             "spectra": ("f32", "f16", "i16")[fmt], "max_rel_err": err,
             "err_sample": "2 requests per method with N <= 20000 against the FP64 oracle"}
 

@@ -468,9 +468,7 @@ int smooth_at_least(int n) {
   }
   int best = -1;
   double bc = 1e300;
-  for (int m = n; m <= 2 * n + 64; m++) {
-    int a, b, cc;
-    if (!factor235(m, &a, &b, &cc)) continue;
+  for (int m : smooth235_in(n, 2 * n + 64)) {
     FftPlan p;
     if (!make_plan(m, &p)) continue;
     const double c = plan_cost(m);

@@ -1,6 +1,7 @@
 // Host-side planning: radix schedules and padded correlation lengths.
 #include <math.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -19,6 +20,18 @@ bool factor235(int n, int* a, int* b, int* c) {
   while (n % 3 == 0) { n /= 3; (*b)++; }
   while (n % 5 == 0) { n /= 5; (*c)++; }
   return n == 1;
+}
+
+std::vector<int> smooth235_in(int lo, int hi) {
+  std::vector<int> v;
+  if (lo < 1) lo = 1;
+  if (hi < lo) return v;
+  for (int64_t p5 = 1; p5 <= hi; p5 *= 5)
+    for (int64_t p3 = p5; p3 <= hi; p3 *= 3)
+      for (int64_t p2 = p3; p2 <= hi; p2 *= 2)
+        if (p2 >= lo) v.push_back((int)p2);
+  std::sort(v.begin(), v.end());
+  return v;
 }
 
 static void encode(FftPlan* p) {
@@ -124,20 +137,11 @@ std::vector<std::tuple<int, double, double>> tuned_table(double* reuse) {
   return v;
 }
 
-static bool tuned_cost(int nz, double* cost) {
-  std::lock_guard<std::mutex> lk(g_tune_mu);
-  auto it = g_tuned.find(nz);
-  if (it == g_tuned.end()) return false;
-  *cost = it->second.first + it->second.second / g_reuse;
-  return true;
-}
 
 std::vector<int> usable_lengths(int lo, int hi) {
   std::vector<int> v;
-  for (int nz = lo + (lo & 1); nz <= hi; nz += 2) {
-    int a2, b3, c5;
-    if (factor235(nz, &a2, &b3, &c5) && nz_usable(nz)) v.push_back(nz);
-  }
+  for (int nz : smooth235_in(lo, hi))
+    if (!(nz & 1) && nz_usable(nz)) v.push_back(nz);
   return v;
 }
 
@@ -160,9 +164,14 @@ static int choose_nz_uncached(int N, int M, int mode) {
   if (mode == FPCC_NZ_TUNED_MODE) {
     // the measured cheapest length among those the autotuner timed
     int best = -1;
-    double bc = 1e300, c;
-    for (int nz = need + (need & 1); nz <= 2 * need + 64 && nz <= (1 << 21); nz += 2)
-      if (tuned_cost(nz, &c) && c < bc) { bc = c; best = nz; }
+    double bc = 1e300;
+    const int hi = std::min(2 * need + 64, 1 << 21);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (auto it = g_tuned.lower_bound(need + (need & 1)); it != g_tuned.end() && it->first <= hi; ++it) {
+      if (it->first & 1) continue;
+      const double c = it->second.first + it->second.second / g_reuse;
+      if (c < bc) { bc = c; best = it->first; }
+    }
     return best;
   }
   if (mode >= 2) {
@@ -176,9 +185,8 @@ static int choose_nz_uncached(int N, int M, int mode) {
   // candidates: menu lengths and four-step lengths 2^a 3^b 5^c up to 2^20
   int best = -1;
   double bc = 1e300;
-  for (int nz = need + (need & 1); nz <= 2 * need + 64 && nz <= (1 << 21); nz += 2) {
-    int a2, b3, c5;
-    if (!factor235(nz, &a2, &b3, &c5) || !nz_usable(nz)) continue;
+  for (int nz : smooth235_in(need, std::min(2 * need + 64, 1 << 21))) {
+    if ((nz & 1) || !nz_usable(nz)) continue;
     // the pair transform (Nz/2) dominates a batch of correlations
     const double cost = length_cost(nz / 2) + 0.1 * length_cost(nz);
     if (cost < bc) { bc = cost; best = nz; }

@@ -16,6 +16,10 @@ constexpr int kMaxCtaLen = 21120;
 // Factor n into 2^a 3^b 5^c; false for any other prime factor.
 bool factor235(int n, int* a, int* b, int* c);
 
+// Every 2^a 3^b 5^c in [lo, hi], ascending (about a hundred per octave near 1e5,
+// against tens of thousands of integers: length searches walk this list).
+std::vector<int> smooth235_in(int lo, int hi);
+
 // Radix schedule for an in-block transform of length n (2,3,5-smooth):
 // ceil(a/4) power-of-two passes with the exponent spread evenly, then the 5s
 // and 3s.  When `forced` is non-null it lists the radices to use instead.

@@ -15,8 +15,12 @@
 // lengths N that are not on the menu (the N-point analytic signal, :104-124).
 #include <float.h>
 
+#include <cooperative_groups.h>
+
 #include "kernels.cuh"
 #include "menu.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace fpcc {
 
@@ -273,19 +277,39 @@ __global__ void __launch_bounds__(256) k_phase_store(PhaseArgs a) {
 }
 
 // ------------------------------------------------------------ int16 rows
-// One block per row: the row maximum, then the block-scaled int16 row.
-__global__ void __launch_bounds__(256) k_quantize_i16(const float2* __restrict__ in, int64_t ldin, int n,
-                                                      char* __restrict__ out, int64_t ldo_bytes) {
+// One cluster of kQCluster blocks per row: each block takes a segment, the
+// blocks exchange their segment maxima through distributed shared memory
+// (hardware cluster barriers), and each writes its segment of the block-scaled
+// int16 row; block 0 writes the header.  The row maximum does not depend on the
+// split, so the row is the same as one block would write.
+constexpr int kQCluster = 8;
+
+__global__ void __cluster_dims__(kQCluster, 1, 1) __launch_bounds__(256)
+    k_quantize_i16(const float2* __restrict__ in, int64_t ldin, int n, char* __restrict__ out, int64_t ldo_bytes) {
   __shared__ float scratch[32];
-  const float2* r = in + (int64_t)blockIdx.x * ldin;
+  __shared__ float seg_max;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int seg = (n + kQCluster - 1) / kQCluster;
+  const int k0 = rank * seg, k1 = min(n, k0 + seg);
+  const float2* r = in + (int64_t)blockIdx.y * ldin;
   float m = 0.0f;
-  for (int k = threadIdx.x; k < n; k += 256) m = fmaxf(m, fmaxf(fabsf(r[k].x), fabsf(r[k].y)));
+  for (int k = k0 + threadIdx.x; k < k1; k += 256) m = fmaxf(m, fmaxf(fabsf(r[k].x), fabsf(r[k].y)));
   m = block_max(m, scratch);
+  if (threadIdx.x == 0) seg_max = m;
+  cluster.sync();
+  if (threadIdx.x < 32) {
+    float v = (threadIdx.x < kQCluster) ? *cluster.map_shared_rank(&seg_max, (unsigned)threadIdx.x) : 0.0f;
+    v = warp_max(v);
+    if (threadIdx.x == 0) scratch[0] = v;
+  }
+  cluster.sync();   // every block has read the others' maxima before any exits
+  m = scratch[0];
   const float inv = (m > 0.0f) ? kI16Max / m : 0.0f;
-  char* row = out + (int64_t)blockIdx.x * ldo_bytes;
-  if (threadIdx.x < 4) reinterpret_cast<float*>(row)[threadIdx.x] = (threadIdx.x == 0) ? m / kI16Max : 0.0f;
+  char* row = out + (int64_t)blockIdx.y * ldo_bytes;
+  if (rank == 0 && threadIdx.x < 4) reinterpret_cast<float*>(row)[threadIdx.x] = (threadIdx.x == 0) ? m / kI16Max : 0.0f;
   short2* o = reinterpret_cast<short2*>(row + kI16Header);
-  for (int k = threadIdx.x; k < n; k += 256) o[k] = make_short2(i16_quant(r[k].x, inv), i16_quant(r[k].y, inv));
+  for (int k = k0 + threadIdx.x; k < k1; k += 256) o[k] = make_short2(i16_quant(r[k].x, inv), i16_quant(r[k].y, inv));
 }
 
 // ------------------------------------------------------------ generic passes
@@ -495,7 +519,11 @@ cudaError_t launch_pairs(const PairArgs& a, cudaStream_t st) {
 cudaError_t launch_quantize_i16(const float2* in, int64_t ldin, int n, int nrows, void* out, int64_t ldo,
                                 cudaStream_t st) {
   if (nrows <= 0) return cudaSuccess;
-  k_quantize_i16<<<nrows, 256, 0, st>>>(in, ldin, n, reinterpret_cast<char*>(out), ldo * 4);
+  for (int r0 = 0; r0 < nrows; r0 += 65535) {
+    const int nr = nrows - r0 < 65535 ? nrows - r0 : 65535;
+    k_quantize_i16<<<dim3(kQCluster, nr), 256, 0, st>>>(in + (int64_t)r0 * ldin, ldin, n,
+                                                        reinterpret_cast<char*>(out) + (int64_t)r0 * ldo * 4, ldo * 4);
+  }
   return cudaGetLastError();
 }
 

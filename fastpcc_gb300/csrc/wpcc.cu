@@ -68,10 +68,8 @@ int wpcc_choose_nz(const WpccSetup& su, unsigned N, int nz_mode) {
   for (unsigned s = 0; s < su.wf.S; s++) capped |= (su.wf.Ls[s] >= su.Nz0);
   if (nz_mode == 0 || capped) return wpcc_len_ok((int)su.Nz_ref) ? (int)su.Nz_ref : -1;
   const int need = (int)(N + su.M + su.Ls0);
-  for (int nz = need + (need & 1); nz <= (int)su.Nz_ref; nz += 2) {
-    int a2, b3, c5;
-    if (factor235(nz, &a2, &b3, &c5) && wpcc_len_ok(nz)) return nz;
-  }
+  for (int nz : smooth235_in(need, (int)su.Nz_ref))
+    if (!(nz & 1) && wpcc_len_ok(nz)) return nz;
   return wpcc_len_ok((int)su.Nz_ref) ? (int)su.Nz_ref : -1;
 }
 
