@@ -24,6 +24,7 @@
 #include "wpcc.h"
 #include "precise.cuh"
 #include "multi.cuh"
+#include "stack.cuh"
 
 using namespace fpcc;
 
@@ -63,7 +64,7 @@ struct fpcc_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  DevBuf dev[40];
+  DevBuf dev[48];
   DevBuf pin[8];
   cudaStream_t stream2 = nullptr;   // second stream of the pipelined drop-ins
   cudaEvent_t chunk_ev[8] = {};     // pair-stage chunks whose results stream2 downloads
@@ -319,7 +320,8 @@ enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_
             S_ANA_B = 7, S_RSTAT = 8, S_LARGE_T = 9, S_WP_X = 10, S_WP_BAND = 11, S_WP_RMAX = 12,
             S_WP_Y = 13, S_WP_STAGE = 14, S_BLUE_O = 23, S_P64_D = 24, S_P64_A = 25, S_P64_B = 26,
             S_P64_CNT = 27, S_I16_Q = 28, S_MULTI_A = 29, S_MULTI_B = 30, S_MULTI_AN = 31, S_EPART = 32,
-            S_CONV_X = 33, S_CONV_Y = 34 };
+            S_CONV_X = 33, S_CONV_Y = 34, S_STK_SPEC = 35, S_STK_A = 36, S_STK_B = 37, S_STK_X = 38,
+            S_STK_T = 39, S_STK_T2 = 40, S_STK_Y = 41, S_STK_Y2 = 42, S_STK_R = 43, S_STK_AN = 44 };
 
 constexpr size_t kLargeChunkBytes = size_t(512) << 20;   // four-step intermediate per chunk
 
@@ -1799,4 +1801,144 @@ extern "C" int cuda_tspcc2_set_freq(float** y0, float** x01, float** x02, unsign
   cudaFree(p.W);
   cudaFree(p.a);
   return rc ? -1 : 0;
+}
+
+// ============================================================== stacks over windows
+namespace {
+
+// M-point spectra (FFT / M, float2) of the L-periodic CWT kernels of every scale:
+// rows [0, S): forward (conjugate taps at offsets c - l), rows [S, 2S): the
+// reconstruction (taps at offsets l - c).
+int stack_spectra(fpcc_ctx* c, const WaveletFamily& wf, int L, int M, float2** out) {
+  const int S = (int)wf.S;
+  std::vector<double2> h((size_t)2 * S * M, make_double2(0.0, 0.0));
+  for (int s = 0; s < S; s++) {
+    double2* f = h.data() + (size_t)s * M;
+    double2* r = h.data() + (size_t)(S + s) * M;
+    const int cs = wf.center[s];
+    for (int l = 0; l < (int)wf.Ls[s]; l++) {
+      const std::complex<double> w = wf.taps[s][l];
+      // index of offset d in the layout: d mod L placed at [0, L) or, for the
+      // negative representative, at M - (L - d mod L)
+      auto at = [&](int d) {
+        int k = d % L;
+        if (k < 0) k += L;
+        return k;
+      };
+      const int kf = at(cs - l), kr = at(l - cs);
+      f[kf] = make_double2(f[kf].x + w.real() / M, f[kf].y - w.imag() / M);
+      r[kr] = make_double2(r[kr].x + w.real() / M, r[kr].y + w.imag() / M);
+    }
+    // the L-periodic kernel on M points: values at [0, L) and their copies at
+    // M - L + k for k in [1, L) (offsets -(L-1)..-1)
+    for (double2* row : {f, r})
+      for (int k = 1; k < L; k++) row[M - L + k] = row[k];
+  }
+  void *A, *B, *spec;
+  int rc;
+  if ((rc = dev_buf(c, S_STK_A, h.size() * sizeof(double2), &A)) ||
+      (rc = dev_buf(c, S_STK_B, h.size() * sizeof(double2), &B)) ||
+      (rc = dev_buf(c, S_STK_SPEC, h.size() * sizeof(float2), &spec)))
+    return rc;
+  CK(cudaMemcpyAsync(A, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  double2* res = nullptr;
+  if ((rc = passes64(c, (double2*)A, (double2*)B, M, 2 * S, -1, &res))) return rc;
+  CK(launch_multi_convert<float2>(res, (float2*)spec, (int64_t)h.size(), c->stream));
+  g_launches++;
+  *out = (float2*)spec;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int fpcc_stack(fpcc_ctx* c, int mode, const float* d_y, int64_t ldy, int K, int L, int ngroups,
+                          double nu, double pmin, double pmax, int V, int type, double op1, float* d_out,
+                          int64_t ldo) {
+  if (!c || !d_y || !d_out) return fail(FPCC_EARG, "null argument");
+  if (K <= 0 || L < 2 || ngroups <= 0 || ldy < L || ldo < L || !(nu >= 0))
+    return fail(FPCC_EARG, "stack: K >= 1, L >= 2, groups >= 1, strides >= L and nu >= 0 are required");
+  if (mode < FPCC_STACK_LINEAR || mode > FPCC_STACK_TSPWS) return fail(FPCC_EARG, "unknown stack mode %d", mode);
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  int rc;
+  if (mode == FPCC_STACK_LINEAR) {
+    for (int g0 = 0; g0 < ngroups; g0 += 65535) {
+      const int G = std::min(65535, ngroups - g0);
+      CK(launch_stack_mean(d_y + (size_t)g0 * K * ldy, ldy, K, L, G, d_out + (size_t)g0 * ldo, ldo, c->stream));
+      g_launches++;
+    }
+    return 0;
+  }
+  const int M = conv_class_len(L);
+  if (mode == FPCC_STACK_PWS) {
+    // analytic signals of the rows (packed stage of the phase methods, FP32), per chunk of groups
+    const int Gc = (int)std::max<int64_t>(1, std::min<int64_t>(65535, ((int64_t)4096) / K));
+    for (int g0 = 0; g0 < ngroups; g0 += Gc) {
+      const int G = std::min(Gc, ngroups - g0);
+      const int n = G * K;
+      void* an;
+      if ((rc = dev_buf(c, S_STK_AN, (size_t)n * L * sizeof(float2), &an))) return rc;
+      std::vector<MultiRow> rows(n);
+      for (int r = 0; r < n; r++) {
+        rows[r] = MultiRow{};
+        rows[r].x = d_y + ((size_t)g0 * K + r) * ldy;
+        rows[r].out = (float2*)an + (size_t)r * L;
+        rows[r].N = L;
+      }
+      if ((rc = multi_group<float2>(c, rows, M))) return rc;
+      CK(launch_stack_pws((const float2*)an, L, d_y + (size_t)g0 * K * ldy, ldy, K, L, G, nu,
+                          d_out + (size_t)g0 * ldo, ldo, c->stream));
+      g_launches++;
+    }
+    return 0;
+  }
+  WaveletFamily wf;
+  double cpsi = 0;
+  if (stack_family((unsigned)L, pmin, pmax, (unsigned)V, type, op1, &wf, &cpsi))
+    return fail(FPCC_EARG, "stack: invalid wavelet parameters (pmin %g, pmax %g, V %d, type %d)", pmin, pmax, V, type);
+  const int S = (int)wf.S;
+  float2* spec = nullptr;
+  if ((rc = stack_spectra(c, wf, L, M, &spec))) return rc;
+  // groups per chunk: transform buffers of (G K + G) rows under 256 MB
+  const int64_t per_group = (int64_t)(K + 1) * M * (int64_t)sizeof(float2);
+  const int Gc = (int)std::max<int64_t>(1, std::min<int64_t>(65535 / (K + 1), ((int64_t)256 << 20) / per_group));
+  if ((int64_t)(K + 1) > 65535) return fail(FPCC_EARG, "stack: at most 65534 traces per group");
+  for (int g0 = 0; g0 < ngroups; g0 += Gc) {
+    const int G = std::min(Gc, ngroups - g0);
+    const int rows = G * K + G;
+    void *X, *T, *T2, *Y, *Y2, *R;
+    if ((rc = dev_buf(c, S_STK_X, (size_t)rows * M * sizeof(float2), &X)) ||
+        (rc = dev_buf(c, S_STK_T, (size_t)rows * M * sizeof(float2), &T)) ||
+        (rc = dev_buf(c, S_STK_T2, (size_t)rows * M * sizeof(float2), &T2)) ||
+        (rc = dev_buf(c, S_STK_Y, (size_t)G * M * sizeof(float2), &Y)) ||
+        (rc = dev_buf(c, S_STK_Y2, (size_t)G * M * sizeof(float2), &Y2)) ||
+        (rc = dev_buf(c, S_STK_R, (size_t)G * M * sizeof(float2), &R)))
+      return rc;
+    // spectra of the traces, and of each group's linear stack in rows G K + g
+    CK(launch_stack_load(d_y + (size_t)g0 * K * ldy, ldy, G * K, L, (float2*)X, M, c->stream));
+    float2* xs = nullptr;
+    if ((rc = passes(c, (float2*)X, (float2*)T, M, G * K, -1, &xs))) return rc;
+    if (xs != (float2*)X) CK(cudaMemcpyAsync(X, xs, (size_t)G * K * M * sizeof(float2), cudaMemcpyDeviceToDevice,
+                                             c->stream));
+    CK(launch_stack_xlin((float2*)X, K, G, M, c->stream));
+    g_launches += 2;
+    for (int s = 0; s < S; s++) {
+      // CWT of every trace and of the linear stacks at scale s
+      CK(launch_stack_mul((const float2*)X, rows, M, spec + (size_t)s * M, (float2*)T, c->stream));
+      float2* W = nullptr;
+      if ((rc = passes(c, (float2*)T, (float2*)T2, M, rows, +1, &W))) return rc;
+      // weighted linear-stack coefficients, back to the spectrum, times the reconstruction kernel
+      CK(launch_stack_coherence(W, K, G, L, M, nu, (float2*)Y, c->stream));
+      float2* Z = nullptr;
+      if ((rc = passes(c, (float2*)Y, (float2*)Y2, M, G, -1, &Z))) return rc;
+      const float a = (float)(std::log(2.0) / (2 * cpsi * V * wf.scale[s]));
+      CK(launch_stack_acc(Z, G, M, spec + (size_t)(S + s) * M, a, s == 0, (float2*)R, c->stream));
+      g_launches += 3;
+    }
+    float2* r = nullptr;
+    if ((rc = passes(c, (float2*)R, (float2*)Y, M, G, +1, &r))) return rc;
+    CK(launch_stack_real(r, G, L, M, d_out + (size_t)g0 * ldo, ldo, c->stream));
+    g_launches++;
+  }
+  return 0;
 }

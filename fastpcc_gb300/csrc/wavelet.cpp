@@ -100,4 +100,38 @@ int wpcc_setup(unsigned N, int Lag1, int Lag2, double pmin, double pmax, unsigne
   return 0;
 }
 
+// Admissibility constants of the reconstruction: Morlet_Cpsi (the running sum
+// of src/FWTa/wavelet_def_v7.c:133-144, kept step for step) and
+// MexicanHat_Cpsi (:146-148).
+double wavelet_cpsi(int type, double w0) {
+  if (type == -3) return (4.0 / 3.0) * std::sqrt(kPi);
+  double c = 0.0;
+  for (double w = 0.01; w < 100; w += 0.01) {
+    const double a = w - w0;
+    c += std::exp(-a * a) / w;
+  }
+  return c * 0.01 * std::sqrt(kPi) / 2;
+}
+
+// Family of a ts-PWS stack over traces of L samples: s0 and the default w0
+// from pmin as src/FFTapps.c:1097-1105, J = round(1/V + log2(pmax/pmin))
+// (:1106), taps capped at L.  Returns 0 or -3.
+int stack_family(unsigned L, double pmin, double pmax, unsigned V, int type, double op1, WaveletFamily* wf,
+                 double* cpsi) {
+  double s0;
+  if (type == -3) {
+    s0 = pmin / (std::sqrt(2.0) * kPi);
+  } else if (type == -1 || type == -2) {
+    if (op1 == 0) op1 = kPi * std::sqrt(2 / std::log(2.0));
+    s0 = pmin * op1 / (2 * kPi);
+  } else {
+    return -3;
+  }
+  if (V == 0 || !(pmin > 0) || !(pmax > pmin) || L < 2) return -3;
+  const unsigned J = (unsigned)std::lround(1. / (double)V + std::log(pmax / pmin) / std::log(2.0));
+  if (J == 0 || !make_wavelet_family(type, J, V, L, s0, op1, wf)) return -3;
+  *cpsi = wavelet_cpsi(type, op1);
+  return 0;
+}
+
 }  // namespace fpcc

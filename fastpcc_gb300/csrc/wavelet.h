@@ -42,4 +42,11 @@ struct WpccSetup {
 int wpcc_setup(unsigned N, int Lag1, int Lag2, double pmin, double pmax, unsigned V, int type, double op1,
                WpccSetup* out);
 
+// Reconstruction constant Cpsi of the wavelet type (w0 for the Morlets).
+double wavelet_cpsi(int type, double w0);
+// Family of a ts-PWS stack over traces of L samples (s0 and w0 from pmin, J from
+// pmax/pmin, taps capped at L) and its Cpsi.  Returns 0 or -3.
+int stack_family(unsigned L, double pmin, double pmax, unsigned V, int type, double op1, WaveletFamily* wf,
+                 double* cpsi);
+
 }  // namespace fpcc

@@ -190,6 +190,31 @@ int fpcc_whiten_rows(fpcc_ctx *ctx, float *d_x, int64_t ldx, int nrows, int N, d
                      double dt);
 const char *fpcc_prep_last_error(void);
 
+/* ---- stacks of correlation traces over windows (device memory) -------------
+ * The obin output is written for an external stacking code (ts-PWS,
+ * src/PCC_fullpair_1b.c:568-569) whose source is not part of the reference;
+ * stacking on the device instead keeps the per-window correlations in HBM.
+ * ngroups groups of K traces of L samples: trace j of group g is row g*K + j
+ * of d_y (stride ldy); group g's stack goes to row g of d_out (stride ldo).
+ *   FPCC_STACK_LINEAR  the mean of the group's traces
+ *   FPCC_STACK_PWS     the mean times |mean_j a_j / |a_j||^nu, a_j the analytic
+ *                      signal of trace j (the rule of src/FFTapps.c:45-80);
+ *                      phase-weighted stack of Schimmel and Paulssen (1997)
+ *   FPCC_STACK_TSPWS   the inverse CWT of |mean_j W_j / |W_j||^nu * CWT(mean),
+ *                      W_j the CWT of trace j; time-scale phase-weighted stack
+ *                      of Ventosa, Schimmel and Stutzmann (2017), with the CWT
+ *                      and the inverse of the reference's wavelet library
+ *                      (complex_1D_wavelet_dec, Re_complex_1D_wavelet_rec,
+ *                      src/FWTa/wavelet_v7.c:43-150: circular over the trace)
+ *                      and its family (type -1/-2 Morlet, -3 Mexican hat; V
+ *                      voices; s0 from pmin, the octaves from pmax/pmin, both in
+ *                      samples, as src/FFTapps.c:1097-1107; op1 = w0, 0 for the
+ *                      default).  pmin, pmax, V, type, op1 are unused otherwise.
+ * Phasors of zero modulus count as zero.  Returns 0, FPCC_EARG or a CUDA error. */
+enum fpcc_stack_mode { FPCC_STACK_LINEAR = 0, FPCC_STACK_PWS = 1, FPCC_STACK_TSPWS = 2 };
+int fpcc_stack(fpcc_ctx *ctx, int mode, const float *d_y, int64_t ldy, int K, int L, int ngroups, double nu,
+               double pmin, double pmax, int V, int type, double op1, float *d_out, int64_t ldo);
+
 /* ---- host-buffer entry points (row-pointer arrays like the reference's *_set)
  * x1, x2: Tr rows of N floats (station 1 / station 2 windows); y: Tr rows of L.
  * The "batched" calls run each stage once over all windows; the plain drop-ins

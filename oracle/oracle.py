@@ -72,6 +72,16 @@ def lib():
                                              np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS"),
                                              C.c_void_p]
             L.orc_wavelet_family.restype = u
+            L.orc_stack.argtypes = [_f64p, _f32p, u, u, i, d, d, d, u, i, d]
+            L.orc_stack_family.argtypes = [u, d, d, u, i, d, C.POINTER(d), C.POINTER(d), C.POINTER(u)]
+            L.orc_stack_family.restype = u
+            L.orc_cpsi.argtypes = [i, d]
+            L.orc_cpsi.restype = d
+            L.orc_cwt.argtypes = [_c128p, _f64p, u, u, np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS"),
+                                  np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS"), _c128p]
+            L.orc_icwt.argtypes = [_f64p, _c128p, u, u, u, d, _f64p,
+                                   np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS"),
+                                   np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS"), _c128p]
             _lib = L
     return _lib
 
@@ -196,6 +206,46 @@ def wpcc_band(x1, x2, Lag1, Lag2, pmin, pmax, s_lo, s_hi, V=2, wtype=-3, op1=0.0
     _check(lib().orc_wpcc_band(y, x1, x2, N, Tr, Lag1, Lag2, pmin, pmax, V, wtype, op1, rule, s_lo, s_hi),
            "orc_wpcc_band")
     return y
+
+
+STACK_LINEAR, STACK_PWS, STACK_TSPWS = 0, 1, 2
+
+
+def stack(y, mode, nu=2.0, pmin=0.0, pmax=0.0, V=4, wtype=-1, op1=0.0):
+    """Stack of the rows of y (K, L): linear mean, time-domain phase-weighted, or
+    time-scale phase-weighted (oracle64.c orc_stack).  Returns float64 (L,)."""
+    y = np.ascontiguousarray(y, np.float32)
+    K, L = y.shape
+    out = np.empty(L, np.float64)
+    _check(lib().orc_stack(out, y, K, L, mode, nu, pmin, pmax, V, wtype, op1), "orc_stack")
+    return out
+
+
+def stack_family(L, pmin, pmax, V, wtype, op1=0.0):
+    """(S, J, s0, op1, scale, Ls, center, taps, cpsi) of a ts-PWS stack over L samples."""
+    s0, op, J = C.c_double(0), C.c_double(0), C.c_uint(0)
+    S = lib().orc_stack_family(L, pmin, pmax, V, wtype, op1, C.byref(s0), C.byref(op), C.byref(J))
+    if S == 0:
+        raise ValueError("invalid stack parameters")
+    scale, Ls, center, taps = wavelet_family(wtype, J.value, V, L, s0.value, op.value)
+    return dict(S=int(S), J=int(J.value), s0=float(s0.value), op1=float(op.value), scale=scale, Ls=Ls,
+                center=center, taps=taps, cpsi=float(lib().orc_cpsi(wtype, op.value)))
+
+
+def cwt(x, fam):
+    """CWT rows (S, L) of a real trace with a stack_family family."""
+    x = np.ascontiguousarray(x, np.float64)
+    W = np.empty((fam["S"], x.size), np.complex128)
+    lib().orc_cwt(W, x, x.size, fam["S"], fam["Ls"], fam["center"], fam["taps"])
+    return W
+
+
+def icwt(W, fam, V):
+    W = np.ascontiguousarray(W, np.complex128)
+    L = W.shape[1]
+    x = np.empty(L, np.float64)
+    lib().orc_icwt(x, W, L, fam["S"], V, fam["cpsi"], fam["scale"], fam["Ls"], fam["center"], fam["taps"])
+    return x
 
 
 # ---------------------------------------------------------------------------

@@ -429,3 +429,143 @@ int orc_wpcc_set(double *y, const float *x1, const float *x2, unsigned N, unsign
                  double op1, int rule) {
     return orc_wpcc_band(y, x1, x2, N, Tr, Lag1, Lag2, pmin, pmax, V, type, op1, rule, 0, ~0u);
 }
+
+/* ---- stacking of correlation traces ---------------------------------------
+ * The consumer of the obin files (src/PCC_fullpair_1b.c:568-569) stacks the
+ * per-window correlations of a channel pair.  Its source is not part of the
+ * reference; the stacks here restate the published methods on the reference's
+ * own wavelet library (src/FWTa):
+ *   linear:  mean_j c_j[n]
+ *   PWS:     linear * |mean_j a_j[n] / |a_j[n]||^nu, a_j the analytic signal of
+ *            trace j (Schimmel & Paulssen 1997), by the analytic-signal rule of
+ *            src/FFTapps.c:45-80
+ *   ts-PWS:  inverse CWT of  |mean_j W_j / |W_j||^nu * mean_j W_j,  W_j the CWT of
+ *            trace j (Ventosa, Schimmel & Stutzmann 2017), with the CWT of
+ *            complex_1D_wavelet_dec (src/FWTa/wavelet_v7.c:43-64, cdotx_dc
+ *            src/FWTa/cdotx.c:35-71: circular, conjugate taps) and the inverse of
+ *            Re_complex_1D_wavelet_rec (wavelet_v7.c:124-150: the dual frame of
+ *            FillDualFrame wavelet_def_v7.c:152-190 through re_cdotx_cc,
+ *            cdotx.c:176-211, weighted by ln(a0) / (2 Cpsi V scale_s), a0 = 2).
+ * Phasors of zero modulus count as zero. */
+
+/* Morlet_Cpsi (src/FWTa/wavelet_def_v7.c:133-144, the same running sum) and
+ * MexicanHat_Cpsi (:146-148). */
+double orc_cpsi(int type, double w0) {
+    if (type == -3) return (4. / 3.) * sqrt(ORC_PI);
+    double c = 0;
+    for (double w = 0.01; w < 100; w += 0.01) {
+        double a = w - w0;
+        c += exp(-a * a) / w;
+    }
+    return c * 0.01 * sqrt(ORC_PI) / 2;
+}
+
+/* Family of a ts-PWS stack over traces of L samples: s0 and the default w0
+ * from pmin as src/FFTapps.c:1097-1105, J = round(1/V + log2(pmax/pmin)) (:1106),
+ * taps capped at L (CreateWaveletFamily with N = L).  Returns S or 0. */
+unsigned orc_stack_family(unsigned L, double pmin, double pmax, unsigned V, int type, double op1_in,
+                          double *s0_out, double *op1_out, unsigned *J_out) {
+    double s0, op1 = op1_in;
+    if (type == -3) s0 = pmin / (sqrt(2.0) * ORC_PI);
+    else if (type == -1 || type == -2) {
+        if (op1 == 0) op1 = ORC_PI * sqrt(2 / log(2.0));
+        s0 = pmin * op1 / (2 * ORC_PI);
+    } else return 0;
+    if (V == 0 || !(pmax > pmin) || !(pmin > 0) || L == 0) return 0;
+    unsigned J = (unsigned)round(1. / (double)V + log(pmax / pmin) / log(2.0));
+    *s0_out = s0; *op1_out = op1; *J_out = J;
+    return J * V;
+}
+
+/* CWT of one real trace: W[s*L + n] = sum_l x[(n - c_s + l) mod L] conj(w_s[l]). */
+void orc_cwt(double complex *W, const double *x, unsigned L, unsigned S, const unsigned *Ls,
+             const int *center, const double complex *taps) {
+    const double complex *w = taps;
+    for (unsigned s = 0; s < S; s++) {
+        for (unsigned n = 0; n < L; n++) {
+            double complex acc = 0;
+            for (unsigned l = 0; l < Ls[s]; l++) {
+                long m = ((long)n - center[s] + (long)l) % (long)L;
+                if (m < 0) m += L;
+                acc += x[m] * conj(w[l]);
+            }
+            W[(size_t)s * L + n] = acc;
+        }
+        w += Ls[s];
+    }
+}
+
+/* Inverse: x[n] = sum_s ln2 / (2 Cpsi V scale_s) Re sum_l w_s[l] W[s][(n + c_s - l) mod L]. */
+void orc_icwt(double *x, const double complex *W, unsigned L, unsigned S, unsigned V, double cpsi,
+              const double *scale, const unsigned *Ls, const int *center, const double complex *taps) {
+    for (unsigned n = 0; n < L; n++) x[n] = 0;
+    const double complex *w = taps;
+    for (unsigned s = 0; s < S; s++) {
+        const double aux = log(2.0) / (2 * cpsi * V * scale[s]);
+        for (unsigned n = 0; n < L; n++) {
+            double acc = 0;
+            for (unsigned l = 0; l < Ls[s]; l++) {
+                long m = ((long)n + center[s] - (long)l) % (long)L;
+                if (m < 0) m += L;
+                acc += creal(w[l] * W[(size_t)s * L + m]);
+            }
+            x[n] += aux * acc;
+        }
+        w += Ls[s];
+    }
+}
+
+static double complex unit(double complex z) {
+    const double a = cabs(z);
+    return a > 0 ? z / a : 0;
+}
+
+int orc_stack(double *out, const float *y, unsigned K, unsigned L, int mode, double nu, double pmin,
+              double pmax, unsigned V, int type, double op1) {
+    if (!out || !y || K == 0 || L == 0) return -1;
+    double *lin = (double *)calloc(L, sizeof(double));
+    for (unsigned j = 0; j < K; j++)
+        for (unsigned n = 0; n < L; n++) lin[n] += (double)y[(size_t)j * L + n];
+    for (unsigned n = 0; n < L; n++) lin[n] /= K;
+    if (mode == 0) {
+        memcpy(out, lin, L * sizeof(double));
+        free(lin);
+        return 0;
+    }
+    if (mode == 1) {
+        double complex *a = (double complex *)malloc(L * sizeof(double complex));
+        double complex *u = (double complex *)calloc(L, sizeof(double complex));
+        for (unsigned j = 0; j < K; j++) {
+            orc_analytic(a, y + (size_t)j * L, L);
+            for (unsigned n = 0; n < L; n++) u[n] += unit(a[n]);
+        }
+        for (unsigned n = 0; n < L; n++) out[n] = lin[n] * pow(cabs(u[n]) / K, nu);
+        free(a); free(u); free(lin);
+        return 0;
+    }
+    if (mode != 2) { free(lin); return -3; }
+    double s0, op;
+    unsigned J;
+    const unsigned S = orc_stack_family(L, pmin, pmax, V, type, op1, &s0, &op, &J);
+    if (!S) { free(lin); return -3; }
+    double *scale = (double *)malloc(S * sizeof(double));
+    unsigned *Ls = (unsigned *)malloc(S * sizeof(unsigned));
+    int *center = (int *)malloc(S * sizeof(int));
+    const unsigned nt = orc_wavelet_family(type, J, V, L, s0, op, scale, Ls, center, NULL);
+    double complex *taps = (double complex *)malloc(nt * sizeof(double complex));
+    orc_wavelet_family(type, J, V, L, s0, op, scale, Ls, center, taps);
+    double complex *W = (double complex *)malloc((size_t)S * L * sizeof(double complex));
+    double complex *U = (double complex *)calloc((size_t)S * L, sizeof(double complex));
+    double complex *Wl = (double complex *)malloc((size_t)S * L * sizeof(double complex));
+    double *x = (double *)malloc(L * sizeof(double));
+    for (unsigned j = 0; j < K; j++) {
+        for (unsigned n = 0; n < L; n++) x[n] = (double)y[(size_t)j * L + n];
+        orc_cwt(W, x, L, S, Ls, center, taps);
+        for (size_t i = 0; i < (size_t)S * L; i++) U[i] += unit(W[i]);
+    }
+    orc_cwt(Wl, lin, L, S, Ls, center, taps);        /* mean_j W_j by linearity */
+    for (size_t i = 0; i < (size_t)S * L; i++) Wl[i] *= pow(cabs(U[i]) / K, nu);
+    orc_icwt(out, Wl, L, S, V, orc_cpsi(type, op), scale, Ls, center, taps);
+    free(scale); free(Ls); free(center); free(taps); free(W); free(U); free(Wl); free(x); free(lin);
+    return 0;
+}

@@ -94,4 +94,19 @@ int orc_wpcc_band(double *y, const float *x1, const float *x2, unsigned N, unsig
 #ifdef __cplusplus
 }
 #endif
+
+/* Stacks of K correlation traces of L samples (row-major y): mode 0 linear,
+ * 1 phase-weighted (time domain), 2 time-scale phase-weighted; nu the
+ * coherence power; pmin/pmax (samples), V, type, op1 select the wavelet
+ * family of mode 2.  out: L values.  Returns 0, -1 or -3. */
+int orc_stack(double *out, const float *y, unsigned K, unsigned L, int mode, double nu, double pmin,
+              double pmax, unsigned V, int type, double op1);
+unsigned orc_stack_family(unsigned L, double pmin, double pmax, unsigned V, int type, double op1_in,
+                          double *s0_out, double *op1_out, unsigned *J_out);
+double orc_cpsi(int type, double w0);
+void orc_cwt(double complex *W, const double *x, unsigned L, unsigned S, const unsigned *Ls,
+             const int *center, const double complex *taps);
+void orc_icwt(double *x, const double complex *W, unsigned L, unsigned S, unsigned V, double cpsi,
+              const double *scale, const unsigned *Ls, const int *center, const double complex *taps);
+
 #endif
