@@ -111,7 +111,7 @@ def lib():
             L.fpcc_clip_rows.argtypes = [vp, vp, i64, i, i]
             L.fpcc_whiten_rows.argtypes = [vp, vp, i64, i, i, d, d, d]
             L.fpcc_prep_last_error.restype = C.c_char_p
-            L.fpcc_stack.argtypes = [vp, i, vp, i64, i, i, i, d, d, d, i, i, d, vp, i64]
+            L.fpcc_stack.argtypes = [vp, i, vp, i64, i64, i, i, i, d, d, d, i, i, d, vp, i64]
             L.fpcc_server_create.argtypes = [C.POINTER(vp), i, C.c_size_t, i]
             L.fpcc_server_set_format.argtypes = [vp, i]
             L.fpcc_server_set_nz_mode.argtypes = [vp, i]
@@ -282,11 +282,14 @@ class Context:
                                        C.c_void_p(d_out), ldo))
 
     def stack(self, mode, d_y, ldy, K, L, ngroups, d_out, ldo, nu=2.0, pmin=0.0, pmax=0.0, V=4, type=-1,
-              op1=0.0):
-        """Stacks of ngroups groups of K traces (rows g*K + j of d_y) into rows of d_out:
-        STACK_LINEAR, STACK_PWS (phase-weighted) or STACK_TSPWS (time-scale
-        phase-weighted; pmin/pmax in samples, V voices, wavelet type)."""
-        check(lib().fpcc_stack(self._h, mode, C.c_void_p(d_y), ldy, K, L, ngroups, float(nu), float(pmin),
+              op1=0.0, ldg=None, ldj=None):
+        """Stacks of ngroups groups of K traces into rows of d_out: STACK_LINEAR,
+        STACK_PWS (phase-weighted) or STACK_TSPWS (time-scale phase-weighted;
+        pmin/pmax in samples, V voices, wavelet type).  Trace j of group g starts
+        at d_y + g*ldg + j*ldj floats (default: rows g*K + j of stride ldy)."""
+        ldj = ldy if ldj is None else ldj
+        ldg = K * ldy if ldg is None else ldg
+        check(lib().fpcc_stack(self._h, mode, C.c_void_p(d_y), ldg, ldj, K, L, ngroups, float(nu), float(pmin),
                                float(pmax), V, type, float(op1), C.c_void_p(d_out), ldo))
 
     def energy_stage(self, d_x, ldx, nrows, N, d_E, ldE):

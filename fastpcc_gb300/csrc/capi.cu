@@ -67,7 +67,8 @@ struct fpcc_ctx {
   DevBuf dev[48];
   DevBuf pin[8];
   cudaStream_t stream2 = nullptr;   // second stream of the pipelined drop-ins
-  cudaEvent_t chunk_ev[8] = {};     // pair-stage chunks whose results stream2 downloads
+  cudaEvent_t chunk_ev[16] = {};    // pair-stage chunks whose results stream2 downloads
+  cudaEvent_t up_ev[4] = {};        // station-row chunks that stream2 has uploaded
   // the context's device buffers and caches come from a pool of its own, allocated
   // and freed in the order of `stream` (no device synchronisation when a buffer
   // grows); ord_ev orders them against the second stream when it exists
@@ -235,6 +236,8 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);
   for (cudaEvent_t e : c->chunk_ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->up_ev)
     if (e) cudaEventDestroy(e);
   {
     std::lock_guard<std::mutex> lk(g_default_mu);
@@ -1216,14 +1219,17 @@ int make_layout(int method, int N, int Lag1, int Lag2, int nz_mode, int fmt, Lay
 // split >= 0 gives rows [0, split) the station-1 rule and the rest the station-2
 // rule; split < 0 computes both variants (rows [0,nsta) and [nsta,2 nsta)) and
 // expects each pair's station-2 index to point into the second half.
-// Station stage(s), then the pair stage.  With h_y (FP32 results wanted in host
-// memory) and enough pairs, the pair stage runs in chunks of consecutive pairs
-// and the second stream downloads each chunk's rows once its kernels are done,
-// so the download of one chunk overlaps the correlation of the next; every
-// kernel is queued before the first copy, so pageable host memory (whose
-// copies return only when done) does not hold back the launches.
+// Station stage(s), then the pair stage.  With h_x (the station windows in host
+// memory, one method rule), the windows go up in four row chunks on the second
+// stream and the station stage of each chunk starts as soon as its rows have
+// arrived.  With h_y (FP32 results wanted in host memory) and enough pairs, the
+// pair stage runs in chunks of consecutive pairs and the second stream
+// downloads each chunk's rows once its kernels are done, so the download of one
+// chunk overlaps the correlation of the next; every kernel is queued before the
+// first download, so pageable host memory (whose copies return only when done)
+// does not hold back the launches.
 int run_device(fpcc_ctx* c, const Layout& Ly, const float* d_x, int nsta, const int32_t* d_pairs, int npairs,
-               float v, float* d_y, int64_t* d_num, int split, float* h_y = nullptr) {
+               float v, float* d_y, int64_t* d_num, int split, float* h_y = nullptr, const float* h_x = nullptr) {
   void* d_st = nullptr;
   int rc;
   const int method = Ly.method;
@@ -1246,6 +1252,27 @@ int run_device(fpcc_ctx* c, const Layout& Ly, const float* d_x, int nsta, const 
                                    FPCC_SIGN_GT, base + (size_t)split * rowb, Ly.lds)))
         return rc;
     }
+  } else if (h_x) {
+    if (!c->stream2 && cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(FPCC_ECUDA, "stream creation failed");
+    for (int k = 0; k < 4; k++)
+      if (!c->up_ev[k] && cudaEventCreateWithFlags(&c->up_ev[k], cudaEventDisableTiming) != cudaSuccess)
+        return fail(FPCC_ECUDA, "event creation failed");
+    // the uploads follow everything queued on the main stream (buffer allocations included)
+    CK(cudaEventRecord(c->ord_ev, c->stream));
+    CK(cudaStreamWaitEvent(c->stream2, c->ord_ev, 0));
+    const int per = (nsta + 3) / 4;
+    for (int k = 0; k < 4; k++) {
+      const int r0 = k * per, n = std::min(per, nsta - r0);
+      if (n <= 0) break;
+      CK(cudaMemcpyAsync((float*)d_x + (size_t)r0 * Ly.N, h_x + (size_t)r0 * Ly.N, (size_t)n * Ly.N * sizeof(float),
+                         cudaMemcpyHostToDevice, c->stream2));
+      CK(cudaEventRecord(c->up_ev[k], c->stream2));
+      CK(cudaStreamWaitEvent(c->stream, c->up_ev[k], 0));
+      if ((rc = fpcc_station_stage(c, method, d_x + (size_t)r0 * Ly.N, Ly.N, n, Ly.N, Ly.Nz, Ly.fmt, FPCC_AMP_F_REG,
+                                   base + (size_t)r0 * rowb, Ly.lds)))
+        return rc;
+    }
   } else {
     if ((rc = fpcc_station_stage(c, method, d_x, Ly.N, nsta, Ly.N, Ly.Nz, Ly.fmt, FPCC_AMP_F_REG, d_st, Ly.lds)))
       return rc;
@@ -1260,7 +1287,9 @@ int run_device(fpcc_ctx* c, const Layout& Ly, const float* d_x, int nsta, const 
   if (!h_y)
     return fpcc_pair_stage(c, method, d_st, Ly.lds, Ly.fmt, d_pairs, npairs, Ly.N, Ly.Nz, Ly.lag0,
                            Ly.lag0 + Ly.L - 1, v, d_E, Ly.N + 1, d_y, Ly.L, d_num);
-  const int nch = npairs >= 8192 ? 8 : 1;
+  // chunks of about 6000 correlations (at most 16): the first download starts
+  // after a short first chunk, and the rest overlap the following chunks
+  const int nch = (int)std::max<int64_t>(1, std::min<int64_t>(16, npairs / 6000));
   if (nch > 1 && !c->stream2 && cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess)
     return fail(FPCC_ECUDA, "stream creation failed");
   for (int k = 0; k < nch; k++)
@@ -1362,9 +1391,9 @@ extern "C" int fpcc_allpairs_host(fpcc_ctx* c, int method, const float* h_x, int
   if ((rc = dev_buf(c, S_HOST_X, xbytes, &d_x)) || (rc = dev_buf(c, S_Y, ybytes, &d_y)) ||
       (rc = dev_buf(c, S_PAIRS, pbytes, &d_p)))
     return rc;
-  CK(cudaMemcpyAsync(d_x, h_x, xbytes, cudaMemcpyHostToDevice, c->stream));
   if (Ly.two_rules) {
     // station 2 of each pair reads the station-2-rule variant (second half of the rows)
+    CK(cudaMemcpyAsync(d_x, h_x, xbytes, cudaMemcpyHostToDevice, c->stream));
     std::vector<int32_t> hp(h_pairs, h_pairs + 2 * (size_t)npairs);
     for (int i = 0; i < npairs; i++) hp[2 * i + 1] += nsta;
     CK(cudaMemcpyAsync(d_p, hp.data(), pbytes, cudaMemcpyHostToDevice, c->stream));
@@ -1372,8 +1401,9 @@ extern "C" int fpcc_allpairs_host(fpcc_ctx* c, int method, const float* h_x, int
   } else {
     CK(cudaMemcpyAsync(d_p, h_pairs, pbytes, cudaMemcpyHostToDevice, c->stream));
   }
+  // one-rule methods: the windows go up in chunks that the station stage consumes as they arrive
   if ((rc = run_device(c, Ly, (const float*)d_x, nsta, (const int32_t*)d_p, npairs, v, (float*)d_y, nullptr, -1,
-                       h_y)))
+                       h_y, Ly.two_rules ? nullptr : h_x)))
     return rc;
   CK(cudaStreamSynchronize(c->stream));
   return 0;
@@ -1851,12 +1881,13 @@ int stack_spectra(fpcc_ctx* c, const WaveletFamily& wf, int L, int M, float2** o
 
 }  // namespace
 
-extern "C" int fpcc_stack(fpcc_ctx* c, int mode, const float* d_y, int64_t ldy, int K, int L, int ngroups,
-                          double nu, double pmin, double pmax, int V, int type, double op1, float* d_out,
-                          int64_t ldo) {
+extern "C" int fpcc_stack(fpcc_ctx* c, int mode, const float* d_y, int64_t ldg, int64_t ldj, int K, int L,
+                          int ngroups, double nu, double pmin, double pmax, int V, int type, double op1,
+                          float* d_out, int64_t ldo) {
   if (!c || !d_y || !d_out) return fail(FPCC_EARG, "null argument");
-  if (K <= 0 || L < 2 || ngroups <= 0 || ldy < L || ldo < L || !(nu >= 0))
-    return fail(FPCC_EARG, "stack: K >= 1, L >= 2, groups >= 1, strides >= L and nu >= 0 are required");
+  if (K <= 0 || L < 2 || ngroups <= 0 || ldo < L || !(nu >= 0) || (K > 1 && ldj < L) ||
+      (ngroups > 1 && ldg < L))
+    return fail(FPCC_EARG, "stack: K >= 1, L >= 2, groups >= 1, nu >= 0 and strides of at least L are required");
   if (mode < FPCC_STACK_LINEAR || mode > FPCC_STACK_TSPWS) return fail(FPCC_EARG, "unknown stack mode %d", mode);
   std::lock_guard<std::mutex> lk(c->mu);
   CK(cudaSetDevice(c->device));
@@ -1864,7 +1895,7 @@ extern "C" int fpcc_stack(fpcc_ctx* c, int mode, const float* d_y, int64_t ldy, 
   if (mode == FPCC_STACK_LINEAR) {
     for (int g0 = 0; g0 < ngroups; g0 += 65535) {
       const int G = std::min(65535, ngroups - g0);
-      CK(launch_stack_mean(d_y + (size_t)g0 * K * ldy, ldy, K, L, G, d_out + (size_t)g0 * ldo, ldo, c->stream));
+      CK(launch_stack_mean(d_y + (size_t)g0 * ldg, ldg, ldj, K, L, G, d_out + (size_t)g0 * ldo, ldo, c->stream));
       g_launches++;
     }
     return 0;
@@ -1881,12 +1912,12 @@ extern "C" int fpcc_stack(fpcc_ctx* c, int mode, const float* d_y, int64_t ldy, 
       std::vector<MultiRow> rows(n);
       for (int r = 0; r < n; r++) {
         rows[r] = MultiRow{};
-        rows[r].x = d_y + ((size_t)g0 * K + r) * ldy;
+        rows[r].x = d_y + (size_t)(g0 + r / K) * ldg + (size_t)(r % K) * ldj;
         rows[r].out = (float2*)an + (size_t)r * L;
         rows[r].N = L;
       }
       if ((rc = multi_group<float2>(c, rows, M))) return rc;
-      CK(launch_stack_pws((const float2*)an, L, d_y + (size_t)g0 * K * ldy, ldy, K, L, G, nu,
+      CK(launch_stack_pws((const float2*)an, L, d_y + (size_t)g0 * ldg, ldg, ldj, K, L, G, nu,
                           d_out + (size_t)g0 * ldo, ldo, c->stream));
       g_launches++;
     }
@@ -1915,7 +1946,7 @@ extern "C" int fpcc_stack(fpcc_ctx* c, int mode, const float* d_y, int64_t ldy, 
         (rc = dev_buf(c, S_STK_R, (size_t)G * M * sizeof(float2), &R)))
       return rc;
     // spectra of the traces, and of each group's linear stack in rows G K + g
-    CK(launch_stack_load(d_y + (size_t)g0 * K * ldy, ldy, G * K, L, (float2*)X, M, c->stream));
+    CK(launch_stack_load(d_y + (size_t)g0 * ldg, ldg, ldj, K, G, L, (float2*)X, M, c->stream));
     float2* xs = nullptr;
     if ((rc = passes(c, (float2*)X, (float2*)T, M, G * K, -1, &xs))) return rc;
     if (xs != (float2*)X) CK(cudaMemcpyAsync(X, xs, (size_t)G * K * M * sizeof(float2), cudaMemcpyDeviceToDevice,

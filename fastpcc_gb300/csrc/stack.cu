@@ -12,42 +12,66 @@ dim3 grid_cols(int n, int G) {
   return dim3(gx, G);
 }
 
-__device__ __forceinline__ double2 unit_d(float2 z) {
-  const double x = z.x, y = z.y;
-  const double a = sqrt(x * x + y * y);
-  return a > 0.0 ? make_double2(x / a, y / a) : make_double2(0.0, 0.0);
+// Unit phasor z / |z| in FP32 (0 for z = 0; FP32 keeps 1e-7 relative, the sums
+// over traces run in FP64).
+__device__ __forceinline__ float2 unit_f(float2 z) {
+  const float m2 = z.x * z.x + z.y * z.y;
+  if (!(m2 > 0.0f)) return make_float2(0.0f, 0.0f);
+  const float r = rsqrtf(m2);
+  return make_float2(z.x * r, z.y * r);
 }
 
-__global__ void k_stack_mean(const float* __restrict__ y, int64_t ldy, int K, int L, float* out, int64_t ldo) {
+// Coherence (|U| / K)^nu from U's squared modulus: nu = 2 and nu = 1 without
+// the general power.
+__device__ __forceinline__ double coherence(double ux, double uy, int K, double nu) {
+  const double m2 = (ux * ux + uy * uy) / ((double)K * (double)K);
+  if (nu == 2.0) return m2;
+  if (nu == 1.0) return (double)sqrtf((float)m2);
+  if (nu == 0.0) return 1.0;
+  return (double)powf((float)m2, (float)(0.5 * nu));
+}
+
+__global__ void k_stack_mean(const float* __restrict__ y, int64_t ldg, int64_t ldj, int K, int L, float* out,
+                             int64_t ldo) {
   const int g = blockIdx.y;
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < L; n += gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int j = 0; j < K; j++) s += (double)__ldg(y + ((int64_t)g * K + j) * ldy + n);
-    out[(int64_t)g * ldo + n] = (float)(s / K);
+    // four independent sums keep several loads in flight per thread
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    const float* p = y + (int64_t)g * ldg + n;
+    int j = 0;
+    for (; j + 4 <= K; j += 4) {
+      s0 += (double)__ldg(p + (int64_t)j * ldj);
+      s1 += (double)__ldg(p + (int64_t)(j + 1) * ldj);
+      s2 += (double)__ldg(p + (int64_t)(j + 2) * ldj);
+      s3 += (double)__ldg(p + (int64_t)(j + 3) * ldj);
+    }
+    for (; j < K; j++) s0 += (double)__ldg(p + (int64_t)j * ldj);
+    out[(int64_t)g * ldo + n] = (float)(((s0 + s1) + (s2 + s3)) / K);
   }
 }
 
-__global__ void k_stack_pws(const float2* __restrict__ a, int64_t lda, const float* __restrict__ y, int64_t ldy,
-                            int K, int L, double nu, float* out, int64_t ldo) {
+__global__ void k_stack_pws(const float2* __restrict__ a, int64_t lda, const float* __restrict__ y, int64_t ldg,
+                            int64_t ldj, int K, int L, double nu, float* out, int64_t ldo) {
   const int g = blockIdx.y;
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < L; n += gridDim.x * blockDim.x) {
     double s = 0.0, ux = 0.0, uy = 0.0;
     for (int j = 0; j < K; j++) {
       const int64_t r = (int64_t)g * K + j;
-      s += (double)__ldg(y + r * ldy + n);
-      const double2 u = unit_d(a[r * lda + n]);
+      s += (double)__ldg(y + (int64_t)g * ldg + (int64_t)j * ldj + n);
+      const float2 u = unit_f(a[r * lda + n]);
       ux += u.x;
       uy += u.y;
     }
-    const double c = sqrt(ux * ux + uy * uy) / K;
-    out[(int64_t)g * ldo + n] = (float)((s / K) * pow(c, nu));
+    out[(int64_t)g * ldo + n] = (float)((s / K) * coherence(ux, uy, K, nu));
   }
 }
 
-__global__ void k_stack_load(const float* __restrict__ y, int64_t ldy, int L, float2* X, int M) {
+__global__ void k_stack_load(const float* __restrict__ y, int64_t ldg, int64_t ldj, int K, int L, float2* X,
+                             int M) {
   const int64_t r = blockIdx.y;
+  const float* row = y + (r / K) * ldg + (r % K) * ldj;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x)
-    X[r * M + m] = make_float2(m < L ? __ldg(y + r * ldy + m) : 0.0f, 0.0f);
+    X[r * M + m] = make_float2(m < L ? __ldg(row + m) : 0.0f, 0.0f);
 }
 
 __global__ void k_stack_xlin(float2* X, int K, int G, int M) {
@@ -77,13 +101,20 @@ __global__ void k_stack_coherence(const float2* __restrict__ W, int K, int G, in
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < M; n += gridDim.x * blockDim.x) {
     float2 out = make_float2(0.0f, 0.0f);
     if (n < L) {
+      // FP32 partial sums over runs of 32 traces, accumulated in FP64
       double ux = 0.0, uy = 0.0;
-      for (int j = 0; j < K; j++) {
-        const double2 u = unit_d(W[((int64_t)g * K + j) * M + n]);
-        ux += u.x;
-        uy += u.y;
+      for (int j0 = 0; j0 < K; j0 += 32) {
+        float px = 0.0f, py = 0.0f;
+        const int j1 = min(K, j0 + 32);
+        for (int j = j0; j < j1; j++) {
+          const float2 u = unit_f(W[((int64_t)g * K + j) * M + n]);
+          px += u.x;
+          py += u.y;
+        }
+        ux += px;
+        uy += py;
       }
-      const double c = pow(sqrt(ux * ux + uy * uy) / K, nu);
+      const double c = coherence(ux, uy, K, nu);
       const float2 w = W[((int64_t)G * K + g) * M + n];
       out = make_float2((float)(c * w.x), (float)(c * w.y));
     }
@@ -112,23 +143,25 @@ bool rows_ok(int rows) { return rows > 0 && rows <= 65535; }
 
 }  // namespace
 
-cudaError_t launch_stack_mean(const float* y, int64_t ldy, int K, int L, int G, float* out, int64_t ldo,
+cudaError_t launch_stack_mean(const float* y, int64_t ldg, int64_t ldj, int K, int L, int G, float* out,
+                              int64_t ldo, cudaStream_t st) {
+  if (!rows_ok(G) || K <= 0 || L <= 0) return cudaErrorInvalidValue;
+  k_stack_mean<<<grid_cols(L, G), 256, 0, st>>>(y, ldg, ldj, K, L, out, ldo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stack_pws(const float2* a, int64_t lda, const float* y, int64_t ldg, int64_t ldj, int K, int L,
+                             int G, double nu, float* out, int64_t ldo, cudaStream_t st) {
+  if (!rows_ok(G) || K <= 0 || L <= 0) return cudaErrorInvalidValue;
+  k_stack_pws<<<grid_cols(L, G), 256, 0, st>>>(a, lda, y, ldg, ldj, K, L, nu, out, ldo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stack_load(const float* y, int64_t ldg, int64_t ldj, int K, int G, int L, float2* X, int M,
                               cudaStream_t st) {
-  if (!rows_ok(G) || K <= 0 || L <= 0) return cudaErrorInvalidValue;
-  k_stack_mean<<<grid_cols(L, G), 256, 0, st>>>(y, ldy, K, L, out, ldo);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_stack_pws(const float2* a, int64_t lda, const float* y, int64_t ldy, int K, int L, int G,
-                             double nu, float* out, int64_t ldo, cudaStream_t st) {
-  if (!rows_ok(G) || K <= 0 || L <= 0) return cudaErrorInvalidValue;
-  k_stack_pws<<<grid_cols(L, G), 256, 0, st>>>(a, lda, y, ldy, K, L, nu, out, ldo);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_stack_load(const float* y, int64_t ldy, int rows, int L, float2* X, int M, cudaStream_t st) {
+  const int rows = K * G;
   if (!rows_ok(rows)) return cudaErrorInvalidValue;
-  k_stack_load<<<grid_cols(M, rows), 256, 0, st>>>(y, ldy, L, X, M);
+  k_stack_load<<<grid_cols(M, rows), 256, 0, st>>>(y, ldg, ldj, K, L, X, M);
   return cudaGetLastError();
 }
 

@@ -1,8 +1,9 @@
 // Stacks of correlation traces over windows (linear, phase-weighted,
 // time-scale phase-weighted), the device side of fpcc_stack.
 //
-// Groups of K rows of L samples: row g*K + j of the input is trace j of group
-// g.  The CWT of src/FWTa (complex_1D_wavelet_dec: W_s[n] = sum_l
+// Groups of K traces of L samples: trace j of group g starts at
+// y + g * ldg + j * ldj (so groups of adjacent rows and window-major outputs of
+// the pair stage both stack in place).  The CWT of src/FWTa (complex_1D_wavelet_dec: W_s[n] = sum_l
 // x[(n - c_s + l) mod L] conj(w_s[l])) and its inverse (Re_complex_1D_wavelet_rec:
 // x[n] = sum_s a_s Re sum_l w_s[l] W_s[(n + c_s - l) mod L]) are circular
 // convolutions of length L; they run as M-point transforms (M >= 2L - 1) with
@@ -14,15 +15,16 @@
 
 namespace fpcc {
 
-// out[g][n] = mean_j y[g K + j][n] (FP64 sums).
-cudaError_t launch_stack_mean(const float* y, int64_t ldy, int K, int L, int G, float* out, int64_t ldo,
+// out[g][n] = mean_j y_gj[n] (FP64 sums).
+cudaError_t launch_stack_mean(const float* y, int64_t ldg, int64_t ldj, int K, int L, int G, float* out,
+                              int64_t ldo, cudaStream_t st);
+// out[g][n] = mean_j y_gj * |mean_j a / |a||^nu over the group's traces (a:
+// analytic signals, row g K + j of stride lda; phasors of zero modulus count as zero).
+cudaError_t launch_stack_pws(const float2* a, int64_t lda, const float* y, int64_t ldg, int64_t ldj, int K, int L,
+                             int G, double nu, float* out, int64_t ldo, cudaStream_t st);
+// X[g K + j][m] = y_gj[m] for m < L, else 0 (rows of M complex values).
+cudaError_t launch_stack_load(const float* y, int64_t ldg, int64_t ldj, int K, int G, int L, float2* X, int M,
                               cudaStream_t st);
-// out[g][n] = mean_j y * |mean_j a / |a||^nu over the group's rows (a: analytic
-// signals, stride lda; phasors of zero modulus count as zero).
-cudaError_t launch_stack_pws(const float2* a, int64_t lda, const float* y, int64_t ldy, int K, int L, int G,
-                             double nu, float* out, int64_t ldo, cudaStream_t st);
-// X[r][m] = y[r][m] for m < L, else 0 (rows of M complex values).
-cudaError_t launch_stack_load(const float* y, int64_t ldy, int rows, int L, float2* X, int M, cudaStream_t st);
 // X[G K + g][m] = mean_j X[g K + j][m]: the spectrum of the group's linear stack.
 cudaError_t launch_stack_xlin(float2* X, int K, int G, int M, cudaStream_t st);
 // T[r][m] = X[r][m] F[m], rows r < rows.

@@ -194,8 +194,11 @@ const char *fpcc_prep_last_error(void);
  * The obin output is written for an external stacking code (ts-PWS,
  * src/PCC_fullpair_1b.c:568-569) whose source is not part of the reference;
  * stacking on the device instead keeps the per-window correlations in HBM.
- * ngroups groups of K traces of L samples: trace j of group g is row g*K + j
- * of d_y (stride ldy); group g's stack goes to row g of d_out (stride ldo).
+ * ngroups groups of K traces of L samples: trace j of group g starts at
+ * d_y + g*ldg + j*ldj (groups of adjacent rows: ldj = row stride, ldg = K*ldj;
+ * the window-major rows of an all-pairs pair stage: ldj = pairs per window *
+ * row stride, ldg = row stride); group g's stack goes to row g of d_out
+ * (stride ldo).
  *   FPCC_STACK_LINEAR  the mean of the group's traces
  *   FPCC_STACK_PWS     the mean times |mean_j a_j / |a_j||^nu, a_j the analytic
  *                      signal of trace j (the rule of src/FFTapps.c:45-80);
@@ -212,8 +215,8 @@ const char *fpcc_prep_last_error(void);
  *                      default).  pmin, pmax, V, type, op1 are unused otherwise.
  * Phasors of zero modulus count as zero.  Returns 0, FPCC_EARG or a CUDA error. */
 enum fpcc_stack_mode { FPCC_STACK_LINEAR = 0, FPCC_STACK_PWS = 1, FPCC_STACK_TSPWS = 2 };
-int fpcc_stack(fpcc_ctx *ctx, int mode, const float *d_y, int64_t ldy, int K, int L, int ngroups, double nu,
-               double pmin, double pmax, int V, int type, double op1, float *d_out, int64_t ldo);
+int fpcc_stack(fpcc_ctx *ctx, int mode, const float *d_y, int64_t ldg, int64_t ldj, int K, int L, int ngroups,
+               double nu, double pmin, double pmax, int V, int type, double op1, float *d_out, int64_t ldo);
 
 /* ---- host-buffer entry points (row-pointer arrays like the reference's *_set)
  * x1, x2: Tr rows of N floats (station 1 / station 2 windows); y: Tr rows of L.

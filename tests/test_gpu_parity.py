@@ -250,3 +250,41 @@ def test_example_records_against_reference_cli(F, orc):
         assert relerr(y, ref64[k]) < TOL, k
         assert relerr(y, g[k]) < TOL, k
     assert np.array_equal(F.cc1b_numerators(x1, x2, l1, l2), orc.cc1b_num(x1, x2, l1, l2))
+
+
+def test_allpairs_host_chunked_transfers(F, orc):
+    # all station pairs of every window with host buffers (fpcc_allpairs_host):
+    # 32 stations x 25 windows -> 12,400 correlations, so the windows go up in
+    # four row chunks and the results come down in two chunks on the second
+    # stream; PCC2 equals the device-resident stages bit for bit, and PCC2, GNCC
+    # and 1-bit (two sign rules) agree with the oracle
+    import torch
+    n_sta, n_win, N, lag = 32, 25, 2000, 100
+    x, _ = synth.all_pairs(n_stations=n_sta, n_windows=n_win, N=N, max_delay=60, tag="gpu/allpairs-host")
+    x = np.ascontiguousarray(x.reshape(n_sta * n_win, N))
+    iu, ju = np.triu_indices(n_sta, k=1)
+    w = np.repeat(np.arange(n_win), iu.size)
+    pairs = np.ascontiguousarray(np.stack([np.tile(iu, n_win) * n_win + w, np.tile(ju, n_win) * n_win + w],
+                                          axis=1).astype(np.int32))
+    P, L = pairs.shape[0], 2 * lag + 1
+    sel = np.random.default_rng(7).choice(P, 6, replace=False)
+    ctx = F.Context(0)
+    y = np.zeros((P, L), np.float32)
+    ctx.allpairs_host(F.PCC2, x, pairs, -lag, lag, y)
+    # device-resident stages, the same kernels
+    Nz = F.choose_nz(N, -lag, lag, F.NZ_FAST)
+    d_x = torch.from_numpy(x).cuda()
+    d_p = torch.from_numpy(pairs).cuda()
+    d_s = torch.empty((x.shape[0], 2 * Nz), dtype=torch.float32, device="cuda")
+    d_y = torch.empty((P, L), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    ctx.station_stage(F.PCC2, d_x.data_ptr(), N, x.shape[0], N, Nz, F.F32, F.AMP_F_REG, d_s.data_ptr(), Nz)
+    ctx.pair_stage(F.PCC2, d_s.data_ptr(), Nz, F.F32, d_p.data_ptr(), P, N, Nz, -lag, lag, d_y=d_y.data_ptr(), ldy=L)
+    ctx.sync()
+    assert np.array_equal(y, d_y.cpu().numpy())
+    assert relerr(y[sel], orc.pcc2(x[pairs[sel, 0]], x[pairs[sel, 1]], -lag, lag)) < TOL
+    for method, ref in ((F.GNCC, orc.gncc), (F.CC1B, orc.cc1b)):
+        y[:] = 0
+        ctx.allpairs_host(method, x, pairs, -lag, lag, y)
+        assert relerr(y[sel], ref(x[pairs[sel, 0]], x[pairs[sel, 1]], -lag, lag)) < TOL, method
+    ctx.close()

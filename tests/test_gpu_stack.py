@@ -81,6 +81,27 @@ def test_groups_in_one_call(F, g):
     ctx.close()
 
 
+def test_window_major_rows(F, g):
+    # an all-pairs pair stage writes row w * P + p (window-major); the stack
+    # reads each pair's traces in place with ldj = P * L, ldg = L
+    import torch
+    ctx = F.Context(0)
+    L, K, wt, V, pmin, pmax, nu = _case(g, 0)
+    c = g["c0"].reshape(3, 8, L)                       # (group, trace, lag)
+    wm = np.ascontiguousarray(c.transpose(1, 0, 2))    # (trace, group, lag): window-major
+    d_y = torch.from_numpy(wm.reshape(24, L)).cuda()
+    d_o = torch.zeros((3, L), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    for mode in (F.STACK_LINEAR, F.STACK_PWS, F.STACK_TSPWS):
+        ctx.stack(mode, d_y.data_ptr(), L, 8, L, 3, d_o.data_ptr(), L, nu=nu, pmin=pmin, pmax=pmax, V=V, type=wt,
+                  ldg=L, ldj=3 * L)
+        ctx.sync()
+        y = d_o.cpu().numpy()
+        for k in range(3):
+            assert relerr(y[k], O.stack(c[k], mode, nu, pmin, pmax, V, wt)[None]) < TOL, (mode, k)
+    ctx.close()
+
+
 def test_single_trace_and_errors(F):
     ctx = F.Context(0)
     x = np.random.default_rng(5).standard_normal((1, 700)).astype(np.float32)
