@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-served", action="store_true", help="skip the served (request loop) leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the uneven-batch and request-stream legs")
     ap.add_argument("--mixed-only", action="store_true", help="run only the uneven-batch and request-stream legs")
+    ap.add_argument("--stack-only", action="store_true",
+                    help="run one all-pairs step, then only the stacking leg (profiling of the stacks)")
     return ap.parse_args()
 
 
@@ -654,6 +656,11 @@ def run_ours(args):
     for _ in range(args.warmup):
         step()
     barrier()
+    if args.stack_only:
+        print(json.dumps({"stacks": stack_leg(F, torch, ctx, stream, dev, d_y, n_sta, n_win, L,
+                                              measured_peaks()[0])}), flush=True)
+        ctx.close()
+        return
     # --- timed: device-resident step ---
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with ClockSampler(local) as clk:

@@ -1953,13 +1953,24 @@ extern "C" int fpcc_stack(fpcc_ctx* c, int mode, const float* d_y, int64_t ldg, 
                                              c->stream));
     CK(launch_stack_xlin((float2*)X, K, G, M, c->stream));
     g_launches += 2;
+    const bool inblock = spec_supported(M);
     for (int s = 0; s < S; s++) {
-      // CWT of every trace and of the linear stacks at scale s
-      CK(launch_stack_mul((const float2*)X, rows, M, spec + (size_t)s * M, (float2*)T, c->stream));
+      // CWT of every trace and of the linear stacks at scale s: in one block per
+      // row when M is on the size menu (only the L outputs leave the block),
+      // else a multiply and global radix passes
       float2* W = nullptr;
-      if ((rc = passes(c, (float2*)T, (float2*)T2, M, rows, +1, &W))) return rc;
+      int64_t ldw = M;
+      if (inblock) {
+        CwtRowArgs q{(const float2*)X, rows, M, spec + (size_t)s * M, L, (float2*)T, L};
+        CK(launch_cwt_rows(q, c->stream));
+        W = (float2*)T;
+        ldw = L;
+      } else {
+        CK(launch_stack_mul((const float2*)X, rows, M, spec + (size_t)s * M, (float2*)T, c->stream));
+        if ((rc = passes(c, (float2*)T, (float2*)T2, M, rows, +1, &W))) return rc;
+      }
       // weighted linear-stack coefficients, back to the spectrum, times the reconstruction kernel
-      CK(launch_stack_coherence(W, K, G, L, M, nu, (float2*)Y, c->stream));
+      CK(launch_stack_coherence(W, ldw, K, G, L, M, nu, (float2*)Y, c->stream));
       float2* Z = nullptr;
       if ((rc = passes(c, (float2*)Y, (float2*)Y2, M, G, -1, &Z))) return rc;
       const float a = (float)(std::log(2.0) / (2 * cpsi * V * wf.scale[s]));

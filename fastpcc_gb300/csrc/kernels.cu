@@ -120,6 +120,29 @@ __global__ void __launch_bounds__(T, 1) k_spec(SpecArgs a) {
   }
 }
 
+// ------------------------------------------------------------ CWT rows
+// One block per row: X[row][m] * F[m] in shared memory, the inverse transform
+// (unnormalised; F carries the 1/M), the first L values stored (stride ldo).
+template <int T, typename RAD>
+__global__ void __launch_bounds__(T, 1) k_cwt_rows(CwtRowArgs a) {
+  constexpr int NZ = rad_len(RAD{});
+  extern __shared__ float4 smem_raw[];
+  float2* s = reinterpret_cast<float2*>(smem_raw);
+  float2* lo = s + padded_len(NZ);
+  float2* hi = lo + 128;
+  build_twiddles(lo, hi, NZ);
+  const int row = blockIdx.x;
+  const float2* x = a.X + (int64_t)row * NZ;
+  for (int m = threadIdx.x; m < NZ; m += T) {
+    const float2 u = x[m], f = __ldg(a.F + m);
+    s[PADI(m)] = make_float2(u.x * f.x - u.y * f.y, u.x * f.y + u.y * f.x);
+  }
+  __syncthreads();
+  ct_fft<+1, T, 1>(s, 1, 0, TwTab{lo, hi}, RAD{});
+  float2* o = a.out + (int64_t)row * a.ldo;
+  for (int k = threadIdx.x; k < a.L; k += T) o[k] = s[PADI(k)];
+}
+
 // ------------------------------------------------------------ pairs
 // Cross-spectrum bin at position p in [0, Nz).  Full storage holds Nz bins;
 // Hermitian storage (real traces) holds bins 0..Nz/2.
@@ -490,6 +513,19 @@ cudaError_t launch_spec(const SpecArgs& a, cudaStream_t st) {
   case SZ: return launch_k(k_spec<T, Radices<__VA_ARGS__>>, a.nrows, T, smem, st, &a);
     FPCC_SIZE_MENU(FPCC_SPEC_CASE)
 #undef FPCC_SPEC_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_cwt_rows(const CwtRowArgs& a, cudaStream_t st) {
+  if (a.nrows <= 0) return cudaSuccess;
+  if (a.L > a.M) return cudaErrorInvalidValue;
+  const size_t smem = spec_smem_bytes(a.M);
+  switch (a.M) {
+#define FPCC_CWT_CASE(SZ, T, ...) \
+  case SZ: return launch_k(k_cwt_rows<T, Radices<__VA_ARGS__>>, a.nrows, T, smem, st, &a);
+    FPCC_SIZE_MENU(FPCC_CWT_CASE)
+#undef FPCC_CWT_CASE
     default: return cudaErrorInvalidValue;
   }
 }

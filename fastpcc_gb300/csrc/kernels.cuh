@@ -45,6 +45,17 @@ struct SpecArgs {
   int64_t ldo;
 };
 
+// Rows of one CWT scale: out[r][k] = IDFT_M(X[r] * F)[k], k < L (in-block, M on the menu).
+struct CwtRowArgs {
+  const float2* X;       // nrows x M spectra
+  int nrows;
+  int M;
+  const float2* F;       // M-point kernel spectrum (with the 1/M)
+  int L;
+  float2* out;           // nrows x ldo
+  int64_t ldo;
+};
+
 struct PairArgs {
   const void* spec;      // station spectra
   int64_t ldspec;
@@ -83,6 +94,7 @@ size_t spec_smem_bytes(int Nz);
 size_t pair_smem_bytes(int Nz);
 
 cudaError_t launch_spec(const SpecArgs& a, cudaStream_t st);
+cudaError_t launch_cwt_rows(const CwtRowArgs& a, cudaStream_t st);
 cudaError_t launch_pairs(const PairArgs& a, cudaStream_t st);
 cudaError_t launch_phase_store(const PhaseArgs& a, cudaStream_t st);
 // Block-scaled int16 rows (header + n short2, row stride ldo four-byte elements)

@@ -95,8 +95,8 @@ __global__ void k_stack_mul(const float2* __restrict__ X, int M, const float2* _
   }
 }
 
-__global__ void k_stack_coherence(const float2* __restrict__ W, int K, int G, int L, int M, double nu,
-                                  float2* Y) {
+__global__ void k_stack_coherence(const float2* __restrict__ W, int64_t ldw, int K, int G, int L, int M,
+                                  double nu, float2* Y) {
   const int g = blockIdx.y;
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < M; n += gridDim.x * blockDim.x) {
     float2 out = make_float2(0.0f, 0.0f);
@@ -107,7 +107,7 @@ __global__ void k_stack_coherence(const float2* __restrict__ W, int K, int G, in
         float px = 0.0f, py = 0.0f;
         const int j1 = min(K, j0 + 32);
         for (int j = j0; j < j1; j++) {
-          const float2 u = unit_f(W[((int64_t)g * K + j) * M + n]);
+          const float2 u = unit_f(W[((int64_t)g * K + j) * ldw + n]);
           px += u.x;
           py += u.y;
         }
@@ -115,7 +115,7 @@ __global__ void k_stack_coherence(const float2* __restrict__ W, int K, int G, in
         uy += py;
       }
       const double c = coherence(ux, uy, K, nu);
-      const float2 w = W[((int64_t)G * K + g) * M + n];
+      const float2 w = W[((int64_t)G * K + g) * ldw + n];
       out = make_float2((float)(c * w.x), (float)(c * w.y));
     }
     Y[(int64_t)g * M + n] = out;
@@ -177,10 +177,10 @@ cudaError_t launch_stack_mul(const float2* X, int rows, int M, const float2* F, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_stack_coherence(const float2* W, int K, int G, int L, int M, double nu, float2* Y,
+cudaError_t launch_stack_coherence(const float2* W, int64_t ldw, int K, int G, int L, int M, double nu, float2* Y,
                                    cudaStream_t st) {
   if (!rows_ok(G)) return cudaErrorInvalidValue;
-  k_stack_coherence<<<grid_cols(M, G), 256, 0, st>>>(W, K, G, L, M, nu, Y);
+  k_stack_coherence<<<grid_cols(M, G), 256, 0, st>>>(W, ldw, K, G, L, M, nu, Y);
   return cudaGetLastError();
 }
 

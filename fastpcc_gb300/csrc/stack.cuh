@@ -29,10 +29,10 @@ cudaError_t launch_stack_load(const float* y, int64_t ldg, int64_t ldj, int K, i
 cudaError_t launch_stack_xlin(float2* X, int K, int G, int M, cudaStream_t st);
 // T[r][m] = X[r][m] F[m], rows r < rows.
 cudaError_t launch_stack_mul(const float2* X, int rows, int M, const float2* F, float2* T, cudaStream_t st);
-// From the inverse transforms W (rows g K + j: the traces' CWT at one scale;
-// rows G K + g: the linear stack's): Y[g][n] = |mean_j W/|W||^nu * W_lin[n] for
-// n < L, 0 for n >= L.
-cudaError_t launch_stack_coherence(const float2* W, int K, int G, int L, int M, double nu, float2* Y,
+// From the inverse transforms W (rows of stride ldw; rows g K + j: the traces'
+// CWT at one scale; rows G K + g: the linear stack's): Y[g][n] =
+// |mean_j W/|W||^nu * W_lin[n] for n < L, 0 for L <= n < M (rows of stride M).
+cudaError_t launch_stack_coherence(const float2* W, int64_t ldw, int K, int G, int L, int M, double nu, float2* Y,
                                    cudaStream_t st);
 // R[g][m] (+)= a * Z[g][m] F[m] (first: assign).
 cudaError_t launch_stack_acc(const float2* Z, int G, int M, const float2* F, float a, int first, float2* R,
