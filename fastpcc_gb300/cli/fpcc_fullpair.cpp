@@ -4,7 +4,7 @@
 //   fpcc_fullpair filelist1 filelist2 [pcc] [v=] [wpcc] [ccgn] [cc1b] [tl1= tl2= | nl1= nl2=]
 //                 [isac | imsacs] [osac | obin[=prefix]] [clip] [std=] [awhite=f1,f2]
 //                 [mindist=] [maxdist=] [pmin= pmax= VR= V= type= w0=] [Nmax=] [mincc=]
-//                 [NoAutoPairing] [verbose=]
+//                 [NoAutoPairing] [verbose=] [stack=lin,pws,tspws] [nu=]
 //
 // Records are SAC files listed one per line (isac) or MSACS1 files (imsacs).
 // The steps follow the reference's order (PCCfullpair_main :211-521): read both
@@ -13,6 +13,10 @@
 // stations (or pair line by line), whiten, flip reversed components, then
 // correlate with each requested method and write one SAC file per window pair
 // (osac) or one binary file per channel pair (obin, the ts-PWS input format).
+// With stack=, the windows of each channel pair are also stacked on the device
+// (linear, phase-weighted, time-scale phase-weighted; fpcc_stack, coherence
+// power nu=, the ts-PWS wavelet family from pmin= pmax= V= type= w0= as for
+// WPCC) and each stack is written as one SAC file, <pair>_<method>_<kind>.sac.
 //
 // GPU side: the record files are read by a pool of threads straight into
 // pinned memory and the kept windows uploaded asynchronously; clipping and
@@ -188,6 +192,8 @@ struct Options {
   std::string fin1, fin2, obinprefix;
   bool has_prefix = false;
   int autopair = 1, acc = 0, verbose = 1;
+  int stack = 0;      // bit 0 linear, bit 1 PWS, bit 2 ts-PWS
+  double nu = 2;
 };
 
 bool rd_double(double* x, const char* s) { char* e; *x = strtod(s, &e); return e != s; }
@@ -231,7 +237,21 @@ int parse(int argc, char** argv, Options& o) {
     else if (is("w0=")) er += !rd_double(&o.op1, a + 3);
     else if (is("awhite=")) {
       if (sscanf(a + 7, "%lf,%lf", &o.awhite[0], &o.awhite[1]) != 2) er++;
-    } else if (is("NoAutoPairing")) o.autopair = 0;
+    } else if (is("stack=")) {
+      std::string v = a + 6;
+      size_t p0 = 0;
+      while (p0 <= v.size()) {
+        size_t p1 = v.find(',', p0);
+        if (p1 == std::string::npos) p1 = v.size();
+        const std::string k = v.substr(p0, p1 - p0);
+        if (k == "lin") o.stack |= 1;
+        else if (k == "pws") o.stack |= 2;
+        else if (k == "tspws") o.stack |= 4;
+        else er++;
+        p0 = p1 + 1;
+      }
+    } else if (is("nu=")) er += !rd_double(&o.nu, a + 3);
+    else if (is("NoAutoPairing")) o.autopair = 0;
     else if (is("verbose=")) er += !rd_int(&o.verbose, a + 8);
   }
   if (!o.autopair && o.stdn > 0) {
@@ -625,11 +645,59 @@ int run(const Options& o) {
   cudaMemcpyAsync(d_pairs, pairs.data(), pairs.size() * 4, cudaMemcpyHostToDevice, st);
   std::vector<float> y((size_t)Tr * L);
   std::vector<std::thread> writers;
+  // ts-PWS family in samples: pmin/pmax as given (seconds), else the WPCC defaults
+  double spmin = 1.25 * std::sqrt(2.0) * 3.14159265358979323846, spmax = spmin * std::pow(2.0, 3.5);
+  if (o.pmin != 0 && o.pmax != 0) { spmin = o.pmin / dt; spmax = o.pmax / dt; }
+  // stacks of each channel pair's windows (the sets of the binary output), one SAC file per kind
+  auto stack_sets = [&](const char* name) -> int {
+    std::vector<char> done(Tr, 0);
+    float *d_g = nullptr, *d_o = nullptr;
+    if (cudaMalloc(&d_g, (size_t)Tr * L * 4) != cudaSuccess || cudaMalloc(&d_o, (size_t)L * 4) != cudaSuccess)
+      return FPCC_ENOMEM;
+    std::vector<float> ys(L);
+    int rc = 0;
+    for (int next = 0; next < Tr && !rc; next++) {
+      if (done[next]) continue;
+      std::vector<int> set;
+      for (int t = next; t < Tr; t++)
+        if (!done[t] && !strcmp(h1[t].chn, h1[next].chn) && !strcmp(h2[t].chn, h2[next].chn)) {
+          done[t] = 1;
+          set.push_back(t);
+        }
+      const int K = (int)set.size();
+      bool contig = true;
+      for (int i = 1; i < K; i++) contig &= set[i] == set[0] + i;
+      const float* base = d_y + (size_t)set[0] * L;
+      if (!contig) {
+        for (int i = 0; i < K; i++)
+          cudaMemcpyAsync(d_g + (size_t)i * L, d_y + (size_t)set[i] * L, (size_t)L * 4, cudaMemcpyDeviceToDevice, st);
+        base = d_g;
+      }
+      static const char* kinds[3] = {"lin", "pws", "tspws"};
+      for (int k = 0; k < 3 && !rc; k++) {
+        if (!(o.stack & (1 << k))) continue;
+        rc = fpcc_stack(ctx, k, base, (int64_t)K * L, L, K, L, 1, o.nu, spmin, spmax, (int)o.V, o.type, o.op1, d_o, L);
+        if (rc) break;
+        cudaMemcpyAsync(ys.data(), d_o, (size_t)L * 4, cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        const TraceHeader &a = h1[set[0]], &b = h2[set[0]];
+        char fn[200];
+        snprintf(fn, sizeof fn, "%s.%s.%s.%s.%s.%s.%s.%s_%s_%s.sac", a.net, a.sta, a.loc, a.chn, b.net, b.sta, b.loc,
+                 b.chn, name, kinds[k]);
+        if (!write_sac(fn, ys.data(), L, Lag1 * dt, dt, name, a, b)) printf("fpcc_fullpair: error writing %s\n", fn);
+      }
+    }
+    cudaFree(d_g);
+    cudaFree(d_o);
+    return rc;
+  };
+  int stack_rc = 0;
   auto emit = [&](const char* name) {
     cudaMemcpyAsync(y.data(), d_y, y.size() * 4, cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
     if (o.oformat == 1) store_sacs(y, L, Tr, Lag1, h1, h2, dt, name);
     else store_bins(y, L, Tr, Lag1, h1, h2, dt, name, o);
+    if (o.stack && !stack_rc) stack_rc = stack_sets(name);
   };
   const int Nz = fpcc_choose_nz(N, Lag1, Lag2, FPCC_NZ_FAST);
   if (o.pcc) {
@@ -698,6 +766,10 @@ int run(const Options& o) {
                            L, nullptr));
     emit("cc1b");
     cudaFree(d_s);
+  }
+  if (stack_rc) {
+    printf("fpcc_fullpair: stacking failed: %s\n", fpcc_last_error());
+    return 4;
   }
   cudaFree(d_x);
   cudaFree(d_pairs);

@@ -848,6 +848,7 @@ int multi_group(fpcc_ctx* c, std::vector<MultiRow>& rows, int M) {
         (rc = dev_buf(c, S_P64_CNT, (size_t)n * sizeof(MultiRow), &d)))
       return rc;
     CK(cudaMemcpyAsync(d, rows.data() + r0, (size_t)n * sizeof(MultiRow), cudaMemcpyHostToDevice, c->stream));
+    CK(launch_multi_exp((MultiRow*)d, n, c->stream));
     const MultiRow* dr = (const MultiRow*)d;
     auto tr = [&](T* in, T* other, int nr, int dir, T** res) -> int {
       if constexpr (sizeof(T) == 16) return passes64(c, (double2*)in, (double2*)other, M, nr, dir, (double2**)res);

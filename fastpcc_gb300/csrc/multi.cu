@@ -39,6 +39,25 @@ __device__ __forceinline__ double hilbert_im(int n, int N) {
   return 2.0 * c / (s * (double)N);
 }
 
+__global__ void __launch_bounds__(256) k_multi_exp(MultiRow* rows) {
+  __shared__ float sm[8];
+  const MultiRow r = rows[blockIdx.x];
+  float mx = 0.0f;
+  for (int n = threadIdx.x; n < r.N; n += 256) mx = fmaxf(mx, fabsf(__ldg(r.x + n)));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float a = 0.0f;
+    for (int w = 0; w < 8; w++) a = fmaxf(a, sm[w]);
+    rows[blockIdx.x].e = (a > 0.0f) ? ilogbf(a) : kNoSignal;
+  }
+}
+
+// x * 2^-e exactly (0 for a window without signal)
+__device__ __forceinline__ float scaled(float x, int e) { return e == kNoSignal ? 0.0f : scalbnf(x, -e); }
+
 template <typename T>
 __global__ void k_multi_load2(const MultiRow* __restrict__ rows, int nrows, T* A, int M) {
   const int j = blockIdx.y;
@@ -46,10 +65,11 @@ __global__ void k_multi_load2(const MultiRow* __restrict__ rows, int nrows, T* A
   const bool two = 2 * j + 1 < nrows;
   const float* x1 = two ? rows[2 * j + 1].x : nullptr;
   const int N1 = two ? rows[2 * j + 1].N : 0;
+  const int e1 = two ? rows[2 * j + 1].e : kNoSignal;
   T* a = A + (int64_t)j * M;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-    const float u = (m < r0.N) ? __ldg(r0.x + m) : 0.0f;
-    const float v = (m < N1) ? __ldg(x1 + m) : 0.0f;
+    const float u = (m < r0.N) ? scaled(__ldg(r0.x + m), r0.e) : 0.0f;
+    const float v = (m < N1) ? scaled(__ldg(x1 + m), e1) : 0.0f;
     a[m] = mk(u, v, (T*)nullptr);
   }
 }
@@ -83,7 +103,8 @@ __global__ void k_multi_store(const MultiRow* __restrict__ rows, const T* A, int
   const T* a = A + (int64_t)blockIdx.y * M;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < r.N; k += gridDim.x * blockDim.x) {
     const T v = a[k];
-    r.out[k] = make_float2((float)v.x, (float)v.y);
+    r.out[k] = (r.e == kNoSignal) ? make_float2(0.0f, 0.0f)
+                                  : make_float2(scalbnf((float)v.x, r.e), scalbnf((float)v.y, r.e));
   }
 }
 
@@ -139,6 +160,12 @@ dim3 grid2(int len, int nrows) {
 }
 
 }  // namespace
+
+cudaError_t launch_multi_exp(MultiRow* rows, int nrows, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  k_multi_exp<<<nrows, 256, 0, st>>>(rows);
+  return cudaGetLastError();
+}
 
 template <typename T>
 cudaError_t launch_multi_load2(const MultiRow* rows, int nrows, T* A, int M, cudaStream_t st) {

@@ -13,7 +13,13 @@
 // complex row); their spectra are separated by Hermitian symmetry and each
 // multiplied by its own H_N before one inverse transform per window:
 //   A = x_2j + i x_2j+1;  A = FFT_M(A);  B_r = X_r * H_{N_r};  B = IFFT_M(B);  out = B[0, N)
-// 1.5 M-point transforms per window.  T is float2 or double2.
+// 1.5 M-point transforms per window.  Each window enters its row scaled by
+// 2^-e, e the binary exponent of its largest |sample|, and its analytic signal
+// leaves scaled by 2^e: exact in floating point, so results are unchanged, but
+// the two windows of a row have the same magnitude, and the split's rounding
+// (about 1e-7 of the row in FP32) stays at that level relative to each of them
+// instead of relative to the stronger one; an all-zero window gives zeros.
+// T is float2 or double2.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -26,8 +32,13 @@ struct MultiRow {
   float2* out;           // its analytic signal, N values
   const void* filt;      // H_N: M-point kernel spectrum (T) of the window length, including 1/M
   int N;
-  int pad;
+  int e;                 // binary exponent of max |x| (set on the device by launch_multi_exp), kNoSignal if zero
 };
+
+constexpr int kNoSignal = -100000;
+
+// rows[r].e = exponent of max |x_r| over N_r samples (kNoSignal for an all-zero window).
+cudaError_t launch_multi_exp(MultiRow* rows, int nrows, cudaStream_t st);
 
 // A[j][m] = x_{2j}[m] + i x_{2j+1}[m] (zero beyond each window's N and for a
 // missing odd row), (nrows + 1) / 2 rows of stride M.

@@ -102,7 +102,9 @@ def _run(F, args, cwd):
 
 
 def _outputs(cwd, tag):
-    fs = sorted(f for f in os.listdir(cwd) if f.endswith(".sac") and f"_{tag}_" in f)
+    # per-window files: the window's start date follows the method tag (stack files end in _lin/_pws/_tspws)
+    fs = sorted(f for f in os.listdir(cwd)
+                if f.endswith(".sac") and f"_{tag}_" in f and f.split(f"_{tag}_")[1][:1].isdigit())
     return fs, np.stack([_read_sac(os.path.join(cwd, f))[0] for f in fs])
 
 
@@ -147,3 +149,23 @@ def test_cli_binary_output(F, g, tmp_path):
     assert ours[:head] == ref[:head]             # header, start times, zero-lag offsets
     y, yr = np.frombuffer(ours[head:], "<f4").reshape(nseq, L), np.frombuffer(ref[head:], "<f4").reshape(nseq, L)
     assert relerr(y, yr) < TOL
+
+
+def test_cli_stacks_over_windows(F, g, tmp_path):
+    # stack=lin,pws,tspws: each channel pair's windows stacked on the device, one
+    # SAC file per kind; checked against the oracle's stacks of the program's own
+    # per-window outputs and of the reference CLI's (ts-PWS family: the WPCC
+    # options, pmin/pmax in seconds, Mexican hat, 2 voices by default)
+    from oracle import oracle as O
+    l1, l2 = _write_inputs(str(tmp_path), g)
+    d = tmp_path / "stack"
+    d.mkdir()
+    _run(F, [l1, l2, "tl1=-12000", "tl2=12000", "pcc", "stack=lin,pws,tspws", "nu=2", "pmin=25", "pmax=330"], str(d))
+    _, per_window = _outputs(str(d), "pcc2")
+    dt = float(g["dt"])
+    for mode, kind in ((O.STACK_LINEAR, "lin"), (O.STACK_PWS, "pws"), (O.STACK_TSPWS, "tspws")):
+        y, _ = _read_sac(str(d / f"G.CAN.00.LHZ.G.ECH.00.LHZ_pcc2_{kind}.sac"))
+        ours = O.stack(per_window, mode, 2.0, 25.0 / dt, 330.0 / dt, 2, -3)
+        assert relerr(y[None], ours[None]) < TOL, kind
+        ref = O.stack(g["pcc2"], mode, 2.0, 25.0 / dt, 330.0 / dt, 2, -3)
+        assert relerr(y[None], ref[None]) < 3 * TOL, kind

@@ -299,3 +299,21 @@ def test_server_int16_storage(F, orc):
         if m == 4 and len(a) > 5000:
             continue   # the FP64 direct-sum oracle is slow at this length
         assert relerr(out, _oracle(orc, m, a, b, l1, l2, v)) < TOL, (m, len(a), l1, l2)
+
+
+def test_packed_station_stage_weak_window(F, orc):
+    # a window 1e-5 times weaker than the others, at a length whose analytic
+    # signals go through the packed stage (3001 samples, no gaps: FP32), shares a
+    # transform with a strong window; each window is scaled by its own power of
+    # two inside the shared row, so the weak one keeps its own precision
+    x = _stations(4, 1, 3001, "serve/weak")[:, 0].copy()
+    x[2] *= 1e-5
+    srv = F.Server(hbm_budget=1 << 30)
+    for s in range(4):
+        srv.put(s, 0, x[s])
+    reqs = [(m, 2, s2, 0, -300, 300, 0.0) for m in (F.PCC2, F.PCC1) for s2 in (0, 1, 3)]
+    outs = _run(F, srv, reqs)
+    srv.close()
+    for (m, s1, s2, w, l1, l2, v), out in zip(reqs, outs):
+        ref = _oracle(orc, m, x[s1], x[s2], l1, l2, v)
+        assert relerr(out, ref) < TOL, (m, s2, relerr(out, ref))

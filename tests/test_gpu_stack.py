@@ -118,3 +118,23 @@ def test_single_trace_and_errors(F):
     with pytest.raises(F.FpccError):
         _stack(F, ctx, 7, x, 1)                                                    # unknown mode
     ctx.close()
+
+
+def test_long_traces_many_windows_and_zero_trace(F):
+    # L = 12001: CWT length class 24576 is beyond the in-block menu (global
+    # radix passes); K = 40 > 32 exercises the coherence's runs of 32 traces; one
+    # all-zero trace contributes zero phasors; nu = 1.5 takes the general power
+    rng = np.random.default_rng(11)
+    L, K = 12001, 40
+    t = np.arange(L) - L // 2
+    pulse = np.exp(-0.5 * ((t - 800) / 30.0) ** 2) * np.cos(2 * np.pi * (t - 800) / 90.0)
+    c = (0.8 * rng.standard_normal((K, L)) + (0.5 + rng.random((K, 1))) * pulse).astype(np.float32)
+    c[7] = 0.0
+    ctx = F.Context(0)
+    for mode, kw in ((F.STACK_LINEAR, {}), (F.STACK_PWS, dict(nu=1.5)),
+                     (F.STACK_TSPWS, dict(nu=1.5, pmin=20.0, pmax=80.0, V=2, type=-1))):
+        y = _stack(F, ctx, mode, c, K, **kw)
+        ref = O.stack(c, mode, kw.get("nu", 2.0), kw.get("pmin", 0.0), kw.get("pmax", 0.0), kw.get("V", 4),
+                      kw.get("type", -1))
+        assert relerr(y, ref[None]) < TOL, (mode, relerr(y, ref[None]))
+    ctx.close()
