@@ -281,7 +281,10 @@ bool grow(Server* s, Slab& sl, int need_rows) {
   sl.key_of.resize(ncap, -1);
   sl.pin.resize(ncap, 0);
   sl.pos.resize(ncap);
-  for (int r = sl.cap; r < ncap; r++) {
+  // new rows at the least-recently-used end, the lowest last, so that claims
+  // (taken from that end) come out ascending and a batch's new products are
+  // usually one contiguous run of rows
+  for (int r = ncap - 1; r >= sl.cap; r--) {
     sl.lru.push_back(r);
     sl.pos[r] = std::prev(sl.lru.end());
   }
@@ -446,17 +449,30 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   int rc = ensure_raw(s, pk.N, miss_keys, raw_rows, fl);
   if (rc) return rc;
   Slab& raw = slab_of(s, Product{0, pk.N, 0, 0});
-  // gather raw rows contiguously, compute, scatter into the slab
+  // the station stage reads the raw rows and writes the slab rows in place when
+  // each set is one ascending run of rows (the usual case: fresh rows are claimed
+  // in order); otherwise it gathers / scatters through scratch rows
+  auto ascending = [](const std::vector<int>& r) {
+    for (size_t i = 1; i < r.size(); i++)
+      if (r[i] != r[0] + (int)i) return false;
+    return true;
+  };
+  const bool in_place_x = ascending(raw_rows), in_place_p = ascending(miss_rows);
   const int64_t N = pk.N;
-  void* dx = dbuf(s, &s->d_tmp_x, &s->n_tmp_x, (size_t)n * round16(N * 4));
-  void* dp = dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)n * sl.row_bytes);
+  void* dx = in_place_x ? (char*)raw.base + (int64_t)raw_rows[0] * raw.row_bytes
+                        : dbuf(s, &s->d_tmp_x, &s->n_tmp_x, (size_t)n * round16(N * 4));
+  void* dp = in_place_p ? (char*)sl.base + (int64_t)miss_rows[0] * sl.row_bytes
+                        : dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)n * sl.row_bytes);
   void* di = dbuf(s, &s->d_idx, &s->n_idx, (size_t)2 * n * sizeof(int) + 64);
   if (!dx || !dp || !di) return FPCC_ENOMEM;
-  std::vector<int> idx(2 * n);
-  for (int i = 0; i < n; i++) { idx[i] = raw_rows[i]; idx[n + i] = miss_rows[i]; }
-  if (upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st) != cudaSuccess) return FPCC_ECUDA;
-  const int64_t ldx = round16(N * 4) / 4;
-  if (copy_rows(raw.base, raw.row_bytes, (const int*)di, dx, ldx * 4, nullptr, n, N * 4, s->st) != cudaSuccess)
+  if (!in_place_x || !in_place_p) {
+    std::vector<int> idx(2 * n);
+    for (int i = 0; i < n; i++) { idx[i] = raw_rows[i]; idx[n + i] = miss_rows[i]; }
+    if (upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st) != cudaSuccess) return FPCC_ECUDA;
+  }
+  const int64_t ldx = round16(N * 4) / 4;   // = raw.row_bytes / 4
+  if (!in_place_x &&
+      copy_rows(raw.base, raw.row_bytes, (const int*)di, dx, ldx * 4, nullptr, n, N * 4, s->st) != cudaSuccess)
     return FPCC_ECUDA;
   int method = FPCC_PCC2, rule = FPCC_AMP_F_REG;
   int64_t ldo = sl.row_bytes / (pk.fmt ? 4 : 8);
@@ -486,8 +502,9 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
                                f64.data(), (int)f64.size());
   }
   if (rc) return rc;
-  if (copy_rows(dp, sl.row_bytes, nullptr, sl.base, sl.row_bytes, (const int*)di + n, n, sl.row_bytes, s->st) !=
-      cudaSuccess)
+  if (!in_place_p &&
+      copy_rows(dp, sl.row_bytes, nullptr, sl.base, sl.row_bytes, (const int*)di + n, n, sl.row_bytes, s->st) !=
+          cudaSuccess)
     return FPCC_ECUDA;
   s->station_rows += n;
   return 0;
