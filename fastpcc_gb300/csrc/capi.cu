@@ -12,6 +12,7 @@
 #include <string>
 #include <algorithm>
 #include <vector>
+#include <type_traits>
 
 #include "../../include/fastpcc_gb300.h"
 #include "direct.cuh"
@@ -78,6 +79,7 @@ struct fpcc_ctx {
   std::map<int, float2*> bluestein;  // per window length N: M-point filter spectra, forward then inverse
   std::map<int, double2*> twiddles64;   // FP64 tables exp(-2 pi i t/n)
   std::map<int, double2*> bluestein64;  // FP64 filter spectra per N, forward then inverse
+  std::map<int, float4*> twiddles_df;   // double-float tables exp(-2 pi i t/n)
   // filter spectra of the packed path per (N, M, fp64): forward then inverse, M values each,
   // held in blocks of one batched computation
   std::map<std::tuple<int, int, int>, void*> multi_filters;
@@ -227,6 +229,7 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
   for (auto& kv : c->bluestein) ctx_free(c, kv.second);
   for (auto& kv : c->twiddles64) ctx_free(c, kv.second);
   for (auto& kv : c->bluestein64) ctx_free(c, kv.second);
+  for (auto& kv : c->twiddles_df) ctx_free(c, kv.second);
   for (void* b : c->multi_blocks) ctx_free(c, b);
   cudaStreamSynchronize(c->stream);
   if (c->stream2) cudaStreamSynchronize(c->stream2);
@@ -528,6 +531,61 @@ int passes64(fpcc_ctx* c, double2* A, double2* B, int n, int nrows, int dir, dou
   int cur = 0, Ns = 1;
   for (int R : rad) {
     CK(launch_pass64(R, dir, bufs[cur], bufs[cur ^ 1], n, Ns, nrows, tw, c->stream));
+    g_launches++;
+    cur ^= 1;
+    Ns *= R;
+  }
+  *res = bufs[cur];
+  return 0;
+}
+
+// Double-float twiddle table of n points, from the FP64 table.
+int twiddle_df(fpcc_ctx* c, int n, const float4** out) {
+  auto it = c->twiddles_df.find(n);
+  if (it != c->twiddles_df.end()) { *out = it->second; return 0; }
+  const double2* t64 = nullptr;
+  int rc = twiddle64(c, n, &t64);
+  if (rc) return rc;
+  float4* d = nullptr;
+  cudaError_t e = ctx_alloc(c, (void**)&d, (size_t)n * sizeof(float4));
+  if (e != cudaSuccess) return fail(FPCC_ENOMEM, "double-float twiddle table: %s", cudaGetErrorString(e));
+  if ((e = launch_df_from_double(t64, d, n, c->stream)) != cudaSuccess) {
+    ctx_free(c, d);
+    return cuda_fail(e, "double-float twiddle table");
+  }
+  g_launches++;
+  c->twiddles_df[n] = d;
+  *out = d;
+  return 0;
+}
+
+DfConsts df_consts() {
+  auto split = [](double v) {
+    const float h = (float)v;
+    return df{h, (float)(v - (double)h)};
+  };
+  const double pi = 3.14159265358979323846;
+  DfConsts k;
+  k.s3 = split(std::sin(2 * pi / 3));
+  k.c1 = split(std::cos(2 * pi / 5));
+  k.c2 = split(std::cos(4 * pi / 5));
+  k.s1 = split(std::sin(2 * pi / 5));
+  k.s2 = split(std::sin(4 * pi / 5));
+  return k;
+}
+
+// n-point double-float transforms of nrows rows held in A (ping-pong with B).
+int passes_df(fpcc_ctx* c, float4* A, float4* B, int n, int nrows, int dir, float4** res) {
+  const std::vector<int> rad = radices64(n);
+  if (rad.empty() && n != 1) return fail(FPCC_EUNSUP, "length %d is not 2,3,5-smooth", n);
+  const float4* tw = nullptr;
+  int rc = twiddle_df(c, n, &tw);
+  if (rc) return rc;
+  static const DfConsts kc = df_consts();
+  float4* bufs[2] = {A, B};
+  int cur = 0, Ns = 1;
+  for (int R : rad) {
+    CK(launch_pass_df(R, dir, bufs[cur], bufs[cur ^ 1], n, Ns, nrows, tw, kc, c->stream));
     g_launches++;
     cur ^= 1;
     Ns *= R;
@@ -850,18 +908,23 @@ int multi_group(fpcc_ctx* c, std::vector<MultiRow>& rows, int M) {
     CK(cudaMemcpyAsync(d, rows.data() + r0, (size_t)n * sizeof(MultiRow), cudaMemcpyHostToDevice, c->stream));
     CK(launch_multi_exp((MultiRow*)d, n, c->stream));
     const MultiRow* dr = (const MultiRow*)d;
+    constexpr bool dfl = std::is_same<T, float4>::value;
     auto tr = [&](T* in, T* other, int nr, int dir, T** res) -> int {
-      if constexpr (sizeof(T) == 16) return passes64(c, (double2*)in, (double2*)other, M, nr, dir, (double2**)res);
+      if constexpr (dfl) return passes_df(c, (float4*)in, (float4*)other, M, nr, dir, (float4**)res);
+      else if constexpr (sizeof(T) == 16) return passes64(c, (double2*)in, (double2*)other, M, nr, dir, (double2**)res);
       else return passes(c, (float2*)in, (float2*)other, M, nr, dir, (float2**)res);
     };
     T* z = nullptr;
-    CK(launch_multi_load2<T>(dr, n, (T*)A, M, c->stream));
+    if constexpr (dfl) CK(launch_multi_load2_df(dr, n, (float4*)A, M, c->stream));
+    else CK(launch_multi_load2<T>(dr, n, (T*)A, M, c->stream));
     if ((rc = tr((T*)A, (T*)B, np, -1, &z))) return rc;
     T* y = (z == (T*)A) ? (T*)B : (T*)A;
-    CK(launch_multi_split<T>(dr, n, z, y, M, c->stream));
+    if constexpr (dfl) CK(launch_multi_split_df(dr, n, (const float4*)z, (float4*)y, M, c->stream));
+    else CK(launch_multi_split<T>(dr, n, z, y, M, c->stream));
     T* res = nullptr;
     if ((rc = tr(y, z, n, +1, &res))) return rc;
-    CK(launch_multi_store<T>(dr, n, res, M, c->stream));
+    if constexpr (dfl) CK(launch_multi_store_df(dr, n, (const float4*)res, M, c->stream));
+    else CK(launch_multi_store<T>(dr, n, res, M, c->stream));
     g_launches += 3;
   }
   return 0;
@@ -912,7 +975,8 @@ extern "C" int fpcc_station_stage_multi(fpcc_ctx* c, int method, const fpcc_stat
   }
   for (auto& kv : groups) {
     const int M = kv.first.first;
-    rc = kv.first.second ? multi_group<double2>(c, kv.second, M) : multi_group<float2>(c, kv.second, M);
+    // windows with gaps: double-float transforms (FP32 pipes, about 44 significant bits)
+    rc = kv.first.second ? multi_group<float4>(c, kv.second, M) : multi_group<float2>(c, kv.second, M);
     if (rc) return rc;
   }
   void* dall;

@@ -1,5 +1,6 @@
 // Analytic signals of windows of different lengths in shared launches (see multi.cuh).
 #include "multi.cuh"
+#include "dfloat.cuh"
 
 #include <algorithm>
 
@@ -22,6 +23,10 @@ __device__ __forceinline__ T mul(T a, T b) {
 template <typename T>
 __device__ __forceinline__ T cvt(double2 v) {
   return mk(v.x, v.y, (T*)nullptr);
+}
+template <>
+__device__ __forceinline__ float4 cvt<float4>(double2 v) {
+  return dfc(df_from_double(v.x), df_from_double(v.y));
 }
 
 // Im h(n), 0 < n < N, of h = IDFT_N(mask): for even N, (2/N) cot(pi n / N) at
@@ -127,6 +132,133 @@ __global__ void k_multi_convert(const double2* __restrict__ src, T* dst, int64_t
     dst[i] = cvt<T>(src[i]);
 }
 
+// ---- double-float (float4) variants of the row kernels and the radix passes
+__global__ void k_multi_load2_df(const MultiRow* __restrict__ rows, int nrows, float4* A, int M) {
+  const int j = blockIdx.y;
+  const MultiRow r0 = rows[2 * j];
+  const bool two = 2 * j + 1 < nrows;
+  const float* x1 = two ? rows[2 * j + 1].x : nullptr;
+  const int N1 = two ? rows[2 * j + 1].N : 0;
+  const int e1 = two ? rows[2 * j + 1].e : kNoSignal;
+  float4* a = A + (int64_t)j * M;
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+    const float u = (m < r0.N) ? scaled(__ldg(r0.x + m), r0.e) : 0.0f;
+    const float v = (m < N1) ? scaled(__ldg(x1 + m), e1) : 0.0f;
+    a[m] = make_float4(u, v, 0.0f, 0.0f);
+  }
+}
+
+__global__ void k_multi_split_df(const MultiRow* __restrict__ rows, int nrows, const float4* __restrict__ Z,
+                                 float4* B, int M) {
+  const int j = blockIdx.y;
+  const bool two = 2 * j + 1 < nrows;
+  const float4* z = Z + (int64_t)j * M;
+  const float4* H0 = reinterpret_cast<const float4*>(rows[2 * j].filt);
+  const float4* H1 = two ? reinterpret_cast<const float4*>(rows[2 * j + 1].filt) : nullptr;
+  float4* b0 = B + (int64_t)(2 * j) * M;
+  float4* b1 = B + (int64_t)(2 * j + 1) * M;
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+    const float4 p = z[m];
+    const float4 q = z[m == 0 ? 0 : M - m];
+    // X0 = (Z[m] + conj Z[-m]) / 2,  X1 = (Z[m] - conj Z[-m]) / 2i
+    const df pr = df_re(p), pi = df_im(p), qr = df_re(q), qi = df_im(q);
+    const float4 x0 = dfc(df_scale2(df_add(pr, qr), 0.5f), df_scale2(df_sub(pi, qi), 0.5f));
+    b0[m] = dfc_mul(x0, H0[m]);
+    if (two) {
+      const float4 x1 = dfc(df_scale2(df_add(pi, qi), 0.5f), df_scale2(df_sub(qr, pr), 0.5f));
+      b1[m] = dfc_mul(x1, H1[m]);
+    }
+  }
+}
+
+__global__ void k_multi_store_df(const MultiRow* __restrict__ rows, const float4* A, int M) {
+  const MultiRow r = rows[blockIdx.y];
+  const float4* a = A + (int64_t)blockIdx.y * M;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < r.N; k += gridDim.x * blockDim.x) {
+    const float4 v = a[k];
+    r.out[k] = (r.e == kNoSignal) ? make_float2(0.0f, 0.0f)
+                                  : make_float2(scalbnf(df_to_float(df_re(v)), r.e), scalbnf(df_to_float(df_im(v)), r.e));
+  }
+}
+
+// v <- DFT_R(v) with kernel exp(DIR 2 pi i jk / R), natural output order (double-float)
+template <int R, int DIR>
+__device__ __forceinline__ void dft_df(float4* v, const DfConsts& k) {
+  if constexpr (R == 2) {
+    const float4 a = v[0], b = v[1];
+    v[0] = dfc_add(a, b);
+    v[1] = dfc_sub(a, b);
+  } else if constexpr (R == 3) {
+    const float4 t1 = dfc_add(v[1], v[2]);
+    const float4 t2 = dfc_sub(v[0], dfc_scale2(t1, 0.5f));
+    float4 t3 = dfc_muli(dfc_mul_r(dfc_sub(v[1], v[2]), k.s3));
+    if (DIR < 0) t3 = dfc_scale2(t3, -1.0f);
+    v[0] = dfc_add(v[0], t1);
+    v[1] = dfc_add(t2, t3);
+    v[2] = dfc_sub(t2, t3);
+  } else if constexpr (R == 4) {
+    const float4 a = dfc_add(v[0], v[2]), b = dfc_sub(v[0], v[2]);
+    const float4 c = dfc_add(v[1], v[3]);
+    float4 d = dfc_muli(dfc_sub(v[1], v[3]));
+    if (DIR < 0) d = dfc_scale2(d, -1.0f);
+    v[0] = dfc_add(a, c);
+    v[2] = dfc_sub(a, c);
+    v[1] = dfc_add(b, d);
+    v[3] = dfc_sub(b, d);
+  } else {   // R == 5
+    const float4 a1 = dfc_add(v[1], v[4]), a2 = dfc_add(v[2], v[3]);
+    const float4 b1 = dfc_sub(v[1], v[4]), b2 = dfc_sub(v[2], v[3]);
+    const float4 x0 = v[0];
+    const float4 p1 = dfc_add(x0, dfc_add(dfc_mul_r(a1, k.c1), dfc_mul_r(a2, k.c2)));
+    const float4 p2 = dfc_add(x0, dfc_add(dfc_mul_r(a1, k.c2), dfc_mul_r(a2, k.c1)));
+    float4 q1 = dfc_muli(dfc_add(dfc_mul_r(b1, k.s1), dfc_mul_r(b2, k.s2)));
+    float4 q2 = dfc_muli(dfc_sub(dfc_mul_r(b1, k.s2), dfc_mul_r(b2, k.s1)));
+    if (DIR < 0) {
+      q1 = dfc_scale2(q1, -1.0f);
+      q2 = dfc_scale2(q2, -1.0f);
+    }
+    v[0] = dfc_add(x0, dfc_add(a1, a2));
+    v[1] = dfc_add(p1, q1);
+    v[4] = dfc_sub(p1, q1);
+    v[2] = dfc_add(p2, q2);
+    v[3] = dfc_sub(p2, q2);
+  }
+}
+
+// One radix-R Stockham pass over nrows rows of n points (as the FP64 pass):
+// 32-bit indices (callers keep n * nrows below 2^31).
+template <int R, int DIR>
+__global__ void __launch_bounds__(256) k_pass_df(const float4* __restrict__ in, float4* __restrict__ out, int n,
+                                                 int Ns, int nrows, const float4* __restrict__ tw, DfConsts kc) {
+  const int m = n / R;
+  const int total = m * nrows;
+  const int tstride = n / (Ns * R);
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    const int row = g / m;
+    const int j = g - row * m;
+    const float4* x = in + (int64_t)row * n;
+    float4 v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = x[j + r * m];
+    const int k = j % Ns;
+    if (k != 0) {
+#pragma unroll
+      for (int r = 1; r < R; r++) v[r] = dfc_mul_c(v[r], __ldg(tw + k * r * tstride), DIR > 0);
+    }
+    dft_df<R, DIR>(v, kc);
+    float4* o = out + (int64_t)row * n + (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) o[r * Ns] = v[r];
+  }
+}
+
+__global__ void k_df_from_double(const double2* __restrict__ src, float4* dst, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 v = src[i];
+    dst[i] = dfc(df_from_double(v.x), df_from_double(v.y));
+  }
+}
+
 __global__ void __launch_bounds__(256) k_multi_rowstats(const MultiRow* __restrict__ rows, float* rmax,
                                                         float* rsum) {
   __shared__ float sm[8], ss[8];
@@ -160,6 +292,53 @@ dim3 grid2(int len, int nrows) {
 }
 
 }  // namespace
+
+cudaError_t launch_multi_load2_df(const MultiRow* rows, int nrows, float4* A, int M, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  const int np = (nrows + 1) / 2;
+  if (np > 65535) return cudaErrorInvalidValue;
+  k_multi_load2_df<<<grid2(M, np), 256, 0, st>>>(rows, nrows, A, M);
+  return cudaGetLastError();
+}
+cudaError_t launch_multi_split_df(const MultiRow* rows, int nrows, const float4* Z, float4* B, int M,
+                                  cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  const int np = (nrows + 1) / 2;
+  if (np > 65535) return cudaErrorInvalidValue;
+  k_multi_split_df<<<grid2(M, np), 256, 0, st>>>(rows, nrows, Z, B, M);
+  return cudaGetLastError();
+}
+cudaError_t launch_multi_store_df(const MultiRow* rows, int nrows, const float4* A, int M, cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  if (nrows > 65535) return cudaErrorInvalidValue;
+  k_multi_store_df<<<grid2(M / 2, nrows), 256, 0, st>>>(rows, A, M);
+  return cudaGetLastError();
+}
+cudaError_t launch_pass_df(int R, int dir, const float4* in, float4* out, int n, int Ns, int nrows, const float4* tw,
+                           const DfConsts& kc, cudaStream_t st) {
+  if ((int64_t)n * nrows >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
+  const int64_t work = (int64_t)(n / R) * nrows;
+  int64_t b = (work + 255) / 256;
+  const int grid = (int)(b < 1 ? 1 : (b < 152 * 16 ? b : 152 * 16));
+#define FPCC_PASS_DF(RR)                                                                      \
+  if (R == RR) {                                                                              \
+    if (dir < 0) k_pass_df<RR, -1><<<grid, 256, 0, st>>>(in, out, n, Ns, nrows, tw, kc);      \
+    else k_pass_df<RR, 1><<<grid, 256, 0, st>>>(in, out, n, Ns, nrows, tw, kc);               \
+    return cudaGetLastError();                                                                \
+  }
+  FPCC_PASS_DF(2)
+  FPCC_PASS_DF(3)
+  FPCC_PASS_DF(4)
+  FPCC_PASS_DF(5)
+#undef FPCC_PASS_DF
+  return cudaErrorInvalidValue;
+}
+cudaError_t launch_df_from_double(const double2* src, float4* dst, int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int g = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  k_df_from_double<<<g, 256, 0, st>>>(src, dst, n);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_multi_exp(MultiRow* rows, int nrows, cudaStream_t st) {
   if (nrows <= 0) return cudaSuccess;
@@ -217,5 +396,6 @@ template cudaError_t launch_multi_store<float2>(const MultiRow*, int, const floa
 template cudaError_t launch_multi_store<double2>(const MultiRow*, int, const double2*, int, cudaStream_t);
 template cudaError_t launch_multi_convert<float2>(const double2*, float2*, int64_t, cudaStream_t);
 template cudaError_t launch_multi_convert<double2>(const double2*, double2*, int64_t, cudaStream_t);
+template cudaError_t launch_multi_convert<float4>(const double2*, float4*, int64_t, cudaStream_t);
 
 }  // namespace fpcc

@@ -25,6 +25,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "dfloat.cuh"
+
 namespace fpcc {
 
 struct MultiRow {
@@ -58,6 +60,19 @@ cudaError_t launch_multi_hkernel(const int* Ns, int nrows, double2* B, int M, cu
 // dst[i] = src[i] rounded to T (n values).
 template <typename T>
 cudaError_t launch_multi_convert(const double2* src, T* dst, int64_t n, cudaStream_t st);
+// Double-float (float4 = re.hi, im.hi, re.lo, im.lo) variants for the windows
+// that need more than FP32 (dfloat.cuh): load, split and store as above, one
+// radix-R (2, 3, 4, 5) Stockham pass, and double -> double-float conversion.
+struct DfConsts {
+  df s3, c1, c2, s1, s2;   // sin(2 pi/3), cos(2 pi/5), cos(4 pi/5), sin(2 pi/5), sin(4 pi/5)
+};
+cudaError_t launch_multi_load2_df(const MultiRow* rows, int nrows, float4* A, int M, cudaStream_t st);
+cudaError_t launch_multi_split_df(const MultiRow* rows, int nrows, const float4* Z, float4* B, int M,
+                                  cudaStream_t st);
+cudaError_t launch_multi_store_df(const MultiRow* rows, int nrows, const float4* A, int M, cudaStream_t st);
+cudaError_t launch_pass_df(int R, int dir, const float4* in, float4* out, int n, int Ns, int nrows, const float4* tw,
+                           const DfConsts& kc, cudaStream_t st);
+cudaError_t launch_df_from_double(const double2* src, float4* dst, int n, cudaStream_t st);
 // Per row: max |a|^2 and sum |a|^2 over the row's N values.
 cudaError_t launch_multi_rowstats(const MultiRow* rows, int nrows, float* rmax, float* rsum, cudaStream_t st);
 
