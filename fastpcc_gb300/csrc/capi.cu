@@ -869,13 +869,19 @@ int multi_filters(fpcc_ctx* c, const std::vector<int>& Ns, int M, std::vector<co
       return rc;
     CK(cudaMemcpyAsync(dN, lens.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     CK(launch_multi_hkernel((const int*)dN, n, (double2*)B, M, c->stream));
-    double2* r = nullptr;
-    if ((rc = passes64(c, (double2*)B, (double2*)A, M, n, -1, &r))) return rc;
     void* block = nullptr;
     CK(ctx_alloc(c, &block, (size_t)n * M * sizeof(T)));
     c->multi_blocks.push_back(block);
     c->multi_filter_bytes += (size_t)n * M * sizeof(T);
-    CK(launch_multi_convert<T>(r, (T*)block, (int64_t)n * M, c->stream));
+    // the kernel values (FP64) split into double-floats and transformed in
+    // double-float, then kept as double-floats or rounded to float2
+    CK(launch_df_from_double((const double2*)B, (float4*)A, n * M, c->stream));
+    float4* r = nullptr;
+    if ((rc = passes_df(c, (float4*)A, (float4*)B, M, n, -1, &r))) return rc;
+    if constexpr (std::is_same<T, float4>::value)
+      CK(cudaMemcpyAsync(block, r, (size_t)n * M * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+    else
+      CK(launch_df_to_float2(r, (float2*)block, n * M, c->stream));
     g_launches += 2;
     for (int j = 0; j < n; j++)
       c->multi_filters[std::make_tuple(lens[j], M, f64)] = (char*)block + (size_t)j * M * sizeof(T);

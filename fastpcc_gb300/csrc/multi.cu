@@ -117,12 +117,18 @@ __global__ void k_multi_hkernel(const int* __restrict__ Ns, double2* B, int M) {
   const int N = Ns[blockIdx.y];
   double2* b = B + (int64_t)blockIdx.y * M;
   const double inv = 1.0 / (double)M;
-  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-    double re = 0.0, im = 0.0;
-    if (m == 0) re = inv;
-    else if (m < N) im = hilbert_im(m, N) * inv;
-    else if (m > M - N) im = hilbert_im(N - M + m, N) * inv;
-    b[m] = make_double2(re, im);
+  // the kernel is odd (Im h(N - e) = -Im h(e)), so each value also fills its
+  // mirror entry M - e; entries above M - N are written by their mirror
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m <= M - N; m += gridDim.x * blockDim.x) {
+    if (m == 0) {
+      b[0] = make_double2(inv, 0.0);
+    } else if (m < N) {
+      const double v = hilbert_im(m, N) * inv;
+      b[m] = make_double2(0.0, v);
+      b[M - m] = make_double2(0.0, -v);
+    } else {
+      b[m] = make_double2(0.0, 0.0);
+    }
   }
 }
 
@@ -252,6 +258,13 @@ __global__ void __launch_bounds__(256) k_pass_df(const float4* __restrict__ in, 
   }
 }
 
+__global__ void k_df_to_float2(const float4* __restrict__ src, float2* dst, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 v = src[i];
+    dst[i] = make_float2(df_to_float(df_re(v)), df_to_float(df_im(v)));
+  }
+}
+
 __global__ void k_df_from_double(const double2* __restrict__ src, float4* dst, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double2 v = src[i];
@@ -333,6 +346,13 @@ cudaError_t launch_pass_df(int R, int dir, const float4* in, float4* out, int n,
 #undef FPCC_PASS_DF
   return cudaErrorInvalidValue;
 }
+cudaError_t launch_df_to_float2(const float4* src, float2* dst, int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int g = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  k_df_to_float2<<<g, 256, 0, st>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_df_from_double(const double2* src, float4* dst, int n, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const int g = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;

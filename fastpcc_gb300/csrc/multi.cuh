@@ -73,6 +73,7 @@ cudaError_t launch_multi_store_df(const MultiRow* rows, int nrows, const float4*
 cudaError_t launch_pass_df(int R, int dir, const float4* in, float4* out, int n, int Ns, int nrows, const float4* tw,
                            const DfConsts& kc, cudaStream_t st);
 cudaError_t launch_df_from_double(const double2* src, float4* dst, int n, cudaStream_t st);
+cudaError_t launch_df_to_float2(const float4* src, float2* dst, int n, cudaStream_t st);
 // Per row: max |a|^2 and sum |a|^2 over the row's N values.
 cudaError_t launch_multi_rowstats(const MultiRow* rows, int nrows, float* rmax, float* rsum, cudaStream_t st);
 
