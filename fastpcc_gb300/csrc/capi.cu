@@ -571,13 +571,26 @@ DfConsts df_consts() {
   k.c2 = split(std::cos(4 * pi / 5));
   k.s1 = split(std::sin(2 * pi / 5));
   k.s2 = split(std::sin(4 * pi / 5));
+  k.c8 = split(std::cos(pi / 8));
+  k.s8 = split(std::sin(pi / 8));
+  k.r2 = split(std::sqrt(0.5));
   return k;
 }
 
 // n-point double-float transforms of nrows rows held in A (ping-pong with B).
 int passes_df(fpcc_ctx* c, float4* A, float4* B, int n, int nrows, int dir, float4** res) {
-  const std::vector<int> rad = radices64(n);
-  if (rad.empty() && n != 1) return fail(FPCC_EUNSUP, "length %d is not 2,3,5-smooth", n);
+  const std::vector<int> r64 = radices64(n);
+  if (r64.empty() && n != 1) return fail(FPCC_EUNSUP, "length %d is not 2,3,5-smooth", n);
+  // two consecutive radix-4 levels run as one radix-16 pass (half the global traffic)
+  std::vector<int> rad;
+  for (size_t i = 0; i < r64.size(); i++) {
+    if (r64[i] == 4 && i + 1 < r64.size() && r64[i + 1] == 4) {
+      rad.push_back(16);
+      i++;
+    } else {
+      rad.push_back(r64[i]);
+    }
+  }
   const float4* tw = nullptr;
   int rc = twiddle_df(c, n, &tw);
   if (rc) return rc;

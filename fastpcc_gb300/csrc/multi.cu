@@ -231,6 +231,41 @@ __device__ __forceinline__ void dft_df(float4* v, const DfConsts& k) {
   }
 }
 
+// DFT_16 (natural order) as 4 x 4: DFT_4 over n2 of x[4 n2 + n1], twiddles
+// w16^(n1 k1), DFT_4 over n1; w16 = exp(DIR 2 pi i / 16).
+template <int DIR>
+__device__ __forceinline__ void dft16_df(float4* v, const DfConsts& k) {
+  float4 y[4][4];
+#pragma unroll
+  for (int n1 = 0; n1 < 4; n1++) {
+    float4 t[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
+    dft_df<4, DIR>(t, k);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) y[n1][k1] = t[k1];
+  }
+  // w16^e for e = n1 k1 in {1, 2, 3, 4, 6, 9}
+  const float s = (float)DIR;
+  const float4 w1 = dfc(k.c8, df{s * k.s8.hi, s * k.s8.lo});
+  const float4 w2 = dfc(k.r2, df{s * k.r2.hi, s * k.r2.lo});
+  const float4 w3 = dfc(k.s8, df{s * k.c8.hi, s * k.c8.lo});
+  y[1][1] = dfc_mul(y[1][1], w1);
+  y[1][2] = dfc_mul(y[1][2], w2);
+  y[1][3] = dfc_mul(y[1][3], w3);
+  y[2][1] = dfc_mul(y[2][1], w2);
+  y[2][2] = (DIR < 0) ? dfc_scale2(dfc_muli(y[2][2]), -1.0f) : dfc_muli(y[2][2]);                        // w^4
+  y[2][3] = dfc_mul(y[2][3], dfc(df{-k.r2.hi, -k.r2.lo}, df{s * k.r2.hi, s * k.r2.lo}));                // w^6
+  y[3][1] = dfc_mul(y[3][1], w3);
+  y[3][2] = dfc_mul(y[3][2], dfc(df{-k.r2.hi, -k.r2.lo}, df{s * k.r2.hi, s * k.r2.lo}));                // w^6
+  y[3][3] = dfc_mul(y[3][3], dfc(df{-k.c8.hi, -k.c8.lo}, df{-s * k.s8.hi, -s * k.s8.lo}));              // w^9
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    float4 t[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+    dft_df<4, DIR>(t, k);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) v[k1 + 4 * k2] = t[k2];
+  }
+}
+
 // One radix-R Stockham pass over nrows rows of n points (as the FP64 pass):
 // 32-bit indices (callers keep n * nrows below 2^31).
 template <int R, int DIR>
@@ -251,7 +286,8 @@ __global__ void __launch_bounds__(256) k_pass_df(const float4* __restrict__ in, 
 #pragma unroll
       for (int r = 1; r < R; r++) v[r] = dfc_mul_c(v[r], __ldg(tw + k * r * tstride), DIR > 0);
     }
-    dft_df<R, DIR>(v, kc);
+    if constexpr (R == 16) dft16_df<DIR>(v, kc);
+    else dft_df<R, DIR>(v, kc);
     float4* o = out + (int64_t)row * n + (j - k) * R + k;
 #pragma unroll
     for (int r = 0; r < R; r++) o[r * Ns] = v[r];
@@ -343,6 +379,7 @@ cudaError_t launch_pass_df(int R, int dir, const float4* in, float4* out, int n,
   FPCC_PASS_DF(3)
   FPCC_PASS_DF(4)
   FPCC_PASS_DF(5)
+  FPCC_PASS_DF(16)
 #undef FPCC_PASS_DF
   return cudaErrorInvalidValue;
 }

@@ -62,9 +62,10 @@ template <typename T>
 cudaError_t launch_multi_convert(const double2* src, T* dst, int64_t n, cudaStream_t st);
 // Double-float (float4 = re.hi, im.hi, re.lo, im.lo) variants for the windows
 // that need more than FP32 (dfloat.cuh): load, split and store as above, one
-// radix-R (2, 3, 4, 5) Stockham pass, and double -> double-float conversion.
+// radix-R (2, 3, 4, 5, 16) Stockham pass, and double -> double-float conversion.
 struct DfConsts {
   df s3, c1, c2, s1, s2;   // sin(2 pi/3), cos(2 pi/5), cos(4 pi/5), sin(2 pi/5), sin(4 pi/5)
+  df c8, s8, r2;           // cos(pi/8), sin(pi/8), sqrt(1/2) (radix 16)
 };
 cudaError_t launch_multi_load2_df(const MultiRow* rows, int nrows, float4* A, int M, cudaStream_t st);
 cudaError_t launch_multi_split_df(const MultiRow* rows, int nrows, const float4* Z, float4* B, int M,
