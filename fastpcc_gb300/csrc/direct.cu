@@ -118,8 +118,10 @@ template <int MODE, int FMT>   // MODE 1: v = 1, 2: v = 2, 0: general power
 __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
   __shared__ float2 s1[kTile];
   __shared__ float2 s2[kTile + kLagBlock];
-  const int p = blockIdx.x;
-  const int lblk = blockIdx.y * kLagBlock;       // first lag index of the block
+  // grid (lag blocks, pairs): blocks are issued pair by pair, so descriptors
+  // ordered by decreasing window length start the longest blocks first
+  const int p = blockIdx.y;
+  const int lblk = blockIdx.x * kLagBlock;       // first lag index of the block
   const int l = lblk + threadIdx.x;
   int N, Lag1, L;
   const void* R1;
@@ -223,8 +225,8 @@ __device__ __forceinline__ uint32_t bits_at(const uint32_t* r, int nw, int b) {
 
 // numerator(lag) = overlap - 2 * popcount(b1[n] xor b2[n+lag]) over the overlap.
 __global__ void __launch_bounds__(256) k_cc1b_popcount(Cc1bArgs a) {
-  const int p = blockIdx.x;
-  const int l = blockIdx.y * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y;   // grid (lag blocks, pairs), as k_pccv
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
   int N, lag0;
   const uint32_t* B1;
   const uint32_t* B2;
@@ -283,21 +285,31 @@ cudaError_t launch_energy_prefix(const float* x, int64_t ldx, int nrows, int N, 
 
 cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st) {
   if (a.npairs <= 0 || a.L <= 0) return cudaSuccess;
-  if ((a.L + kLagBlock - 1) / kLagBlock > 65535) return cudaErrorInvalidValue;
-  dim3 grid(a.npairs, (a.L + kLagBlock - 1) / kLagBlock);
+  if (a.half < 0 || a.half > 2) return cudaErrorInvalidValue;
   const int mode = (a.v == 1.0f) ? 1 : (a.v == 2.0f ? 2 : 0);
+  const int lb = (a.L + kLagBlock - 1) / kLagBlock;
+  for (int p0 = 0; p0 < a.npairs; p0 += 65535) {   // grid.y holds at most 65535 pairs
+    PccvArgs b = a;
+    b.npairs = a.npairs - p0 < 65535 ? a.npairs - p0 : 65535;
+    if (a.desc) {
+      b.desc = a.desc + p0;
+    } else {
+      b.pairs = a.pairs + p0;
+      b.y = a.y + (int64_t)p0 * a.ldy;
+    }
+    const dim3 grid(lb, b.npairs);
 #define FPCC_PCCV_FMT(F)                                                  \
-  if (a.half == F) {                                                      \
-    if (mode == 1) k_pccv<1, F><<<grid, kLagBlock, 0, st>>>(a);           \
-    else if (mode == 2) k_pccv<2, F><<<grid, kLagBlock, 0, st>>>(a);      \
-    else k_pccv<0, F><<<grid, kLagBlock, 0, st>>>(a);                     \
-    return cudaGetLastError();                                            \
-  }
-  FPCC_PCCV_FMT(0)
-  FPCC_PCCV_FMT(1)
-  FPCC_PCCV_FMT(2)
+    if (a.half == F) {                                                    \
+      if (mode == 1) k_pccv<1, F><<<grid, kLagBlock, 0, st>>>(b);         \
+      else if (mode == 2) k_pccv<2, F><<<grid, kLagBlock, 0, st>>>(b);    \
+      else k_pccv<0, F><<<grid, kLagBlock, 0, st>>>(b);                   \
+    }
+    FPCC_PCCV_FMT(0)
+    FPCC_PCCV_FMT(1)
+    FPCC_PCCV_FMT(2)
 #undef FPCC_PCCV_FMT
-  return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_sign_bits(const float* x, int64_t ldx, int nrows, int N, uint32_t* bits, int64_t ldb,
@@ -311,9 +323,18 @@ cudaError_t launch_sign_bits(const float* x, int64_t ldx, int nrows, int N, uint
 
 cudaError_t launch_cc1b_popcount(const Cc1bArgs& a, cudaStream_t st) {
   if (a.npairs <= 0 || a.L <= 0) return cudaSuccess;
-  if ((a.L + 255) / 256 > 65535) return cudaErrorInvalidValue;
-  dim3 grid(a.npairs, (a.L + 255) / 256);
-  k_cc1b_popcount<<<grid, 256, 0, st>>>(a);
+  for (int p0 = 0; p0 < a.npairs; p0 += 65535) {   // grid.y holds at most 65535 pairs
+    Cc1bArgs b = a;
+    b.npairs = a.npairs - p0 < 65535 ? a.npairs - p0 : 65535;
+    if (a.desc) {
+      b.desc = a.desc + p0;
+    } else {
+      b.pairs = a.pairs + p0;
+      if (b.y) b.y = a.y + (int64_t)p0 * a.ldy;
+      if (b.num) b.num = a.num + (int64_t)p0 * a.ldy;
+    }
+    k_cc1b_popcount<<<dim3((a.L + 255) / 256, b.npairs), 256, 0, st>>>(b);
+  }
   return cudaGetLastError();
 }
 

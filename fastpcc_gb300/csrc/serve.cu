@@ -773,6 +773,11 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
     e.scale = (m == FPCC_PCC2) ? 1.0f / ((float)Nz * (float)q.N) : (fft ? (float)(1.0 / (double)Nz) : 0.0f);
     maxL = std::max(maxL, q.L);
   }
+  // direct sums: a block's work grows with its window length, and blocks are
+  // issued descriptor by descriptor, so the longest windows go first (each
+  // descriptor names its own output row: the order changes no result)
+  if (m == FPCC_PCC1 || m == FPCC_PCCV || m == FPCC_CC1B_POPCOUNT)
+    std::stable_sort(d.begin(), d.end(), [](const fpcc_pair_desc& a, const fpcc_pair_desc& b) { return a.N > b.N; });
   if (upload(fl, dd, d.data(), d.size() * sizeof(fpcc_pair_desc), s->st) != cudaSuccess) return FPCC_ECUDA;
   rc = fpcc_pair_stage_packed(s->ctx, m, g.fmt, Nz, (const fpcc_pair_desc*)dd, n, maxL, g.v,
                               m == FPCC_CC1B_POPCOUNT);
