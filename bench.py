@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-served", action="store_true", help="skip the served (request loop) leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the uneven-batch and request-stream legs")
     ap.add_argument("--mixed-only", action="store_true", help="run only the uneven-batch and request-stream legs")
+    ap.add_argument("--multi-only", action="store_true",
+                    help="run only the packed analytic-signal stage leg (profiling); --windows sets its count")
     ap.add_argument("--stack-only", action="store_true",
                     help="run one all-pairs step, then only the stacking leg (profiling of the stacks)")
     return ap.parse_args()
@@ -522,6 +524,38 @@ def wpcc_leg(F, torch, ctx, stream, dev, peak, n_pairs=16, n_win=24, N=65536, la
             "achieved_GBs": alg / ms / 1e6, "frac_of_measured_hbm": alg / ms / 1e6 / peak, "max_rel_err": err}
 
 
+def multi_station_leg(F, torch, ctx, stream, dev, peak, n=512, lo=24000, hi=32000):
+    """The packed analytic-signal stage (fpcc_station_stage_multi, PCC1 phase
+    signals) on n windows of lengths uniform in [lo, hi) with 5 % of samples in
+    gaps: double-float transforms (the gapped path) and FP32 transforms on the
+    same windows; kernel spectra cached (a second call, as in serving).  The
+    class length is 65536 for these lengths: per window 1.5 transforms of four
+    radix-16 passes, each pass moving 32 bytes per point (double-float) or 16
+    (FP32), the rate reported against the measured copy bandwidth."""
+    from fastpcc_gb300 import synth
+    rng = np.random.default_rng(17)
+    lengths = np.sort(rng.integers(lo, hi, n))
+    win = synth.uneven_windows(lengths, 1, gap_frac=0.05, tag="multi-station")
+    Nmax = int(lengths.max())
+    x = np.zeros((n, Nmax), np.float32)
+    for i in range(n):
+        x[i, :lengths[i]] = win[i][0]
+    d_x = torch.from_numpy(x).to(dev)
+    d_o = torch.empty((n, 2 * Nmax), dtype=torch.float32, device=dev)
+    M = 65536
+    out = {"workload": f"{n} windows, lengths {lo}-{hi} (class length {M}), 5 % gaps, PCC1 phase signals"}
+    for name, f64 in (("double_float", 1), ("fp32", 0)):
+        rows = [(d_x.data_ptr() + i * Nmax * 4, int(lengths[i]), 0, f64) for i in range(n)]
+        ms = _time_ms(torch, stream, lambda: ctx.station_stage_multi(F.PCC1, rows, F.F32, F.AMP_F_REG,
+                                                                     d_o.data_ptr(), Nmax), reps=3)
+        esz = 32 if f64 else 16             # bytes a point-pass reads and writes
+        pp = n * 1.5 * M * 4                # point-passes: 1.5 transforms x 4 radix-16 passes per window
+        out[name] = {"kernel_ms": ms, "windows_per_s": n / ms * 1e3, "point_passes_per_s": pp / ms * 1e3,
+                     "pass_bytes_GBs": pp * esz / ms / 1e6, "pass_frac_of_measured_hbm": pp * esz / ms / 1e6 / peak,
+                     "note": "the whole stage (load, split, store, row statistics, phase store) over the pass bytes"}
+    return out
+
+
 def stack_leg(F, torch, ctx, stream, dev, d_y, n_sta, n_win, L, peak):
     """Stacks over the windows of every channel pair, read in place from the
     window-major rows of the all-pairs pair stage (row w * P + p): linear,
@@ -619,6 +653,14 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     F.build()
+    if args.multi_only:
+        stream = torch.cuda.Stream(device=torch.device("cuda", local))
+        ctx = F.Context(local)
+        ctx.set_stream(stream.cuda_stream)
+        print(json.dumps({"multi_station": multi_station_leg(F, torch, ctx, stream, torch.device("cuda", local),
+                                                             measured_peaks()[0], n=args.windows * 8)}), flush=True)
+        ctx.close()
+        return
     if args.mixed_only:
         fmt = {"f32": F.F32, "f16": F.F16, "i16": F.I16}[args.fmt]
         tune = autotune(F)
@@ -763,6 +805,7 @@ def run_ours(args):
     if rank == 0 and not args.no_mixed:
         methods = method_legs(F, torch, ctx, stream, dev, x, d_x, pairs, Nz, peak)
         methods["wpcc_config"] = wpcc_leg(F, torch, ctx, stream, dev, peak)
+        methods["multi_station"] = multi_station_leg(F, torch, ctx, stream, dev, peak)
 
     stacks = None
     if rank == 0 and not args.no_mixed:

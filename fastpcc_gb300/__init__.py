@@ -112,6 +112,7 @@ def lib():
             L.fpcc_whiten_rows.argtypes = [vp, vp, i64, i, i, d, d, d]
             L.fpcc_prep_last_error.restype = C.c_char_p
             L.fpcc_stack.argtypes = [vp, i, vp, i64, i64, i, i, i, d, d, d, i, i, d, vp, i64]
+            L.fpcc_station_stage_multi.argtypes = [vp, i, vp, i, i, i, vp, i64]
             L.fpcc_server_create.argtypes = [C.POINTER(vp), i, C.c_size_t, i]
             L.fpcc_server_set_format.argtypes = [vp, i]
             L.fpcc_server_set_nz_mode.argtypes = [vp, i]
@@ -291,6 +292,17 @@ class Context:
         ldg = K * ldy if ldg is None else ldg
         check(lib().fpcc_stack(self._h, mode, C.c_void_p(d_y), ldg, ldj, K, L, ngroups, float(nu), float(pmin),
                                float(pmax), V, type, float(op1), C.c_void_p(d_out), ldo))
+
+    def station_stage_multi(self, method, rows, fmt, rule, d_out, ldo):
+        """Station stage of windows of different lengths in shared launches:
+        rows = [(d_x, N, Nz, f64)] ordered by (N, Nz); row r is written at
+        d_out + r * ldo elements of the format."""
+        class _Row(C.Structure):
+            _fields_ = [("d_x", C.c_void_p), ("N", C.c_int32), ("Nz", C.c_int32), ("f64", C.c_int32),
+                        ("pad", C.c_int32)]
+        arr = (_Row * len(rows))(*[_Row(int(x), int(n), int(nz), int(f), 0) for (x, n, nz, f) in rows])
+        check(lib().fpcc_station_stage_multi(self._h, method, C.addressof(arr), len(rows), fmt, rule,
+                                             C.c_void_p(d_out), ldo))
 
     def energy_stage(self, d_x, ldx, nrows, N, d_E, ldE):
         check(lib().fpcc_energy_stage(self._h, C.c_void_p(d_x), ldx, nrows, N, C.c_void_p(d_E), ldE))

@@ -1005,8 +1005,28 @@ extern "C" int fpcc_station_stage_multi(fpcc_ctx* c, int method, const fpcc_stat
   float* rsum = rmax + nrows;
   CK(launch_multi_rowstats((const MultiRow*)dall, nrows, rmax, rsum, c->stream));
   g_launches++;
-  // normalisation, zero padding and DFT_Nz (or the phase signal) per (N, Nz) run of rows
   const size_t oesz = fmt == FPCC_F32 ? 8 : 4;
+  if (method != FPCC_PCC2) {
+    // phase signals: one launch over every row, each with its own offset and length
+    std::vector<int64_t> roff(off.begin(), off.begin() + nrows);
+    std::vector<int> rN(nrows);
+    int Nmax = 0;
+    for (int r = 0; r < nrows; r++) { rN[r] = h_rows[r].N; Nmax = std::max(Nmax, rN[r]); }
+    void* dmeta;
+    if ((rc = dev_buf(c, S_CONV_X, (size_t)nrows * (sizeof(int64_t) + sizeof(int)), &dmeta))) return rc;
+    CK(cudaMemcpyAsync(dmeta, roff.data(), (size_t)nrows * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync((char*)dmeta + (size_t)nrows * sizeof(int64_t), rN.data(), (size_t)nrows * sizeof(int),
+                       cudaMemcpyHostToDevice, c->stream));
+    PhaseArgs a{};
+    a.in = (const float2*)an; a.ldin = 0; a.nrows = nrows; a.N = Nmax; a.rule = rule;
+    a.rowstat = (rule == FPCC_AMP_SUMTHR) ? rsum : rmax; a.fmt = fmt; a.out = d_out; a.ldo = ldo;
+    a.row_in = (const int64_t*)dmeta;
+    a.row_N = (const int*)((char*)dmeta + (size_t)nrows * sizeof(int64_t));
+    CK(launch_phase_store(a, c->stream));
+    g_launches++;
+    return 0;
+  }
+  // normalisation, zero padding and DFT_Nz per (N, Nz) run of rows
   for (int r0 = 0; r0 < nrows;) {
     int r1 = r0 + 1;
     while (r1 < nrows && h_rows[r1].N == h_rows[r0].N && h_rows[r1].Nz == h_rows[r0].Nz) r1++;

@@ -288,9 +288,9 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
 __global__ void __launch_bounds__(256) k_phase_store(PhaseArgs a) {
   const int row = blockIdx.x;
   const int n = blockIdx.y * blockDim.x + threadIdx.x;
-  if (n >= a.N) return;
+  if (n >= (a.row_N ? a.row_N[row] : a.N)) return;
   const float eps = amp_eps(a.rule, a.rowstat[row]);
-  const float2 v = a.in[(int64_t)row * a.ldin + n];
+  const float2 v = a.row_in ? a.in[a.row_in[row] + n] : a.in[(int64_t)row * a.ldin + n];
   const float2 p = cscale(v, amp_factor(a.rule, v.x * v.x + v.y * v.y, eps));
   if (a.fmt == SPEC_I16)   // |p| <= 1: fixed scale 1/32767
     reinterpret_cast<short2*>(a.out)[(int64_t)row * a.ldo + n] = make_short2(i16_quant(p.x, kI16Max),

@@ -80,12 +80,14 @@ struct PhaseArgs {
   const float2* in;      // analytic signal rows
   int64_t ldin;
   int nrows;
-  int N;
+  int N;                 // samples per row (the largest, with row_N)
   int rule;
   const float* rowstat;
-  int fmt;               // 0: float2, 1: half2
+  int fmt;               // 0: float2, 1: half2, 2: int16 of scale 1/32767
   void* out;
   int64_t ldo;
+  const int64_t* row_in; // optional (device): row r starts at in + row_in[r] ...
+  const int* row_N;      //   ... and has row_N[r] samples (rows of different lengths in one launch)
 };
 
 bool spec_supported(int Nz);
