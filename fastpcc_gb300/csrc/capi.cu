@@ -78,7 +78,6 @@ struct fpcc_ctx {
   std::map<int, float2*> twiddles;   // device tables exp(-2 pi i t/n), per n
   std::map<int, float2*> bluestein;  // per window length N: M-point filter spectra, forward then inverse
   std::map<int, double2*> twiddles64;   // FP64 tables exp(-2 pi i t/n)
-  std::map<int, double2*> bluestein64;  // FP64 filter spectra per N, forward then inverse
   std::map<int, float4*> twiddles_df;   // double-float tables exp(-2 pi i t/n)
   // filter spectra of the packed path per (N, M, fp64): forward then inverse, M values each,
   // held in blocks of one batched computation
@@ -228,7 +227,6 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
   for (auto& kv : c->twiddles) ctx_free(c, kv.second);
   for (auto& kv : c->bluestein) ctx_free(c, kv.second);
   for (auto& kv : c->twiddles64) ctx_free(c, kv.second);
-  for (auto& kv : c->bluestein64) ctx_free(c, kv.second);
   for (auto& kv : c->twiddles_df) ctx_free(c, kv.second);
   for (void* b : c->multi_blocks) ctx_free(c, b);
   cudaStreamSynchronize(c->stream);
@@ -607,38 +605,8 @@ int passes_df(fpcc_ctx* c, float4* A, float4* B, int n, int nrows, int dir, floa
   return 0;
 }
 
-// DFT_N (dir) of nrows FP64 rows of stride N in D, in place, by Bluestein
-// transforms of length M on the buffers A and B.
-int bluestein64(fpcc_ctx* c, double2* D, double2* A, double2* B, int N, int M, int nrows, int dir) {
-  double2* F = nullptr;
-  auto it = c->bluestein64.find(N);
-  if (it == c->bluestein64.end()) {
-    CK(ctx_alloc(c, (void**)&F, (size_t)2 * M * sizeof(double2)));
-    for (int d = 0; d < 2; d++) {
-      double2* f = F + (size_t)d * M;
-      CK(launch_blue_filter64(f, N, M, d ? +1 : -1, c->stream));
-      double2* r = nullptr;
-      int rc = passes64(c, f, B, M, 1, -1, &r);
-      if (rc) { ctx_free(c, F); return rc; }
-      if (r != f) CK(cudaMemcpyAsync(f, r, (size_t)M * sizeof(double2), cudaMemcpyDeviceToDevice, c->stream));
-    }
-    c->bluestein64[N] = F;
-  } else {
-    F = it->second;
-  }
-  CK(launch_blue_pre64(D, N, A, N, M, dir, nrows, c->stream));
-  double2* r1 = nullptr;
-  int rc = passes64(c, A, B, M, nrows, -1, &r1);
-  if (rc) return rc;
-  CK(launch_blue_mul64(r1, F + (size_t)(dir > 0 ? 1 : 0) * M, M, nrows, c->stream));
-  double2* r2 = nullptr;
-  if ((rc = passes64(c, r1, r1 == A ? B : A, M, nrows, +1, &r2))) return rc;
-  CK(launch_blue_post64(r2, M, D, N, N, dir, nrows, c->stream));
-  g_launches += 3;
-  return 0;
-}
-
-// Rows whose analytic signals are to be computed in FP64 under the context's mode.
+// Rows whose analytic signals are to be computed in more than FP32 (double-float)
+// under the context's mode.
 int precise_rows(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, std::vector<int>* rows) {
   rows->clear();
   if (c->precision == FPCC_ANALYTIC_F32 || nrows <= 0) return 0;
@@ -659,47 +627,25 @@ int precise_rows(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, s
   return 0;
 }
 
+template <typename T>
+int multi_group(fpcc_ctx* c, std::vector<MultiRow>& rows, int M);
+int conv_class_len(int N);
+
 // Overwrites the listed rows of the FP32 analytic signals `an` (stride ldan)
-// with FP64 analytic signals of the same rows of x, rounded to float2.
+// with analytic signals of the same rows of x computed in double-float (the
+// packed convolution stage: about 44 significant bits on the FP32 pipes),
+// rounded to float2.
 int refine_analytic(fpcc_ctx* c, const float* d_x, int64_t ldx, int N, const std::vector<int>& rows, float2* an,
                     int64_t ldan) {
   if (rows.empty()) return 0;
-  const bool smooth = !radices64(N).empty();
-  const int M = smooth ? N : smooth_at_least(2 * N - 1);
-  const size_t per_row = (size_t)N * sizeof(double2) + (smooth ? (size_t)N : (size_t)2 * M) * sizeof(double2);
-  int chunk = (int)std::max<size_t>(1, ((size_t)512 << 20) / per_row);
-  if (chunk > 65535) chunk = 65535;
-  if (chunk > (int)rows.size()) chunk = (int)rows.size();
-  void *D, *A, *B, *ridx;
-  int rc;
-  if ((rc = dev_buf(c, S_P64_D, (size_t)chunk * N * sizeof(double2), &D)) ||
-      (rc = dev_buf(c, S_P64_A, (size_t)chunk * M * sizeof(double2), &A)) ||
-      (rc = dev_buf(c, S_P64_B, (size_t)chunk * M * sizeof(double2), &B)) ||
-      (rc = dev_buf(c, S_P64_CNT, rows.size() * sizeof(int), &ridx)))
-    return rc;
-  CK(cudaMemcpyAsync(ridx, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-  for (size_t r0 = 0; r0 < rows.size(); r0 += chunk) {
-    const int n = (int)std::min<size_t>(chunk, rows.size() - r0);
-    const int* ri = (const int*)ridx + r0;
-    double2* d = (double2*)D;
-    if (smooth) {
-      CK(launch_gather64(d_x, ldx, ri, n, N, N, (double2*)A, c->stream));
-      double2* r1 = nullptr;
-      if ((rc = passes64(c, (double2*)A, (double2*)B, N, n, -1, &r1))) return rc;
-      CK(launch_mask64(r1, N, n, c->stream));
-      double2* r2 = nullptr;
-      if ((rc = passes64(c, r1, r1 == (double2*)A ? (double2*)B : (double2*)A, N, n, +1, &r2))) return rc;
-      d = r2;
-    } else {
-      CK(launch_gather64(d_x, ldx, ri, n, N, N, d, c->stream));
-      if ((rc = bluestein64(c, d, (double2*)A, (double2*)B, N, M, n, -1))) return rc;
-      CK(launch_mask64(d, N, n, c->stream));
-      if ((rc = bluestein64(c, d, (double2*)A, (double2*)B, N, M, n, +1))) return rc;
-    }
-    CK(launch_store64(d, N, ri, n, N, an, ldan, c->stream));
-    g_launches += 3;
+  std::vector<MultiRow> mr(rows.size());
+  for (size_t i = 0; i < rows.size(); i++) {
+    mr[i] = MultiRow{};
+    mr[i].x = d_x + (int64_t)rows[i] * ldx;
+    mr[i].out = an + (int64_t)rows[i] * ldan;
+    mr[i].N = N;
   }
-  return 0;
+  return multi_group<float4>(c, mr, conv_class_len(N));
 }
 
 // Analytic signal for window lengths with a prime factor above 5, by Bluestein

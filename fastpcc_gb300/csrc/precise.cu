@@ -120,73 +120,6 @@ __global__ void k_gather64(const float* __restrict__ x, int64_t ldx, const int* 
     dst[n] = make_double2(n < N ? (double)__ldg(src + n) : 0.0, 0.0);
 }
 
-__global__ void k_mask64(double2* a, int n) {
-  double2* r = a + (int64_t)blockIdx.y * n;
-  const double d = 1.0 / (double)n;
-  const int half = (n + 1) >> 1;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    double f;
-    if (k == 0) f = d;
-    else if (k < half) f = 2.0 * d;
-    else if (!(n & 1) && k == (n >> 1)) f = d;
-    else f = 0.0;
-    r[k] = dscale(r[k], f);
-  }
-}
-
-// exp(dir i pi n^2 / N), the argument reduced exactly: n^2 mod 2N.
-__device__ __forceinline__ double2 chirp64(int n, int N, int dir) {
-  const long long q = ((long long)n * (long long)n) % (2LL * N);
-  double s, c;
-  sincospi((double)q / (double)N, &s, &c);
-  return make_double2(c, dir * s);
-}
-
-__global__ void k_blue_pre64(const double2* __restrict__ in, int64_t ldin, double2* __restrict__ a, int N, int M,
-                             int dir) {
-  const int r = blockIdx.y;
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < M; n += gridDim.x * blockDim.x)
-    a[(int64_t)r * M + n] = (n < N) ? dmul(in[(int64_t)r * ldin + n], chirp64(n, N, dir)) : make_double2(0.0, 0.0);
-}
-
-__global__ void k_blue_mul64(double2* a, const double2* __restrict__ B, int M) {
-  const int r = blockIdx.y;
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < M; n += gridDim.x * blockDim.x)
-    a[(int64_t)r * M + n] = dmul(a[(int64_t)r * M + n], B[n]);
-}
-
-__global__ void k_blue_post64(const double2* __restrict__ a, int M, double2* __restrict__ out, int64_t ldo, int N,
-                              int dir) {
-  const int r = blockIdx.y;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x)
-    out[(int64_t)r * ldo + k] = dmul(a[(int64_t)r * M + k], chirp64(k, N, dir));
-}
-
-__global__ void k_blue_filter64(double2* b, int N, int M, int dir) {
-  const double inv = 1.0 / (double)M;
-  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-    int t = -1;
-    if (m < N) t = m;
-    else if (m > M - N) t = M - m;
-    double2 v = make_double2(0.0, 0.0);
-    if (t >= 0) {
-      const double2 c = chirp64(t, N, dir);
-      v = make_double2(c.x * inv, -c.y * inv);
-    }
-    b[m] = v;
-  }
-}
-
-__global__ void k_store64(const double2* __restrict__ a, int64_t lda, const int* __restrict__ rows, int N,
-                          float2* __restrict__ out, int64_t ldo) {
-  const int r = blockIdx.y;
-  float2* dst = out + (int64_t)rows[r] * ldo;
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
-    const double2 v = a[(int64_t)r * lda + n];
-    dst[n] = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
-  }
-}
-
 dim3 rows_grid(int len, int nrows) {
   int gx = (len + 255) / 256;
   if (gx > 64) gx = 64;
@@ -237,51 +170,6 @@ cudaError_t launch_pass64(int R, int dir, const double2* in, double2* out, int n
   FPCC_P64(5)
 #undef FPCC_P64
   return cudaErrorInvalidValue;
-}
-
-cudaError_t launch_mask64(double2* a, int n, int nrows, cudaStream_t st) {
-  if (nrows <= 0) return cudaSuccess;
-  if (nrows > 65535) return cudaErrorInvalidValue;
-  k_mask64<<<rows_grid(n, nrows), 256, 0, st>>>(a, n);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_blue_pre64(const double2* in, int64_t ldin, double2* a, int N, int M, int dir, int nrows,
-                              cudaStream_t st) {
-  if (nrows <= 0) return cudaSuccess;
-  if (nrows > 65535) return cudaErrorInvalidValue;
-  k_blue_pre64<<<rows_grid(M, nrows), 256, 0, st>>>(in, ldin, a, N, M, dir);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_blue_mul64(double2* a, const double2* B, int M, int nrows, cudaStream_t st) {
-  if (nrows <= 0) return cudaSuccess;
-  if (nrows > 65535) return cudaErrorInvalidValue;
-  k_blue_mul64<<<rows_grid(M, nrows), 256, 0, st>>>(a, B, M);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_blue_post64(const double2* a, int M, double2* out, int64_t ldo, int N, int dir, int nrows,
-                               cudaStream_t st) {
-  if (nrows <= 0) return cudaSuccess;
-  if (nrows > 65535) return cudaErrorInvalidValue;
-  k_blue_post64<<<rows_grid(N, nrows), 256, 0, st>>>(a, M, out, ldo, N, dir);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_blue_filter64(double2* b, int N, int M, int dir, cudaStream_t st) {
-  int gx = (M + 255) / 256;
-  if (gx > 1024) gx = 1024;
-  k_blue_filter64<<<gx, 256, 0, st>>>(b, N, M, dir);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_store64(const double2* a, int64_t lda, const int* rows, int nsel, int N, float2* out,
-                           int64_t ldo, cudaStream_t st) {
-  if (nsel <= 0) return cudaSuccess;
-  if (nsel > 65535) return cudaErrorInvalidValue;
-  k_store64<<<rows_grid(N, nsel), 256, 0, st>>>(a, lda, rows, N, out, ldo);
-  return cudaGetLastError();
 }
 
 }  // namespace fpcc
