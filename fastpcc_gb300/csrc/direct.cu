@@ -114,15 +114,22 @@ __device__ __forceinline__ float2 phase_at(const void* row, int n) {
   }
 }
 
-template <int MODE, int FMT>   // MODE 1: v = 1, 2: v = 2, 0: general power
+// S threads per lag (S = 1: one lag per thread, 256 lags per block; S = 4: 64
+// lags per block, each lag's tile sum split over 4 threads and their FP64
+// partial sums added in a fixed order), so a block's duration is N / S tiles of
+// work: long windows no longer make a few very long blocks.
+template <int MODE, int FMT, int S>   // MODE 1: v = 1, 2: v = 2, 0: general power
 __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
+  constexpr int LB = kLagBlock / S;               // lags per block
   __shared__ float2 s1[kTile];
-  __shared__ float2 s2[kTile + kLagBlock];
+  __shared__ float2 s2[kTile + LB];
+  __shared__ double red[S > 1 ? kLagBlock : 1];
   // grid (lag blocks, pairs): blocks are issued pair by pair, so descriptors
   // ordered by decreasing window length start the longest blocks first
   const int p = blockIdx.y;
-  const int lblk = blockIdx.x * kLagBlock;       // first lag index of the block
-  const int l = lblk + threadIdx.x;
+  const int sub = threadIdx.x / LB, li = threadIdx.x - sub * LB;
+  const int lblk = blockIdx.x * LB;               // first lag index of the block
+  const int l = lblk + li;
   int N, Lag1, L;
   const void* R1;
   const void* R2;
@@ -150,7 +157,7 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
   const float V = 0.5f * a.v;
   double acc = 0.0;
   // samples n of station 1 that overlap any lag of the block
-  int nlo = -(lagb + kLagBlock - 1);
+  int nlo = -(lagb + LB - 1);
   if (nlo < 0) nlo = 0;
   int nhi = N - lagb;
   if (nhi > N) nhi = N;
@@ -161,7 +168,7 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
       if (n < N) v = phase_at<FMT>(R1, n);
       s1[i] = v;
     }
-    for (int i = threadIdx.x; i < kTile + kLagBlock; i += kLagBlock) {
+    for (int i = threadIdx.x; i < kTile + LB; i += kLagBlock) {
       const int n = n0 + lagb + i;
       float2 v = make_float2(0.f, 0.f);
       if (n >= 0 && n < N) v = phase_at<FMT>(R2, n);
@@ -169,9 +176,10 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
     }
     __syncthreads();
     float part = 0.0f;
-    const float2* b = s2 + threadIdx.x;
+    const float2* b = s2 + li;
+    constexpr int span = kTile / S;
 #pragma unroll 8
-    for (int i = 0; i < kTile; i++) {
+    for (int i = sub * span; i < (sub + 1) * span; i++) {
       const float2 u = s1[i];
       const float2 w = b[i];
       const float sx = u.x + w.x, sy = u.y + w.y;
@@ -184,6 +192,14 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
     }
     acc += (double)part;
     __syncthreads();
+  }
+  if constexpr (S > 1) {
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (sub != 0) return;
+    acc = red[li];
+#pragma unroll
+    for (int s = 1; s < S; s++) acc += red[s * LB + li];
   }
   if (l < L) {
     const int lag = Lag1 + l;
@@ -287,7 +303,11 @@ cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st) {
   if (a.npairs <= 0 || a.L <= 0) return cudaSuccess;
   if (a.half < 0 || a.half > 2) return cudaErrorInvalidValue;
   const int mode = (a.v == 1.0f) ? 1 : (a.v == 2.0f ? 2 : 0);
-  const int lb = (a.L + kLagBlock - 1) / kLagBlock;
+  // packed launches (windows of any lengths) split each lag over 4 threads; the
+  // choice depends on the launch form only, so a request's result does not
+  // depend on the other windows in its launch
+  const bool split = a.desc != nullptr;
+  const int lb = (a.L + (split ? kLagBlock / 4 : kLagBlock) - 1) / (split ? kLagBlock / 4 : kLagBlock);
   for (int p0 = 0; p0 < a.npairs; p0 += 65535) {   // grid.y holds at most 65535 pairs
     PccvArgs b = a;
     b.npairs = a.npairs - p0 < 65535 ? a.npairs - p0 : 65535;
@@ -298,16 +318,19 @@ cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st) {
       b.y = a.y + (int64_t)p0 * a.ldy;
     }
     const dim3 grid(lb, b.npairs);
-#define FPCC_PCCV_FMT(F)                                                  \
-    if (a.half == F) {                                                    \
-      if (mode == 1) k_pccv<1, F><<<grid, kLagBlock, 0, st>>>(b);         \
-      else if (mode == 2) k_pccv<2, F><<<grid, kLagBlock, 0, st>>>(b);    \
-      else k_pccv<0, F><<<grid, kLagBlock, 0, st>>>(b);                   \
+#define FPCC_PCCV_S(F, SS)                                                    \
+    if (mode == 1) k_pccv<1, F, SS><<<grid, kLagBlock, 0, st>>>(b);           \
+    else if (mode == 2) k_pccv<2, F, SS><<<grid, kLagBlock, 0, st>>>(b);      \
+    else k_pccv<0, F, SS><<<grid, kLagBlock, 0, st>>>(b);
+#define FPCC_PCCV_FMT(F)                                                      \
+    if (a.half == F) {                                                        \
+      if (split) { FPCC_PCCV_S(F, 4) } else { FPCC_PCCV_S(F, 1) }             \
     }
     FPCC_PCCV_FMT(0)
     FPCC_PCCV_FMT(1)
     FPCC_PCCV_FMT(2)
 #undef FPCC_PCCV_FMT
+#undef FPCC_PCCV_S
   }
   return cudaGetLastError();
 }
