@@ -325,7 +325,8 @@ enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_
             S_WP_Y = 13, S_WP_STAGE = 14, S_BLUE_O = 23, S_P64_D = 24, S_P64_A = 25, S_P64_B = 26,
             S_P64_CNT = 27, S_I16_Q = 28, S_MULTI_A = 29, S_MULTI_B = 30, S_MULTI_AN = 31, S_EPART = 32,
             S_CONV_X = 33, S_CONV_Y = 34, S_STK_SPEC = 35, S_STK_A = 36, S_STK_B = 37, S_STK_X = 38,
-            S_STK_T = 39, S_STK_T2 = 40, S_STK_Y = 41, S_STK_Y2 = 42, S_STK_R = 43, S_STK_AN = 44 };
+            S_STK_T = 39, S_STK_T2 = 40, S_STK_Y = 41, S_STK_Y2 = 42, S_STK_R = 43, S_STK_AN = 44,
+            S_HK_TAB = 45 };
 
 constexpr size_t kLargeChunkBytes = size_t(512) << 20;   // four-step intermediate per chunk
 
@@ -794,18 +795,21 @@ constexpr size_t kMultiFilterCache = (size_t)4 << 30;   // bytes of cached filte
 
 // Kernel spectra H_N = FFT_M(kernel) / M of every window length in Ns, for
 // transforms of M points in precision T; returns a device pointer per entry of
-// Ns.  New lengths are computed together in FP64 (their kernels as rows of one
-// batched transform), rounded to T and cached in blocks; the cache is emptied
-// first when it would grow past kMultiFilterCache.
+// Ns.  The spectra are real (float for T = float2, double-float float2 for
+// T = float4).  New lengths are computed together, two kernels per row of one
+// batched double-float transform (launch_hk_rows), and cached in blocks; the
+// cache is emptied first when it would grow past kMultiFilterCache.
 template <typename T>
 int multi_filters(fpcc_ctx* c, const std::vector<int>& Ns, int M, std::vector<const void*>& filt) {
-  const int f64 = sizeof(T) == 16;
+  constexpr bool dfl = std::is_same<T, float4>::value;
+  constexpr size_t hsz = dfl ? sizeof(float2) : sizeof(float);
+  const int f64 = dfl ? 1 : 0;
   std::vector<int> missing;
   for (int N : Ns)
     if (!c->multi_filters.count(std::make_tuple(N, M, f64)) &&
         std::find(missing.begin(), missing.end(), N) == missing.end())
       missing.push_back(N);
-  const size_t need = missing.size() * (size_t)M * sizeof(T);
+  const size_t need = missing.size() * (size_t)M * hsz;
   if (need && c->multi_filter_bytes + need > kMultiFilterCache && c->multi_filter_bytes) {
     for (void* b : c->multi_blocks) ctx_free(c, b);   // in stream order: later work cannot read them
     c->multi_blocks.clear();
@@ -815,35 +819,33 @@ int multi_filters(fpcc_ctx* c, const std::vector<int>& Ns, int M, std::vector<co
     for (int N : Ns)
       if (std::find(missing.begin(), missing.end(), N) == missing.end()) missing.push_back(N);
   }
-  // lengths per batch: at most 64, and FP64 work buffers of at most 256 MB each
-  const size_t per = std::max<size_t>(1, std::min<size_t>(64, ((size_t)256 << 20) / ((size_t)M * sizeof(double2))));
+  // lengths per batch: at most 128, and transform buffers of at most 256 MB each
+  const size_t rows_max = std::max<size_t>(1, ((size_t)256 << 20) / ((size_t)M * sizeof(float4)));
+  const size_t per = std::min<size_t>(128, 2 * rows_max);
+  const int ldt = hk_table_len(M);
   for (size_t i0 = 0; i0 < missing.size(); i0 += per) {
     const int n = (int)std::min<size_t>(per, missing.size() - i0);
+    const int rows = (n + 1) / 2;
     const std::vector<int> lens(missing.begin() + i0, missing.begin() + i0 + n);
-    void *B, *A, *dN;
+    void *B, *A, *dN, *tab;
     int rc;
-    if ((rc = dev_buf(c, S_MULTI_B, (size_t)n * M * sizeof(double2), &B)) ||
-        (rc = dev_buf(c, S_MULTI_A, (size_t)n * M * sizeof(double2), &A)) ||
-        (rc = dev_buf(c, S_P64_CNT, (size_t)n * sizeof(int), &dN)))
+    if ((rc = dev_buf(c, S_MULTI_B, (size_t)rows * M * sizeof(float4), &B)) ||
+        (rc = dev_buf(c, S_MULTI_A, (size_t)rows * M * sizeof(float4), &A)) ||
+        (rc = dev_buf(c, S_P64_CNT, (size_t)n * sizeof(int), &dN)) ||
+        (rc = dev_buf(c, S_HK_TAB, (size_t)n * ldt * sizeof(double2), &tab)))
       return rc;
     CK(cudaMemcpyAsync(dN, lens.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    CK(launch_multi_hkernel((const int*)dN, n, (double2*)B, M, c->stream));
+    CK(launch_hk_rows((const int*)dN, n, (double2*)tab, (float4*)A, M, c->stream));
     void* block = nullptr;
-    CK(ctx_alloc(c, &block, (size_t)n * M * sizeof(T)));
+    CK(ctx_alloc(c, &block, (size_t)n * M * hsz));
     c->multi_blocks.push_back(block);
-    c->multi_filter_bytes += (size_t)n * M * sizeof(T);
-    // the kernel values (FP64) split into double-floats and transformed in
-    // double-float, then kept as double-floats or rounded to float2
-    CK(launch_df_from_double((const double2*)B, (float4*)A, n * M, c->stream));
+    c->multi_filter_bytes += (size_t)n * M * hsz;
     float4* r = nullptr;
-    if ((rc = passes_df(c, (float4*)A, (float4*)B, M, n, -1, &r))) return rc;
-    if constexpr (std::is_same<T, float4>::value)
-      CK(cudaMemcpyAsync(block, r, (size_t)n * M * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
-    else
-      CK(launch_df_to_float2(r, (float2*)block, n * M, c->stream));
-    g_launches += 2;
+    if ((rc = passes_df(c, (float4*)A, (float4*)B, M, rows, -1, &r))) return rc;
+    CK(launch_hk_extract(r, n, M, dfl, block, c->stream));
+    g_launches += 3;
     for (int j = 0; j < n; j++)
-      c->multi_filters[std::make_tuple(lens[j], M, f64)] = (char*)block + (size_t)j * M * sizeof(T);
+      c->multi_filters[std::make_tuple(lens[j], M, f64)] = (char*)block + (size_t)j * M * hsz;
   }
   filt.resize(Ns.size());
   for (size_t i = 0; i < Ns.size(); i++) filt[i] = c->multi_filters.at(std::make_tuple(Ns[i], M, f64));

@@ -29,19 +29,94 @@ __device__ __forceinline__ float4 cvt<float4>(double2 v) {
   return dfc(df_from_double(v.x), df_from_double(v.y));
 }
 
-// Im h(n), 0 < n < N, of h = IDFT_N(mask): for even N, (2/N) cot(pi n / N) at
-// odd n and 0 at even n; for odd N, (1/N) (cos(pi n/N) - (-1)^n) / sin(pi n/N),
-// written with half angles as cot(pi n / 2N) / N at odd n and -tan(pi n / 2N) / N
-// at even n (no cancellation; the angles lie in (0, pi/2)).
-__device__ __forceinline__ double hilbert_im(int n, int N) {
-  double s, c;
-  if (N & 1) {
-    sincospi((double)n / (2.0 * (double)N), &s, &c);
-    return (n & 1) ? c / (s * (double)N) : -s / (c * (double)N);
+// Im h(n), 0 < n < N, of h = IDFT_N(mask) has closed forms: for even N,
+// (2/N) cot(pi n / N) at odd n and 0 at even n; for odd N, cot(pi n / 2N) / N at
+// odd n and -tan(pi n / 2N) / N at even n.  Each is +-f cot(pi m / D) with m odd
+// and m <= D / 2 (D = N for even N, 2N for odd N): m = n or N - n, using
+// cot(pi - a) = -cot(a) and tan(a) = cot(pi/2 - a).  The angle pi m / D, in the
+// first quadrant, is the sum of pi 256 a / D and pi b / D (m = 256 a + b), whose
+// sines and cosines come from FP64 tables (k_hk_tables); then
+// sin = sa cb + ca sb has no cancellation, so small sines keep their relative
+// precision, and cot = cos / sin.
+__global__ void k_hk_tables(const int* __restrict__ Ns, int nk, double2* T, int ldt) {
+  const int k = blockIdx.y;
+  if (k >= nk) return;
+  const int N = Ns[k];
+  const int D = (N & 1) ? 2 * N : N;
+  const int nt = 256 + D / 512 + 1;
+  double2* t = T + (int64_t)k * ldt;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
+    const double num = i < 256 ? (double)i : 256.0 * (double)(i - 256);
+    double sn, cs;
+    sincospi(num / (double)D, &sn, &cs);
+    t[i] = make_double2(cs, sn);
   }
-  if (!(n & 1)) return 0.0;
-  sincospi((double)n / (double)N, &s, &c);
-  return 2.0 * c / (s * (double)N);
+}
+
+// f * Im h(n) * N / (1 or 2), i.e. Im h(n) times the row factor f / (2/N or 1/N)
+__device__ __forceinline__ double hk_value(int n, int N, const double2* __restrict__ t, double f) {
+  int m;
+  bool neg;
+  if (N & 1) {
+    neg = !(n & 1);
+    m = neg ? N - n : n;
+  } else {
+    if (!(n & 1)) return 0.0;
+    neg = 2 * n > N;
+    m = neg ? N - n : n;
+  }
+  const double2 cb = __ldg(t + (m & 255)), ca = __ldg(t + 256 + (m >> 8));
+  const double sn = fma(ca.y, cb.x, ca.x * cb.y);
+  const double cs = fma(ca.x, cb.x, -(ca.y * cb.y));
+  const double v = f * (cs / sn);
+  return neg ? -v : v;
+}
+
+// Rows of two kernels each (lengths Ns[2j] and Ns[2j+1]; none for the second
+// when nk is odd), double-float: B[j][m] = g_A[m] + i g_B[m] with
+// g_N[m] = Im h(m) / M (0 < m < N), g_N[M - m] = -g_N[m], 0 elsewhere.
+__global__ void k_hk_rows(const int* __restrict__ Ns, int nk, const double2* __restrict__ T, int ldt, float4* B,
+                          int M) {
+  const int j = blockIdx.y;
+  const int NA = Ns[2 * j], NB = (2 * j + 1 < nk) ? Ns[2 * j + 1] : 0;
+  const double2* tA = T + (int64_t)(2 * j) * ldt;
+  const double2* tB = tA + ldt;
+  const double fA = ((NA & 1) ? 1.0 : 2.0) / ((double)NA * (double)M);
+  const double fB = NB ? ((NB & 1) ? 1.0 : 2.0) / ((double)NB * (double)M) : 0.0;
+  float4* row = B + (int64_t)j * M;
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m <= M / 2; m += gridDim.x * blockDim.x) {
+    const double a = (m > 0 && m < NA) ? hk_value(m, NA, tA, fA) : 0.0;
+    const double b = (m > 0 && m < NB) ? hk_value(m, NB, tB, fB) : 0.0;
+    row[m] = dfc(df_from_double(a), df_from_double(b));
+    if (m > 0 && M - m != m) row[M - m] = dfc(df_from_double(-a), df_from_double(-b));
+  }
+}
+
+// g_N is real and odd, so FFT_M(g_N) = -i S_N with S_N real, and the kernel
+// spectrum is H_N = 1/M + S_N (real; the 1/M is the transform of the delta at
+// 0).  A transformed row Z = FFT(g_A + i g_B) = S_B - i S_A gives
+// H_A = 1/M - Im Z and H_B = 1/M + Re Z: double-float reals (float2 hi, lo)
+// or rounded to float.
+template <bool DF>
+__global__ void k_hk_extract(const float4* __restrict__ Z, int nk, int M, void* out) {
+  const int j = blockIdx.y;
+  const bool two = 2 * j + 1 < nk;
+  const df c = df_from_double(1.0 / (double)M);
+  const float4* z = Z + (int64_t)j * M;
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+    const float4 v = z[m];
+    const df ha = df_sub(c, df_im(v));
+    const df hb = df_add(c, df_re(v));
+    if constexpr (DF) {
+      float2* o = reinterpret_cast<float2*>(out);
+      o[(int64_t)(2 * j) * M + m] = make_float2(ha.hi, ha.lo);
+      if (two) o[(int64_t)(2 * j + 1) * M + m] = make_float2(hb.hi, hb.lo);
+    } else {
+      float* o = reinterpret_cast<float*>(out);
+      o[(int64_t)(2 * j) * M + m] = df_to_float(ha);
+      if (two) o[(int64_t)(2 * j + 1) * M + m] = df_to_float(hb);
+    }
+  }
 }
 
 __global__ void __launch_bounds__(256) k_multi_exp(MultiRow* rows) {
@@ -85,8 +160,8 @@ __global__ void k_multi_split(const MultiRow* __restrict__ rows, int nrows, cons
   const int j = blockIdx.y;
   const bool two = 2 * j + 1 < nrows;
   const T* z = Z + (int64_t)j * M;
-  const T* H0 = reinterpret_cast<const T*>(rows[2 * j].filt);
-  const T* H1 = two ? reinterpret_cast<const T*>(rows[2 * j + 1].filt) : nullptr;
+  const S* H0 = reinterpret_cast<const S*>(rows[2 * j].filt);
+  const S* H1 = two ? reinterpret_cast<const S*>(rows[2 * j + 1].filt) : nullptr;
   T* b0 = B + (int64_t)(2 * j) * M;
   T* b1 = B + (int64_t)(2 * j + 1) * M;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
@@ -94,10 +169,12 @@ __global__ void k_multi_split(const MultiRow* __restrict__ rows, int nrows, cons
     const T q = z[m == 0 ? 0 : M - m];
     // X0 = (Z[m] + conj Z[-m]) / 2,  X1 = (Z[m] - conj Z[-m]) / 2i
     const T x0 = mk((p.x + q.x) * (S)0.5, (p.y - q.y) * (S)0.5, (T*)nullptr);
-    b0[m] = mul(x0, H0[m]);
+    const S h0 = H0[m];
+    b0[m] = mk(x0.x * h0, x0.y * h0, (T*)nullptr);
     if (two) {
       const T x1 = mk((p.y + q.y) * (S)0.5, (q.x - p.x) * (S)0.5, (T*)nullptr);
-      b1[m] = mul(x1, H1[m]);
+      const S h1 = H1[m];
+      b1[m] = mk(x1.x * h1, x1.y * h1, (T*)nullptr);
     }
   }
 }
@@ -110,25 +187,6 @@ __global__ void k_multi_store(const MultiRow* __restrict__ rows, const T* A, int
     const T v = a[k];
     r.out[k] = (r.e == kNoSignal) ? make_float2(0.0f, 0.0f)
                                   : make_float2(scalbnf((float)v.x, r.e), scalbnf((float)v.y, r.e));
-  }
-}
-
-__global__ void k_multi_hkernel(const int* __restrict__ Ns, double2* B, int M) {
-  const int N = Ns[blockIdx.y];
-  double2* b = B + (int64_t)blockIdx.y * M;
-  const double inv = 1.0 / (double)M;
-  // the kernel is odd (Im h(N - e) = -Im h(e)), so each value also fills its
-  // mirror entry M - e; entries above M - N are written by their mirror
-  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m <= M - N; m += gridDim.x * blockDim.x) {
-    if (m == 0) {
-      b[0] = make_double2(inv, 0.0);
-    } else if (m < N) {
-      const double v = hilbert_im(m, N) * inv;
-      b[m] = make_double2(0.0, v);
-      b[M - m] = make_double2(0.0, -v);
-    } else {
-      b[m] = make_double2(0.0, 0.0);
-    }
   }
 }
 
@@ -159,8 +217,8 @@ __global__ void k_multi_split_df(const MultiRow* __restrict__ rows, int nrows, c
   const int j = blockIdx.y;
   const bool two = 2 * j + 1 < nrows;
   const float4* z = Z + (int64_t)j * M;
-  const float4* H0 = reinterpret_cast<const float4*>(rows[2 * j].filt);
-  const float4* H1 = two ? reinterpret_cast<const float4*>(rows[2 * j + 1].filt) : nullptr;
+  const float2* H0 = reinterpret_cast<const float2*>(rows[2 * j].filt);
+  const float2* H1 = two ? reinterpret_cast<const float2*>(rows[2 * j + 1].filt) : nullptr;
   float4* b0 = B + (int64_t)(2 * j) * M;
   float4* b1 = B + (int64_t)(2 * j + 1) * M;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
@@ -169,10 +227,12 @@ __global__ void k_multi_split_df(const MultiRow* __restrict__ rows, int nrows, c
     // X0 = (Z[m] + conj Z[-m]) / 2,  X1 = (Z[m] - conj Z[-m]) / 2i
     const df pr = df_re(p), pi = df_im(p), qr = df_re(q), qi = df_im(q);
     const float4 x0 = dfc(df_scale2(df_add(pr, qr), 0.5f), df_scale2(df_sub(pi, qi), 0.5f));
-    b0[m] = dfc_mul(x0, H0[m]);
+    const float2 h0 = H0[m];
+    b0[m] = dfc_mul_r(x0, df{h0.x, h0.y});
     if (two) {
       const float4 x1 = dfc(df_scale2(df_add(pi, qi), 0.5f), df_scale2(df_sub(qr, pr), 0.5f));
-      b1[m] = dfc_mul(x1, H1[m]);
+      const float2 h1 = H1[m];
+      b1[m] = dfc_mul_r(x1, df{h1.x, h1.y});
     }
   }
 }
@@ -426,10 +486,22 @@ cudaError_t launch_multi_store(const MultiRow* rows, int nrows, const T* A, int 
   k_multi_store<T><<<grid2(M / 2, nrows), 256, 0, st>>>(rows, A, M);
   return cudaGetLastError();
 }
-cudaError_t launch_multi_hkernel(const int* Ns, int nrows, double2* B, int M, cudaStream_t st) {
-  if (nrows <= 0) return cudaSuccess;
-  if (nrows > 65535) return cudaErrorInvalidValue;
-  k_multi_hkernel<<<grid2(M, nrows), 256, 0, st>>>(Ns, B, M);
+int hk_table_len(int M) { return 256 + (M + 1) / 512 + 2; }
+
+cudaError_t launch_hk_rows(const int* Ns, int nk, double2* T, float4* B, int M, cudaStream_t st) {
+  if (nk <= 0) return cudaSuccess;
+  if (nk > 65535) return cudaErrorInvalidValue;
+  const int ldt = hk_table_len(M);
+  k_hk_tables<<<dim3((ldt + 255) / 256, nk), 256, 0, st>>>(Ns, nk, T, ldt);
+  k_hk_rows<<<grid2(M / 2 + 1, (nk + 1) / 2), 256, 0, st>>>(Ns, nk, T, ldt, B, M);
+  return cudaGetLastError();
+}
+cudaError_t launch_hk_extract(const float4* Z, int nk, int M, bool df_out, void* out, cudaStream_t st) {
+  if (nk <= 0) return cudaSuccess;
+  const int rows = (nk + 1) / 2;
+  if (rows > 65535) return cudaErrorInvalidValue;
+  if (df_out) k_hk_extract<true><<<grid2(M, rows), 256, 0, st>>>(Z, nk, M, out);
+  else k_hk_extract<false><<<grid2(M, rows), 256, 0, st>>>(Z, nk, M, out);
   return cudaGetLastError();
 }
 template <typename T>

@@ -8,12 +8,14 @@
 // N equals a circular convolution of any length M >= 2N - 1 with the kernel
 // laid out at offsets -(N-1)..(N-1), so windows whose lengths fall in the same
 // class of M (2^a, 3 2^a or 5 2^a) share every M-point pass; only the kernel
-// spectrum H_N = FFT_M(kernel) / M depends on each window's own N.  Two real
+// spectrum H_N = FFT_M(kernel) / M (real: the kernel is i times an odd real
+// sequence, plus the delta) depends on each window's own N.  Two real
 // windows share one forward transform (as the real and imaginary parts of one
 // complex row); their spectra are separated by Hermitian symmetry and each
 // multiplied by its own H_N before one inverse transform per window:
 //   A = x_2j + i x_2j+1;  A = FFT_M(A);  B_r = X_r * H_{N_r};  B = IFFT_M(B);  out = B[0, N)
-// 1.5 M-point transforms per window.  Each window enters its row scaled by
+// 1.5 M-point transforms per window, and half a transform per new window length
+// (two kernel spectra share one transform, launch_hk_rows).  Each window enters its row scaled by
 // 2^-e, e the binary exponent of its largest |sample|, and its analytic signal
 // leaves scaled by 2^e: exact in floating point, so results are unchanged, but
 // the two windows of a row have the same magnitude, and the split's rounding
@@ -32,7 +34,8 @@ namespace fpcc {
 struct MultiRow {
   const float* x;        // the window's samples (real)
   float2* out;           // its analytic signal, N values
-  const void* filt;      // H_N: M-point kernel spectrum (T) of the window length, including 1/M
+  const void* filt;      // H_N: M-point kernel spectrum of the window length, including 1/M; real
+                         // (float, or double-float as float2 hi, lo, for the double-float rows)
   int N;
   int e;                 // binary exponent of max |x| (set on the device by launch_multi_exp), kNoSignal if zero
 };
@@ -53,10 +56,15 @@ cudaError_t launch_multi_split(const MultiRow* rows, int nrows, const T* Z, T* B
 // out_r[k] = A[r][k], k < N_r (rounded to float2).
 template <typename T>
 cudaError_t launch_multi_store(const MultiRow* rows, int nrows, const T* A, int M, cudaStream_t st);
-// Kernel rows in FP64 before their forward transform: for window length Ns[r],
-// b[r][0] = 1/M, b[r][m] = i Im h(m) / M (0 < m < N), b[r][m] = i Im h(N - M + m) / M
-// (m > M - N), else 0.
-cudaError_t launch_multi_hkernel(const int* Ns, int nrows, double2* B, int M, cudaStream_t st);
+// Kernel spectra, two window lengths per M-point row.  launch_hk_rows writes
+// (nk + 1) / 2 double-float rows B[j] = g_A + i g_B for the lengths Ns[2j],
+// Ns[2j + 1] (g_N[m] = Im h(m) / M for 0 < m < N, g_N[M - m] = -g_N[m], else 0;
+// T: nk FP64 tables of hk_table_len(M) entries); after their forward transform Z,
+// launch_hk_extract writes the real spectra H_k = 1/M -+ (Im, Re) Z, kernel k at
+// out + k M (double-float float2 when df_out, else float).
+int hk_table_len(int M);
+cudaError_t launch_hk_rows(const int* Ns, int nk, double2* T, float4* B, int M, cudaStream_t st);
+cudaError_t launch_hk_extract(const float4* Z, int nk, int M, bool df_out, void* out, cudaStream_t st);
 // dst[i] = src[i] rounded to T (n values).
 template <typename T>
 cudaError_t launch_multi_convert(const double2* src, T* dst, int64_t n, cudaStream_t st);

@@ -145,6 +145,20 @@ struct WaveletCfg {
   int type = -1, rule = FPCC_AMP_D_REG, S = 0;
 };
 
+// A lane: a context of its own (stream, scratch, caches).  Station stages of
+// independent product classes run on the lanes in turn, so that the many small
+// per-length stages of a batch with uneven windows overlap on the GPU instead of
+// following one another on one stream.
+struct Lane {
+  fpcc_ctx* ctx = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  bool dirty = false;                   // work queued since the last join
+  void* d_tmp = nullptr; size_t n_tmp = 0;
+  void* d_idx = nullptr; size_t n_idx = 0;
+};
+constexpr int kLanes = 4;
+
 struct Server {
   int device = 0;
   size_t budget = 0, used = 0;
@@ -156,10 +170,23 @@ struct Server {
   std::map<std::tuple<int, int, int>, fpcc_wpcc_plan*> wplans;  // (N, Nz, cap)   [worker]
   cudaStream_t st = nullptr;
   fpcc_ctx* ctx = nullptr;
+  std::vector<Lane> lanes;
+  int next_lane = 0;
+  cudaEvent_t main_ev = nullptr;        // marks the server's stream for the lanes
   // device memory of slabs and scratch: a pool of the server's own whose freed
   // blocks stay mapped, allocated and freed in the order of the server's stream,
   // so growing a slab or releasing one needs no device synchronisation
   cudaMemPool_t pool = nullptr;
+  // small slabs are carved from larger pool blocks (chunks), so that a batch
+  // with many product classes (every window its own length) makes a few pool
+  // allocations instead of one per class; see slab_alloc
+  struct Chunk {
+    char* base;
+    size_t size, used;
+    std::map<size_t, size_t> free;   // offset -> length of each free range
+  };
+  std::vector<Chunk> chunks;
+  size_t chunk_bytes = 0;
   // host copies of registered windows
   std::mutex mu;
   std::condition_variable cv, cv_done;
@@ -234,6 +261,106 @@ void dfree(Server* s, void* p) {
   if (p) cudaFreeAsync(p, s->st);
 }
 
+// Lane work starts after everything queued on the server's stream so far (raw
+// window uploads, slab copies and frees), and the server's stream waits for all
+// lane work queued so far before it touches slab memory again (lanes_join):
+// before a pair stage, and before a slab is copied or freed.
+// Lane 0 takes the packed phase stages (its kernel spectrum cache stays warm);
+// the per-length stages go round the others.
+Lane& lane_begin(Server* s, bool packed = false) {
+  const size_t k = s->lanes.size();
+  Lane& l = (packed || k == 1) ? s->lanes[0] : s->lanes[1 + (size_t)(s->next_lane++) % (k - 1)];
+  cudaEventRecord(s->main_ev, s->st);
+  cudaStreamWaitEvent(l.st, s->main_ev, 0);
+  l.dirty = true;
+  return l;
+}
+
+void lanes_join(Server* s) {
+  for (auto& l : s->lanes)
+    if (l.dirty) {
+      cudaEventRecord(l.ev, l.st);
+      cudaStreamWaitEvent(s->st, l.ev, 0);
+      l.dirty = false;
+    }
+}
+
+// Scratch of a lane, allocated and freed in its own stream's order.
+void* lane_buf(Server* s, Lane& l, void** p, size_t* n, size_t need) {
+  if (*n < need) {
+    if (*p) cudaFreeAsync(*p, l.st);
+    *p = nullptr;
+    *n = 0;
+    const size_t nn = need + need / 2;
+    if (cudaMallocFromPoolAsync(p, nn, s->pool, l.st) != cudaSuccess) {
+      cudaGetLastError();
+      *p = nullptr;
+      return nullptr;
+    }
+    *n = nn;
+  }
+  return *p;
+}
+
+// Slab memory.  Blocks up to a quarter of a chunk come first-fit from the
+// chunks (256-byte granules); larger ones straight from the pool.  Every kernel
+// and copy that touches slab memory runs on the server's stream, so a range
+// freed here may be handed out again at once: its next user is queued after
+// every earlier reader, the ordering cudaFreeAsync gives on one stream.
+constexpr size_t kGranule = 256;
+
+void* slab_alloc(Server* s, size_t bytes) {
+  const size_t b = (bytes + kGranule - 1) & ~(kGranule - 1);
+  if (b > s->chunk_bytes / 4) return dalloc(s, bytes);
+  for (auto& c : s->chunks)
+    for (auto it = c.free.begin(); it != c.free.end(); ++it)
+      if (it->second >= b) {
+        const size_t off = it->first, len = it->second;
+        c.free.erase(it);
+        if (len > b) c.free[off + b] = len - b;
+        c.used += b;
+        return c.base + off;
+      }
+  char* base = (char*)dalloc(s, s->chunk_bytes);
+  if (!base) return nullptr;
+  Server::Chunk c{base, s->chunk_bytes, b, {}};
+  c.free[b] = s->chunk_bytes - b;
+  s->chunks.push_back(std::move(c));
+  return base;
+}
+
+void slab_free(Server* s, void* p, size_t bytes) {
+  if (!p) return;
+  lanes_join(s);
+  const size_t b = (bytes + kGranule - 1) & ~(kGranule - 1);
+  for (size_t i = 0; i < s->chunks.size(); i++) {
+    Server::Chunk& c = s->chunks[i];
+    if ((char*)p < c.base || (char*)p >= c.base + c.size) continue;
+    size_t off = (size_t)((char*)p - c.base), len = b;
+    auto nx = c.free.lower_bound(off);
+    if (nx != c.free.end() && nx->first == off + len) {   // merge with the next free range
+      len += nx->second;
+      nx = c.free.erase(nx);
+    }
+    if (nx != c.free.begin()) {                            // and with the previous one
+      auto pv = std::prev(nx);
+      if (pv->first + pv->second == off) {
+        off = pv->first;
+        len += pv->second;
+        c.free.erase(pv);
+      }
+    }
+    c.free[off] = len;
+    c.used -= b;
+    if (c.used == 0) {
+      dfree(s, c.base);
+      s->chunks.erase(s->chunks.begin() + i);
+    }
+    return;
+  }
+  dfree(s, p);
+}
+
 // Frees the least recently used slab (other than `keep`) none of whose rows a
 // batch in flight holds; its products are recomputed when next needed.
 bool release_idle_slab(Server* s, const Slab* keep) {
@@ -247,7 +374,7 @@ bool release_idle_slab(Server* s, const Slab* keep) {
     if (!victim || c.last_use < victim->last_use) victim = &c;
   }
   if (!victim) return false;
-  dfree(s, victim->base);
+  slab_free(s, victim->base, (size_t)victim->cap * victim->row_bytes);
   s->used -= (size_t)victim->cap * victim->row_bytes;
   victim->base = nullptr;
   victim->cap = 0;
@@ -270,12 +397,13 @@ bool grow(Server* s, Slab& sl, int need_rows) {
     if (!release_idle_slab(s, &sl)) return false;
   }
   const size_t add = (size_t)(ncap - sl.cap) * sl.row_bytes;
-  void* nb = dalloc(s, (size_t)ncap * sl.row_bytes);
+  void* nb = slab_alloc(s, (size_t)ncap * sl.row_bytes);
   if (!nb) return false;
   if (sl.base) {
     // queued kernels that read the old rows run before the copy and the free
+    lanes_join(s);
     cudaMemcpyAsync(nb, sl.base, (size_t)sl.cap * sl.row_bytes, cudaMemcpyDeviceToDevice, s->st);
-    dfree(s, sl.base);
+    slab_free(s, sl.base, (size_t)sl.cap * sl.row_bytes);
   }
   sl.base = nb;
   sl.key_of.resize(ncap, -1);
@@ -409,17 +537,40 @@ int ensure_raw(Server* s, int N, const std::vector<int64_t>& keys, std::vector<i
     sl.pin[r]++;
     fl.pinned_rows.push_back({&sl, r});
   }
-  for (int i : miss) {
-    const float* w;
-    {
-      std::lock_guard<std::mutex> lk(s->mu);
-      auto it = s->windows.find({(int)(keys[i] >> 32), (int)(uint32_t)keys[i]});
+  std::vector<const char*> src(miss.size());
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (size_t k = 0; k < miss.size(); k++) {
+      const int64_t key = keys[miss[k]];
+      auto it = s->windows.find({(int)(key >> 32), (int)(uint32_t)key});
       if (it == s->windows.end()) return FPCC_EARG;
-      w = it->second.x;
+      src[k] = (const char*)it->second.x;
     }
-    if (cudaMemcpyAsync((char*)sl.base + (int64_t)rows[i] * sl.row_bytes, w, (size_t)N * 4, cudaMemcpyHostToDevice,
-                        s->st) != cudaSuccess)
-      return FPCC_ECUDA;
+  }
+  // one copy per run of windows that sit at a constant pitch in the pinned
+  // arena (registered one after the other) and go to consecutive rows
+  const int64_t w = (int64_t)N * 4;
+  for (size_t k = 0; k < miss.size();) {
+    const int r0 = rows[miss[k]];
+    size_t k1 = k + 1;
+    int64_t pitch = 0;
+    for (; k1 < miss.size(); k1++) {
+      const int64_t d = src[k1] - src[k];
+      if (rows[miss[k1]] != r0 + (int)(k1 - k)) break;
+      if (k1 == k + 1) {
+        if (d < w || d > ((int64_t)1 << 30)) break;
+        pitch = d;
+      } else if (d != pitch * (int64_t)(k1 - k)) {
+        break;
+      }
+    }
+    char* dst = (char*)sl.base + (int64_t)r0 * sl.row_bytes;
+    const cudaError_t e = (k1 - k == 1)
+        ? cudaMemcpyAsync(dst, src[k], (size_t)w, cudaMemcpyHostToDevice, s->st)
+        : cudaMemcpy2DAsync(dst, (size_t)sl.row_bytes, src[k], (size_t)pitch, (size_t)w, k1 - k,
+                            cudaMemcpyHostToDevice, s->st);
+    if (e != cudaSuccess) return FPCC_ECUDA;
+    k = k1;
   }
   return 0;
 }
@@ -486,8 +637,10 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
     case 8: method = FPCC_CC1B_POPCOUNT; rule = FPCC_SIGN_GT; ldo = sl.row_bytes / 4; break;
     default: break;
   }
+  // in place, the stage touches only slab rows (no server scratch): it runs on a lane
+  fpcc_ctx* cx = (in_place_x && in_place_p) ? lane_begin(s).ctx : s->ctx;
   if (pk.kind == 5) {
-    rc = fpcc_energy_stage(s->ctx, (const float*)dx, ldx, n, pk.N, (double*)dp, sl.row_bytes / 8);
+    rc = fpcc_energy_stage(cx, (const float*)dx, ldx, n, pk.N, (double*)dp, sl.row_bytes / 8);
   } else {
     // FP64 analytic signals for windows with zero runs (known from the host copies)
     std::vector<int32_t> f64;
@@ -498,7 +651,7 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
         if (it != s->windows.end() && it->second.zeros >= FPCC_F64_ZERO_SAMPLES) f64.push_back(i);
       }
     }
-    rc = fpcc_station_stage_ex(s->ctx, method, (const float*)dx, ldx, n, pk.N, pk.Nz, pk.fmt, rule, dp, ldo,
+    rc = fpcc_station_stage_ex(cx, method, (const float*)dx, ldx, n, pk.N, pk.Nz, pk.fmt, rule, dp, ldo,
                                f64.data(), (int)f64.size());
   }
   if (rc) return rc;
@@ -510,7 +663,8 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   return 0;
 }
 
-int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base) {
+int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base,
+              bool products_only) {
   const int n = (int)reqs.size();
   const int m = g.method;
   std::vector<int64_t> k1(n), k2(n);
@@ -543,6 +697,8 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
     e1.assign(rr.begin(), rr.begin() + n);
     e2.assign(rr.begin() + n, rr.end());
   }
+  if (products_only) return 0;
+  lanes_join(s);
   // pair list: rows in one slab (both roles share a slab except the 1-bit methods,
   // whose station-2 rows are offset by the station-1 slab capacity after a merge)
   Slab& s1 = slab_of(s, p1);
@@ -617,21 +773,26 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
 // (FP64 analytic signal), is made here; the per-length path makes the rest.
 // Which path makes a product depends only on its window, so a result is the
 // same alone and in any mix.
-int prefetch_phase(Server* s, const GroupKey& g, int kind, std::vector<Req*>& reqs, InFlight& fl) {
-  const int Nz = (kind == 1) ? g.Nz : 0;
+// All the batch's groups of one kind (1: PCC2 phase spectra, Nz per group;
+// 6: phase signals of PCC1 / PCC_v) go through one call, so that windows of
+// every length and padded length share the packed stage's launches.
+int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int, std::vector<Req*>*>>& sets,
+                   InFlight& fl) {
   struct Miss {
-    int N;
+    int N, Nz;
     int64_t key;
     Slab* sl;
     int row;
     int f64;
   };
   std::vector<Miss> miss;
-  std::set<std::pair<int, int64_t>> seen;
-  for (Req* q : reqs) {
+  std::set<std::tuple<int, int, int64_t>> seen;
+  for (const auto& set : sets)
+  for (Req* q : *set.second) {
+    const int Nz = set.first;
     for (int side = 0; side < 2; side++) {
       const int64_t key = wkey(side ? q->r.sta2 : q->r.sta1, q->r.window);
-      if (!seen.insert({q->N, key}).second) continue;
+      if (!seen.insert(std::make_tuple(q->N, Nz, key)).second) continue;
       int zeros = 0;
       {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -641,17 +802,18 @@ int prefetch_phase(Server* s, const GroupKey& g, int kind, std::vector<Req*>& re
       int a2, b3, c5;
       const int f64 = zeros >= FPCC_F64_ZERO_SAMPLES;
       if (factor235(q->N, &a2, &b3, &c5) && !f64) continue;
-      Slab& sl = slab_of(s, Product{kind, q->N, Nz, g.fmt});
+      Slab& sl = slab_of(s, Product{kind, q->N, Nz, fmt});
       if (find_row(sl, key) >= 0) continue;
       const int r = claim_row(s, sl, key, 1);
       if (r < 0) return FPCC_ENOMEM;
       sl.pin[r]++;
       fl.pinned_rows.push_back({&sl, r});
-      miss.push_back({q->N, key, &sl, r, f64});
+      miss.push_back({q->N, Nz, key, &sl, r, f64});
     }
   }
   if (miss.empty()) return 0;
-  std::stable_sort(miss.begin(), miss.end(), [](const Miss& a, const Miss& b) { return a.N < b.N; });
+  std::stable_sort(miss.begin(), miss.end(),
+                   [](const Miss& a, const Miss& b) { return std::tie(a.N, a.Nz) < std::tie(b.N, b.Nz); });
   const int n = (int)miss.size();
   std::vector<int> rawrow(n);
   int rc;
@@ -665,7 +827,7 @@ int prefetch_phase(Server* s, const GroupKey& g, int kind, std::vector<Req*>& re
     i0 = i1;
   }
   // all rows claimed: addresses are stable from here on
-  const int64_t esz = g.fmt == FPCC_F32 ? 8 : 4;
+  const int64_t esz = fmt == FPCC_F32 ? 8 : 4;
   int64_t ldo = 0;
   for (auto& m : miss) ldo = std::max<int64_t>(ldo, m.sl->row_bytes / esz);
   std::vector<fpcc_station_row> rows(n);
@@ -673,26 +835,27 @@ int prefetch_phase(Server* s, const GroupKey& g, int kind, std::vector<Req*>& re
     Slab& raw = slab_of(s, Product{0, miss[i].N, 0, 0});
     rows[i].d_x = (const float*)((const char*)raw.base + (int64_t)rawrow[i] * raw.row_bytes);
     rows[i].N = miss[i].N;
-    rows[i].Nz = Nz;
+    rows[i].Nz = miss[i].Nz;
     rows[i].f64 = miss[i].f64;
     rows[i].pad = 0;
   }
-  void* tmp = dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)n * ldo * esz);
-  void* dc = dbuf(s, &s->d_idx, &s->n_idx, (size_t)n * sizeof(RowCopy) + 64);
+  Lane& ln = lane_begin(s, true);
+  void* tmp = lane_buf(s, ln, &ln.d_tmp, &ln.n_tmp, (size_t)n * ldo * esz);
+  void* dc = lane_buf(s, ln, &ln.d_idx, &ln.n_idx, (size_t)n * sizeof(RowCopy) + 64);
   if (!tmp || !dc) return FPCC_ENOMEM;
   const int method = (kind == 1) ? FPCC_PCC2 : FPCC_PCC1;
-  if ((rc = fpcc_station_stage_multi(s->ctx, method, rows.data(), n, g.fmt, FPCC_AMP_F_REG, tmp, ldo))) return rc;
+  if ((rc = fpcc_station_stage_multi(ln.ctx, method, rows.data(), n, fmt, FPCC_AMP_F_REG, tmp, ldo))) return rc;
   std::vector<RowCopy> cp(n);
   for (int i = 0; i < n; i++)
     cp[i] = RowCopy{(const char*)tmp + (size_t)i * ldo * esz,
                     (char*)miss[i].sl->base + (int64_t)miss[i].row * miss[i].sl->row_bytes, miss[i].sl->row_bytes};
-  if (upload(fl, dc, cp.data(), cp.size() * sizeof(RowCopy), s->st) != cudaSuccess) return FPCC_ECUDA;
+  if (upload(fl, dc, cp.data(), cp.size() * sizeof(RowCopy), ln.st) != cudaSuccess) return FPCC_ECUDA;
   for (int i0 = 0; i0 < n; i0 += 65535) {
     const int k = std::min(65535, n - i0);
     int64_t mx = 0;
     for (int i = i0; i < i0 + k; i++) mx = std::max(mx, cp[i].bytes);
     const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(64, (mx / 16 + 255) / 256));
-    k_scatter_rows<<<dim3(gx, k), 256, 0, s->st>>>((const RowCopy*)dc + i0);
+    k_scatter_rows<<<dim3(gx, k), 256, 0, ln.st>>>((const RowCopy*)dc + i0);
     if (cudaGetLastError() != cudaSuccess) return FPCC_ECUDA;
   }
   s->station_rows += n;
@@ -702,7 +865,8 @@ int prefetch_phase(Server* s, const GroupKey& g, int kind, std::vector<Req*>& re
 // A group whose pair kernel takes descriptors: window lengths and lag windows
 // vary per request; products are ensured per window length, then every
 // correlation of the group runs in one launch reading its rows in place.
-int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base) {
+int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base,
+                     bool products_only) {
   const int n = (int)reqs.size();
   const int m = g.method;
   int kind1, kind2;
@@ -713,8 +877,6 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
   for (int i = 0; i < n; i++) byN[reqs[i]->N].push_back(i);
   std::vector<int> r1(n), r2(n), e1(n), e2(n);
   int rc;
-  if (m == FPCC_PCC2 && (rc = prefetch_phase(s, g, 1, reqs, fl))) return rc;
-  if ((m == FPCC_PCC1 || m == FPCC_PCCV) && (rc = prefetch_phase(s, g, 6, reqs, fl))) return rc;
   for (auto& kv : byN) {
     const int N = kv.first;
     const std::vector<int>& ix = kv.second;
@@ -741,6 +903,8 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
       for (int j = 0; j < k; j++) { e1[ix[j]] = rr[j]; e2[ix[j]] = rr[k + j]; }
     }
   }
+  if (products_only) return 0;
+  lanes_join(s);
   // every product is in place (slabs no longer move): descriptors with row addresses
   const size_t osz = (m == FPCC_CC1B_POPCOUNT) ? 8 : 4;
   size_t total = 0;
@@ -848,6 +1012,7 @@ int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlig
     }
     s->station_rows += (int64_t)miss_keys.size();
   }
+  lanes_join(s);
   std::vector<int32_t> pairs(2 * n);
   for (int i = 0; i < n; i++) { pairs[2 * i] = rows[i]; pairs[2 * i + 1] = rows[n + i]; }
   const size_t ybytes = (size_t)n * g.L * 4;
@@ -1011,6 +1176,27 @@ void worker_main(Server* s) {
                                  &fl->up_bytes);
     int err = (fl->h_out && fl->h_up) ? 0 : FPCC_ENOMEM;
     fl->reqs.reserve(batch.size());
+    // the phase products of the packed groups first, one packed stage per kind
+    if (!err) {
+      std::vector<std::pair<int, std::vector<Req*>*>> ph[2];
+      for (auto& kv : groups) {
+        const GroupKey& g = kv.first;
+        if (g.N >= 0) continue;
+        if (g.method == FPCC_PCC2) ph[0].push_back({g.Nz, &kv.second});
+        else if (g.method == FPCC_PCC1 || g.method == FPCC_PCCV) ph[1].push_back({0, &kv.second});
+      }
+      const int f = product_fmt(s, FPCC_PCC2);
+      if (!ph[0].empty()) err = prefetch_phase(s, 1, f, ph[0], *fl);
+      if (!err && !ph[1].empty()) err = prefetch_phase(s, 6, f, ph[1], *fl);
+    }
+    // then every other group's products (station stages on the lanes), so that
+    // they overlap one another; the pair stages follow on the server's stream
+    for (auto& kv : groups) {
+      if (err) break;
+      const GroupKey& g = kv.first;
+      if (g.method == FPCC_WPCC) continue;
+      err = (g.N < 0) ? run_group_packed(s, g, kv.second, *fl, 0, true) : run_group(s, g, kv.second, *fl, 0, true);
+    }
     size_t off = 0;
     for (auto& kv : groups) {
       if (err) break;
@@ -1022,11 +1208,12 @@ void worker_main(Server* s) {
       }
       const GroupKey& g = kv.first;
       if (g.method == FPCC_WPCC) err = run_group_wpcc(s, g, kv.second, *fl, base);
-      else if (g.N < 0) err = run_group_packed(s, g, kv.second, *fl, base);
-      else err = run_group(s, g, kv.second, *fl, base);
+      else if (g.N < 0) err = run_group_packed(s, g, kv.second, *fl, base, false);
+      else err = run_group(s, g, kv.second, *fl, base, false);
       s->pair_stages++;
     }
     if (err) {
+      lanes_join(s);
       cudaStreamSynchronize(s->st);
       fl->reqs.clear();
       for (auto& q : batch) fl->reqs.push_back(q);
@@ -1056,11 +1243,32 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
   s->device = device;
   s->budget = hbm_budget_bytes ? hbm_budget_bytes : (size_t)150 << 30;
   s->max_batch = max_batch > 0 ? max_batch : 4096;
+  s->chunk_bytes = std::min<size_t>((size_t)64 << 20, std::max<size_t>((size_t)1 << 20, s->budget / 8)) &
+                   ~(kGranule - 1);
   if (fpcc_create(&s->ctx, device)) {
     delete s;
     return FPCC_ECUDA;
   }
   s->st = (cudaStream_t)fpcc_get_stream(s->ctx);
+  bool lanes_ok = cudaEventCreateWithFlags(&s->main_ev, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; i < kLanes && lanes_ok; i++) {
+    Lane l;
+    if (fpcc_create(&l.ctx, device)) { lanes_ok = false; break; }
+    l.st = (cudaStream_t)fpcc_get_stream(l.ctx);
+    if (cudaEventCreateWithFlags(&l.ev, cudaEventDisableTiming) != cudaSuccess) {
+      fpcc_destroy(l.ctx);
+      lanes_ok = false;
+      break;
+    }
+    s->lanes.push_back(l);
+  }
+  if (!lanes_ok) {
+    for (auto& l : s->lanes) { cudaEventDestroy(l.ev); fpcc_destroy(l.ctx); }
+    if (s->main_ev) cudaEventDestroy(s->main_ev);
+    fpcc_destroy(s->ctx);
+    delete s;
+    return FPCC_ECUDA;
+  }
   cudaMemPoolProps pp = {};
   pp.allocType = cudaMemAllocationTypePinned;
   pp.location.type = cudaMemLocationTypeDevice;
@@ -1070,6 +1278,8 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
   if (cudaSetDevice(device) != cudaSuccess || cudaMemPoolCreate(&s->pool, &pp) != cudaSuccess ||
       cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
     if (s->pool) cudaMemPoolDestroy(s->pool);
+    for (auto& l : s->lanes) { cudaEventDestroy(l.ev); fpcc_destroy(l.ctx); }
+    cudaEventDestroy(s->main_ev);
     fpcc_destroy(s->ctx);
     delete s;
     return FPCC_ECUDA;
@@ -1095,13 +1305,24 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
   s->cv_c.notify_all();
   for (auto& t : s->completers) t.join();
   cudaSetDevice(s->device);
-  for (auto& kv : s->slabs) dfree(s, kv.second.base);
+  for (auto& kv : s->slabs) slab_free(s, kv.second.base, (size_t)kv.second.cap * kv.second.row_bytes);
+  for (auto& c : s->chunks) dfree(s, c.base);
   for (void** p : {&s->d_tmp_x, &s->d_tmp_p, &s->d_idx, &s->d_y, &s->d_pl, &s->d_desc}) dfree(s, *p);
+  for (auto& l : s->lanes) {
+    if (l.d_tmp) cudaFreeAsync(l.d_tmp, l.st);
+    if (l.d_idx) cudaFreeAsync(l.d_idx, l.st);
+    cudaStreamSynchronize(l.st);
+  }
   cudaStreamSynchronize(s->st);
   cudaMemPoolDestroy(s->pool);
   for (auto& kv : s->wplans) fpcc_wpcc_plan_destroy(kv.second);
   for (size_t i = 0; i < s->pinned_pool.size(); i += 2) cudaFreeHost(s->pinned_pool[i]);
   for (char* a : s->arena) cudaFreeHost(a);
+  for (auto& l : s->lanes) {
+    cudaEventDestroy(l.ev);
+    fpcc_destroy(l.ctx);
+  }
+  if (s->main_ev) cudaEventDestroy(s->main_ev);
   fpcc_destroy(s->ctx);
   delete s;
   return 0;
