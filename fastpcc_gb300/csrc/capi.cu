@@ -630,7 +630,6 @@ int precise_rows(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, s
 
 template <typename T>
 int multi_group(fpcc_ctx* c, std::vector<MultiRow>& rows, int M);
-int conv_class_len(int N);
 
 // Overwrites the listed rows of the FP32 analytic signals `an` (stride ldan)
 // with analytic signals of the same rows of x computed in double-float (the
@@ -776,20 +775,6 @@ int analytic_rows_p64(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int
 }
 
 // ---------------------------------------------------------------- packed analytic signals
-// Transform length class of a window length in the packed analytic-signal
-// stage: the smallest 2^a, 3 2^a or 5 2^a >= 2N - 1 (about three classes per
-// octave, so windows of nearby lengths share their transforms).
-int conv_class_len(int N) {
-  const int need = 2 * N - 1;
-  int best = -1;
-  for (int base : {1, 3, 5})
-    for (long long m = base; m <= (1LL << 26); m *= 2)
-      if (m >= need) {
-        if (best < 0 || m < best) best = (int)m;
-        break;
-      }
-  return best;
-}
 
 constexpr size_t kMultiFilterCache = (size_t)4 << 30;   // bytes of cached filter spectra per context
 

@@ -194,4 +194,16 @@ static int choose_nz_uncached(int N, int M, int mode) {
   return best;
 }
 
+int conv_class_len(int N) {
+  const int need = 2 * N - 1;
+  int best = -1;
+  for (int base : {1, 3, 5})
+    for (long long m = base; m <= (1LL << 26); m *= 2)
+      if (m >= need) {
+        if (best < 0 || m < best) best = (int)m;
+        break;
+      }
+  return best;
+}
+
 }  // namespace fpcc

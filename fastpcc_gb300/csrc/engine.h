@@ -20,6 +20,11 @@ bool factor235(int n, int* a, int* b, int* c);
 // against tens of thousands of integers: length searches walk this list).
 std::vector<int> smooth235_in(int lo, int hi);
 
+// Transform length class of a window length in the packed analytic-signal
+// stage: the smallest 2^a, 3 2^a or 5 2^a >= 2N - 1 (about three classes per
+// octave, so windows of nearby lengths share their transforms).
+int conv_class_len(int N);
+
 // Radix schedule for an in-block transform of length n (2,3,5-smooth):
 // ceil(a/4) power-of-two passes with the exponent spread evenly, then the 5s
 // and 3s.  When `forced` is non-null it lists the radices to use instead.

@@ -173,6 +173,12 @@ struct Server {
   std::vector<Lane> lanes;
   int next_lane = 0;
   cudaEvent_t main_ev = nullptr;        // marks the server's stream for the lanes
+  uint64_t lane_seq = 0;                // lane work items queued so far
+  std::vector<int>* lane_rec = nullptr; // when set, lanes given work are noted here
+  std::vector<cudaEvent_t> ev_pool;     // marks of lane progress for the pair stages
+  size_t ev_used = 0;                   // of ev_pool, in the batch being formed
+  const std::vector<cudaEvent_t>* pair_waits = nullptr;   // what the next pair stage waits for
+  uint64_t pair_seq = 0;                // lane_seq when the group's pair phase began
   // device memory of slabs and scratch: a pool of the server's own whose freed
   // blocks stay mapped, allocated and freed in the order of the server's stream,
   // so growing a slab or releasing one needs no device synchronisation
@@ -265,15 +271,38 @@ void dfree(Server* s, void* p) {
 // window uploads, slab copies and frees), and the server's stream waits for all
 // lane work queued so far before it touches slab memory again (lanes_join):
 // before a pair stage, and before a slab is copied or freed.
-// Lane 0 takes the packed phase stages (its kernel spectrum cache stays warm);
-// the per-length stages go round the others.
-Lane& lane_begin(Server* s, bool packed = false) {
-  const size_t k = s->lanes.size();
-  Lane& l = (packed || k == 1) ? s->lanes[0] : s->lanes[1 + (size_t)(s->next_lane++) % (k - 1)];
+Lane& lane_at(Server* s, int k) {
+  Lane& l = s->lanes[(size_t)k];
   cudaEventRecord(s->main_ev, s->st);
   cudaStreamWaitEvent(l.st, s->main_ev, 0);
   l.dirty = true;
+  s->lane_seq++;
+  if (s->lane_rec) s->lane_rec->push_back(k);
   return l;
+}
+
+// Per-length stages go round the lanes.
+Lane& lane_begin(Server* s) { return lane_at(s, s->next_lane++ % (int)s->lanes.size()); }
+
+// Events marking, on each lane in `used`, the work queued so far (appended to out).
+void lane_marks(Server* s, std::vector<int>& used, std::vector<cudaEvent_t>& out) {
+  std::sort(used.begin(), used.end());
+  used.erase(std::unique(used.begin(), used.end()), used.end());
+  for (int k : used) {
+    if (s->ev_used == s->ev_pool.size()) {
+      cudaEvent_t e;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+        out.clear();   // no event: the pair stage waits for every lane instead
+        out.push_back(nullptr);
+        return;
+      }
+      s->ev_pool.push_back(e);
+    }
+    cudaEvent_t e = s->ev_pool[s->ev_used++];
+    cudaEventRecord(e, s->lanes[(size_t)k].st);
+    out.push_back(e);
+  }
+  used.clear();
 }
 
 void lanes_join(Server* s) {
@@ -283,6 +312,18 @@ void lanes_join(Server* s) {
       cudaStreamWaitEvent(s->st, l.ev, 0);
       l.dirty = false;
     }
+}
+
+// Before a pair stage: the server's stream waits for the lane work that made the
+// group's products (all lane work when the marks are missing, or when the pair
+// phase itself queued lane work).
+void pair_join(Server* s) {
+  const std::vector<cudaEvent_t>* w = s->pair_waits;
+  if (!w || s->lane_seq != s->pair_seq || std::find(w->begin(), w->end(), nullptr) != w->end()) {
+    lanes_join(s);
+    return;
+  }
+  for (cudaEvent_t e : *w) cudaStreamWaitEvent(s->st, e, 0);
 }
 
 // Scratch of a lane, allocated and freed in its own stream's order.
@@ -698,7 +739,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
     e2.assign(rr.begin() + n, rr.end());
   }
   if (products_only) return 0;
-  lanes_join(s);
+  pair_join(s);
   // pair list: rows in one slab (both roles share a slab except the 1-bit methods,
   // whose station-2 rows are offset by the station-1 slab capacity after a merge)
   Slab& s1 = slab_of(s, p1);
@@ -839,24 +880,50 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
     rows[i].f64 = miss[i].f64;
     rows[i].pad = 0;
   }
-  Lane& ln = lane_begin(s, true);
-  void* tmp = lane_buf(s, ln, &ln.d_tmp, &ln.n_tmp, (size_t)n * ldo * esz);
-  void* dc = lane_buf(s, ln, &ln.d_idx, &ln.n_idx, (size_t)n * sizeof(RowCopy) + 64);
-  if (!tmp || !dc) return FPCC_ENOMEM;
+  // whole conversion classes (rows sharing M-point transforms) go to the lanes,
+  // longest work first onto the least loaded lane; one packed stage per lane
+  std::map<int, std::vector<int>> byM;
+  for (int i = 0; i < n; i++) byM[conv_class_len(miss[i].N)].push_back(i);
+  std::vector<std::pair<double, int>> work;
+  for (auto& kv : byM) work.push_back({(double)kv.second.size() * (double)kv.first, kv.first});
+  std::sort(work.rbegin(), work.rend());
+  const int K = (int)s->lanes.size();
+  std::vector<double> load(K, 0.0);
+  std::vector<std::vector<int>> part(K);
+  for (auto& w : work) {
+    const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[l] += w.first;
+    const std::vector<int>& v = byM[w.second];
+    part[l].insert(part[l].end(), v.begin(), v.end());
+  }
   const int method = (kind == 1) ? FPCC_PCC2 : FPCC_PCC1;
-  if ((rc = fpcc_station_stage_multi(ln.ctx, method, rows.data(), n, fmt, FPCC_AMP_F_REG, tmp, ldo))) return rc;
-  std::vector<RowCopy> cp(n);
-  for (int i = 0; i < n; i++)
-    cp[i] = RowCopy{(const char*)tmp + (size_t)i * ldo * esz,
-                    (char*)miss[i].sl->base + (int64_t)miss[i].row * miss[i].sl->row_bytes, miss[i].sl->row_bytes};
-  if (upload(fl, dc, cp.data(), cp.size() * sizeof(RowCopy), ln.st) != cudaSuccess) return FPCC_ECUDA;
-  for (int i0 = 0; i0 < n; i0 += 65535) {
-    const int k = std::min(65535, n - i0);
-    int64_t mx = 0;
-    for (int i = i0; i < i0 + k; i++) mx = std::max(mx, cp[i].bytes);
-    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(64, (mx / 16 + 255) / 256));
-    k_scatter_rows<<<dim3(gx, k), 256, 0, ln.st>>>((const RowCopy*)dc + i0);
-    if (cudaGetLastError() != cudaSuccess) return FPCC_ECUDA;
+  for (int l = 0; l < K; l++) {
+    std::vector<int>& ix = part[l];
+    if (ix.empty()) continue;
+    std::sort(ix.begin(), ix.end());   // (N, Nz) order, as the packed stage requires
+    const int m = (int)ix.size();
+    std::vector<fpcc_station_row> sub(m);
+    for (int i = 0; i < m; i++) sub[i] = rows[ix[i]];
+    Lane& ln = lane_at(s, l);
+    void* tmp = lane_buf(s, ln, &ln.d_tmp, &ln.n_tmp, (size_t)m * ldo * esz);
+    void* dc = lane_buf(s, ln, &ln.d_idx, &ln.n_idx, (size_t)m * sizeof(RowCopy) + 64);
+    if (!tmp || !dc) return FPCC_ENOMEM;
+    if ((rc = fpcc_station_stage_multi(ln.ctx, method, sub.data(), m, fmt, FPCC_AMP_F_REG, tmp, ldo))) return rc;
+    std::vector<RowCopy> cp(m);
+    for (int i = 0; i < m; i++) {
+      const Miss& q = miss[ix[i]];
+      cp[i] = RowCopy{(const char*)tmp + (size_t)i * ldo * esz, (char*)q.sl->base + (int64_t)q.row * q.sl->row_bytes,
+                      q.sl->row_bytes};
+    }
+    if (upload(fl, dc, cp.data(), cp.size() * sizeof(RowCopy), ln.st) != cudaSuccess) return FPCC_ECUDA;
+    for (int i0 = 0; i0 < m; i0 += 65535) {
+      const int k = std::min(65535, m - i0);
+      int64_t mx = 0;
+      for (int i = i0; i < i0 + k; i++) mx = std::max(mx, cp[i].bytes);
+      const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(64, (mx / 16 + 255) / 256));
+      k_scatter_rows<<<dim3(gx, k), 256, 0, ln.st>>>((const RowCopy*)dc + i0);
+      if (cudaGetLastError() != cudaSuccess) return FPCC_ECUDA;
+    }
   }
   s->station_rows += n;
   return 0;
@@ -904,7 +971,7 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
     }
   }
   if (products_only) return 0;
-  lanes_join(s);
+  pair_join(s);
   // every product is in place (slabs no longer move): descriptors with row addresses
   const size_t osz = (m == FPCC_CC1B_POPCOUNT) ? 8 : 4;
   size_t total = 0;
@@ -1172,34 +1239,60 @@ void worker_main(Server* s) {
     size_t total = 0;
     for (auto& q : batch) total += (size_t)q.L * (q.r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
     fl->h_out = (char*)pinned_get(s, total, &fl->h_bytes);
-    fl->h_up = (char*)pinned_get(s, (size_t)(16 * 4 + sizeof(fpcc_pair_desc)) * batch.size() + 1024 * (groups.size() + 4),
+    fl->h_up = (char*)pinned_get(s, (size_t)(16 * 4 + sizeof(fpcc_pair_desc)) * batch.size() +
+                                     1024 * (groups.size() + 4 + 2 * s->lanes.size()),
                                  &fl->up_bytes);
     int err = (fl->h_out && fl->h_up) ? 0 : FPCC_ENOMEM;
     fl->reqs.reserve(batch.size());
-    // the phase products of the packed groups first, one packed stage per kind
+    // Station products first, all on the lanes: the phase products of the
+    // packed groups in packed stages (one kind at a time, the direct sums'
+    // phase signals first), then every other group's products.  Then the pair
+    // stages on the server's stream, each after the lane work that made its own
+    // products, so that the first pair stages overlap later station stages.
+    // Groups go direct-sum methods first: theirs are the longest pair stages.
+    std::vector<std::pair<const GroupKey, std::vector<Req*>>*> order;
+    for (auto& kv : groups) order.push_back(&kv);
+    std::stable_partition(order.begin(), order.end(), [](const std::pair<const GroupKey, std::vector<Req*>>* kv) {
+      const int m = kv->first.method;
+      return m == FPCC_PCC1 || m == FPCC_PCCV || m == FPCC_CC1B_POPCOUNT;
+    });
+    s->ev_used = 0;
+    std::vector<std::vector<cudaEvent_t>> waits(order.size());
+    std::vector<cudaEvent_t> marks6, marks1;
+    std::vector<int> used;
     if (!err) {
       std::vector<std::pair<int, std::vector<Req*>*>> ph[2];
-      for (auto& kv : groups) {
-        const GroupKey& g = kv.first;
+      for (auto* kv : order) {
+        const GroupKey& g = kv->first;
         if (g.N >= 0) continue;
-        if (g.method == FPCC_PCC2) ph[0].push_back({g.Nz, &kv.second});
-        else if (g.method == FPCC_PCC1 || g.method == FPCC_PCCV) ph[1].push_back({0, &kv.second});
+        if (g.method == FPCC_PCC2) ph[0].push_back({g.Nz, &kv->second});
+        else if (g.method == FPCC_PCC1 || g.method == FPCC_PCCV) ph[1].push_back({0, &kv->second});
       }
       const int f = product_fmt(s, FPCC_PCC2);
-      if (!ph[0].empty()) err = prefetch_phase(s, 1, f, ph[0], *fl);
-      if (!err && !ph[1].empty()) err = prefetch_phase(s, 6, f, ph[1], *fl);
+      s->lane_rec = &used;
+      if (!ph[1].empty()) err = prefetch_phase(s, 6, f, ph[1], *fl);
+      lane_marks(s, used, marks6);
+      if (!err && !ph[0].empty()) err = prefetch_phase(s, 1, f, ph[0], *fl);
+      lane_marks(s, used, marks1);
+      s->lane_rec = nullptr;
     }
-    // then every other group's products (station stages on the lanes), so that
-    // they overlap one another; the pair stages follow on the server's stream
-    for (auto& kv : groups) {
+    for (size_t i = 0; i < order.size(); i++) {
       if (err) break;
-      const GroupKey& g = kv.first;
+      const GroupKey& g = order[i]->first;
       if (g.method == FPCC_WPCC) continue;
-      err = (g.N < 0) ? run_group_packed(s, g, kv.second, *fl, 0, true) : run_group(s, g, kv.second, *fl, 0, true);
+      s->lane_rec = &used;
+      err = (g.N < 0) ? run_group_packed(s, g, order[i]->second, *fl, 0, true)
+                      : run_group(s, g, order[i]->second, *fl, 0, true);
+      s->lane_rec = nullptr;
+      lane_marks(s, used, waits[i]);
+      if (g.N < 0 && g.method == FPCC_PCC2) waits[i].insert(waits[i].end(), marks1.begin(), marks1.end());
+      if (g.N < 0 && (g.method == FPCC_PCC1 || g.method == FPCC_PCCV))
+        waits[i].insert(waits[i].end(), marks6.begin(), marks6.end());
     }
     size_t off = 0;
-    for (auto& kv : groups) {
+    for (size_t i = 0; i < order.size(); i++) {
       if (err) break;
+      auto& kv = *order[i];
       const size_t base = off;
       for (Req* q : kv.second) {
         fl->reqs.push_back(*q);
@@ -1207,11 +1300,16 @@ void worker_main(Server* s) {
         off += (size_t)q->L * (q->r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
       }
       const GroupKey& g = kv.first;
+      s->pair_waits = &waits[i];
+      s->pair_seq = s->lane_seq;
       if (g.method == FPCC_WPCC) err = run_group_wpcc(s, g, kv.second, *fl, base);
       else if (g.N < 0) err = run_group_packed(s, g, kv.second, *fl, base, false);
       else err = run_group(s, g, kv.second, *fl, base, false);
+      s->pair_waits = nullptr;
       s->pair_stages++;
     }
+    // later batches' lane work and slab frees follow everything of this one
+    lanes_join(s);
     if (err) {
       lanes_join(s);
       cudaStreamSynchronize(s->st);
@@ -1323,6 +1421,7 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
     fpcc_destroy(l.ctx);
   }
   if (s->main_ev) cudaEventDestroy(s->main_ev);
+  for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
   fpcc_destroy(s->ctx);
   delete s;
   return 0;
