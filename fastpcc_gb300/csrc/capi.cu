@@ -65,6 +65,7 @@ struct fpcc_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  bool own_pool = true;             // false: the pool belongs to a server sharing it
   DevBuf dev[48];
   DevBuf pin[8];
   cudaStream_t stream2 = nullptr;   // second stream of the pipelined drop-ins
@@ -220,6 +221,17 @@ extern "C" int fpcc_create(fpcc_ctx** out, int device) {
   return 0;
 }
 
+namespace fpcc {
+// For a server: a context made by fpcc_create and not used yet gives up its own
+// pool and allocates from the server's.
+int ctx_share_pool(fpcc_ctx* c, cudaMemPool_t pool) {
+  if (c->own_pool) cudaMemPoolDestroy(c->pool);
+  c->pool = pool;
+  c->own_pool = false;
+  return 0;
+}
+}  // namespace fpcc
+
 extern "C" int fpcc_destroy(fpcc_ctx* c) {
   if (!c) return 0;
   cudaSetDevice(c->device);
@@ -232,7 +244,7 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
   cudaStreamSynchronize(c->stream);
   if (c->stream2) cudaStreamSynchronize(c->stream2);
   for (auto& b : c->pin) if (b.p) cudaFreeHost(b.p);
-  cudaMemPoolDestroy(c->pool);
+  if (c->own_pool) cudaMemPoolDestroy(c->pool);
   cudaEventDestroy(c->ord_ev);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   if (c->stream2) cudaStreamDestroy(c->stream2);

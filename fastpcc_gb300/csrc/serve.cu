@@ -42,6 +42,10 @@
 #include "wpcc.h"
 
 namespace fpcc {
+
+// Makes a freshly created context allocate from `pool` (which it does not own).
+int ctx_share_pool(fpcc_ctx* c, cudaMemPool_t pool);
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -1343,44 +1347,61 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
   s->max_batch = max_batch > 0 ? max_batch : 4096;
   s->chunk_bytes = std::min<size_t>((size_t)64 << 20, std::max<size_t>((size_t)1 << 20, s->budget / 8)) &
                    ~(kGranule - 1);
-  if (fpcc_create(&s->ctx, device)) {
-    delete s;
-    return FPCC_ECUDA;
-  }
-  s->st = (cudaStream_t)fpcc_get_stream(s->ctx);
-  bool lanes_ok = cudaEventCreateWithFlags(&s->main_ev, cudaEventDisableTiming) == cudaSuccess;
-  for (int i = 0; i < kLanes && lanes_ok; i++) {
-    Lane l;
-    if (fpcc_create(&l.ctx, device)) { lanes_ok = false; break; }
-    l.st = (cudaStream_t)fpcc_get_stream(l.ctx);
-    if (cudaEventCreateWithFlags(&l.ev, cudaEventDisableTiming) != cudaSuccess) {
-      fpcc_destroy(l.ctx);
-      lanes_ok = false;
-      break;
-    }
-    s->lanes.push_back(l);
-  }
-  if (!lanes_ok) {
-    for (auto& l : s->lanes) { cudaEventDestroy(l.ev); fpcc_destroy(l.ctx); }
-    if (s->main_ev) cudaEventDestroy(s->main_ev);
-    fpcc_destroy(s->ctx);
-    delete s;
-    return FPCC_ECUDA;
-  }
+  // one pool for the slabs and for the scratch of every context of the server
+  // (the main one and the lanes): freed blocks stay mapped up to the budget and a
+  // quarter again, and memory one lane frees serves the others
   cudaMemPoolProps pp = {};
   pp.allocType = cudaMemAllocationTypePinned;
   pp.location.type = cudaMemLocationTypeDevice;
   pp.location.id = device;
-  // freed blocks are kept up to the budget and a quarter again (slabs and scratch)
   uint64_t keep = (uint64_t)s->budget + (uint64_t)s->budget / 4;
   if (cudaSetDevice(device) != cudaSuccess || cudaMemPoolCreate(&s->pool, &pp) != cudaSuccess ||
       cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
     if (s->pool) cudaMemPoolDestroy(s->pool);
-    for (auto& l : s->lanes) { cudaEventDestroy(l.ev); fpcc_destroy(l.ctx); }
-    cudaEventDestroy(s->main_ev);
-    fpcc_destroy(s->ctx);
     delete s;
     return FPCC_ECUDA;
+  }
+  auto undo = [s]() {
+    for (auto& l : s->lanes) {
+      fpcc_destroy(l.ctx);
+      if (l.ev) cudaEventDestroy(l.ev);
+    }
+    if (s->main_ev) cudaEventDestroy(s->main_ev);
+    if (s->ctx) fpcc_destroy(s->ctx);
+    cudaMemPoolDestroy(s->pool);
+    delete s;
+    return FPCC_ECUDA;
+  };
+  if (fpcc_create(&s->ctx, device)) {
+    s->ctx = nullptr;
+    return undo();
+  }
+  ctx_share_pool(s->ctx, s->pool);
+  s->st = (cudaStream_t)fpcc_get_stream(s->ctx);
+  if (cudaEventCreateWithFlags(&s->main_ev, cudaEventDisableTiming) != cudaSuccess) {
+    s->main_ev = nullptr;
+    return undo();
+  }
+  for (int i = 0; i < kLanes; i++) {
+    Lane l;
+    if (fpcc_create(&l.ctx, device)) return undo();
+    ctx_share_pool(l.ctx, s->pool);
+    l.st = (cudaStream_t)fpcc_get_stream(l.ctx);
+    s->lanes.push_back(l);
+    if (cudaEventCreateWithFlags(&s->lanes.back().ev, cudaEventDisableTiming) != cudaSuccess) {
+      s->lanes.back().ev = nullptr;
+      return undo();
+    }
+  }
+  // map a first reserve of the pool now, at start-up, rather than block by
+  // block under the first batches
+  void* warm = nullptr;
+  const size_t reserve = std::min<size_t>((size_t)2 << 30, s->budget / 4);
+  if (reserve && cudaMallocFromPoolAsync(&warm, reserve, s->pool, s->st) == cudaSuccess) {
+    cudaFreeAsync(warm, s->st);
+    cudaStreamSynchronize(s->st);
+  } else {
+    cudaGetLastError();
   }
   s->worker = std::thread(worker_main, s);
   for (int i = 0; i < 4; i++) s->completers.emplace_back(completer_main, s);
@@ -1406,23 +1427,21 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
   for (auto& kv : s->slabs) slab_free(s, kv.second.base, (size_t)kv.second.cap * kv.second.row_bytes);
   for (auto& c : s->chunks) dfree(s, c.base);
   for (void** p : {&s->d_tmp_x, &s->d_tmp_p, &s->d_idx, &s->d_y, &s->d_pl, &s->d_desc}) dfree(s, *p);
+  for (auto& kv : s->wplans) fpcc_wpcc_plan_destroy(kv.second);
+  // the contexts share the server's pool: they go first, the pool last
   for (auto& l : s->lanes) {
     if (l.d_tmp) cudaFreeAsync(l.d_tmp, l.st);
     if (l.d_idx) cudaFreeAsync(l.d_idx, l.st);
-    cudaStreamSynchronize(l.st);
+    fpcc_destroy(l.ctx);   // frees its buffers and waits for its stream
+    cudaEventDestroy(l.ev);
   }
   cudaStreamSynchronize(s->st);
+  fpcc_destroy(s->ctx);
   cudaMemPoolDestroy(s->pool);
-  for (auto& kv : s->wplans) fpcc_wpcc_plan_destroy(kv.second);
   for (size_t i = 0; i < s->pinned_pool.size(); i += 2) cudaFreeHost(s->pinned_pool[i]);
   for (char* a : s->arena) cudaFreeHost(a);
-  for (auto& l : s->lanes) {
-    cudaEventDestroy(l.ev);
-    fpcc_destroy(l.ctx);
-  }
   if (s->main_ev) cudaEventDestroy(s->main_ev);
   for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
-  fpcc_destroy(s->ctx);
   delete s;
   return 0;
 }
