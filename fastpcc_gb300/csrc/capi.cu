@@ -222,6 +222,10 @@ extern "C" int fpcc_create(fpcc_ctx** out, int device) {
 }
 
 namespace fpcc {
+// The calling thread's message for fpcc_last_error (a server hands its worker's
+// message to the thread that collects a failed request).
+void set_last_error(const char* msg) { g_err = msg ? msg : ""; }
+
 // For a server: a context made by fpcc_create and not used yet gives up its own
 // pool and allocates from the server's.
 int ctx_share_pool(fpcc_ctx* c, cudaMemPool_t pool) {

@@ -23,12 +23,14 @@
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <list>
 #include <map>
 #include <mutex>
 #include <set>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -45,6 +47,17 @@ namespace fpcc {
 
 // Makes a freshly created context allocate from `pool` (which it does not own).
 int ctx_share_pool(fpcc_ctx* c, cudaMemPool_t pool);
+void set_last_error(const char* msg);
+
+namespace {
+// A failed CUDA call of the server itself: status FPCC_ECUDA with a message.
+int cuda_err(cudaError_t e, const char* what) {
+  char buf[256];
+  snprintf(buf, sizeof buf, "server: %s: %s", what, cudaGetErrorString(e));
+  set_last_error(buf);
+  return cuda_err(cudaGetLastError(), "row copy");
+}
+}  // namespace
 
 namespace {
 
@@ -129,6 +142,7 @@ struct InFlight {
   size_t up_bytes = 0, up_used = 0;
   std::vector<std::pair<Slab*, int>> pinned_rows;
   int err = 0;
+  std::string err_msg;             // the worker's message for err
 };
 
 // Copy a small host array into the batch's pinned staging and queue its upload.
@@ -204,6 +218,7 @@ struct Server {
     float* x;      // pinned samples
     int N;
     int zeros;     // zero samples (such windows get FP64 analytic signals)
+    int chunk;     // the pinned arena chunk holding x
   };
   std::map<std::pair<int, int>, Window> windows;
   std::vector<char*> arena;                                       // pinned chunks holding the windows
@@ -236,6 +251,7 @@ struct Server {
   int64_t completed = 0, batches = 0, station_rows = 0, pair_stages = 0;
   double busy_s = 0;
   int last_error = 0;
+  std::string err_msg;                // message of last_error   [mu]
 };
 
 namespace {
@@ -583,6 +599,7 @@ int ensure_raw(Server* s, int N, const std::vector<int64_t>& keys, std::vector<i
     fl.pinned_rows.push_back({&sl, r});
   }
   std::vector<const char*> src(miss.size());
+  std::vector<int> chunk(miss.size());
   {
     std::lock_guard<std::mutex> lk(s->mu);
     for (size_t k = 0; k < miss.size(); k++) {
@@ -590,10 +607,12 @@ int ensure_raw(Server* s, int N, const std::vector<int64_t>& keys, std::vector<i
       auto it = s->windows.find({(int)(key >> 32), (int)(uint32_t)key});
       if (it == s->windows.end()) return FPCC_EARG;
       src[k] = (const char*)it->second.x;
+      chunk[k] = it->second.chunk;
     }
   }
-  // one copy per run of windows that sit at a constant pitch in the pinned
-  // arena (registered one after the other) and go to consecutive rows
+  // one copy per run of windows that sit at a constant pitch in one pinned
+  // arena chunk (registered one after the other) and go to consecutive rows; a
+  // copy never spans two host allocations
   const int64_t w = (int64_t)N * 4;
   for (size_t k = 0; k < miss.size();) {
     const int r0 = rows[miss[k]];
@@ -601,7 +620,7 @@ int ensure_raw(Server* s, int N, const std::vector<int64_t>& keys, std::vector<i
     int64_t pitch = 0;
     for (; k1 < miss.size(); k1++) {
       const int64_t d = src[k1] - src[k];
-      if (rows[miss[k1]] != r0 + (int)(k1 - k)) break;
+      if (chunk[k1] != chunk[k] || rows[miss[k1]] != r0 + (int)(k1 - k)) break;
       if (k1 == k + 1) {
         if (d < w || d > ((int64_t)1 << 30)) break;
         pitch = d;
@@ -614,7 +633,7 @@ int ensure_raw(Server* s, int N, const std::vector<int64_t>& keys, std::vector<i
         ? cudaMemcpyAsync(dst, src[k], (size_t)w, cudaMemcpyHostToDevice, s->st)
         : cudaMemcpy2DAsync(dst, (size_t)sl.row_bytes, src[k], (size_t)pitch, (size_t)w, k1 - k,
                             cudaMemcpyHostToDevice, s->st);
-    if (e != cudaSuccess) return FPCC_ECUDA;
+    if (e != cudaSuccess) return cuda_err(e, "window upload");
     k = k1;
   }
   return 0;
@@ -664,12 +683,12 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   if (!in_place_x || !in_place_p) {
     std::vector<int> idx(2 * n);
     for (int i = 0; i < n; i++) { idx[i] = raw_rows[i]; idx[n + i] = miss_rows[i]; }
-    if (upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st) != cudaSuccess) return FPCC_ECUDA;
+    if (cudaError_t ue = upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st)) return cuda_err(ue, "upload");
   }
   const int64_t ldx = round16(N * 4) / 4;   // = raw.row_bytes / 4
   if (!in_place_x &&
       copy_rows(raw.base, raw.row_bytes, (const int*)di, dx, ldx * 4, nullptr, n, N * 4, s->st) != cudaSuccess)
-    return FPCC_ECUDA;
+    return cuda_err(cudaGetLastError(), "row copy");
   int method = FPCC_PCC2, rule = FPCC_AMP_F_REG;
   int64_t ldo = sl.row_bytes / (pk.fmt ? 4 : 8);
   switch (pk.kind) {
@@ -683,7 +702,7 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
     default: break;
   }
   // in place, the stage touches only slab rows (no server scratch): it runs on a lane
-  fpcc_ctx* cx = (in_place_x && in_place_p) ? lane_begin(s).ctx : s->ctx;
+  fpcc_ctx* cx = (in_place_x && in_place_p && !s->lanes.empty()) ? lane_begin(s).ctx : s->ctx;
   if (pk.kind == 5) {
     rc = fpcc_energy_stage(cx, (const float*)dx, ldx, n, pk.N, (double*)dp, sl.row_bytes / 8);
   } else {
@@ -703,7 +722,7 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   if (!in_place_p &&
       copy_rows(dp, sl.row_bytes, nullptr, sl.base, sl.row_bytes, (const int*)di + n, n, sl.row_bytes, s->st) !=
           cudaSuccess)
-    return FPCC_ECUDA;
+    return cuda_err(cudaGetLastError(), "row copy");
   s->station_rows += n;
   return 0;
 }
@@ -758,11 +777,11 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
     if (!merged || !di) return FPCC_ENOMEM;
     std::vector<int> idx(2 * n);
     for (int i = 0; i < n; i++) { idx[i] = r1[i]; idx[n + i] = r2[i]; }
-    if (upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st) != cudaSuccess) return FPCC_ECUDA;
+    if (cudaError_t ue = upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st)) return cuda_err(ue, "upload");
     if (copy_rows(s1.base, rb, (const int*)di, merged, rb, nullptr, n, rb, s->st) != cudaSuccess ||
         copy_rows(s2.base, rb, (const int*)di + n, (char*)merged + (size_t)n * rb, rb, nullptr, n, rb, s->st) !=
             cudaSuccess)
-      return FPCC_ECUDA;
+      return cuda_err(cudaGetLastError(), "row copy");
     base = merged;
     for (int i = 0; i < n; i++) { pairs[2 * i] = i; pairs[2 * i + 1] = n + i; }
   } else {
@@ -782,12 +801,12 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
     if (!tmp || !di) return FPCC_ENOMEM;
     std::vector<int> idx(4 * n);
     for (int i = 0; i < n; i++) { idx[i] = r1[i]; idx[n + i] = r2[i]; idx[2 * n + i] = e1[i]; idx[3 * n + i] = e2[i]; }
-    if (upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st) != cudaSuccess) return FPCC_ECUDA;
+    if (cudaError_t ue = upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st)) return cuda_err(ue, "upload");
     char* spec = (char*)tmp;
     char* en = spec + (size_t)2 * n * rb;
     if (copy_rows(s1.base, rb, (const int*)di, spec, rb, nullptr, 2 * n, rb, s->st) != cudaSuccess ||
         copy_rows(se.base, eb, (const int*)di + 2 * n, en, eb, nullptr, 2 * n, eb, s->st) != cudaSuccess)
-      return FPCC_ECUDA;
+      return cuda_err(cudaGetLastError(), "row copy");
     base = spec;
     E = (const double*)en;
     ldE = eb / 8;
@@ -798,7 +817,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
   void* dpl = dbuf(s, &s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
   void* dy = dbuf(s, &s->d_y, &s->n_y, ybytes);
   if (!dpl || !dy) return FPCC_ENOMEM;
-  if (upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st) != cudaSuccess) return FPCC_ECUDA;
+  if (cudaError_t ue = upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st)) return cuda_err(ue, "upload");
   const int64_t lds = slab_of(s, p1).row_bytes / ((m == FPCC_CC1B_POPCOUNT) ? 4 : (g.fmt ? 4 : 8));
   if (m == FPCC_CC1B_POPCOUNT) {
     rc = fpcc_pair_stage(s->ctx, m, base, lds, 0, (const int32_t*)dpl, n, g.N, 0, g.lag0, g.lag0 + g.L - 1, 0.f,
@@ -891,7 +910,7 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
   std::vector<std::pair<double, int>> work;
   for (auto& kv : byM) work.push_back({(double)kv.second.size() * (double)kv.first, kv.first});
   std::sort(work.rbegin(), work.rend());
-  const int K = (int)s->lanes.size();
+  const int K = std::max(1, (int)s->lanes.size());
   std::vector<double> load(K, 0.0);
   std::vector<std::vector<int>> part(K);
   for (auto& w : work) {
@@ -908,25 +927,31 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
     const int m = (int)ix.size();
     std::vector<fpcc_station_row> sub(m);
     for (int i = 0; i < m; i++) sub[i] = rows[ix[i]];
-    Lane& ln = lane_at(s, l);
-    void* tmp = lane_buf(s, ln, &ln.d_tmp, &ln.n_tmp, (size_t)m * ldo * esz);
-    void* dc = lane_buf(s, ln, &ln.d_idx, &ln.n_idx, (size_t)m * sizeof(RowCopy) + 64);
+    // without lanes: the server's own context, stream and scratch
+    const bool lane = !s->lanes.empty();
+    Lane* ln = lane ? &lane_at(s, l) : nullptr;
+    fpcc_ctx* cx = lane ? ln->ctx : s->ctx;
+    cudaStream_t st = lane ? ln->st : s->st;
+    void* tmp = lane ? lane_buf(s, *ln, &ln->d_tmp, &ln->n_tmp, (size_t)m * ldo * esz)
+                     : dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)m * ldo * esz);
+    void* dc = lane ? lane_buf(s, *ln, &ln->d_idx, &ln->n_idx, (size_t)m * sizeof(RowCopy) + 64)
+                    : dbuf(s, &s->d_idx, &s->n_idx, (size_t)m * sizeof(RowCopy) + 64);
     if (!tmp || !dc) return FPCC_ENOMEM;
-    if ((rc = fpcc_station_stage_multi(ln.ctx, method, sub.data(), m, fmt, FPCC_AMP_F_REG, tmp, ldo))) return rc;
+    if ((rc = fpcc_station_stage_multi(cx, method, sub.data(), m, fmt, FPCC_AMP_F_REG, tmp, ldo))) return rc;
     std::vector<RowCopy> cp(m);
     for (int i = 0; i < m; i++) {
       const Miss& q = miss[ix[i]];
       cp[i] = RowCopy{(const char*)tmp + (size_t)i * ldo * esz, (char*)q.sl->base + (int64_t)q.row * q.sl->row_bytes,
                       q.sl->row_bytes};
     }
-    if (upload(fl, dc, cp.data(), cp.size() * sizeof(RowCopy), ln.st) != cudaSuccess) return FPCC_ECUDA;
+    if (cudaError_t ue = upload(fl, dc, cp.data(), cp.size() * sizeof(RowCopy), st)) return cuda_err(ue, "upload");
     for (int i0 = 0; i0 < m; i0 += 65535) {
       const int k = std::min(65535, m - i0);
       int64_t mx = 0;
       for (int i = i0; i < i0 + k; i++) mx = std::max(mx, cp[i].bytes);
       const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(64, (mx / 16 + 255) / 256));
-      k_scatter_rows<<<dim3(gx, k), 256, 0, ln.st>>>((const RowCopy*)dc + i0);
-      if (cudaGetLastError() != cudaSuccess) return FPCC_ECUDA;
+      k_scatter_rows<<<dim3(gx, k), 256, 0, st>>>((const RowCopy*)dc + i0);
+      if (cudaError_t ke = cudaGetLastError()) return cuda_err(ke, "row scatter");
     }
   }
   s->station_rows += n;
@@ -1013,7 +1038,7 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
   // descriptor names its own output row: the order changes no result)
   if (m == FPCC_PCC1 || m == FPCC_PCCV || m == FPCC_CC1B_POPCOUNT)
     std::stable_sort(d.begin(), d.end(), [](const fpcc_pair_desc& a, const fpcc_pair_desc& b) { return a.N > b.N; });
-  if (upload(fl, dd, d.data(), d.size() * sizeof(fpcc_pair_desc), s->st) != cudaSuccess) return FPCC_ECUDA;
+  if (cudaError_t ue = upload(fl, dd, d.data(), d.size() * sizeof(fpcc_pair_desc), s->st)) return cuda_err(ue, "upload");
   rc = fpcc_pair_stage_packed(s->ctx, m, g.fmt, Nz, (const fpcc_pair_desc*)dd, n, maxL, g.v,
                               m == FPCC_CC1B_POPCOUNT);
   if (rc) return rc;
@@ -1090,7 +1115,7 @@ int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlig
   void* dpl = dbuf(s, &s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
   void* dy = dbuf(s, &s->d_y, &s->n_y, ybytes);
   if (!dpl || !dy) return FPCC_ENOMEM;
-  if (upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st) != cudaSuccess) return FPCC_ECUDA;
+  if (cudaError_t ue = upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st)) return cuda_err(ue, "upload");
   if ((rc = fpcc_wpcc_pair_stage(s->ctx, p, sl.base, g.fmt, (const int32_t*)dpl, n, (float*)dy, g.L))) return rc;
   cudaMemcpyAsync((char*)fl.h_out + out_base, dy, ybytes, cudaMemcpyDeviceToHost, s->st);
   return 0;
@@ -1136,7 +1161,10 @@ void deliver(Server* s, InFlight& fl) {
       s->lat_ms.push_back(std::chrono::duration<double, std::milli>(now - q.t_submit).count());
     }
     s->completed += (int64_t)fl.reqs.size();
-    if (err) s->last_error = err;
+    if (err) {
+      s->last_error = err;
+      s->err_msg = fl.err_msg;
+    }
   }
   s->cv_done.notify_all();
 }
@@ -1320,6 +1348,7 @@ void worker_main(Server* s) {
       fl->reqs.clear();
       for (auto& q : batch) fl->reqs.push_back(q);
       fl->err = err;
+      fl->err_msg = fpcc_last_error();
     } else {
       cudaEventCreateWithFlags(&fl->done, cudaEventDisableTiming);
       cudaEventRecord(fl->done, s->st);
@@ -1359,7 +1388,7 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
       cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
     if (s->pool) cudaMemPoolDestroy(s->pool);
     delete s;
-    return FPCC_ECUDA;
+    return cuda_err(cudaGetLastError(), "row copy");
   }
   auto undo = [s]() {
     for (auto& l : s->lanes) {
@@ -1370,7 +1399,7 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
     if (s->ctx) fpcc_destroy(s->ctx);
     cudaMemPoolDestroy(s->pool);
     delete s;
-    return FPCC_ECUDA;
+    return cuda_err(cudaGetLastError(), "row copy");
   };
   if (fpcc_create(&s->ctx, device)) {
     s->ctx = nullptr;
@@ -1382,7 +1411,10 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
     s->main_ev = nullptr;
     return undo();
   }
-  for (int i = 0; i < kLanes; i++) {
+  // FPCC_SERVER_LANES sets the number of lanes (0: everything on the server's stream)
+  int nlanes = kLanes;
+  if (const char* e = getenv("FPCC_SERVER_LANES")) nlanes = std::max(0, std::min(16, atoi(e)));
+  for (int i = 0; i < nlanes; i++) {
     Lane l;
     if (fpcc_create(&l.ctx, device)) return undo();
     ctx_share_pool(l.ctx, s->pool);
@@ -1504,7 +1536,7 @@ extern "C" int fpcc_put_station_window(fpcc_server* h, int32_t sta, int32_t wind
   memcpy(dst, x, (size_t)N * 4);
   int zeros = 0;
   for (int n = 0; n < N; n++) zeros += (x[n] == 0.0f);
-  s->windows[{sta, window}] = Server::Window{dst, N, zeros};
+  s->windows[{sta, window}] = Server::Window{dst, N, zeros, (int)s->arena.size() - 1};
   return 0;
 }
 
@@ -1578,6 +1610,7 @@ extern "C" int fpcc_poll(fpcc_server* h, int64_t id) {
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->status.find(id);
   if (it == s->status.end()) return FPCC_EARG;
+  if (it->second < 0) set_last_error(s->err_msg.c_str());
   return it->second;
 }
 
@@ -1595,7 +1628,9 @@ extern "C" int fpcc_wait(fpcc_server* h, int64_t id, double timeout_s) {
     s->cv_done.wait(lk, pred);
   }
   auto it = s->status.find(id);
-  return it == s->status.end() ? FPCC_EARG : it->second;
+  if (it == s->status.end()) return FPCC_EARG;
+  if (it->second < 0) set_last_error(s->err_msg.c_str());
+  return it->second;
 }
 
 extern "C" int fpcc_server_drain(fpcc_server* h) {
@@ -1603,6 +1638,7 @@ extern "C" int fpcc_server_drain(fpcc_server* h) {
   if (!s) return FPCC_EARG;
   std::unique_lock<std::mutex> lk(s->mu);
   s->cv_done.wait(lk, [&] { return s->pending.empty() && s->completed >= s->next_id; });
+  if (s->last_error) set_last_error(s->err_msg.c_str());
   return s->last_error;
 }
 
