@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--mixed-only", action="store_true", help="run only the uneven-batch and request-stream legs")
     ap.add_argument("--multi-only", action="store_true",
                     help="run only the packed analytic-signal stage leg (profiling); --windows sets its count")
+    ap.add_argument("--profile-uneven", metavar="TRACE_JSON",
+                    help="profile one cold pass of the uneven batch (torch profiler), write its chrome trace "
+                         "to TRACE_JSON and print the kernel and stream summary")
     ap.add_argument("--stack-only", action="store_true",
                     help="run one all-pairs step, then only the stacking leg (profiling of the stacks)")
     return ap.parse_args()
@@ -249,6 +252,90 @@ def autotune(F, max_nz=1 << 20):
     return {"lengths_timed": len(table) if table else None, "seconds": time.perf_counter() - t0}
 
 
+def _uneven_case(n, seed, tag):
+    """n pairs of windows (log-uniform lengths 2^12-2^17, 5 % gaps) and their
+    requests [(method, s1, s2, window, Lag1, Lag2)]."""
+    from fastpcc_gb300 import synth
+    rng = np.random.default_rng(seed)
+    lengths = np.round(2.0 ** rng.uniform(12, 17, n)).astype(int)
+    win = synth.uneven_windows(lengths, 2, gap_frac=0.05, tag=tag)
+    methods = rng.choice(list(MIX_BATCH), size=n, p=list(MIX_BATCH.values()))
+    reqs = []
+    for i in range(n):
+        M = max(1, int(rng.uniform(0.01, 0.10) * lengths[i]))
+        reqs.append((int(methods[i]), 0, 1, i, -M, M))
+    return win, reqs
+
+
+def _uneven_server(F, win, fmt, nz_mode):
+    srv = F.Server(hbm_budget=150 << 30, max_batch=8192, fmt=fmt, nz_mode=nz_mode)
+    for w in range(len(win)):
+        srv.put(0, w, win[w][0])
+        srv.put(1, w, win[w][1])
+    return srv
+
+
+def uneven_profile(F, path, n_pairs=500, fmt=2, nz_mode=1):
+    """One cold pass of the uneven batch under the torch profiler (CUDA
+    activity): the chrome trace goes to `path`; returns the kernel table (launches,
+    total time, share of kernel time) and the overlap of the server's streams
+    (busy time per stream, the union over streams, idle time of the span)."""
+    import collections
+    import re
+    import torch
+    from torch.profiler import profile, ProfilerActivity
+    wwin, wreqs = _uneven_case(60, 141, "uneven-batch-warmup")
+    srv = _uneven_server(F, wwin, fmt, nz_mode)
+    arr, _ = _serve_requests(F, srv, wreqs, lambda s, w: s)
+    srv.submit_many(arr)
+    srv.drain()
+    srv.close()
+    win, reqs = _uneven_case(n_pairs, 41, "uneven-batch")
+    for rep in range(2):   # the profiler's first session records no device activity
+        srv = _uneven_server(F, win if rep else wwin, fmt, nz_mode)
+        arr, _ = _serve_requests(F, srv, reqs if rep else wreqs, lambda s, w: s)
+        torch.cuda.synchronize()
+        with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
+            t0 = time.perf_counter()
+            srv.submit_many(arr)
+            srv.drain()
+            wall = time.perf_counter() - t0
+        srv.close()
+    prof.export_chrome_trace(path)
+    with open(path) as f:
+        ev = json.load(f)["traceEvents"]
+    ops = sorted([e for e in ev if e.get("cat") in ("kernel", "gpu_memcpy", "gpu_memset") and "dur" in e],
+                 key=lambda e: e["ts"])
+    t_a, t_b = ops[0]["ts"], max(e["ts"] + e["dur"] for e in ops)
+    busy, cur_s, cur_e = 0.0, None, None
+    for e in ops:
+        s, en = e["ts"], e["ts"] + e["dur"]
+        if cur_e is None or s > cur_e:
+            if cur_e is not None:
+                busy += cur_e - cur_s
+            cur_s, cur_e = s, en
+        else:
+            cur_e = max(cur_e, en)
+    busy += cur_e - cur_s
+    per_stream = collections.defaultdict(float)
+    table = collections.defaultdict(lambda: [0, 0.0])
+    for e in ops:
+        per_stream[e["args"].get("stream")] += e["dur"]
+        name = re.sub(r"\(.*$", "", e["name"].replace("(anonymous namespace)::", "").replace("fpcc::", "")
+                      .replace("void ", ""))
+        name = re.sub(r"Radices<[^>]*>", "R", name)
+        table[name][0] += 1
+        table[name][1] += e["dur"]
+    total = sum(v[1] for v in table.values())
+    top = sorted(table.items(), key=lambda kv: -kv[1][1])[:25]
+    return {"wall_ms": wall * 1e3, "gpu_span_ms": (t_b - t_a) / 1e3, "gpu_busy_union_ms": busy / 1e3,
+            "gpu_idle_ms": (t_b - t_a - busy) / 1e3, "operations": len(ops),
+            "busy_ms_per_stream": {str(k): round(v / 1e3, 3) for k, v in per_stream.items()},
+            "kernels": [{"name": k, "launches": v[0], "total_ms": round(v[1] / 1e3, 3),
+                         "share": round(v[1] / total, 4)} for k, v in top],
+            "note": "times under the profiler; wall time of the same pass without it is the bench's batched leg"}
+
+
 def uneven_batch_leg(F, n_pairs=500, fmt=2, nz_mode=1):
     """500 pairs with window lengths log-uniform in 2^12-2^17 (5 % of samples in
     gaps), lags +-(1-10 %) of the length, methods 40/30/20/10 % PCC2 / 1-bit /
@@ -258,23 +345,10 @@ def uneven_batch_leg(F, n_pairs=500, fmt=2, nz_mode=1):
     from oracle import oracle as O
     from fastpcc_gb300 import synth
 
-    def case(n, seed, tag):
-        rng = np.random.default_rng(seed)
-        lengths = np.round(2.0 ** rng.uniform(12, 17, n)).astype(int)
-        win = synth.uneven_windows(lengths, 2, gap_frac=0.05, tag=tag)
-        methods = rng.choice(list(MIX_BATCH), size=n, p=list(MIX_BATCH.values()))
-        reqs = []
-        for i in range(n):
-            M = max(1, int(rng.uniform(0.01, 0.10) * lengths[i]))
-            reqs.append((int(methods[i]), 0, 1, i, -M, M))
-        return win, reqs
+    case = _uneven_case
 
     def server(win):
-        srv = F.Server(hbm_budget=150 << 30, max_batch=8192, fmt=fmt, nz_mode=nz_mode)
-        for w in range(len(win)):
-            srv.put(0, w, win[w][0])
-            srv.put(1, w, win[w][1])
-        return srv
+        return _uneven_server(F, win, fmt, nz_mode)
 
     # warm-up on another batch of the same distribution (other lengths), through
     # both arms: loads every kernel once in this process; each timed arm below
@@ -660,6 +734,12 @@ def run_ours(args):
         print(json.dumps({"multi_station": multi_station_leg(F, torch, ctx, stream, torch.device("cuda", local),
                                                              measured_peaks()[0], n=args.windows * 8)}), flush=True)
         ctx.close()
+        return
+    if args.profile_uneven:
+        autotune(F)
+        fmt = {"f32": F.F32, "f16": F.F16, "i16": F.I16}[args.fmt]
+        print(json.dumps({"uneven_profile": uneven_profile(F, args.profile_uneven, fmt=fmt, nz_mode=F.NZ_TUNED)}),
+              flush=True)
         return
     if args.mixed_only:
         fmt = {"f32": F.F32, "f16": F.F16, "i16": F.I16}[args.fmt]
