@@ -189,6 +189,7 @@ struct Server {
   cudaStream_t st = nullptr;
   fpcc_ctx* ctx = nullptr;
   std::vector<Lane> lanes;
+  Lane dlane;                           // pair stages of direct-sum groups, started early
   int next_lane = 0;
   cudaEvent_t main_ev = nullptr;        // marks the server's stream for the lanes
   uint64_t lane_seq = 0;                // lane work items queued so far
@@ -332,6 +333,11 @@ void lanes_join(Server* s) {
       cudaStreamWaitEvent(s->st, l.ev, 0);
       l.dirty = false;
     }
+  if (s->dlane.dirty) {
+    cudaEventRecord(s->dlane.ev, s->dlane.st);
+    cudaStreamWaitEvent(s->st, s->dlane.ev, 0);
+    s->dlane.dirty = false;
+  }
 }
 
 // Before a pair stage: the server's stream waits for the lane work that made the
@@ -962,7 +968,7 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
 // vary per request; products are ensured per window length, then every
 // correlation of the group runs in one launch reading its rows in place.
 int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base,
-                     bool products_only) {
+                     bool products_only, Lane* on = nullptr) {
   const int n = (int)reqs.size();
   const int m = g.method;
   int kind1, kind2;
@@ -1000,13 +1006,38 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
     }
   }
   if (products_only) return 0;
-  pair_join(s);
+  // the pair stage runs on the server's stream, or on the lane `on` (its own
+  // context, stream and output buffers), which first waits for the server's
+  // stream and for the lane work that made the group's products
+  fpcc_ctx* cx = s->ctx;
+  cudaStream_t st = s->st;
+  if (on) {
+    cx = on->ctx;
+    st = on->st;
+    cudaEventRecord(s->main_ev, s->st);
+    cudaStreamWaitEvent(st, s->main_ev, 0);
+    const std::vector<cudaEvent_t>* w = s->pair_waits;
+    const bool all = !w || s->lane_seq != s->pair_seq || std::find(w->begin(), w->end(), nullptr) != w->end();
+    if (all) {
+      for (auto& l : s->lanes)
+        if (l.dirty) {
+          cudaEventRecord(l.ev, l.st);
+          cudaStreamWaitEvent(st, l.ev, 0);
+        }
+    } else {
+      for (cudaEvent_t e : *w) cudaStreamWaitEvent(st, e, 0);
+    }
+    on->dirty = true;
+  } else {
+    pair_join(s);
+  }
   // every product is in place (slabs no longer move): descriptors with row addresses
   const size_t osz = (m == FPCC_CC1B_POPCOUNT) ? 8 : 4;
   size_t total = 0;
   for (int i = 0; i < n; i++) total += (size_t)reqs[i]->L * osz;
-  char* dy = (char*)dbuf(s, &s->d_y, &s->n_y, total);
-  void* dd = dbuf(s, &s->d_desc, &s->n_desc, (size_t)n * sizeof(fpcc_pair_desc));
+  char* dy = (char*)(on ? lane_buf(s, *on, &on->d_tmp, &on->n_tmp, total) : dbuf(s, &s->d_y, &s->n_y, total));
+  void* dd = on ? lane_buf(s, *on, &on->d_idx, &on->n_idx, (size_t)n * sizeof(fpcc_pair_desc))
+                : dbuf(s, &s->d_desc, &s->n_desc, (size_t)n * sizeof(fpcc_pair_desc));
   if (!dy || !dd) return FPCC_ENOMEM;
   std::vector<fpcc_pair_desc> d(n);
   size_t off = 0;
@@ -1038,11 +1069,10 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
   // descriptor names its own output row: the order changes no result)
   if (m == FPCC_PCC1 || m == FPCC_PCCV || m == FPCC_CC1B_POPCOUNT)
     std::stable_sort(d.begin(), d.end(), [](const fpcc_pair_desc& a, const fpcc_pair_desc& b) { return a.N > b.N; });
-  if (cudaError_t ue = upload(fl, dd, d.data(), d.size() * sizeof(fpcc_pair_desc), s->st)) return cuda_err(ue, "upload");
-  rc = fpcc_pair_stage_packed(s->ctx, m, g.fmt, Nz, (const fpcc_pair_desc*)dd, n, maxL, g.v,
-                              m == FPCC_CC1B_POPCOUNT);
+  if (cudaError_t ue = upload(fl, dd, d.data(), d.size() * sizeof(fpcc_pair_desc), st)) return cuda_err(ue, "upload");
+  rc = fpcc_pair_stage_packed(cx, m, g.fmt, Nz, (const fpcc_pair_desc*)dd, n, maxL, g.v, m == FPCC_CC1B_POPCOUNT);
   if (rc) return rc;
-  cudaMemcpyAsync((char*)fl.h_out + out_base, dy, total, cudaMemcpyDeviceToHost, s->st);
+  cudaMemcpyAsync((char*)fl.h_out + out_base, dy, total, cudaMemcpyDeviceToHost, st);
   return 0;
 }
 
@@ -1308,6 +1338,22 @@ void worker_main(Server* s) {
       lane_marks(s, used, marks1);
       s->lane_rec = nullptr;
     }
+    // output offsets of every group, in group order
+    std::vector<size_t> base(order.size());
+    {
+      size_t off = 0;
+      for (size_t i = 0; i < order.size(); i++) {
+        base[i] = off;
+        for (Req* q : order[i]->second) {
+          fl->reqs.push_back(*q);
+          fl->out_off.push_back((int64_t)off);
+          off += (size_t)q->L * (q->r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
+        }
+      }
+    }
+    // a packed direct-sum group starts its pair stage on the direct lane as
+    // soon as its own products are queued, overlapping the later station stages
+    std::vector<char> early(order.size(), 0);
     for (size_t i = 0; i < order.size(); i++) {
       if (err) break;
       const GroupKey& g = order[i]->first;
@@ -1320,23 +1366,27 @@ void worker_main(Server* s) {
       if (g.N < 0 && g.method == FPCC_PCC2) waits[i].insert(waits[i].end(), marks1.begin(), marks1.end());
       if (g.N < 0 && (g.method == FPCC_PCC1 || g.method == FPCC_PCCV))
         waits[i].insert(waits[i].end(), marks6.begin(), marks6.end());
+      const bool direct = g.method == FPCC_PCC1 || g.method == FPCC_PCCV || g.method == FPCC_CC1B_POPCOUNT;
+      if (!err && direct && g.N < 0 && s->dlane.ctx) {
+        s->pair_waits = &waits[i];
+        s->pair_seq = s->lane_seq;
+        err = run_group_packed(s, g, order[i]->second, *fl, base[i], false, &s->dlane);
+        s->pair_waits = nullptr;
+        early[i] = 1;
+        s->pair_stages++;
+      }
     }
-    size_t off = 0;
     for (size_t i = 0; i < order.size(); i++) {
       if (err) break;
+      if (early[i]) continue;
       auto& kv = *order[i];
-      const size_t base = off;
-      for (Req* q : kv.second) {
-        fl->reqs.push_back(*q);
-        fl->out_off.push_back((int64_t)off);
-        off += (size_t)q->L * (q->r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
-      }
+      const size_t base_i = base[i];
       const GroupKey& g = kv.first;
       s->pair_waits = &waits[i];
       s->pair_seq = s->lane_seq;
-      if (g.method == FPCC_WPCC) err = run_group_wpcc(s, g, kv.second, *fl, base);
-      else if (g.N < 0) err = run_group_packed(s, g, kv.second, *fl, base, false);
-      else err = run_group(s, g, kv.second, *fl, base, false);
+      if (g.method == FPCC_WPCC) err = run_group_wpcc(s, g, kv.second, *fl, base_i);
+      else if (g.N < 0) err = run_group_packed(s, g, kv.second, *fl, base_i, false);
+      else err = run_group(s, g, kv.second, *fl, base_i, false);
       s->pair_waits = nullptr;
       s->pair_stages++;
     }
@@ -1395,6 +1445,8 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
       fpcc_destroy(l.ctx);
       if (l.ev) cudaEventDestroy(l.ev);
     }
+    if (s->dlane.ctx) fpcc_destroy(s->dlane.ctx);
+    if (s->dlane.ev) cudaEventDestroy(s->dlane.ev);
     if (s->main_ev) cudaEventDestroy(s->main_ev);
     if (s->ctx) fpcc_destroy(s->ctx);
     cudaMemPoolDestroy(s->pool);
@@ -1422,6 +1474,18 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
     s->lanes.push_back(l);
     if (cudaEventCreateWithFlags(&s->lanes.back().ev, cudaEventDisableTiming) != cudaSuccess) {
       s->lanes.back().ev = nullptr;
+      return undo();
+    }
+  }
+  if (nlanes > 0) {
+    if (fpcc_create(&s->dlane.ctx, device)) {
+      s->dlane.ctx = nullptr;
+      return undo();
+    }
+    ctx_share_pool(s->dlane.ctx, s->pool);
+    s->dlane.st = (cudaStream_t)fpcc_get_stream(s->dlane.ctx);
+    if (cudaEventCreateWithFlags(&s->dlane.ev, cudaEventDisableTiming) != cudaSuccess) {
+      s->dlane.ev = nullptr;
       return undo();
     }
   }
@@ -1466,6 +1530,12 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
     if (l.d_idx) cudaFreeAsync(l.d_idx, l.st);
     fpcc_destroy(l.ctx);   // frees its buffers and waits for its stream
     cudaEventDestroy(l.ev);
+  }
+  if (s->dlane.ctx) {
+    if (s->dlane.d_tmp) cudaFreeAsync(s->dlane.d_tmp, s->dlane.st);
+    if (s->dlane.d_idx) cudaFreeAsync(s->dlane.d_idx, s->dlane.st);
+    fpcc_destroy(s->dlane.ctx);
+    cudaEventDestroy(s->dlane.ev);
   }
   cudaStreamSynchronize(s->st);
   fpcc_destroy(s->ctx);
