@@ -317,3 +317,35 @@ def test_packed_station_stage_weak_window(F, orc):
     for (m, s1, s2, w, l1, l2, v), out in zip(reqs, outs):
         ref = _oracle(orc, m, x[s1], x[s2], l1, l2, v)
         assert relerr(out, ref) < TOL, (m, s2, relerr(out, ref))
+
+
+def test_server_lanes_give_the_same_results(F, orc, monkeypatch):
+    # station stages on lanes (and direct sums on their own lane) against everything
+    # on the server's stream: the same kernels on the same rows, so the same results
+    lengths = [2003, 2999, 4096, 5003, 6143, 8191]
+    xs = _uneven_windows(lengths, "serve/lanes")
+    reqs = _uneven(11, 90, lengths, [0, 0, 1, 2, 3, 4, 4, 5])
+    reqs = [(m, s1, s2, w, min(l1, l2) if m == 5 else l1, max(l1, l2) if m == 5 else l2, 1.5 if m == 5 else v)
+            for (m, s1, s2, w, l1, l2, v) in reqs]
+    outs = {}
+    for lanes in ("0", "4"):
+        monkeypatch.setenv("FPCC_SERVER_LANES", lanes)
+        srv = F.Server(hbm_budget=2 << 30, max_batch=4096)
+        for w, x in xs.items():
+            for s in range(5):
+                srv.put(s, w, x[s])
+        outs[lanes] = _run_many(F, srv, reqs)
+        assert srv.stats()["completed"] == len(reqs)
+        srv.close()
+    for (m, s1, s2, w, l1, l2, v), o0, o4 in zip(reqs, outs["0"], outs["4"]):
+        if m == F.CC1B_POPCOUNT:
+            assert np.array_equal(o0, o4)
+        else:
+            assert np.max(np.abs(o0 - o4)) <= 1e-6 * max(1e-30, float(np.max(np.abs(o0)))), (m, lengths[w], l1, l2)
+    for i in range(0, len(reqs), 9):
+        m, s1, s2, w, l1, l2, v = reqs[i]
+        a, b = xs[w][s1], xs[w][s2]
+        if m == F.CC1B_POPCOUNT:
+            assert np.array_equal(outs["4"][i], orc.cc1b_num(a[None], b[None], l1, l2)[0])
+        else:
+            assert relerr(outs["4"][i], _oracle(orc, m, a, b, l1, l2, v)) < TOL, (m, lengths[w], l1, l2)
