@@ -1167,21 +1167,44 @@ void* pinned_get(Server* s, size_t bytes, size_t* got) {
   return p;
 }
 
+constexpr int kDeliverThreads = 4;                   // threads copying out one large batch
+constexpr size_t kDeliverChunk = (size_t)16 << 20;   // bytes per delivering thread, at least
+
 void pinned_put(Server* s, void* p, size_t bytes) {
   s->pinned_pool.push_back(p);
   s->pinned_pool.push_back((void*)bytes);
 }
 
-// Deliver a batch's results and record its latencies (completer threads).
+// Copies results [i0, i1) of a batch into the callers' buffers.
+void deliver_range(InFlight* fl, size_t i0, size_t i1) {
+  for (size_t i = i0; i < i1; i++) {
+    Req& q = fl->reqs[i];
+    if (q.r.method == FPCC_CC1B_POPCOUNT) {
+      if (q.r.num) memcpy(q.r.num, (char*)fl->h_out + fl->out_off[i], (size_t)q.L * 8);
+    } else if (q.r.y) {
+      memcpy(q.r.y, (char*)fl->h_out + fl->out_off[i], (size_t)q.L * 4);
+    }
+  }
+}
+
+// Deliver a batch's results and record its latencies (completer threads).  A
+// large batch is copied out by several threads: one thread's memcpy into the
+// callers' (pageable) buffers is slower than the GPU makes the results.
 void deliver(Server* s, InFlight& fl) {
   const int err = fl.err;
   const auto now = Clock::now();
-  for (size_t i = 0; i < fl.reqs.size() && !err; i++) {
-    Req& q = fl.reqs[i];
-    if (q.r.method == FPCC_CC1B_POPCOUNT) {
-      if (q.r.num) memcpy(q.r.num, (char*)fl.h_out + fl.out_off[i], (size_t)q.L * 8);
-    } else if (q.r.y) {
-      memcpy(q.r.y, (char*)fl.h_out + fl.out_off[i], (size_t)q.L * 4);
+  if (!err) {
+    size_t bytes = 0;
+    for (const Req& q : fl.reqs) bytes += (size_t)q.L * (q.r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
+    const size_t n = fl.reqs.size();
+    const int k = (int)std::min<size_t>(kDeliverThreads, std::max<size_t>(1, bytes / kDeliverChunk));
+    if (k <= 1 || n < (size_t)k) {
+      deliver_range(&fl, 0, n);
+    } else {
+      std::vector<std::thread> th;
+      for (int t = 1; t < k; t++) th.emplace_back(deliver_range, &fl, n * t / k, n * (t + 1) / k);
+      deliver_range(&fl, 0, n / k);
+      for (auto& t : th) t.join();
     }
   }
   {
@@ -1210,7 +1233,13 @@ void completer_main(Server* s) {
       fl = s->launched.front();
       s->launched.pop_front();
     }
-    if (fl->done && cudaEventSynchronize(fl->done) != cudaSuccess) fl->err = FPCC_ECUDA;
+    if (fl->done) {
+      const cudaError_t e = cudaEventSynchronize(fl->done);
+      if (e != cudaSuccess) {
+        fl->err = FPCC_ECUDA;
+        fl->err_msg = std::string("server: batch completion: ") + cudaGetErrorString(e);
+      }
+    }
     deliver(s, *fl);
     {
       std::lock_guard<std::mutex> lk(s->mu_c);
