@@ -879,7 +879,6 @@ int multi_group(fpcc_ctx* c, std::vector<MultiRow>& rows, int M) {
     constexpr bool dfl = std::is_same<T, float4>::value;
     auto tr = [&](T* in, T* other, int nr, int dir, T** res) -> int {
       if constexpr (dfl) return passes_df(c, (float4*)in, (float4*)other, M, nr, dir, (float4**)res);
-      else if constexpr (sizeof(T) == 16) return passes64(c, (double2*)in, (double2*)other, M, nr, dir, (double2**)res);
       else return passes(c, (float2*)in, (float2*)other, M, nr, dir, (float2**)res);
     };
     T* z = nullptr;

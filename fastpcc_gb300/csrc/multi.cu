@@ -24,10 +24,6 @@ template <typename T>
 __device__ __forceinline__ T cvt(double2 v) {
   return mk(v.x, v.y, (T*)nullptr);
 }
-template <>
-__device__ __forceinline__ float4 cvt<float4>(double2 v) {
-  return dfc(df_from_double(v.x), df_from_double(v.y));
-}
 
 // Im h(n), 0 < n < N, of h = IDFT_N(mask) has closed forms: for even N,
 // (2/N) cot(pi n / N) at odd n and 0 at even n; for odd N, cot(pi n / 2N) / N at
@@ -354,12 +350,6 @@ __global__ void __launch_bounds__(256) k_pass_df(const float4* __restrict__ in, 
   }
 }
 
-__global__ void k_df_to_float2(const float4* __restrict__ src, float2* dst, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float4 v = src[i];
-    dst[i] = make_float2(df_to_float(df_re(v)), df_to_float(df_im(v)));
-  }
-}
 
 __global__ void k_df_from_double(const double2* __restrict__ src, float4* dst, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -443,12 +433,6 @@ cudaError_t launch_pass_df(int R, int dir, const float4* in, float4* out, int n,
 #undef FPCC_PASS_DF
   return cudaErrorInvalidValue;
 }
-cudaError_t launch_df_to_float2(const float4* src, float2* dst, int n, cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
-  const int g = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
-  k_df_to_float2<<<g, 256, 0, st>>>(src, dst, n);
-  return cudaGetLastError();
-}
 
 cudaError_t launch_df_from_double(const double2* src, float4* dst, int n, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
@@ -518,13 +502,8 @@ cudaError_t launch_multi_rowstats(const MultiRow* rows, int nrows, float* rmax, 
 }
 
 template cudaError_t launch_multi_load2<float2>(const MultiRow*, int, float2*, int, cudaStream_t);
-template cudaError_t launch_multi_load2<double2>(const MultiRow*, int, double2*, int, cudaStream_t);
 template cudaError_t launch_multi_split<float2>(const MultiRow*, int, const float2*, float2*, int, cudaStream_t);
-template cudaError_t launch_multi_split<double2>(const MultiRow*, int, const double2*, double2*, int, cudaStream_t);
 template cudaError_t launch_multi_store<float2>(const MultiRow*, int, const float2*, int, cudaStream_t);
-template cudaError_t launch_multi_store<double2>(const MultiRow*, int, const double2*, int, cudaStream_t);
 template cudaError_t launch_multi_convert<float2>(const double2*, float2*, int64_t, cudaStream_t);
-template cudaError_t launch_multi_convert<double2>(const double2*, double2*, int64_t, cudaStream_t);
-template cudaError_t launch_multi_convert<float4>(const double2*, float4*, int64_t, cudaStream_t);
 
 }  // namespace fpcc

@@ -21,7 +21,7 @@
 // the two windows of a row have the same magnitude, and the split's rounding
 // (about 1e-7 of the row in FP32) stays at that level relative to each of them
 // instead of relative to the stronger one; an all-zero window gives zeros.
-// T is float2 or double2.
+// T is float2 (FP32 rows); the double-float rows have their own kernels (_df).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -82,7 +82,6 @@ cudaError_t launch_multi_store_df(const MultiRow* rows, int nrows, const float4*
 cudaError_t launch_pass_df(int R, int dir, const float4* in, float4* out, int n, int Ns, int nrows, const float4* tw,
                            const DfConsts& kc, cudaStream_t st);
 cudaError_t launch_df_from_double(const double2* src, float4* dst, int n, cudaStream_t st);
-cudaError_t launch_df_to_float2(const float4* src, float2* dst, int n, cudaStream_t st);
 // Per row: max |a|^2 and sum |a|^2 over the row's N values.
 cudaError_t launch_multi_rowstats(const MultiRow* rows, int nrows, float* rmax, float* rsum, cudaStream_t st);
 
