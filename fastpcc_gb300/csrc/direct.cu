@@ -240,21 +240,34 @@ __device__ __forceinline__ uint32_t bits_at(const uint32_t* r, int nw, int b) {
 }
 
 // numerator(lag) = overlap - 2 * popcount(b1[n] xor b2[n+lag]) over the overlap.
+// A block takes 256 consecutive lags of one pair.  The whole words of station 1
+// that lie inside a lag's overlap are counted from shared-memory tiles: the
+// station-1 word is the same for every lag of the block (broadcast) and the
+// station-2 bits of a lag are a funnel shift of two staged words, the upper
+// one carried to the next word, so each word costs two shared loads, a shift,
+// an xor and a popcount.  The partial words at the two ends of the overlap are
+// counted with masks straight from global memory.
+constexpr int kPopTile = 1024;   // station-1 words per tile
+
 __global__ void __launch_bounds__(256) k_cc1b_popcount(Cc1bArgs a) {
+  __shared__ uint32_t s1[kPopTile];
+  __shared__ uint32_t s2[kPopTile + 9];
   const int p = blockIdx.y;   // grid (lag blocks, pairs), as k_pccv
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
-  int N, lag0;
+  const int l0 = blockIdx.x * blockDim.x;
+  const int l = l0 + threadIdx.x;
+  int N, lag0, L;
   const uint32_t* B1;
   const uint32_t* B2;
   if (a.desc) {
     const fpcc_pair_desc& d = a.desc[p];
-    if (l >= d.L) return;
+    L = d.L;
+    if (l0 >= L) return;                          // whole block beyond this pair's lags
     N = d.N;
     lag0 = d.lag0;
     B1 = reinterpret_cast<const uint32_t*>(d.a);
     B2 = reinterpret_cast<const uint32_t*>(d.b);
   } else {
-    if (l >= a.L) return;
+    L = a.L;
     const int2 pr = a.pairs[p];
     N = a.N;
     lag0 = a.lag0;
@@ -262,19 +275,52 @@ __global__ void __launch_bounds__(256) k_cc1b_popcount(Cc1bArgs a) {
     B2 = a.bits + (int64_t)pr.y * a.ldb;
   }
   const int nw = (N + 31) >> 5;
+  const bool active = l < L;
   const int lag = lag0 + l;
-  const int n1 = lag < 0 ? -lag : 0;
+  const int n1 = lag < 0 ? -lag : 0;              // overlap [n1, n2) in station-1 samples
   const int n2 = lag < 0 ? N : N - lag;
   const int cnt = n2 - n1;
+  const bool some = active && n2 > n1;
+  const int wa = (n1 + 31) >> 5, wb = n2 >> 5;    // whole words [wa, wb)
   int mism = 0;
-  for (int n = n1; n < n2; n += 32) {
-    const uint32_t u = bits_at(B1, nw, n);
-    const uint32_t v = bits_at(B2, nw, n + lag);
-    uint32_t d = u ^ v;
-    const int rem = n2 - n;
-    if (rem < 32) d &= (1u << rem) - 1u;
-    mism += __popc(d);
+  if (some) {
+    // partial words: [n1, n2) inside one word, or [n1, 32 wa) and [32 wb, n2)
+    const int s0 = n1, e0 = (wa > wb) ? n2 : 32 * wa;
+    const int s9 = (wa > wb) ? n2 : 32 * wb, e9 = n2;
+    if (e0 > s0) mism += __popc((bits_at(B1, nw, s0) ^ bits_at(B2, nw, s0 + lag)) & ((1u << (e0 - s0)) - 1u));
+    if (e9 > s9) mism += __popc((bits_at(B1, nw, s9) ^ bits_at(B2, nw, s9 + lag)) & ((1u << (e9 - s9)) - 1u));
   }
+  // whole words of any lag of the block: from the largest lag's first to the smallest lag's last
+  const int lagb = lag0 + l0;
+  const int lag_max = lag0 + min(L - 1, l0 + (int)blockDim.x - 1);
+  const int w_lo = (max(0, -lag_max) + 31) >> 5;
+  const int w_hi = max(0, min(N, N - lagb)) >> 5;
+  const int sh = (lagb & 31) + (int)threadIdx.x;   // = lag - 32 floor(lagb / 32)
+  const int q = sh >> 5, r = sh & 31;
+  for (int w0 = w_lo; w0 < w_hi; w0 += kPopTile) {
+    const int ct = min(kPopTile, w_hi - w0);
+    const int base2 = w0 + (lagb >> 5);           // floor(lagb / 32)
+    for (int i = threadIdx.x; i < ct; i += blockDim.x) s1[i] = __ldg(B1 + w0 + i);
+    for (int j = threadIdx.x; j < ct + 9; j += blockDim.x) {
+      const int k = base2 + j;
+      s2[j] = (k >= 0 && k < nw) ? __ldg(B2 + k) : 0u;
+    }
+    __syncthreads();
+    if (some) {
+      const int i0 = max(wa, w0) - w0, i1 = min(wb, w0 + ct) - w0;
+      if (i0 < i1) {
+        uint32_t lo = s2[i0 + q];
+#pragma unroll 4
+        for (int i = i0; i < i1; i++) {
+          const uint32_t hi = s2[i + q + 1];
+          mism += __popc(s1[i] ^ __funnelshift_r(lo, hi, r));
+          lo = hi;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (!active) return;
   const long long num = (long long)cnt - 2LL * mism;
   if (a.desc) {
     if (a.desc_num) reinterpret_cast<long long*>(a.desc[p].y)[l] = num;
