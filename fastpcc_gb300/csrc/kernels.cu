@@ -65,10 +65,6 @@ __device__ __forceinline__ float2 load_bin(const void* base, int i) {
 
 // v / sqrt(e1 e2) for the overlap energies e1, e2 (exact FP64 differences of the
 // prefix sums): FP32 reciprocal square roots in the normal range, FP64 outside it.
-__device__ __forceinline__ float gncc_norm(float v, double e1, double e2) {
-  if (e1 >= 1e-30 && e2 >= 1e-30 && e1 <= 1e30 && e2 <= 1e30) return v * (rsqrtf((float)e1) * rsqrtf((float)e2));
-  return (float)((double)v / sqrt(e1 * e2));
-}
 
 template <int... Rs>
 constexpr int rad_len(Radices<Rs...>) {
@@ -271,11 +267,7 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
       const float2 zz = res[PADI(idx >> 1)];
       float v = ((idx & 1) ? zz.y : zz.x) * (0.5f * scale);
       if (a.norm == 1) {
-        // overlap x1[n11,n12), x2[n21,n22) (src/FFTapps.c:896-902)
-        int n11 = 0, n21 = 0, n12 = N, n22 = N;
-        if (lag > 0) { n21 = lag; n12 -= lag; }
-        else { n11 = -lag; n22 += lag; }
-        v = gncc_norm(v, E1[n12] - E1[n11], E2[n22] - E2[n21]);
+        v = gncc_lag_norm(v, E1, E2, N, lag);
       } else if (a.norm == 2) {
         v = v / (float)(N - abs(lag));
       }

@@ -9,6 +9,27 @@
 
 namespace fpcc {
 
+// GNCC normalisation of one lag (src/FFTapps.c:896-902): the overlap energies
+// of x1[n11, n12) and x2[n21, n22) come from FP64 prefix sums (E[0] = 0, so one
+// of the two is a plain load and only the other a difference), then
+// v / sqrt(e1 e2) with FP32 reciprocal square roots when both energies lie in
+// [1e-30, 1e30] (checked on the values rounded to FP32), else in FP64.  The
+// GB300 issues FP64 at a small fraction of its FP32 rate: this form takes one
+// FP64 subtraction per lag instead of two subtractions and four comparisons.
+__device__ __forceinline__ float gncc_lag_norm(float v, const double* E1, const double* E2, int N, int lag) {
+  double e1, e2;
+  if (lag > 0) {
+    e1 = E1[N - lag];
+    e2 = E2[N] - E2[lag];
+  } else {
+    e1 = E1[N] - E1[-lag];
+    e2 = E2[N + lag];
+  }
+  const float f1 = (float)e1, f2 = (float)e2;
+  if (f1 >= 1e-30f && f2 >= 1e-30f && f1 <= 1e30f && f2 <= 1e30f) return v * (rsqrtf(f1) * rsqrtf(f2));
+  return (float)((double)v / sqrt(e1 * e2));
+}
+
 // One correlation of a packed launch (lengths and lags per entry).
 using PairDesc = fpcc_pair_desc;
 

@@ -231,12 +231,7 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
         if (l < 0 || l >= L) continue;
         float val = (q ? v.y : v.x) * scale;
         if (a.norm == 1) {
-          int n11 = 0, n21 = 0, n12 = N, n22 = N;
-          if (lag > 0) { n21 = lag; n12 -= lag; }
-          else { n11 = -lag; n22 += lag; }
-          const double e1 = E1[n12] - E1[n11], e2 = E2[n22] - E2[n21];
-          if (e1 >= 1e-30 && e2 >= 1e-30 && e1 <= 1e30 && e2 <= 1e30) val *= rsqrtf((float)e1) * rsqrtf((float)e2);
-          else val = (float)((double)val / sqrt(e1 * e2));
+          val = gncc_lag_norm(val, E1, E2, N, lag);
         } else if (a.norm == 2) {
           val = val / (float)(N - abs(lag));
         }
