@@ -49,7 +49,8 @@ __global__ void k_hk_tables(const int* __restrict__ Ns, int nk, double2* T, int 
   }
 }
 
-// f * Im h(n) * N / (1 or 2), i.e. Im h(n) times the row factor f / (2/N or 1/N)
+// +-f cot(pi m / D) for 0 < n < N (t: the length's tables); with f = c / M, c the
+// closed form's factor (2/N for even N, 1/N for odd N), this is Im h(n) / M.
 __device__ __forceinline__ double hk_value(int n, int N, const double2* __restrict__ t, double f) {
   int m;
   bool neg;

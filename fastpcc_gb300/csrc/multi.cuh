@@ -4,7 +4,7 @@
 // mask of src/FFTapps.c:104-124 (1/N at bin 0 and, for even N, at N/2; 2/N on
 // the bins in between; 0 above), is the circular convolution of x with
 // h = IDFT_N(mask): Re h = delta, and Im h has a closed form (the discrete
-// Hilbert kernel; see hilbert_im in multi.cu).  A circular convolution of length
+// Hilbert kernel; see hk_value in multi.cu).  A circular convolution of length
 // N equals a circular convolution of any length M >= 2N - 1 with the kernel
 // laid out at offsets -(N-1)..(N-1), so windows whose lengths fall in the same
 // class of M (2^a, 3 2^a or 5 2^a) share every M-point pass; only the kernel
