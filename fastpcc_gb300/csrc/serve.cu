@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "../../include/fastpcc_gb300.h"
+#include "arena.h"
 #include "engine.h"
 #include "kernels.cuh"
 #include "large.cuh"
@@ -205,12 +206,7 @@ struct Server {
   // small slabs are carved from larger pool blocks (chunks), so that a batch
   // with many product classes (every window its own length) makes a few pool
   // allocations instead of one per class; see slab_alloc
-  struct Chunk {
-    char* base;
-    size_t size, used;
-    std::map<size_t, size_t> free;   // offset -> length of each free range
-  };
-  std::vector<Chunk> chunks;
+  ChunkArena chunks{256};
   size_t chunk_bytes = 0;
   // host copies of registered windows
   std::mutex mu;
@@ -370,62 +366,26 @@ void* lane_buf(Server* s, Lane& l, void** p, size_t* n, size_t need) {
 }
 
 // Slab memory.  Blocks up to a quarter of a chunk come first-fit from the
-// chunks (256-byte granules); larger ones straight from the pool.  Every kernel
-// and copy that touches slab memory runs on the server's stream, so a range
-// freed here may be handed out again at once: its next user is queued after
-// every earlier reader, the ordering cudaFreeAsync gives on one stream.
-constexpr size_t kGranule = 256;
-
+// chunks (256-byte granules, `ChunkArena`); larger ones straight from the pool.
+// Every kernel and copy that touches slab memory runs on the server's stream or
+// on a lane joined to it before the free, so a range freed here may be handed
+// out again at once: its next user is queued after every earlier reader, the
+// ordering cudaFreeAsync gives on one stream.
 void* slab_alloc(Server* s, size_t bytes) {
-  const size_t b = (bytes + kGranule - 1) & ~(kGranule - 1);
-  if (b > s->chunk_bytes / 4) return dalloc(s, bytes);
-  for (auto& c : s->chunks)
-    for (auto it = c.free.begin(); it != c.free.end(); ++it)
-      if (it->second >= b) {
-        const size_t off = it->first, len = it->second;
-        c.free.erase(it);
-        if (len > b) c.free[off + b] = len - b;
-        c.used += b;
-        return c.base + off;
-      }
-  char* base = (char*)dalloc(s, s->chunk_bytes);
+  if (s->chunks.round(bytes) > s->chunk_bytes / 4) return dalloc(s, bytes);
+  if (void* p = s->chunks.take(bytes)) return p;
+  void* base = dalloc(s, s->chunk_bytes);
   if (!base) return nullptr;
-  Server::Chunk c{base, s->chunk_bytes, b, {}};
-  c.free[b] = s->chunk_bytes - b;
-  s->chunks.push_back(std::move(c));
-  return base;
+  return s->chunks.add_chunk(base, s->chunk_bytes, bytes);
 }
 
 void slab_free(Server* s, void* p, size_t bytes) {
   if (!p) return;
   lanes_join(s);
-  const size_t b = (bytes + kGranule - 1) & ~(kGranule - 1);
-  for (size_t i = 0; i < s->chunks.size(); i++) {
-    Server::Chunk& c = s->chunks[i];
-    if ((char*)p < c.base || (char*)p >= c.base + c.size) continue;
-    size_t off = (size_t)((char*)p - c.base), len = b;
-    auto nx = c.free.lower_bound(off);
-    if (nx != c.free.end() && nx->first == off + len) {   // merge with the next free range
-      len += nx->second;
-      nx = c.free.erase(nx);
-    }
-    if (nx != c.free.begin()) {                            // and with the previous one
-      auto pv = std::prev(nx);
-      if (pv->first + pv->second == off) {
-        off = pv->first;
-        len += pv->second;
-        c.free.erase(pv);
-      }
-    }
-    c.free[off] = len;
-    c.used -= b;
-    if (c.used == 0) {
-      dfree(s, c.base);
-      s->chunks.erase(s->chunks.begin() + i);
-    }
-    return;
-  }
-  dfree(s, p);
+  bool found = false;
+  void* empty = s->chunks.give(p, bytes, &found);
+  if (!found) dfree(s, p);
+  else if (empty) dfree(s, empty);
 }
 
 // Frees the least recently used slab (other than `keep`) none of whose rows a
@@ -1454,7 +1414,7 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
   s->budget = hbm_budget_bytes ? hbm_budget_bytes : (size_t)150 << 30;
   s->max_batch = max_batch > 0 ? max_batch : 4096;
   s->chunk_bytes = std::min<size_t>((size_t)64 << 20, std::max<size_t>((size_t)1 << 20, s->budget / 8)) &
-                   ~(kGranule - 1);
+                   ~(size_t)255;
   // one pool for the slabs and for the scratch of every context of the server
   // (the main one and the lanes): freed blocks stay mapped up to the budget and a
   // quarter again, and memory one lane frees serves the others
@@ -1550,7 +1510,7 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
   for (auto& t : s->completers) t.join();
   cudaSetDevice(s->device);
   for (auto& kv : s->slabs) slab_free(s, kv.second.base, (size_t)kv.second.cap * kv.second.row_bytes);
-  for (auto& c : s->chunks) dfree(s, c.base);
+  for (auto& c : s->chunks.chunks()) dfree(s, c.base);
   for (void** p : {&s->d_tmp_x, &s->d_tmp_p, &s->d_idx, &s->d_y, &s->d_pl, &s->d_desc}) dfree(s, *p);
   for (auto& kv : s->wplans) fpcc_wpcc_plan_destroy(kv.second);
   // the contexts share the server's pool: they go first, the pool last
