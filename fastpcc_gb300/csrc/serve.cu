@@ -311,6 +311,7 @@ void lane_marks(Server* s, std::vector<int>& used, std::vector<cudaEvent_t>& out
       if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
         out.clear();   // no event: the pair stage waits for every lane instead
         out.push_back(nullptr);
+        used.clear();
         return;
       }
       s->ev_pool.push_back(e);
