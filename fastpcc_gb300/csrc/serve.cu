@@ -1298,10 +1298,12 @@ void worker_main(Server* s) {
     fl->reqs.reserve(batch.size());
     // Station products first, all on the lanes: the phase products of the
     // packed groups in packed stages (one kind at a time, the direct sums'
-    // phase signals first), then every other group's products.  Then the pair
-    // stages on the server's stream, each after the lane work that made its own
-    // products, so that the first pair stages overlap later station stages.
-    // Groups go direct-sum methods first: theirs are the longest pair stages.
+    // phase signals first), then every other group's products.  A packed
+    // direct-sum group starts its pair stage on the direct-sum lane as soon as
+    // its products are queued; the other pair stages follow on the server's
+    // stream, each after the lane work that made its own products.  Groups go
+    // direct-sum methods first: theirs are the longest pair stages, and they
+    // overlap the later groups' station stages.
     std::vector<std::pair<const GroupKey, std::vector<Req*>>*> order;
     for (auto& kv : groups) order.push_back(&kv);
     std::stable_partition(order.begin(), order.end(), [](const std::pair<const GroupKey, std::vector<Req*>>* kv) {
