@@ -277,7 +277,12 @@ int fpcc_wpcc_host(float **y, float **x1, float **x2, unsigned N, unsigned Tr, i
  * that arrive while a batch is on the GPU join the following one.  Each result
  * depends only on its request, so it is the same alone and in any mix.
  * Station windows are registered once (host samples, copied); products are
- * computed on first use and recycled least-recently-used. */
+ * computed on first use and recycled least-recently-used.  Station stages run
+ * concurrently on lanes of the server (contexts with their own streams; the
+ * environment variable FPCC_SERVER_LANES at creation sets their number, 0 for
+ * one stream).  A failed request's status is a negative FPCC_E* code, and
+ * fpcc_last_error() on the thread that collected it (fpcc_poll, fpcc_wait,
+ * fpcc_server_drain) describes it. */
 typedef struct fpcc_server fpcc_server;
 typedef struct {
   int method;            /* FPCC_PCC2, GNCC, CC1B, CC1B_POPCOUNT, PCC1, PCCV, WPCC    */
@@ -294,7 +299,7 @@ typedef struct {
   int64_t pair_stages;             /* pair-stage launches (one per group of a batch)  */
 } fpcc_server_stats;
 int fpcc_server_create(fpcc_server **out, int device, size_t hbm_budget_bytes, int max_batch);
-/* Storage format (FPCC_F32 / FPCC_F16) of the phase spectra and phase signals
+/* Storage format (FPCC_F32 / FPCC_F16 / FPCC_I16) of the phase spectra and phase signals
  * the server caches (PCC2, PCC1, PCCV, WPCC); before the first request. */
 int fpcc_server_set_format(fpcc_server *s, int fmt);
 /* Padded-length rule of FFT requests (fpcc_nz_mode; default FPCC_NZ_FAST);
