@@ -67,6 +67,18 @@ def test_cc1b_popcount_bit_exact(F, orc, N, Tr, l1, l2, d):
     assert np.max(np.abs(y - orc.cc1b(a, b, l1, l2))) < 1e-6
 
 
+@pytest.mark.parametrize("N,l1,l2", [
+    (70001, -1500, 1500),   # 2188 words: the exact kernel's shared-memory tiles (1024 words) and their seams
+    (40, -39, 39),          # every lag the window allows, windows shorter than two words
+    (33, -1, 31),           # one partial word at each end of every overlap
+])
+def test_cc1b_popcount_long_and_edge_windows(F, orc, N, l1, l2):
+    a, b = _data(N, 2, 7, "cc1b-edge")
+    a[:, ::53] = 0.0
+    num = F.cc1b_numerators(a, b, l1, l2)
+    assert np.array_equal(num, orc.cc1b_num(a, b, l1, l2))
+
+
 @pytest.mark.parametrize("N,Tr,l1,l2,d", [c for c in CASES if c[2] <= c[3]])
 def test_pcc1(F, orc, N, Tr, l1, l2, d):
     a, b = _data(N, Tr, d, "pcc1")
