@@ -118,6 +118,7 @@ def lib():
             L.fpcc_server_set_nz_mode.argtypes = [vp, i]
             L.fpcc_autotune.argtypes = [vp, i, i, C.c_double, C.c_char_p]
             L.fpcc_autotune_load.argtypes = [C.c_char_p]
+            L.fpcc_pair_form.argtypes = [i, i]
             L.fpcc_server_set_wavelet.argtypes = [vp, d, d, u, i, d, i]
             L.fpcc_server_destroy.argtypes = [vp]
             L.fpcc_put_station_window.argtypes = [vp, C.c_int32, C.c_int32, vp, i]
@@ -150,6 +151,17 @@ def choose_nz(N: int, Lag1: int, Lag2: int, mode: int = NZ_FAST) -> int:
     if nz <= 0:
         raise FpccError(-4, f"no supported correlation length for N={N}, lags [{Lag1},{Lag2}]")
     return nz
+
+
+PAIR_BLOCK, PAIR_TILED = 1, 2
+
+
+def pair_form(Nz: int, form: int = 0) -> int:
+    """Pair kernel used at padded length Nz (fpcc_pair_form); form > 0 selects it."""
+    r = lib().fpcc_pair_form(Nz, form)
+    if r < 0:
+        raise FpccError(r, f"pair form {form} does not run Nz={Nz}")
+    return r
 
 
 def load_tuning(path: str) -> dict:

@@ -308,6 +308,12 @@ extern "C" int fpcc_choose_nz(int N, int Lag1, int Lag2, int mode) {
 
 extern "C" int fpcc_max_block_len(void) { return kMenu[kMenuLen - 1]; }
 
+extern "C" int fpcc_pair_form(int Nz, int form) {
+  if (form > 0 && pair_form_set(Nz, form) != 0) return FPCC_EUNSUP;
+  if (!pair_supported(Nz) && !pair_tiled_supported(Nz)) return FPCC_EUNSUP;
+  return pair_form_get(Nz);
+}
+
 extern "C" int64_t fpcc_station_row_bytes(int method, int N, int Nz, int fmt) {
   switch (method) {
     case FPCC_PCC2: return fmt == FPCC_I16 ? 16 + 4 * (int64_t)Nz : (int64_t)Nz * (fmt == FPCC_F16 ? 4 : 8);

@@ -15,6 +15,8 @@
 // lengths N that are not on the menu (the N-point analytic signal, :104-124).
 #include <float.h>
 
+#include <atomic>
+
 #include <cooperative_groups.h>
 
 #include "kernels.cuh"
@@ -47,20 +49,6 @@ __device__ __forceinline__ float amp_factor(int rule, float m2, float eps) {
     return f_isnormal_pos(f) ? f : 0.0f;
   }
   return (m2 > eps) ? rsqrtf(m2) : 0.0f;   // src/ccs_cuda.cu:201-208, 223-230
-}
-
-// Bin i of a spectrum row; for block-scaled int16 rows the bins follow the
-// header and come back unscaled (the pair's scale product goes into the output).
-template <int FMT>
-__device__ __forceinline__ float2 load_bin(const void* base, int i) {
-  if constexpr (FMT == SPEC_F16) {
-    return __half22float2(reinterpret_cast<const __half2*>(base)[i]);
-  } else if constexpr (FMT == SPEC_I16) {
-    const short2 q = i16_row_bins(base)[i];
-    return make_float2((float)q.x, (float)q.y);
-  } else {
-    return reinterpret_cast<const float2*>(base)[i];
-  }
 }
 
 // v / sqrt(e1 e2) for the overlap energies e1, e2 (exact FP64 differences of the
@@ -140,19 +128,6 @@ __global__ void __launch_bounds__(T, 1) k_cwt_rows(CwtRowArgs a) {
 }
 
 // ------------------------------------------------------------ pairs
-// Cross-spectrum bin at position p in [0, Nz).  Full storage holds Nz bins;
-// Hermitian storage (real traces) holds bins 0..Nz/2.
-template <int FMT, bool HERM>
-__device__ __forceinline__ float2 zbin(const void* X1, const void* X2, int p, int Nz) {
-  if constexpr (HERM) {
-    const int h = Nz >> 1;
-    if (p <= h) return cconjmul(load_bin<FMT>(X1, p), load_bin<FMT>(X2, p));
-    return cconj(cconjmul(load_bin<FMT>(X1, Nz - p), load_bin<FMT>(X2, Nz - p)));
-  } else {
-    return cconjmul(load_bin<FMT>(X1, p), load_bin<FMT>(X2, p));
-  }
-}
-
 // Block size of the pair kernel for a half length H: enough threads that every
 // pass stages at most 16-24 complex values per thread.
 __host__ __device__ constexpr int pair_threads(int H) {
@@ -536,8 +511,48 @@ static cudaError_t launch_pairs_t(const PairArgs& a, cudaStream_t st) {
   }
 }
 
+// Pair-kernel form per padded length: the tiled kernel where it exists, unless
+// set otherwise (autotuner, fpcc_pair_form).  Lengths are few; a fixed table
+// with atomic entries is enough.
+namespace {
+constexpr int kFormSlots = 64;
+std::atomic<int> g_form_nz[kFormSlots];
+std::atomic<int> g_form_val[kFormSlots];
+}  // namespace
+
+int pair_form_get(int Nz) {
+  for (int i = 0; i < kFormSlots; i++) {
+    const int n = g_form_nz[i].load(std::memory_order_acquire);
+    if (n == 0) break;
+    if (n == Nz) return g_form_val[i].load(std::memory_order_relaxed);
+  }
+  return pair_tiled_supported(Nz) ? PAIR_FORM_TILED : PAIR_FORM_BLOCK;
+}
+
+int pair_form_set(int Nz, int form) {
+  if (form != PAIR_FORM_BLOCK && form != PAIR_FORM_TILED) return -1;
+  if (form == PAIR_FORM_TILED && !pair_tiled_supported(Nz)) return -1;
+  if (form == PAIR_FORM_BLOCK && !pair_supported(Nz)) return -1;
+  for (int i = 0; i < kFormSlots; i++) {
+    int n = g_form_nz[i].load(std::memory_order_acquire);
+    if (n == 0) {
+      g_form_val[i].store(form, std::memory_order_relaxed);
+      int expect = 0;
+      if (g_form_nz[i].compare_exchange_strong(expect, Nz, std::memory_order_acq_rel)) return 0;
+      n = expect;
+    }
+    if (n == Nz) {
+      g_form_val[i].store(form, std::memory_order_relaxed);
+      return 0;
+    }
+  }
+  return -1;
+}
+
 cudaError_t launch_pairs(const PairArgs& a, cudaStream_t st) {
   if (a.npairs <= 0) return cudaSuccess;
+  if (pair_tiled_supported(a.Nz) && pair_form_get(a.Nz) == PAIR_FORM_TILED) return launch_pairs_tiled(a, st);
+  if (!pair_supported(a.Nz)) return cudaErrorInvalidValue;
   const bool herm = (a.norm != 0);
   if (a.fmt == SPEC_I16) return herm ? cudaErrorInvalidValue : launch_pairs_t<SPEC_I16, false>(a, st);
   if (a.fmt == SPEC_F16) return herm ? launch_pairs_t<SPEC_F16, true>(a, st) : launch_pairs_t<SPEC_F16, false>(a, st);

@@ -111,8 +111,42 @@ struct PhaseArgs {
   const int* row_N;      //   ... and has row_N[r] samples (rows of different lengths in one launch)
 };
 
+// Bin i of a spectrum row; for block-scaled int16 rows the bins follow the
+// header and come back unscaled (the pair's scale product goes into the output).
+template <int FMT>
+__device__ __forceinline__ float2 load_bin(const void* base, int i) {
+  if constexpr (FMT == SPEC_F16) {
+    return __half22float2(reinterpret_cast<const __half2*>(base)[i]);
+  } else if constexpr (FMT == SPEC_I16) {
+    const short2 q = i16_row_bins(base)[i];
+    return make_float2((float)q.x, (float)q.y);
+  } else {
+    return reinterpret_cast<const float2*>(base)[i];
+  }
+}
+
+// Cross-spectrum bin at position p in [0, Nz).  Full storage holds Nz bins;
+// Hermitian storage (real traces) holds bins 0..Nz/2.
+template <int FMT, bool HERM>
+__device__ __forceinline__ float2 zbin(const void* X1, const void* X2, int p, int Nz) {
+  if constexpr (HERM) {
+    const int h = Nz >> 1;
+    if (p <= h) return cconjmul(load_bin<FMT>(X1, p), load_bin<FMT>(X2, p));
+    return cconj(cconjmul(load_bin<FMT>(X1, Nz - p), load_bin<FMT>(X2, Nz - p)));
+  } else {
+    return cconjmul(load_bin<FMT>(X1, p), load_bin<FMT>(X2, p));
+  }
+}
+
 bool spec_supported(int Nz);
 bool pair_supported(int Nz);
+// Tiled pair kernel (pairs_tiled.cu): half lengths R1 x 256 with R1 in {32, 40}.
+bool pair_tiled_supported(int Nz);
+cudaError_t launch_pairs_tiled(const PairArgs& a, cudaStream_t st);
+// Which pair kernel runs a padded length that both forms support.
+enum PairForm : int { PAIR_FORM_BLOCK = 1, PAIR_FORM_TILED = 2 };
+int pair_form_get(int Nz);
+int pair_form_set(int Nz, int form);   // 0, or -1 if the form does not support Nz
 size_t spec_smem_bytes(int Nz);
 size_t pair_smem_bytes(int Nz);
 

@@ -111,6 +111,14 @@ int fpcc_autotune(fpcc_ctx *ctx, int min_nz, int max_nz, double reuse, const cha
 int fpcc_autotune_load(const char *json_path);
 /* Largest length an in-block transform of this build supports. */
 int fpcc_max_block_len(void);
+/* Pair kernel that runs the FFT methods' pair stage at padded length Nz:
+ * FPCC_PAIR_BLOCK (one block per correlation, Stockham passes through shared
+ * memory) or FPCC_PAIR_TILED (Nz/2 = R1 x 256, R1 in {32, 40}: stage 1 in
+ * registers, warp-private second stage).  form > 0 selects it (the autotuner
+ * does this per length), form = 0 only queries.  Returns the form in use, or
+ * FPCC_EUNSUP if the requested form does not run Nz. */
+enum fpcc_pair_form { FPCC_PAIR_BLOCK = 1, FPCC_PAIR_TILED = 2 };
+int fpcc_pair_form(int Nz, int form);
 /* Elements per row of the station product of a method (for sizing buffers). */
 int64_t fpcc_station_row_elems(int method, int N, int Nz);
 /* Bytes per row of the station product of a method in a storage format. */
@@ -336,10 +344,14 @@ int fpcc_server_reset_stats(fpcc_server *s);
  * on `stream` (a cudaStream_t; NULL = legacy default stream).  Every
  * intermediate lives in one fixed device array of fpcc_noalloc_scratch_bytes()
  * (64 MiB) that each GPU loading the library holds until exit; calls needing
- * more are rejected with FPCC_EARG and a message.  The first call on a device
- * looks up that array's address (make it before any stream capture).  Calls
- * share the array: calls whose work overlaps on the GPU race and must be
- * serialised by the caller.  Errors: fpcc_noalloc_last_error(). */
+ * more are rejected with FPCC_EARG and a message.  Each call looks up that
+ * array's address in the current context (cudaGetSymbolAddress allocates
+ * nothing); the first call on a device loads the library's device code, so make
+ * it before any stream capture.  Calls share the array: calls whose work
+ * overlaps on the GPU race and must be serialised by the caller.  A CUDA error
+ * pending from the caller's earlier work is left in place and the call returns
+ * FPCC_ECUDA without running.  Errors: fpcc_noalloc_last_error() (empty after a
+ * successful call). */
 int fpcc_pcc2_noalloc(const float *d_x1, const float *d_x2, int64_t ldx, int N, int Tr, int Lag1, int Lag2,
                       float *d_y, int64_t ldy, void *stream);
 size_t fpcc_noalloc_scratch_bytes(void);
