@@ -11,17 +11,18 @@
 // kNoAllocScratchBytes.  Every GPU that loads the library holds that array until
 // the process exits.
 //
-// The array's host-side name is only a stand-in for the symbol: host code gets
-// the device address with cudaGetSymbolAddress, once per device, the first time
-// the entry point runs on that device (with the device current).  That first
-// call should therefore come before any stream capture.  All calls share the
-// array and it keeps the previous call's contents; this entry point writes every
-// element it later reads, so nothing needs clearing, but two calls whose work
-// overlaps on the GPU (on different streams, or from different host threads)
-// race on the array and must be serialised by the caller.
+// The array's host-side name is only a stand-in for the symbol: every call asks
+// the runtime for the device address in the current context with
+// cudaGetSymbolAddress (which allocates nothing), so the address stays right
+// after cudaDeviceReset or when another context is current.  The first call on a
+// device loads the library's device code there, so it should come before any
+// stream capture.  All calls share the array and it keeps the previous call's
+// contents; this entry point writes every element it later reads, so nothing
+// needs clearing, but two calls whose work overlaps on the GPU (on different
+// streams, or from different host threads) race on the array and must be
+// serialised by the caller.
 #include <cmath>
 #include <cstdio>
-#include <mutex>
 
 #include "../../include/fastpcc_gb300.h"
 #include "engine.h"
@@ -32,10 +33,6 @@ namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;   // 64 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
 
 thread_local char g_msg[256];
 
@@ -60,18 +57,10 @@ __global__ void k_pair_list(int2* pairs, int tr) {
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 int scratch_address(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail_na(FPCC_ECUDA, "cudaGetDevice failed");
-  if (dev < 0 || dev >= kMaxDevices) return fail_na(FPCC_EUNSUP, "device ordinal out of range");
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) return fail_na(FPCC_ECUDA, "cudaGetSymbolAddress of the scratch array failed");
-    g_scratch_addr[dev] = p;
-  }
-  *out = g_scratch_addr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr) return fail_na(FPCC_ECUDA, "cudaGetSymbolAddress of the scratch array failed");
+  *out = p;
   return 0;
 }
 
@@ -110,6 +99,7 @@ extern "C" const char* fpcc_noalloc_last_error(void) { return g_msg; }
 
 extern "C" int fpcc_pcc2_noalloc(const float* d_x1, const float* d_x2, int64_t ldx, int N, int Tr, int Lag1,
                                  int Lag2, float* d_y, int64_t ldy, void* stream) {
+  g_msg[0] = '\0';
   if (!d_x1 || !d_x2 || !d_y) return fail_na(FPCC_EARG, "null device pointer");
   if (N <= 0 || Tr <= 0 || ldx < N) return fail_na(FPCC_EARG, "N, Tr must be positive and ldx >= N");
   const int M = abs(Lag1) > abs(Lag2) ? abs(Lag1) : abs(Lag2);
@@ -136,6 +126,14 @@ extern "C" int fpcc_pcc2_noalloc(const float* d_x1, const float* d_x2, int64_t l
              need, kNoAllocScratchBytes);
     return FPCC_EARG;
   }
+  // An error left by the caller's earlier work stays with the caller (peek, do
+  // not clear); this call then reports that it did not run.
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) {
+    snprintf(g_msg, sizeof g_msg, "fpcc_pcc2_noalloc: not run, a CUDA error is pending from earlier work: %s",
+             cudaGetErrorString(e));
+    return FPCC_ECUDA;
+  }
   void* base = nullptr;
   int rc = scratch_address(&base);
   if (rc) return rc;
@@ -147,7 +145,6 @@ extern "C" int fpcc_pcc2_noalloc(const float* d_x1, const float* d_x2, int64_t l
   float2* spec = (float2*)(s + b_tw + b_st + 2 * b_an);
   int2* pairs = (int2*)(s + b_tw + b_st + 2 * b_an + b_sp);
   cudaStream_t cs = (cudaStream_t)stream;
-  cudaError_t e;
   k_twiddle_table<<<(N + 255) / 256 < 1024 ? (N + 255) / 256 : 1024, 256, 0, cs>>>(tw, N);
   k_pair_list<<<(Tr + 255) / 256, 256, 0, cs>>>(pairs, Tr);
   if ((e = cudaGetLastError()) != cudaSuccess) return fail_na(FPCC_ECUDA, cudaGetErrorString(e));
