@@ -38,7 +38,7 @@ _i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
 
 def build(ref: bool = False) -> None:
     """Compile the oracle (and, when asked and present, the reference CPU path)."""
-    subprocess.run(["make", "-s", "-C", HERE, "liboracle64.so"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle64.so", "libcpuref.so"], check=True)
     if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
