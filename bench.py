@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-served", action="store_true", help="skip the served (request loop) leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the uneven-batch and request-stream legs")
+    ap.add_argument("--no-config1", action="store_true", help="skip the plain-config leg (24 x 36000, +-3000)")
     ap.add_argument("--mixed-only", action="store_true", help="run only the uneven-batch and request-stream legs")
     ap.add_argument("--multi-only", action="store_true",
                     help="run only the packed analytic-signal stage leg (profiling); --windows sets its count")
@@ -245,9 +246,9 @@ def autotune(F, max_nz=1 << 20):
     """Measured padded-length table on this GPU (fpcc_autotune), outside any timed region."""
     ctx = F.Context(0)
     t0 = time.perf_counter()
-    path = os.path.join(ROOT, "gpurun_out", "autotune.json") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) \
-        else None
-    table = ctx.autotune(min_nz=512, max_nz=max_nz, reuse=8.0, path=path)
+    import tempfile
+    with tempfile.TemporaryDirectory(prefix="fpcc-tune-") as d:
+        table = ctx.autotune(min_nz=512, max_nz=max_nz, reuse=8.0, path=os.path.join(d, "autotune.json"))
     ctx.close()
     return {"lengths_timed": len(table) if table else None, "seconds": time.perf_counter() - t0}
 
@@ -658,60 +659,154 @@ def stack_leg(F, torch, ctx, stream, dev, d_y, n_sta, n_win, L, peak):
     return out
 
 
-def cpu_baseline(x, pairs, budget_s=12.0):
-    """The oracle's PCC2 on host cores over a bounded sample of the workload."""
-    from oracle import oracle as O
-    O.build()
-    threads = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    rng = np.random.default_rng(7)
+def _cpu_rate(fn, x1, x2, l1, l2, budget_s, batch):
+    """Correlations/s of fn over batches of (x1, x2) rows until budget_s has passed
+    (at least one batch); x1, x2 are callables giving the next batch."""
     done, t0 = 0, time.perf_counter()
-    batch = max(threads, 16)
-    while time.perf_counter() - t0 < budget_s:
-        sel = rng.choice(pairs.shape[0], batch, replace=False)
-        O.pcc2(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)
-        done += batch
+    while True:
+        a, b = x1(), x2()
+        fn(a, b, l1, l2)
+        done += a.shape[0]
+        dt = time.perf_counter() - t0
+        if dt >= budget_s:
+            return done / dt, done, dt
+
+
+def cpu_baseline(x, pairs, budget_s=10.0):
+    """The reference's pcc2_set arithmetic (single-precision transforms, seven per
+    correlation; oracle/cpuref.py) on the host cores over random pair-windows of
+    the all-pairs workload."""
+    from oracle import cpuref
+    threads = cpuref.threads()
+    rng = np.random.default_rng(7)
+    sel = []
+    batch = 16 * threads          # as the reference arm's steps
+
+    def take(col):
+        if col == 0:
+            sel.append(rng.choice(pairs.shape[0], batch, replace=False))
+        return x[pairs[sel[-1], col]]
+
+    cpuref.pcc2_set(x[pairs[:batch, 0]], x[pairs[:batch, 1]], -LAG, LAG)    # warm: thread pool, FFT plans
+    rate, done, dt = _cpu_rate(cpuref.pcc2_set, lambda: take(0), lambda: take(1), -LAG, LAG, budget_s, batch)
+    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "dtype": "f32",
+            "cpu_model": cpuref.cpu_model(),
+            "sample": f"{done} random pair-windows of the all-pairs workload, {dt:.1f} s: the reference's pcc2_set "
+                      f"steps (src/FFTapps.c:785-881) in single precision, seven transforms per correlation at the "
+                      f"reference padding 2^ceil(log2(N+M)), scipy FFT on {threads} threads in place of FFTW"}
+
+
+def cpu_methods_leg(x, pairs, budget_s=4.0):
+    """Per-method CPU rates of the reference's arithmetic (oracle/cpuref.py): the plain config (24 windows x 36,000, +-3000, every
+    window) and sampled pair-windows of the all-pairs config."""
+    from fastpcc_gb300 import synth
+    from oracle import cpuref
+    threads = cpuref.threads()
+    out = {"cores": threads, "cpu_model": cpuref.cpu_model(), "unit": UNIT,
+           "note": "single precision for PCC2, 1-bit and PCC1 (double sums), double for GNCC and WPCC, as the "
+                   "reference's CPU paths; scipy FFT in place of FFTW"}
+    a, b = synth.plain_pair(N=36000, n_windows=24, delay=150, tag="config1")
+    c1 = {}
+    for name, fn in cpuref.METHODS.items():
+        t0 = time.perf_counter()
+        fn(a, b, -3000, 3000)
+        c1[name] = 24 / (time.perf_counter() - t0)
+    out["config1"] = {"workload": "24 windows x 36000 samples, lags +-3000, every window", **c1}
+    rng = np.random.default_rng(9)
+    c2 = {}
+    for name, fn in cpuref.METHODS.items():
+        batch = threads if name == "pcc1" else 16 * threads
+        sel = []
+
+        def take(col):
+            if col == 0:
+                sel.append(rng.choice(pairs.shape[0], batch, replace=False))
+            return x[pairs[sel[-1], col]]
+
+        rate, done, dt = _cpu_rate(fn, lambda: take(0), lambda: take(1), -LAG, LAG, budget_s, batch)
+        c2[name] = {"value": rate, "sample": f"{done} random pair-windows, {dt:.1f} s"}
+    out["allpairs"] = {"workload": f"all-pairs: {N_SAMP} samples, lags +-{LAG}, random pair-windows", **c2}
+    nw = max(2, threads)
+    w1, w2, _ = synth.wavelet_pairs(n_pairs=nw, n_windows=1, N=65536, tag="bench/wpcc-cpu")
+    w1, w2 = w1.reshape(-1, 65536), w2.reshape(-1, 65536)
+    kw = dict(pmin=WAVELET["pmin"], pmax=WAVELET["pmax"], V=WAVELET["V"], wtype=WAVELET["type"])
+    cpuref.wpcc_set(w1[:1], w2[:1], -4000, 4000, **kw)        # wavelet spectra built outside the timing
+    t0 = time.perf_counter()
+    cpuref.wpcc_set(w1, w2, -4000, 4000, **kw)
     dt = time.perf_counter() - t0
-    return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{done} random pair-windows of the all-pairs workload (FP64 oracle, "
-                      f"reference padding 2^ceil(log2(N+M)), OpenMP over windows), {dt:.1f} s"}
+    out["wpcc"] = {"value": nw / dt, "sample": f"{nw} pair-windows of the wavelet config (65536 samples, 40 scales, "
+                                               f"+-4000), double precision, {dt:.1f} s"}
+    return out
+
+
+def config1_leg(F, cpu=None):
+    """The plain config: stations A and B, 24 windows of 36,000 samples, lags
+    +-3000, padded length 2^17; GNCC, 1-bit, PCC2 and PCC1 for the 24 same-index
+    window pairs through the batched host entry point and the plain per-pair
+    drop-in, each against the FP64 oracle."""
+    from fastpcc_gb300 import synth
+    from oracle import oracle as O
+    a, b = synth.plain_pair(N=36000, n_windows=24, delay=150, tag="config1")
+    l1, l2, nz = -3000, 3000, 1 << 17
+    calls = {"gncc": (F.GNCC, O.gncc), "cc1b": (F.CC1B, O.cc1b), "pcc2": (F.PCC2, O.pcc2), "pcc1": (F.PCC1, O.pcc1)}
+    out = {"workload": "24 windows x 36000 samples, lags +-3000, Nz = 131072 (FFT methods)", "unit": UNIT}
+    for name, (m, orc) in calls.items():
+        mode = nz if m != F.PCC1 else F.NZ_FAST
+        r = {}
+        for arm, plain in (("batched", False), ("plain", True)):
+            F.correlate(m, a[:2], b[:2], l1, l2, plain=plain, nz_mode=mode)     # warm (kernels, plans)
+            t0 = time.perf_counter()
+            y = F.correlate(m, a, b, l1, l2, plain=plain, nz_mode=mode)
+            r[arm] = 24 / (time.perf_counter() - t0)
+            k = 24 if m != F.PCC1 else 3
+            r[f"max_rel_err_{arm}"] = float(O.relerr(y[:k], orc(a[:k], b[:k], l1, l2)).max())
+        r["err_sample"] = "all 24 windows" if m != F.PCC1 else "3 windows"
+        if cpu is not None:
+            r["cpu"] = cpu["config1"].get(name)
+        out[name] = r
+    return out
 
 
 def run_reference(args):
+    """The reference arm: the reference's pcc2_set arithmetic on the host cores
+    (oracle/cpuref.py: single-precision transforms, seven per correlation, all
+    host threads), random pair-windows of the same all-pairs workload."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from fastpcc_gb300 import synth
+    from oracle import cpuref
     n_sta, n_win = args.stations, args.windows
     x, _ = synth.all_pairs(n_stations=n_sta, n_windows=n_win, N=N_SAMP)
     x = x.reshape(n_sta * n_win, N_SAMP)
     pairs = all_pairs_index(n_sta, n_win)
-    from oracle import oracle as O
-    O.build()
-    threads = os.cpu_count() or 1
+    threads = cpuref.threads()
     rng = np.random.default_rng(11)
-    per_step = max(2 * threads, 32)
+    per_step = 16 * threads
     for _ in range(args.warmup):
         sel = rng.choice(pairs.shape[0], threads, replace=False)
-        O.pcc2(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)
+        cpuref.pcc2_set(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)
     times = []
     for _ in range(args.steps):
         sel = rng.choice(pairs.shape[0], per_step, replace=False)
         t0 = time.perf_counter()
-        O.pcc2(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)
+        cpuref.pcc2_set(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = per_step * args.steps / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded noise + shared band-passed component)",
         "config": {"workload": f"all-pairs PCC2: {n_sta} stations x {n_win} windows x {N_SAMP} samples, "
                                f"lags +-{LAG}", "sample_per_step": per_step},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{per_step} random pair-windows per step (FP64 oracle port of "
-                                   f"src/FFTapps.c pcc2_set; the reference's own source is absent on this host)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "dtype": "f32",
+                         "cpu_model": cpuref.cpu_model(),
+                         "sample": f"{per_step} random pair-windows per step: the reference's pcc2_set steps "
+                                   f"(src/FFTapps.c:785-881) in single precision, seven transforms per "
+                                   f"correlation, scipy FFT on {threads} threads in place of FFTW (the reference's "
+                                   f"own sources are not on this host)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -836,6 +931,12 @@ def run_ours(args):
     if traffic is not None:
         # the profile is of the default workload with F32 spectra
         traffic = traffic * P / float(N_STA * (N_STA - 1) // 2 * N_WIN) if fmt == F.F32 else None
+    # FP32 work of the pair kernel per correlation: the Nz/2-point inverse
+    # transform (5 H log2 H) and the cross-spectrum packing (4 complex products
+    # and 13 further operations per two packed points: 19 per point of Nz/2)
+    H = Nz // 2
+    flops = P * (5.0 * H * np.log2(H) + 19.0 * H)
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12      # nominal: 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
 
     # --- parity spot check against the oracle ---
     err = None
@@ -899,8 +1000,14 @@ def run_ours(args):
                  "serving": serving_leg(F, nz_mode=F.NZ_TUNED)}
 
     cpu = None
+    cpu_methods = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(x, pairs)
+        cpu_methods = cpu_methods_leg(x, pairs)
+
+    config1 = None
+    if rank == 0 and not args.no_config1:
+        config1 = config1_leg(F, cpu_methods)
 
     if rank == 0:
         line = {
@@ -924,9 +1031,17 @@ def run_ours(args):
             "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_pairs (PCC2 pair stage)", "kernel_ms": t_pair * 1e3,
-                         "alg_bytes_per_launch": alg_bytes},
+                         "traffic_source": "profiles/pcc2_pairs_allpairs.txt (ncu dram__bytes of the pair kernel "
+                                           "on 16 windows, scaled by windows); not measured in this run",
+                         "kernel": f"PCC2 pair stage ({'tiled' if F.pair_form(Nz) == F.PAIR_TILED else 'block'} "
+                                   f"kernel)", "kernel_ms": t_pair * 1e3,
+                         "alg_bytes_per_launch": alg_bytes,
+                         "fp32": {"flops_per_launch": flops, "achieved_tflops": flops / t_pair / 1e12,
+                                  "peak_tflops": fp32_peak, "peak_kind": "nominal",
+                                  "frac": flops / t_pair / 1e12 / fp32_peak}},
             "cpu_baseline": cpu,
+            "cpu_methods": cpu_methods,
+            "config1": config1,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

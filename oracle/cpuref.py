@@ -24,6 +24,12 @@ do not travel to the machine that runs the benchmark, so this is a port:
 * ``pcc1_set``  :611-783 (CPU branch): single-precision analytic signals and
   AmpNormf, then pcc1f_lowlevel (:251-278) with the station-2 phase first:
   float square roots, double sums (cpuref.c, OpenMP over windows and lags).
+* ``wpcc_set``  tspcc2_set :1076-1255 (CPU branch): double precision, 4S+3
+  transforms of the padded length per correlation; the wavelet family comes
+  from the oracle's restatement of CreateWaveletFamily.
+
+Windows are spread over the host threads, each with single-threaded FFTs, as
+the reference's OpenMP loops over windows.
 """
 from __future__ import annotations
 
@@ -57,8 +63,11 @@ def cpu_model() -> str:
                 return line.split(":", 1)[1].strip()
     parts = sorted({line.split(":", 1)[1].strip() for line in text.splitlines() if line.startswith("CPU part")})
     impl = sorted({line.split(":", 1)[1].strip() for line in text.splitlines() if line.startswith("CPU implementer")})
+    arm = {"0xd4f": "Arm Neoverse V2", "0xd40": "Arm Neoverse V1", "0xd0c": "Arm Neoverse N1",
+           "0xd49": "Arm Neoverse N2", "0xd8e": "Arm Neoverse N3", "0xd84": "Arm Neoverse V3"}
     if parts:
-        return f"CPU implementer {','.join(impl)} part {','.join(parts)}"
+        names = [arm.get(p, f"part {p}") for p in parts] if impl == ["0x41"] else [f"part {p}" for p in parts]
+        return f"{', '.join(names)} (CPU implementer {','.join(impl)})"
     return "unknown"
 
 
@@ -76,6 +85,27 @@ def _cpulib():
             L.cpu_pcc1f_set.restype = None
             _lib = L
     return _lib
+
+
+_pool = None
+
+
+def _rows_in_parallel(fn, x1, x2, Lag1, Lag2):
+    """fn over row blocks of (x1, x2) on all host threads, one block per thread with
+    single-threaded FFTs (the reference's OpenMP loop over windows); numpy and
+    scipy release the GIL inside their kernels."""
+    global _pool
+    n = threads()
+    Tr = x1.shape[0]
+    if n == 1 or Tr < 2:
+        return fn(x1, x2, Lag1, Lag2, 1)
+    import concurrent.futures as cf
+    with _lock:
+        if _pool is None:
+            _pool = cf.ThreadPoolExecutor(max_workers=n)
+    cuts = np.linspace(0, Tr, min(n, Tr) + 1).astype(int)
+    futs = [_pool.submit(fn, x1[lo:hi], x2[lo:hi], Lag1, Lag2, 1) for lo, hi in zip(cuts[:-1], cuts[1:]) if hi > lo]
+    return np.concatenate([f.result() for f in futs])
 
 
 def _lags(Lag1, Lag2):
@@ -122,7 +152,8 @@ def ampnormf(a):
 
 
 def pcc2_set(x1, x2, Lag1, Lag2, workers=None):
-    workers = workers or threads()
+    if workers is None:
+        return _rows_in_parallel(pcc2_set, x1, x2, Lag1, Lag2)
     Tr, N = x1.shape
     Nz = nz_rule(N, Lag1, Lag2)
 
@@ -153,7 +184,8 @@ def _overlap_norms(x1, x2, lags):
 
 
 def ccgn_set(x1, x2, Lag1, Lag2, workers=None):
-    workers = workers or threads()
+    if workers is None:
+        return _rows_in_parallel(ccgn_set, x1, x2, Lag1, Lag2)
     Tr, N = x1.shape
     Nz = nz_rule(N, Lag1, Lag2)
     a = x1.astype(np.float64)
@@ -167,7 +199,8 @@ def ccgn_set(x1, x2, Lag1, Lag2, workers=None):
 
 
 def cc1b_set(x1, x2, Lag1, Lag2, workers=None):
-    workers = workers or threads()
+    if workers is None:
+        return _rows_in_parallel(cc1b_set, x1, x2, Lag1, Lag2)
     Tr, N = x1.shape
     Nz = nz_rule(N, Lag1, Lag2)
     s1 = np.where(x1 >= 0, np.float32(1), np.float32(-1))
@@ -190,6 +223,80 @@ def pcc1_set(x1, x2, Lag1, Lag2, workers=None):
     L = Lag2 - Lag1 + 1
     y = np.zeros((Tr, L), np.float32)
     _cpulib().cpu_pcc1f_set(y, p1.reshape(-1), p2.reshape(-1), N, Tr, Lag1, Lag2, L)
+    return y
+
+
+_family = {}
+
+
+def _wavelet_spectra(N, Lag1, Lag2, pmin, pmax, V, wtype, op1):
+    """Padded length, scales, Ls0, C and the S wavelet spectra (FP64) of
+    src/FFTapps.c:1087-1147, from the oracle's restatement of the family."""
+    key = (N, Lag1, Lag2, pmin, pmax, V, wtype, op1)
+    with _lock:
+        if key in _family:
+            return _family[key]
+    from oracle import oracle as O
+    st = O.wpcc_setup(N, Lag1, Lag2, pmin, pmax, V, wtype, op1)
+    M = max(abs(Lag1), abs(Lag2))
+    Nz0 = 1 << math.ceil(math.log2(N + M))
+    scale, Ls, center, taps = O.wavelet_family(wtype, st["J"], V, Nz0, st["s0"], st["op1"])
+    Nz, S = st["Nz"], st["S"]
+    fw = np.zeros((S, Nz), np.complex128)
+    off = 0
+    for k in range(S):
+        c, l = int(center[k]), int(Ls[k])
+        t = taps[off:off + l]
+        fw[k, :l - c] = t[c:]
+        if c:
+            fw[k, Nz - c:] = t[:c]
+        off += l
+    fw = sfft.fft(fw, axis=1, workers=threads())
+    C = 1.0 / (float(np.sum(1.0 / scale)) * N)
+    fam = (Nz, scale, int(Ls[-1]), C, fw)
+    with _lock:
+        _family[key] = fam
+    return fam
+
+
+def _ampnorm(a):
+    """AmpNorm (src/FFTapps.c:147-175): x / sqrt(|x|^2 + 1e-6 max|x|^2), double."""
+    m2 = a.real * a.real + a.imag * a.imag
+    eps = 1e-6 * np.max(m2, axis=-1, keepdims=True)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        f = 1.0 / np.sqrt(m2 + eps)
+    return np.where(np.isfinite(f), a * f, 0)
+
+
+def wpcc_set(x1, x2, Lag1, Lag2, pmin, pmax, V=2, wtype=-3, op1=0.0, workers=None):
+    """tspcc2_set (src/FFTapps.c:1076-1255), CPU path, double precision: traces at
+    offset Ls0 scaled by 1/Nz, DFT; per scale the band IDFT(X W_s), AmpNorm, DFT;
+    sum_s conj(P1_s) P2_s / (scale_s Nz), IDFT; C Re(.) at the lags."""
+    if workers is None:
+        return _rows_in_parallel(lambda a, b, l1, l2, w: wpcc_set(a, b, l1, l2, pmin, pmax, V, wtype, op1, w),
+                                 x1, x2, Lag1, Lag2)
+    Tr, N = x1.shape
+    Nz, scale, Ls0, Cc, fw = _wavelet_spectra(N, Lag1, Lag2, pmin, pmax, V, wtype, op1)
+    S = fw.shape[0]
+    lag0, L = _lags(Lag1, Lag2)
+    L = abs(Lag2 - Lag1 + 1)   # :1084
+    y = np.zeros((Tr, L), np.float32)
+    idx = (lag0 + np.arange(L)) % Nz
+    for tr in range(Tr):
+        X = []
+        for x in (x1[tr], x2[tr]):
+            z = np.zeros(Nz, np.complex128)
+            z[Ls0:Ls0 + N] = x.astype(np.float64) / Nz
+            X.append(sfft.fft(z, workers=workers))
+        acc = np.zeros(Nz, np.complex128)
+        for s0 in range(0, S, 8):
+            fs = fw[s0:s0 + 8]
+            P1 = sfft.fft(_ampnorm(sfft.ifft(X[0][None] * fs, axis=1, workers=workers)), axis=1, workers=workers)
+            P2 = sfft.fft(_ampnorm(sfft.ifft(X[1][None] * fs, axis=1, workers=workers)), axis=1, workers=workers)
+            w = 1.0 / (scale[s0:s0 + 8] * Nz)
+            acc += np.sum(w[:, None] * np.conj(P1) * P2, axis=0)
+        out = sfft.ifft(acc, workers=workers) * Nz
+        y[tr] = (Cc * out.real[idx]).astype(np.float32)
     return y
 
 

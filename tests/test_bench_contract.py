@@ -23,3 +23,4 @@ def test_reference_arm_json_line():
     assert d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["value"] == d["value"]
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
     assert "workload" in d["config"]
+    assert d["dtype"] == "f32" and d["cpu_baseline"]["dtype"] == "f32"   # the reference's pcc2_set precision

@@ -32,6 +32,13 @@ def test_pcc1_matches_oracle(orc, cr):
     assert relerr(cr.pcc1_set(a, b, -200, 150), orc.pcc1(a, b, -200, 150)) < 1e-4
 
 
+def test_wpcc_matches_oracle(orc, cr):
+    a, b = synth.plain_pair(N=3000, n_windows=2, delay=30, fs=20.0, band=(0.02, 5.0), tag="cpuref/wpcc")
+    for wt in (-1, -3):
+        y64 = orc.wpcc(a, b, -300, 300, 4.0, 80.0, V=3, wtype=wt)
+        assert relerr(cr.wpcc_set(a, b, -300, 300, 4.0, 80.0, V=3, wtype=wt), y64) < 1e-6
+
+
 def test_reference_padding_and_cpu_model(cr):
     assert cr.nz_rule(36000, -3000, 3000) == 65536
     assert cr.nz_rule(18000, -2000, 2000) == 32768

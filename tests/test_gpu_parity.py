@@ -1,9 +1,10 @@
 """GPU parity: every method through the C ABI against the FP64 oracle.
 
 Error metric: max over lags of |y - y64| divided by max |y64| of the same
-correlation (relative to its own peak).  Tolerance 1e-4 for every FP32 path;
-FP16 spectrum storage is held to 3e-4 (its measured error sits near 1e-4); the
-1-bit popcount numerators must be bit-exact.
+correlation (relative to its own peak).  Tolerance 1e-4 for every FP32 path and
+for block-scaled int16 storage (the 4-byte storage format the library offers
+for the 1e-4 target); the 1-bit popcount numerators must be bit-exact.  FP16
+storage is not within 1e-4 (see test_pcc2_fp16_storage) and is not offered for it.
 """
 import numpy as np
 import pytest
@@ -92,9 +93,16 @@ def test_pccv_gpu_normalisation(F, orc):
 
 
 def test_pcc2_fp16_storage(F, orc):
+    """FP16 phase spectra: each stored value carries a relative rounding error up
+    to 2^-11, about 1e-4 of the peak after the inverse transform (1.0-1.3e-4
+    measured on the all-pairs windows), so FP16 does not meet the 1e-4 target and
+    int16 is the 4-byte format for it.  This guards the FP16 path against
+    regressions at its own measured level, 3e-4."""
     a, b = _data(4500, 3, -200, "f16")
     y64 = orc.pcc2(a, b, -450, 450)
-    assert relerr(F.pcc2_set(a, b, -450, 450, fmt=F.F16), y64) < 3e-4
+    err = relerr(F.pcc2_set(a, b, -450, 450, fmt=F.F16), y64)
+    assert err < 3e-4
+    assert relerr(F.pcc2_set(a, b, -450, 450, fmt=F.I16), y64) < TOL
 
 
 @pytest.mark.parametrize("N,l1,l2,nz", [(1000, -100, 100, 1), (4500, -450, 450, 1), (18000, -2000, 2000, 1),

@@ -214,22 +214,25 @@ def test_server_uneven_lengths_share_launches(F, orc):
         assert np.array_equal(o, outs[i]), reqs[i]
 
 
-def test_server_f16_storage(F, orc):
+def test_server_16bit_storage(F, orc):
+    """Block-scaled int16 storage (the server's 4-byte format for the 1e-4 target)
+    within 1e-4 of the FP64 oracle; FP16 storage on the same requests stays at
+    its own measured level (not offered for 1e-4: each FP16 value carries a
+    relative rounding error up to 2^-11, a few 1e-4 of the peak on these short
+    windows)."""
     lengths = [2048, 3000, 3557]
     xs = _uneven_windows(lengths, "serve/f16")
     reqs = _uneven(9, 40, lengths, [0, 4])
-    srv = F.Server(hbm_budget=1 << 30, fmt=F.F16)
-    for w, x in xs.items():
-        for s in range(5):
-            srv.put(s, w, x[s])
-    outs = _run(F, srv, reqs)
-    srv.close()
-    for (m, s1, s2, w, l1, l2, v), out in zip(reqs, outs):
-        a, b = xs[w][s1], xs[w][s2]
-        # FP16 storage of unit-modulus phase spectra / phase signals, FP32 arithmetic:
-        # each stored value carries a relative rounding error of up to 2^-11, which
-        # leaves about 4e-4 / sqrt(Nz) of the peak on these short windows
-        assert relerr(out, _oracle(orc, m, a, b, l1, l2, v)) < 5e-4, (m, len(a), l1, l2)
+    for fmt, tol in ((F.I16, 1e-4), (F.F16, 5e-4)):
+        srv = F.Server(hbm_budget=1 << 30, fmt=fmt)
+        for w, x in xs.items():
+            for s in range(5):
+                srv.put(s, w, x[s])
+        outs = _run(F, srv, reqs)
+        srv.close()
+        for (m, s1, s2, w, l1, l2, v), out in zip(reqs, outs):
+            a, b = xs[w][s1], xs[w][s2]
+            assert relerr(out, _oracle(orc, m, a, b, l1, l2, v)) < tol, (fmt, m, len(a), l1, l2)
 
 
 def test_server_wpcc_requests(F, orc):
