@@ -36,11 +36,29 @@ _c128p = np.ctypeslib.ndpointer(np.complex128, flags="C_CONTIGUOUS")
 _i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
 
 
+def reference_sources() -> str:
+    """Folder holding the reference's src/: FPCC_REFSRC, else the REFSRC default of
+    this folder's Makefile (the one place that names it)."""
+    env = os.environ.get("FPCC_REFSRC")
+    if env:
+        return env
+    with open(os.path.join(HERE, "Makefile")) as f:
+        for line in f:
+            if line.startswith("REFSRC") and "?=" in line:
+                return line.split("?=", 1)[1].strip()
+    return ""
+
+
+def make_vars() -> list:
+    """REFSRC for make when FPCC_REFSRC overrides the Makefile's default."""
+    return [f"REFSRC={os.environ['FPCC_REFSRC']}"] if os.environ.get("FPCC_REFSRC") else []
+
+
 def build(ref: bool = False) -> None:
     """Compile the oracle (and, when asked and present, the reference CPU path)."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle64.so", "libcpuref.so"], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, *make_vars(), "ref"], check=True)
 
 
 def lib():

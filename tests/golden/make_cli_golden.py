@@ -22,7 +22,10 @@ import tempfile
 import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-EXAMPLES = "/root/reference/examples/G"
+sys.path.insert(0, ROOT)
+from oracle import oracle as _O   # noqa: E402
+
+EXAMPLES = os.path.join(os.path.dirname(os.path.normpath(_O.reference_sources())), "examples", "G")
 DAYS = 3
 WPCC = dict(pmin=25.0, pmax=330.0)   # seconds, as in the reference's example script
 AWHITE = (0.005, 0.03)                # Hz, whitening band for the preprocessing run
@@ -39,7 +42,7 @@ def read_sac(path):
 
 
 def main():
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "cli"], check=True)
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), *_O.make_vars(), "cli"], check=True)
     cli = os.path.join(ROOT, "oracle", "_ref", "PCC_fullpair_1b")
     can = sorted(glob.glob(f"{EXAMPLES}/CAN/*.LHZ.*.SACvelbp"))
     ech = sorted(glob.glob(f"{EXAMPLES}/ECH/*.LHZ.*.SACvelbp"))

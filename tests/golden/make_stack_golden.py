@@ -41,7 +41,7 @@ def traces(L, K, seed):
 
 
 def main():
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "wt"], check=True)
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), *O.make_vars(), "wt"], check=True)
     R = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libref_wt.so"))
     R.ref_wt_pair.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint, C.c_int, C.c_uint, C.c_uint,
                               C.c_double, C.c_double]

@@ -68,11 +68,11 @@ def test_reference_cli_links_against_library(libpath):
     """The reference CLI (src/PCC_fullpair_1b.c and FFTapps.c built with -DCUDAON)
     links with libfastpcc_gb300.so in place of ccs_cuda.o and no undefined symbol
     (needs the reference sources, present only where they are mounted)."""
-    src = "/root/reference/src"
-    if not os.path.isdir(src):
+    from oracle import oracle as O
+    if not os.path.isdir(O.reference_sources()):
         pytest.skip("reference sources not present")
-    r = subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-B", "cli_gb300"], capture_output=True,
-                       text=True)
+    r = subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), *O.make_vars(), "-B", "cli_gb300"],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
     exe = os.path.join(ROOT, "oracle", "_ref", "PCC_fullpair_1b_gb300")
     out = subprocess.run(["nm", "-D", "--undefined-only", exe], capture_output=True, text=True, check=True).stdout

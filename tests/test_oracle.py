@@ -132,7 +132,7 @@ def test_nz_independence(orc):
 
 def test_reference_live_if_present(orc):
     """Where the reference sources exist, the restatement equals them on fresh inputs."""
-    if not os.path.isdir("/root/reference/src"):
+    if not os.path.isdir(orc.reference_sources()):
         pytest.skip("reference sources absent")
     orc.build(ref=True)
     a, b = synth.plain_pair(N=1500, n_windows=2, tag="live")
