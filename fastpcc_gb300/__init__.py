@@ -121,6 +121,8 @@ def lib():
             L.fpcc_pair_form.argtypes = [i, i]
             L.fpcc_server_set_wavelet.argtypes = [vp, d, d, u, i, d, i]
             L.fpcc_server_destroy.argtypes = [vp]
+            L.fpcc_server_register_output.argtypes = [vp, vp, C.c_size_t]
+            L.fpcc_server_unregister_output.argtypes = [vp, vp]
             L.fpcc_put_station_window.argtypes = [vp, C.c_int32, C.c_int32, vp, i]
             L.fpcc_submit.argtypes = [vp, C.POINTER(Request)]
             L.fpcc_submit.restype = i64
@@ -326,8 +328,10 @@ class Context:
                                     C.c_void_p(d_y or 0), ldy, C.c_void_p(d_num or 0)))
 
     def autotune(self, min_nz=512, max_nz=1 << 19, reuse=8.0, path=None) -> dict:
-        """Times every usable padded length on this GPU (fpcc_autotune); the table
-        then drives NZ_TUNED.  Returns {Nz: (pair ns per correlation, station ns per window)}."""
+        """Times every usable padded length on this GPU, and both pair kernels where
+        two run a length (fpcc_autotune); the table then drives NZ_TUNED and the
+        faster kernel is selected.  Returns {Nz: (pair ns per correlation,
+        station ns per window, kernel form or 0)}."""
         check(lib().fpcc_autotune(self._h, min_nz, max_nz, float(reuse), path.encode() if path else None))
         return load_tuning(path) if path else {}
 
@@ -387,6 +391,18 @@ class Server:
         except Exception:
             pass
 
+    def register_output(self, arr):
+        """Lets results land in `arr` (a C-contiguous numpy array holding the
+        requests' output rows) straight from the device (fpcc_server_register_output);
+        keep `arr` alive until unregister_output or close."""
+        assert arr.flags.c_contiguous
+        check(lib().fpcc_server_register_output(self._h, arr.ctypes.data, arr.nbytes))
+        self._keep[("out", arr.ctypes.data)] = arr
+
+    def unregister_output(self, arr):
+        check(lib().fpcc_server_unregister_output(self._h, arr.ctypes.data))
+        self._keep.pop(("out", arr.ctypes.data), None)
+
     def put(self, sta: int, window: int, x):
         x = np.ascontiguousarray(x, dtype=np.float32)
         check(lib().fpcc_put_station_window(self._h, sta, window, x.ctypes.data, x.shape[0]))
@@ -434,7 +450,7 @@ class Server:
 
     def drain(self):
         check(lib().fpcc_server_drain(self._h))
-        self._keep.clear()
+        self._keep = {k: v for k, v in self._keep.items() if isinstance(k, tuple)}   # registered outputs stay
 
     def stats(self) -> dict:
         s = ServerStats()

@@ -32,6 +32,7 @@
 #include <set>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -46,6 +47,8 @@
 
 namespace fpcc {
 
+struct Server;
+
 // Makes a freshly created context allocate from `pool` (which it does not own).
 int ctx_share_pool(fpcc_ctx* c, cudaMemPool_t pool);
 void set_last_error(const char* msg);
@@ -56,7 +59,7 @@ int cuda_err(cudaError_t e, const char* what) {
   char buf[256];
   snprintf(buf, sizeof buf, "server: %s: %s", what, cudaGetErrorString(e));
   set_last_error(buf);
-  return cuda_err(cudaGetLastError(), "row copy");
+  return FPCC_ECUDA;
 }
 }  // namespace
 
@@ -141,15 +144,32 @@ struct InFlight {
   size_t h_bytes = 0;
   char* h_up = nullptr;            // pinned upload staging (index arrays), bump-allocated
   size_t up_bytes = 0, up_used = 0;
+  std::vector<std::pair<char*, size_t>> up_full;   // staging blocks this batch has filled
+  Server* srv = nullptr;
+  std::vector<std::pair<char*, size_t>> out_ranges;  // registered result ranges (snapshot at batch start)
+  std::vector<char> direct;        // per request: result copied straight into the caller's buffer
   std::vector<std::pair<Slab*, int>> pinned_rows;
   int err = 0;
   std::string err_msg;             // the worker's message for err
 };
 
+void* pinned_get(Server* s, size_t bytes, size_t* got);
+
 // Copy a small host array into the batch's pinned staging and queue its upload.
+// A batch whose uploads outgrow its staging block (each upload starts on a
+// 256-byte boundary, so many small groups can exceed the estimate) continues in
+// another pinned block; all of them return to the pool with the batch.
 cudaError_t upload(InFlight& fl, void* dst, const void* src, size_t bytes, cudaStream_t st) {
-  const size_t off = (fl.up_used + 255) & ~size_t(255);
-  if (off + bytes > fl.up_bytes) return cudaErrorMemoryAllocation;
+  size_t off = (fl.up_used + 255) & ~size_t(255);
+  if (off + bytes > fl.up_bytes) {
+    size_t got = 0;
+    char* p = (char*)pinned_get(fl.srv, std::max(bytes, fl.up_bytes), &got);
+    if (!p) return cudaErrorMemoryAllocation;
+    if (fl.h_up) fl.up_full.push_back({fl.h_up, fl.up_bytes});
+    fl.h_up = p;
+    fl.up_bytes = got;
+    off = 0;
+  }
   memcpy(fl.h_up + off, src, bytes);
   fl.up_used = off + bytes;
   return cudaMemcpyAsync(dst, fl.h_up + off, bytes, cudaMemcpyHostToDevice, st);
@@ -243,6 +263,8 @@ struct Server {
   void* d_pl = nullptr; size_t n_pl = 0;
   void* d_desc = nullptr; size_t n_desc = 0;
   std::vector<void*> pinned_pool;
+  // host ranges that results may be copied into directly: (base, bytes, registered by the server)   [mu]
+  std::vector<std::tuple<char*, size_t, bool>> out_ranges;
   // stats
   std::vector<double> lat_ms;
   int64_t completed = 0, batches = 0, station_rows = 0, pair_stages = 0;
@@ -456,9 +478,7 @@ Slab& slab_of(Server* s, const Product& p) {
 }
 
 void touch(Slab& sl, int r) {
-  sl.lru.erase(sl.pos[r]);
-  sl.lru.push_front(r);
-  sl.pos[r] = sl.lru.begin();
+  sl.lru.splice(sl.lru.begin(), sl.lru, sl.pos[r]);   // moves the node: no allocation, iterator stays valid
 }
 
 // Row holding `key`, or -1.
@@ -694,8 +714,58 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   return 0;
 }
 
+// Results of a group from the device block dy (requests `reqs` in output order,
+// batch indices first.., the same layout as the batch's result block at
+// out_base) to where they go.  A request whose output lies in a range the caller
+// registered (page-locked host memory) is copied straight into it, and runs of
+// such rows at one stride as a single strided copy; the others go to the batch's
+// pinned block, from which the completer threads copy them out.
+cudaError_t d2h_results(InFlight& fl, const std::vector<Req*>& reqs, size_t first, size_t out_base, const char* dy,
+                        cudaStream_t st) {
+  const size_t n = reqs.size();
+  auto dst_of = [&](size_t i) -> char* {
+    const Req& q = *reqs[i];
+    return q.r.method == FPCC_CC1B_POPCOUNT ? (char*)q.r.num : (char*)q.r.y;
+  };
+  auto bytes_of = [&](size_t i) -> size_t {
+    return (size_t)reqs[i]->L * (reqs[i]->r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
+  };
+  auto registered = [&](size_t i) {
+    const char* d = dst_of(i);
+    if (!d || fl.out_ranges.empty()) return false;
+    const size_t b = bytes_of(i);
+    for (auto& r : fl.out_ranges)
+      if (d >= r.first && d + b <= r.first + r.second) return true;
+    return false;
+  };
+  size_t off = 0;
+  cudaError_t e = cudaSuccess;
+  for (size_t i = 0; i < n && e == cudaSuccess;) {
+    const size_t b = bytes_of(i);
+    size_t j = i + 1, run_bytes = b;
+    if (registered(i)) {
+      // rows of equal length at a constant stride: one strided copy
+      const ptrdiff_t stride = (j < n) ? dst_of(j) - dst_of(i) : (ptrdiff_t)b;
+      if (stride >= (ptrdiff_t)b && stride <= ((ptrdiff_t)1 << 30))
+        while (j < n && bytes_of(j) == b && registered(j) && dst_of(j) - dst_of(j - 1) == stride) j++;
+      for (size_t k = i; k < j; k++) fl.direct[first + k] = 1;
+      if (j - i == 1)
+        e = cudaMemcpyAsync(dst_of(i), dy + off, b, cudaMemcpyDeviceToHost, st);
+      else
+        e = cudaMemcpy2DAsync(dst_of(i), (size_t)stride, dy + off, b, b, j - i, cudaMemcpyDeviceToHost, st);
+      off += b * (j - i);
+    } else {
+      while (j < n && !registered(j)) run_bytes += bytes_of(j++);
+      e = cudaMemcpyAsync((char*)fl.h_out + out_base + off, dy + off, run_bytes, cudaMemcpyDeviceToHost, st);
+      off += run_bytes;
+    }
+    i = j;
+  }
+  return e;
+}
+
 int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base,
-              bool products_only) {
+              bool products_only, size_t first = 0) {
   const int n = (int)reqs.size();
   const int m = g.method;
   std::vector<int64_t> k1(n), k2(n);
@@ -794,7 +864,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
                          g.lag0 + g.L - 1, g.v, E, ldE, (float*)dy, g.L, nullptr);
   }
   if (rc) return rc;
-  cudaMemcpyAsync((char*)fl.h_out + out_base, dy, ybytes, cudaMemcpyDeviceToHost, s->st);
+  if (cudaError_t ce = d2h_results(fl, reqs, first, out_base, (const char*)dy, s->st)) return cuda_err(ce, "results");
   return 0;
 }
 
@@ -929,7 +999,7 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
 // vary per request; products are ensured per window length, then every
 // correlation of the group runs in one launch reading its rows in place.
 int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base,
-                     bool products_only, Lane* on = nullptr) {
+                     bool products_only, Lane* on = nullptr, size_t first = 0) {
   const int n = (int)reqs.size();
   const int m = g.method;
   int kind1, kind2;
@@ -1003,18 +1073,24 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
   std::vector<fpcc_pair_desc> d(n);
   size_t off = 0;
   int maxL = 0;
+  // the slabs of the group's window lengths, looked up once per length
+  int lastN = -1;
+  Slab *sa = nullptr, *sb = nullptr, *se = nullptr;
   for (int i = 0; i < n; i++) {
     const Req& q = *reqs[i];
-    Slab& sa = slab_of(s, Product{kind1, q.N, Nz, g.fmt});
-    Slab& sb = slab_of(s, Product{kind2, q.N, Nz, g.fmt});
+    if (q.N != lastN) {
+      lastN = q.N;
+      sa = &slab_of(s, Product{kind1, q.N, Nz, g.fmt});
+      sb = &slab_of(s, Product{kind2, q.N, Nz, g.fmt});
+      if (m == FPCC_GNCC) se = &slab_of(s, Product{5, q.N, 0, 0});
+    }
     fpcc_pair_desc& e = d[i];
     memset(&e, 0, sizeof(e));
-    e.a = (const char*)sa.base + (int64_t)r1[i] * sa.row_bytes;
-    e.b = (const char*)sb.base + (int64_t)r2[i] * sb.row_bytes;
+    e.a = (const char*)sa->base + (int64_t)r1[i] * sa->row_bytes;
+    e.b = (const char*)sb->base + (int64_t)r2[i] * sb->row_bytes;
     if (m == FPCC_GNCC) {
-      Slab& se = slab_of(s, Product{5, q.N, 0, 0});
-      e.ea = (const double*)((const char*)se.base + (int64_t)e1[i] * se.row_bytes);
-      e.eb = (const double*)((const char*)se.base + (int64_t)e2[i] * se.row_bytes);
+      e.ea = (const double*)((const char*)se->base + (int64_t)e1[i] * se->row_bytes);
+      e.eb = (const double*)((const char*)se->base + (int64_t)e2[i] * se->row_bytes);
     }
     e.y = dy + off;
     off += (size_t)q.L * osz;
@@ -1033,7 +1109,7 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
   if (cudaError_t ue = upload(fl, dd, d.data(), d.size() * sizeof(fpcc_pair_desc), st)) return cuda_err(ue, "upload");
   rc = fpcc_pair_stage_packed(cx, m, g.fmt, Nz, (const fpcc_pair_desc*)dd, n, maxL, g.v, m == FPCC_CC1B_POPCOUNT);
   if (rc) return rc;
-  cudaMemcpyAsync((char*)fl.h_out + out_base, dy, total, cudaMemcpyDeviceToHost, st);
+  if (cudaError_t ce = d2h_results(fl, reqs, first, out_base, dy, st)) return cuda_err(ce, "results");
   return 0;
 }
 
@@ -1059,7 +1135,8 @@ fpcc_wpcc_plan* wpcc_plan_for(Server* s, int N, int Nz, int cap, int Lag1, int L
 // A WPCC group (one window length, padded length and lag window): per-scale
 // phase spectra of each station window are computed into their slab rows
 // directly, then one pair stage runs over the group.
-int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base) {
+int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base,
+                   size_t first) {
   const int n = (int)reqs.size();
   const int lag1 = reqs[0]->r.Lag1, lag2 = reqs[0]->r.Lag2;
   fpcc_wpcc_plan* p = wpcc_plan_for(s, g.N, g.Nz, g.aux, lag1, lag2);
@@ -1108,7 +1185,7 @@ int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlig
   if (!dpl || !dy) return FPCC_ENOMEM;
   if (cudaError_t ue = upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st)) return cuda_err(ue, "upload");
   if ((rc = fpcc_wpcc_pair_stage(s->ctx, p, sl.base, g.fmt, (const int32_t*)dpl, n, (float*)dy, g.L))) return rc;
-  cudaMemcpyAsync((char*)fl.h_out + out_base, dy, ybytes, cudaMemcpyDeviceToHost, s->st);
+  if (cudaError_t ce = d2h_results(fl, reqs, first, out_base, (const char*)dy, s->st)) return cuda_err(ce, "results");
   return 0;
 }
 
@@ -1128,7 +1205,7 @@ void* pinned_get(Server* s, size_t bytes, size_t* got) {
   return p;
 }
 
-constexpr int kDeliverThreads = 4;                   // threads copying out one large batch
+constexpr int kDeliverThreads = 8;                   // threads copying out one large batch
 constexpr size_t kDeliverChunk = (size_t)16 << 20;   // bytes per delivering thread, at least
 
 void pinned_put(Server* s, void* p, size_t bytes) {
@@ -1140,6 +1217,7 @@ void pinned_put(Server* s, void* p, size_t bytes) {
 void deliver_range(InFlight* fl, size_t i0, size_t i1) {
   for (size_t i = i0; i < i1; i++) {
     Req& q = fl->reqs[i];
+    if (fl->direct[i]) continue;
     if (q.r.method == FPCC_CC1B_POPCOUNT) {
       if (q.r.num) memcpy(q.r.num, (char*)fl->h_out + fl->out_off[i], (size_t)q.L * 8);
     } else if (q.r.y) {
@@ -1156,7 +1234,8 @@ void deliver(Server* s, InFlight& fl) {
   const auto now = Clock::now();
   if (!err) {
     size_t bytes = 0;
-    for (const Req& q : fl.reqs) bytes += (size_t)q.L * (q.r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
+    for (size_t i = 0; i < fl.reqs.size(); i++)
+      if (!fl.direct[i]) bytes += (size_t)fl.reqs[i].L * (fl.reqs[i].r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
     const size_t n = fl.reqs.size();
     const int k = (int)std::min<size_t>(kDeliverThreads, std::max<size_t>(1, bytes / kDeliverChunk));
     if (k <= 1 || n < (size_t)k) {
@@ -1222,6 +1301,7 @@ void release_retired(Server* s) {
     for (auto& pr : fl->pinned_rows) pr.first->pin[pr.second]--;
     if (fl->h_out) pinned_put(s, fl->h_out, fl->h_bytes);
     if (fl->h_up) pinned_put(s, fl->h_up, fl->up_bytes);
+    for (auto& b : fl->up_full) pinned_put(s, b.first, b.second);
     if (fl->done) cudaEventDestroy(fl->done);
     delete fl;
     s->in_flight--;
@@ -1278,15 +1358,28 @@ void worker_main(Server* s) {
     // bound the number of batches in flight
     while (s->in_flight >= kMaxInFlight) wait_one_retired(s);
     InFlight* fl = new InFlight();
+    fl->srv = s;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      for (auto& r : s->out_ranges) fl->out_ranges.push_back({std::get<0>(r), std::get<1>(r)});
+    }
     std::map<GroupKey, std::vector<Req*>> groups;
-    for (auto& q : batch) {
-      const int m = q.r.method;
-      const float v = m == FPCC_PCCV ? q.r.v : 0.f;
-      const int f = product_fmt(s, m);
-      // packed groups carry N = -1 (lengths and lags per request)
-      GroupKey g = packable(m, q.Nz) ? GroupKey{m, -1, q.Nz, 0, 0, f, v, 0}
-                                     : GroupKey{m, q.N, q.Nz, q.lag0, q.L, f, v, q.aux};
-      groups[g].push_back(&q);
+    {
+      std::vector<Req*>* last = nullptr;   // requests in a row usually share their group
+      GroupKey last_key{};
+      for (auto& q : batch) {
+        const int m = q.r.method;
+        const float v = m == FPCC_PCCV ? q.r.v : 0.f;
+        const int f = product_fmt(s, m);
+        // packed groups carry N = -1 (lengths and lags per request)
+        GroupKey g = packable(m, q.Nz) ? GroupKey{m, -1, q.Nz, 0, 0, f, v, 0}
+                                       : GroupKey{m, q.N, q.Nz, q.lag0, q.L, f, v, q.aux};
+        if (!last || g < last_key || last_key < g) {
+          last = &groups[g];
+          last_key = g;
+        }
+        last->push_back(&q);
+      }
     }
     size_t total = 0;
     for (auto& q : batch) total += (size_t)q.L * (q.r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
@@ -1331,17 +1424,19 @@ void worker_main(Server* s) {
       s->lane_rec = nullptr;
     }
     // output offsets of every group, in group order
-    std::vector<size_t> base(order.size());
+    std::vector<size_t> base(order.size()), first(order.size());
     {
       size_t off = 0;
       for (size_t i = 0; i < order.size(); i++) {
         base[i] = off;
+        first[i] = fl->reqs.size();
         for (Req* q : order[i]->second) {
           fl->reqs.push_back(*q);
           fl->out_off.push_back((int64_t)off);
           off += (size_t)q->L * (q->r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
         }
       }
+      fl->direct.assign(fl->reqs.size(), 0);
     }
     // a packed direct-sum group starts its pair stage on the direct lane as
     // soon as its own products are queued, overlapping the later station stages
@@ -1362,7 +1457,7 @@ void worker_main(Server* s) {
       if (!err && direct && g.N < 0 && s->dlane.ctx) {
         s->pair_waits = &waits[i];
         s->pair_seq = s->lane_seq;
-        err = run_group_packed(s, g, order[i]->second, *fl, base[i], false, &s->dlane);
+        err = run_group_packed(s, g, order[i]->second, *fl, base[i], false, &s->dlane, first[i]);
         s->pair_waits = nullptr;
         early[i] = 1;
         s->pair_stages++;
@@ -1376,9 +1471,9 @@ void worker_main(Server* s) {
       const GroupKey& g = kv.first;
       s->pair_waits = &waits[i];
       s->pair_seq = s->lane_seq;
-      if (g.method == FPCC_WPCC) err = run_group_wpcc(s, g, kv.second, *fl, base_i);
-      else if (g.N < 0) err = run_group_packed(s, g, kv.second, *fl, base_i, false);
-      else err = run_group(s, g, kv.second, *fl, base_i, false);
+      if (g.method == FPCC_WPCC) err = run_group_wpcc(s, g, kv.second, *fl, base_i, first[i]);
+      else if (g.N < 0) err = run_group_packed(s, g, kv.second, *fl, base_i, false, nullptr, first[i]);
+      else err = run_group(s, g, kv.second, *fl, base_i, false, first[i]);
       s->pair_waits = nullptr;
       s->pair_stages++;
     }
@@ -1389,6 +1484,7 @@ void worker_main(Server* s) {
       cudaStreamSynchronize(s->st);
       fl->reqs.clear();
       for (auto& q : batch) fl->reqs.push_back(q);
+      fl->direct.assign(fl->reqs.size(), 0);
       fl->err = err;
       fl->err_msg = fpcc_last_error();
     } else {
@@ -1497,6 +1593,55 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
   return 0;
 }
 
+extern "C" int fpcc_server_register_output(fpcc_server* h, void* p, size_t bytes) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s || !p || !bytes) return FPCC_EARG;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(s->device);
+  bool owned = false;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+    cudaGetLastError();
+    const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterPortable);
+    if (e != cudaSuccess) {
+      cudaSetDevice(prev);
+      return cuda_err(e, "registering a result buffer");
+    }
+    owned = true;
+  }
+  cudaSetDevice(prev);
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->out_ranges.emplace_back((char*)p, bytes, owned);
+  return 0;
+}
+
+extern "C" int fpcc_server_unregister_output(fpcc_server* h, void* p) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s || !p) return FPCC_EARG;
+  bool owned = false, found = false;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (size_t i = 0; i < s->out_ranges.size(); i++)
+      if (std::get<0>(s->out_ranges[i]) == (char*)p) {
+        owned = std::get<2>(s->out_ranges[i]);
+        s->out_ranges.erase(s->out_ranges.begin() + (ptrdiff_t)i);
+        found = true;
+        break;
+      }
+  }
+  if (!found) return FPCC_EARG;
+  if (owned) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(s->device);
+    const cudaError_t e = cudaHostUnregister(p);
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_err(e, "unregistering a result buffer");
+  }
+  return 0;
+}
+
 extern "C" int fpcc_server_destroy(fpcc_server* h) {
   Server* s = reinterpret_cast<Server*>(h);
   if (!s) return 0;
@@ -1516,6 +1661,9 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
   for (auto& c : s->chunks.chunks()) dfree(s, c.base);
   for (void** p : {&s->d_tmp_x, &s->d_tmp_p, &s->d_idx, &s->d_y, &s->d_pl, &s->d_desc}) dfree(s, *p);
   for (auto& kv : s->wplans) fpcc_wpcc_plan_destroy(kv.second);
+  for (auto& r : s->out_ranges)
+    if (std::get<2>(r)) cudaHostUnregister(std::get<0>(r));
+  s->out_ranges.clear();
   // the contexts share the server's pool: they go first, the pool last
   for (auto& l : s->lanes) {
     if (l.d_tmp) cudaFreeAsync(l.d_tmp, l.st);
@@ -1602,12 +1750,13 @@ extern "C" int fpcc_put_station_window(fpcc_server* h, int32_t sta, int32_t wind
   return 0;
 }
 
-extern "C" int64_t fpcc_submit(fpcc_server* h, const fpcc_request* req) {
-  Server* s = reinterpret_cast<Server*>(h);
-  if (!s || !req) return FPCC_EARG;
-  Req q;
+namespace fpcc {
+namespace {
+
+// Validates a request and fills its planning fields (window length, padded
+// length, lags).  `mu` is taken for the window and wavelet-setup lookups only.
+int prepare_request(Server* s, const fpcc_request* req, Req& q) {
   q.r = *req;
-  q.t_submit = Clock::now();
   int N = 0;
   {
     std::lock_guard<std::mutex> lk(s->mu);
@@ -1656,6 +1805,18 @@ extern "C" int64_t fpcc_submit(fpcc_server* h, const fpcc_request* req) {
   } else {
     return FPCC_EUNSUP;
   }
+  return 0;
+}
+
+}  // namespace
+}  // namespace fpcc
+
+extern "C" int64_t fpcc_submit(fpcc_server* h, const fpcc_request* req) {
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s || !req) return FPCC_EARG;
+  Req q;
+  if (int rc = prepare_request(s, req, q)) return rc;
+  q.t_submit = Clock::now();
   {
     std::lock_guard<std::mutex> lk(s->mu);
     q.id = s->next_id++;
@@ -1734,11 +1895,42 @@ extern "C" int fpcc_server_reset_stats(fpcc_server* h) {
 }
 
 extern "C" int fpcc_submit_many(fpcc_server* h, const fpcc_request* reqs, int n, int64_t* ids) {
-  if (!h || !reqs || n < 0) return FPCC_EARG;
-  for (int i = 0; i < n; i++) {
-    const int64_t id = fpcc_submit(h, reqs + i);
-    if (ids) ids[i] = id;
-    if (id < 0) return (int)id;
+  Server* s = reinterpret_cast<Server*>(h);
+  if (!s || !reqs || n < 0) return FPCC_EARG;
+  // chunks of requests enter the queue under one lock and one wake-up each, so
+  // that the worker can start on the first chunk while the rest are prepared
+  constexpr int kChunk = 1024;
+  std::vector<Req> qs;
+  qs.reserve(std::min(n, kChunk));
+  for (int i0 = 0; i0 < n; i0 += kChunk) {
+    const int i1 = std::min(n, i0 + kChunk);
+    qs.clear();
+    int rc = 0, bad = i1;
+    for (int i = i0; i < i1; i++) {
+      Req q;
+      if ((rc = prepare_request(s, reqs + i, q))) {
+        bad = i;
+        break;
+      }
+      qs.push_back(q);
+    }
+    const auto now = Clock::now();
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      for (size_t k = 0; k < qs.size(); k++) {
+        Req& q = qs[k];
+        q.t_submit = now;
+        q.id = s->next_id++;
+        s->status[q.id] = 0;
+        if (ids) ids[i0 + (int)k] = q.id;
+        s->pending.push_back(std::move(q));
+      }
+    }
+    s->cv.notify_one();
+    if (rc) {
+      if (ids) ids[bad] = rc;
+      return rc;
+    }
   }
   return 0;
 }

@@ -317,6 +317,16 @@ int fpcc_server_set_nz_mode(fpcc_server *s, int mode);
  * before the first request.  WPCC requests fail with FPCC_EARG without it. */
 int fpcc_server_set_wavelet(fpcc_server *s, double pmin, double pmax, unsigned V, int type, double op1,
                             int rule);
+/* A host range [p, p + bytes) that results may be written into straight from
+ * the device: requests whose output rows lie inside it get their results by
+ * device-to-host copies into those rows (rows at one stride as one strided
+ * copy) instead of through the server's pinned buffer and a host copy.  The
+ * range is page-locked here unless it already is (then it is only recorded).
+ * Unregister it (or destroy the server) only when no request writing into it
+ * is pending.  No counterpart in the reference (its calls return results in
+ * the caller's arrays synchronously). */
+int fpcc_server_register_output(fpcc_server *s, void *p, size_t bytes);
+int fpcc_server_unregister_output(fpcc_server *s, void *p);
 int fpcc_server_destroy(fpcc_server *s);
 int fpcc_put_station_window(fpcc_server *s, int32_t sta, int32_t window, const float *x, int N);
 /* Returns a request id (>= 0) or a negative FPCC_E* code. */

@@ -214,6 +214,80 @@ def test_server_uneven_lengths_share_launches(F, orc):
         assert np.array_equal(o, outs[i]), reqs[i]
 
 
+def test_server_one_batch_of_many_small_groups(F, orc):
+    """One cold batch whose requests fall into many small groups (40 window
+    lengths, four methods, every request its own lag window): the batch's small
+    index uploads outgrow its first pinned staging block and continue in further
+    blocks; every request completes and matches the oracle."""
+    rng = np.random.default_rng(21)
+    lengths = sorted({int(n) for n in rng.integers(1200, 6000, 40)})
+    xs = _uneven_windows(lengths, "serve/many-groups")
+    reqs = []
+    for w, N in enumerate(lengths):
+        for m in (0, 1, 2, 4):
+            M = int(rng.integers(10, N // 10))
+            l1, l2 = (-M, int(rng.integers(-M, M + 1)))
+            if m == 4 and l1 > l2:
+                l1, l2 = l2, l1
+            reqs.append((m, 0, 1 + w % 4, w, l1, l2, 0.0))
+    srv = F.Server(hbm_budget=1 << 30, max_batch=4096)
+    for w, x in xs.items():
+        for st in range(5):
+            srv.put(st, w, x[st])
+    outs = _run_many(F, srv, reqs)
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(reqs) and st["batches"] <= 2
+    for k in range(0, len(reqs), 7):
+        m, s1, s2, w, l1, l2, v = reqs[k]
+        a, b = xs[w][s1], xs[w][s2]
+        assert relerr(outs[k], _oracle(orc, m, a, b, l1, l2, v)) < TOL, reqs[k]
+
+
+def test_server_registered_outputs_match(F, orc):
+    """Results copied straight into a registered output array (rows at one
+    stride, strided copies; popcount numerators; rows interleaved with
+    unregistered ones) equal the results delivered through the server's pinned
+    block, bit for bit."""
+    xa = _stations(6, 2, 3000, "serve/reg")
+    reqs = []
+    rng = np.random.default_rng(4)
+    for k in range(48):
+        m = [0, 1, 2, 3, 4][k % 5]
+        s1, s2 = rng.choice(6, 2, replace=False)
+        reqs.append((m, int(s1), int(s2), int(k % 2), -150, 150, 0.0))
+    L = 301
+
+    def run(register):
+        srv = F.Server(hbm_budget=1 << 30)
+        for s in range(6):
+            for w in range(2):
+                srv.put(s, w, xa[s, w])
+        yf = np.zeros((len(reqs), L), np.float32)
+        yi = np.zeros((len(reqs), L), np.int64)
+        if register:
+            srv.register_output(yf)
+            srv.register_output(yi)
+        loose = [np.zeros(L, np.float32) for _ in reqs]   # every third float row stays unregistered
+        rs = []
+        for i, (m, s1, s2, w, l1, l2, v) in enumerate(reqs):
+            o = yi[i] if m == F.CC1B_POPCOUNT else (loose[i] if i % 3 == 0 else yf[i])
+            rs.append(srv.request(m, s1, s2, w, l1, l2, o, v))
+        srv.submit_many(rs)
+        srv.drain()
+        if register:
+            srv.unregister_output(yf)
+        srv.close()
+        return yf, yi, loose
+
+    a = run(False)
+    b = run(True)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert all(np.array_equal(u, v) for u, v in zip(a[2], b[2]))
+    m, s1, s2, w, l1, l2, v = reqs[1]
+    assert relerr(b[0][1], _oracle(orc, m, xa[s1, w], xa[s2, w], l1, l2, v)) < TOL
+
+
 def test_server_16bit_storage(F, orc):
     """Block-scaled int16 storage (the server's 4-byte format for the 1e-4 target)
     within 1e-4 of the FP64 oracle; FP16 storage on the same requests stays at
