@@ -1,4 +1,5 @@
-// Autotuner: measured cost of every usable padded length.
+// Autotuner: measured cost of every usable padded length, and the pair kernel
+// of each length that two kernels can run.
 //
 // Every padded length Nz >= N + max|lag| gives the same correlation; which one
 // is fastest depends on its radix schedule, on whether Nz/2 runs in one block
@@ -6,8 +7,15 @@
 // context's GPU, the pair stage (per correlation) and the station stage (per
 // window) of each usable length and keeps the table for FPCC_NZ_TUNED; a
 // length's cost is pair + station / reuse, reuse being the correlations each
-// station window takes part in.  The table is saved and loaded as JSON:
-//   {"reuse": R, "lengths": {"Nz": [pair_ns, station_ns], ...}}
+// station window takes part in.  Where both the one-block-per-correlation
+// kernel and the tiled kernel run a length, both are timed and the faster one
+// is selected for that length (fpcc_pair_form).  The radix schedules, block
+// sizes and tile shapes inside each kernel are compile-time choices (the
+// register and shared-memory budgets of each shape are fixed by them), so the
+// tuned dimensions are the padded length and the kernel form.  The table is
+// saved and loaded as JSON:
+//   {"reuse": R, "lengths": {"Nz": [pair_ns, station_ns, form], ...}}
+// form: 1 block kernel, 2 tiled kernel, 0 only one kernel runs the length.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -18,6 +26,7 @@
 
 #include "../../include/fastpcc_gb300.h"
 #include "engine.h"
+#include "kernels.cuh"
 
 using namespace fpcc;
 
@@ -29,9 +38,12 @@ int save_table(const char* path) {
   FILE* f = fopen(path, "w");
   if (!f) return FPCC_EARG;
   fprintf(f, "{\"reuse\": %.6g, \"lengths\": {\n", reuse);
-  for (size_t i = 0; i < t.size(); i++)
-    fprintf(f, "  \"%d\": [%.6g, %.6g]%s\n", std::get<0>(t[i]), std::get<1>(t[i]), std::get<2>(t[i]),
+  for (size_t i = 0; i < t.size(); i++) {
+    const int nz = std::get<0>(t[i]);
+    const int form = (pair_tiled_supported(nz) && pair_supported(nz)) ? pair_form_get(nz) : 0;
+    fprintf(f, "  \"%d\": [%.6g, %.6g, %d]%s\n", nz, std::get<1>(t[i]), std::get<2>(t[i]), form,
             i + 1 < t.size() ? "," : "");
+  }
   fprintf(f, "}}\n");
   return fclose(f) == 0 ? 0 : FPCC_EARG;
 }
@@ -87,17 +99,28 @@ extern "C" int fpcc_autotune(fpcc_ctx* ctx, int min_nz, int max_nz, double reuse
     cudaEventRecord(tm.b, st);
     cudaEventSynchronize(tm.b);
     cudaEventElapsedTime(&t_st, tm.a, tm.b);
-    // pair stage: P PCC2 correlations of full F32 spectra, lags +-nz/10
-    for (int k = 0; k <= reps && !rc; k++) {
-      if (k == 1) cudaEventRecord(tm.a, st);
-      rc = fpcc_pair_stage(ctx, FPCC_PCC2, d_spec, nz, FPCC_F32, (const int32_t*)d_pairs, np, N, nz, -M, M, 0.f,
-                           nullptr, 0, (float*)d_y, 2 * M + 1, nullptr);
+    // pair stage: P PCC2 correlations of full F32 spectra, lags +-nz/10; each
+    // kernel form that runs this length, the faster one kept
+    const bool two = pair_tiled_supported(nz) && pair_supported(nz);
+    float best = -1.f;
+    int best_form = 0;
+    for (int form : {PAIR_FORM_BLOCK, PAIR_FORM_TILED}) {
+      if (two) pair_form_set(nz, form);
+      else if (form == PAIR_FORM_TILED) break;
+      for (int k = 0; k <= reps && !rc; k++) {
+        if (k == 1) cudaEventRecord(tm.a, st);
+        rc = fpcc_pair_stage(ctx, FPCC_PCC2, d_spec, nz, FPCC_F32, (const int32_t*)d_pairs, np, N, nz, -M, M, 0.f,
+                             nullptr, 0, (float*)d_y, 2 * M + 1, nullptr);
+      }
+      if (rc) break;
+      cudaEventRecord(tm.b, st);
+      cudaEventSynchronize(tm.b);
+      cudaEventElapsedTime(&t_pr, tm.a, tm.b);
+      if (best < 0.f || t_pr < best) { best = t_pr; best_form = form; }
     }
     if (rc) break;
-    cudaEventRecord(tm.b, st);
-    cudaEventSynchronize(tm.b);
-    cudaEventElapsedTime(&t_pr, tm.a, tm.b);
-    tuned_set(nz, 1e6 * t_pr / (reps * np), 1e6 * t_st / (reps * R));
+    if (two) pair_form_set(nz, best_form);
+    tuned_set(nz, 1e6 * best / (reps * np), 1e6 * t_st / (reps * R));
   }
   cudaFree(d_x);
   cudaFree(d_spec);
@@ -118,8 +141,17 @@ extern "C" int fpcc_autotune_load(const char* json_path) {
     double reuse;
     int nz;
     double a, b;
-    if (sscanf(line, " {\"reuse\": %lf", &reuse) == 1) tuned_set_reuse(reuse);
-    else if (sscanf(line, " \"%d\": [%lf, %lf]", &nz, &a, &b) == 3 && nz_usable(nz)) { tuned_set(nz, a, b); n++; }
+    int form = 0;
+    if (sscanf(line, " {\"reuse\": %lf", &reuse) == 1) {
+      tuned_set_reuse(reuse);
+    } else {
+      const int got = sscanf(line, " \"%d\": [%lf, %lf, %d]", &nz, &a, &b, &form);
+      if (got >= 3 && nz_usable(nz)) {
+        tuned_set(nz, a, b);
+        if (got == 4 && form > 0) pair_form_set(nz, form);   // ignored where the form does not run nz
+        n++;
+      }
+    }
   }
   fclose(f);
   return n > 0 ? 0 : FPCC_EARG;
