@@ -16,6 +16,10 @@ namespace fpcc {
 // [1e-30, 1e30] (checked on the values rounded to FP32), else in FP64.  The
 // GB300 issues FP64 at a small fraction of its FP32 rate: this form takes one
 // FP64 subtraction per lag instead of two subtractions and four comparisons.
+// Narrowing of the two energies uses energy_to_float below rather than a
+// conversion instruction, which would run on the FP64 pipe as well.
+__device__ __forceinline__ float energy_to_float(double d);
+
 __device__ __forceinline__ float gncc_lag_norm(float v, const double* E1, const double* E2, int N, int lag) {
   double e1, e2;
   if (lag > 0) {
@@ -25,9 +29,22 @@ __device__ __forceinline__ float gncc_lag_norm(float v, const double* E1, const 
     e1 = E1[N] - E1[-lag];
     e2 = E2[N + lag];
   }
-  const float f1 = (float)e1, f2 = (float)e2;
+  const float f1 = energy_to_float(e1), f2 = energy_to_float(e2);
   if (f1 >= 1e-30f && f2 >= 1e-30f && f1 <= 1e30f && f2 <= 1e30f) return v * (rsqrtf(f1) * rsqrtf(f2));
   return (float)((double)v / sqrt(e1 * e2));
+}
+
+// A double narrowed to float by truncating its significand (relative error
+// below 2^-23), from the IEEE-754 fields with integer operations; magnitudes
+// below the float normal range give +-0 and above it +-infinity, which the
+// range check of gncc_lag_norm sends to its FP64 branch.
+__device__ __forceinline__ float energy_to_float(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+  if (e <= 0) return __int_as_float((int)sign);
+  if (e >= 255) return __int_as_float((int)(sign | 0x7f800000u));
+  return __int_as_float((int)(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu)));
 }
 
 // One correlation of a packed launch (lengths and lags per entry).
