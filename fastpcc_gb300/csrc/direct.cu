@@ -210,6 +210,169 @@ __global__ void __launch_bounds__(kLagBlock) k_pccv(PccvArgs a) {
   }
 }
 
+// ---------------------------------------------------------------- PCC1 direct
+// PCC at power 1 (the reference's pcc1f_lowlevel, src/FFTapps.c:251-278, and
+// the GPU kernel of src/ccs_cuda.cu:260-321): as k_pccv with v = 1, but each
+// thread takes two adjacent lags, and the station-2 tile is staged as its even
+// and odd samples, so that per pair of samples of station 1 (one broadcast
+// 16-byte load) a thread loads two station-2 values and reuses a third from the
+// previous step for four terms: five shared-memory wavefronts per 128 terms of
+// a warp instead of twelve.
+//
+// Terms: |a + b| - |a - b|.  For |a| = |b| = 1 this equals 2c / sqrt(1 + |s|)
+// with c + i s = a conj(b) (|a +- b|^2 = 2 +- 2c and c^2 + s^2 = 1), one
+// reciprocal square root instead of two square roots; with a or b = 0 both
+// forms give 0.  A tile whose staged samples of both stations all have
+// | |x|^2 - 1 | <= 2^-20 or x = 0 (phase signals of the pure-phase rules,
+// src/ccs_cuda.cu:201-208,223-230) uses it; any other tile (the regularised
+// rules of src/FFTapps.c:147-205, where moduli fall below 1 by 1e-6 max|x|/|x|
+// and much more inside gaps) keeps the two square roots.  The choice depends
+// only on the pair's own samples, so a result does not depend on the launch.
+__device__ __forceinline__ float rsqrt_fast(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ bool unit_or_zero(float2 v) {
+  const float m2 = v.x * v.x + v.y * v.y;
+  return m2 == 0.0f || fabsf(m2 - 1.0f) <= 0x1p-20f;
+}
+
+// |w + u| - |w - u| / 2 for unit-modulus (or zero) w, u
+__device__ __forceinline__ float pcc1_term_unit(float2 w, float ux, float uy) {
+  const float c = fmaf(w.x, ux, w.y * uy);
+  const float sn = fmaf(w.y, ux, -w.x * uy);
+  return c * rsqrt_fast(1.0f + fabsf(sn));
+}
+
+__device__ __forceinline__ float pcc1_term(float2 w, float ux, float uy) {
+  const float sx = w.x + ux, sy = w.y + uy, dx = w.x - ux, dy = w.y - uy;
+  return sqrt_fast(fmaf(sx, sx, sy * sy)) - sqrt_fast(fmaf(dx, dx, dy * dy));
+}
+
+template <int FMT, int S>
+__global__ void __launch_bounds__(kLagBlock) k_pcc1(PccvArgs a) {
+  constexpr int TS = kLagBlock / S;          // threads of one sub-range = lag pairs per block
+  constexpr int LB = 2 * TS;                 // lags per block
+  constexpr int NE = (kTile + LB) / 2 + 1;   // even / odd station-2 samples of a tile
+  __shared__ float4 s1p[kTile / 2];          // station-1 samples 2k, 2k + 1
+  __shared__ float2 s2e[NE], s2o[NE];
+  __shared__ double red[S > 1 ? 2 * kLagBlock : 1];
+  const int p = blockIdx.y;
+  const int sub = threadIdx.x / TS, li = threadIdx.x - sub * TS;
+  const int lblk = blockIdx.x * LB;          // first lag index of the block
+  const int l = lblk + 2 * li;               // this thread's lag indices l, l + 1
+  int N, Lag1, L;
+  const void* R1;
+  const void* R2;
+  float* y;
+  if (a.desc) {
+    const fpcc_pair_desc& d = a.desc[p];
+    N = d.N;
+    Lag1 = d.lag0;
+    L = d.L;
+    R1 = d.a;
+    R2 = d.b;
+    y = reinterpret_cast<float*>(d.y);
+    if (lblk >= L) return;                   // whole block beyond this pair's lags
+  } else {
+    const int2 pr = a.pairs[p];
+    N = a.N;
+    Lag1 = a.Lag1;
+    L = a.L;
+    const int64_t esz = FMT ? 4 : 8;
+    R1 = reinterpret_cast<const char*>(a.phase) + (int64_t)pr.x * a.ldp * esz;
+    R2 = reinterpret_cast<const char*>(a.phase) + (int64_t)pr.y * a.ldp * esz;
+    y = a.y + (int64_t)p * a.ldy;
+  }
+  const int lagb = Lag1 + lblk;              // lag of index lblk
+  double acc0 = 0.0, acc1 = 0.0;
+  int nlo = -(lagb + LB - 1);
+  if (nlo < 0) nlo = 0;
+  int nhi = N - lagb;
+  if (nhi > N) nhi = N;
+  for (int n0 = nlo; n0 < nhi; n0 += kTile) {
+    bool unit = true;
+    for (int i = threadIdx.x; i < kTile / 2; i += kLagBlock) {
+      const int n = n0 + 2 * i;
+      float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
+      if (n < N) v0 = phase_at<FMT>(R1, n);
+      if (n + 1 < N) v1 = phase_at<FMT>(R1, n + 1);
+      unit = unit && unit_or_zero(v0) && unit_or_zero(v1);
+      s1p[i] = make_float4(v0.x, v0.y, v1.x, v1.y);
+    }
+    for (int i = threadIdx.x; i < 2 * NE; i += kLagBlock) {
+      const int n = n0 + lagb + i;           // station-2 sample of tile position i
+      float2 v = make_float2(0.f, 0.f);
+      if (n >= 0 && n < N) v = phase_at<FMT>(R2, n);
+      unit = unit && unit_or_zero(v);
+      if (i & 1) s2o[i >> 1] = v;
+      else s2e[i >> 1] = v;
+    }
+    const bool fast = __syncthreads_and(unit) != 0;
+    // lag l at sample pair k: station-2 positions 2 li + 2k (even) and 2 li + 2k + 1 (odd);
+    // lag l + 1: 2 li + 2k + 1 (odd) and 2 li + 2k + 2 (the next even one)
+    constexpr int span = kTile / 2 / S;
+    const int k0 = sub * span;
+    float part0 = 0.0f, part1 = 0.0f;
+    float2 e0 = s2e[li + k0];
+    if (fast) {
+#pragma unroll 4
+      for (int k = k0; k < k0 + span; k++) {
+        const float4 u = s1p[k];
+        const float2 o0 = s2o[li + k];
+        const float2 e1 = s2e[li + k + 1];
+        part0 += pcc1_term_unit(e0, u.x, u.y) + pcc1_term_unit(o0, u.z, u.w);
+        part1 += pcc1_term_unit(o0, u.x, u.y) + pcc1_term_unit(e1, u.z, u.w);
+        e0 = e1;
+      }
+      part0 *= 2.0f;
+      part1 *= 2.0f;
+    } else {
+#pragma unroll 4
+      for (int k = k0; k < k0 + span; k++) {
+        const float4 u = s1p[k];
+        const float2 o0 = s2o[li + k];
+        const float2 e1 = s2e[li + k + 1];
+        part0 += pcc1_term(e0, u.x, u.y) + pcc1_term(o0, u.z, u.w);
+        part1 += pcc1_term(o0, u.x, u.y) + pcc1_term(e1, u.z, u.w);
+        e0 = e1;
+      }
+    }
+    acc0 += (double)part0;
+    acc1 += (double)part1;
+    __syncthreads();
+  }
+  if constexpr (S > 1) {
+    red[threadIdx.x] = acc0;
+    red[kLagBlock + threadIdx.x] = acc1;
+    __syncthreads();
+    if (sub != 0) return;
+    acc0 = red[li];
+    acc1 = red[kLagBlock + li];
+#pragma unroll
+    for (int k = 1; k < S; k++) {
+      acc0 += red[k * TS + li];
+      acc1 += red[kLagBlock + k * TS + li];
+    }
+  }
+  const double V = 0.5;
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int lh = l + h;
+    if (lh >= L) break;
+    const int lag = Lag1 + lh;
+    if (lag < -N || lag > N) {
+      y[lh] = 0.0f;
+      continue;
+    }
+    const double cnt = (double)(N - abs(lag));
+    const double D = a.norm_gpu ? 2.0 * cnt : exp2(V) * cnt;
+    y[lh] = (float)((h ? acc1 : acc0) / D);
+  }
+}
+
 // ---------------------------------------------------------------- 1-bit bits
 // bit i of word w is 1 when sample 32w+i maps to -1: x < 0 for the station-1
 // rule (x >= 0 -> +1), x <= 0 for the station-2 rule (x > 0 -> +1).
@@ -353,7 +516,9 @@ cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st) {
   // choice depends on the launch form only, so a request's result does not
   // depend on the other windows in its launch
   const bool split = a.desc != nullptr;
-  const int lb = (a.L + (split ? kLagBlock / 4 : kLagBlock) - 1) / (split ? kLagBlock / 4 : kLagBlock);
+  // lags per block: k_pccv one per thread (or sub-range), k_pcc1 two
+  const int per = (split ? kLagBlock / 4 : kLagBlock) * (mode == 1 ? 2 : 1);
+  const int lb = (a.L + per - 1) / per;
   for (int p0 = 0; p0 < a.npairs; p0 += 65535) {   // grid.y holds at most 65535 pairs
     PccvArgs b = a;
     b.npairs = a.npairs - p0 < 65535 ? a.npairs - p0 : 65535;
@@ -365,7 +530,7 @@ cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st) {
     }
     const dim3 grid(lb, b.npairs);
 #define FPCC_PCCV_S(F, SS)                                                    \
-    if (mode == 1) k_pccv<1, F, SS><<<grid, kLagBlock, 0, st>>>(b);           \
+    if (mode == 1) k_pcc1<F, SS><<<grid, kLagBlock, 0, st>>>(b);              \
     else if (mode == 2) k_pccv<2, F, SS><<<grid, kLagBlock, 0, st>>>(b);      \
     else k_pccv<0, F, SS><<<grid, kLagBlock, 0, st>>>(b);
 #define FPCC_PCCV_FMT(F)                                                      \
