@@ -585,7 +585,20 @@ def method_legs(F, torch, ctx, stream, dev, x, d_x, pairs, Nz, peak):
     sfu_peak = 152 * 16 * clk / 2.0    # 16 special-function results per SM per clock, 2 per term
     out["pcc1_pairs"] = {"kernel_ms": ms, "terms": terms, "Gterms_per_s": terms / ms / 1e6,
                          "frac_of_sfu_peak": terms / ms * 1e3 / sfu_peak, "correlations": P1,
+                         "rule": "AmpNormf (regularised moduli): two square roots per term",
                          "sfu_peak_assumed": "152 SMs x 16 sqrt/clk x 2.07 GHz, 2 sqrt per term"}
+    # the same pairs with the pure-phase rule of the reference GPU path: one
+    # reciprocal square root per term
+    ctx.station_stage(F.PCC1, d_x.data_ptr(), N, rows, N, 0, F.F32, F.AMP_PURE, ph.data_ptr(), N)
+    ms = _time_ms(torch, stream, lambda: ctx.pair_stage(F.PCC1, ph.data_ptr(), N, F.F32, d_pairs.data_ptr(), P1, N,
+                                                        0, -LAG, LAG, d_y=d_y.data_ptr(), ldy=L), reps=1)
+    from oracle import oracle as O
+    y64 = O.pcc1(x[pairs[:2, 0]], x[pairs[:2, 1]], -LAG, LAG, rule=O.AMP_PURE)
+    out["pcc1_pairs_pure_rule"] = {"kernel_ms": ms, "terms": terms, "Gterms_per_s": terms / ms / 1e6,
+                                   "frac_of_sfu_peak": terms / ms * 1e3 / (2 * sfu_peak), "correlations": P1,
+                                   "rule": "pure phase x/|x| (reference GPU path): one reciprocal square root "
+                                           "per term",
+                                   "max_rel_err": float(O.relerr(d_y[:2].cpu().numpy(), y64).max())}
     del ph, d_y
     return out
 

@@ -86,6 +86,34 @@ def test_pcc1(F, orc, N, Tr, l1, l2, d):
     assert relerr(F.pcc1_set(a, b, l1, l2), orc.pcc1(a, b, l1, l2)) < TOL
 
 
+@pytest.mark.parametrize("N,l1,l2,gaps", [(3000, -300, 300, False), (4500, -450, 200, True),
+                                         (70001, -600, 600, False), (1200, -1199, 1199, True)])
+def test_pcc1_pure_phase_rule(F, orc, N, l1, l2, gaps):
+    """PCC1 of pure-phase signals (x/|x|, the reference GPU rule): tiles whose
+    samples are all unit-modulus or zero take the one-root form of each term,
+    the others (zero-padded edges included) the two-root form; both against
+    the FP64 oracle with the same rule, with gaps, several tiles and lag
+    windows covering the whole window."""
+    import torch
+    a, b = _data(N, 2, N // 40, "pcc1-pure")
+    if gaps:
+        a = np.stack([synth.gaps(a[k], seed_tag=f"pa{k}") for k in range(2)])
+        b = np.stack([synth.gaps(b[k], seed_tag=f"pb{k}") for k in range(2)])
+    y64 = orc.pcc1(a, b, l1, l2, rule=orc.AMP_PURE)
+    ctx = F.Context(0)
+    x = torch.from_numpy(np.ascontiguousarray(np.concatenate([a, b]))).cuda()
+    ph = torch.empty((4, 2 * N), dtype=torch.float32, device="cuda")
+    pairs = torch.tensor([[0, 2], [1, 3]], dtype=torch.int32, device="cuda")
+    L = l2 - l1 + 1
+    y = torch.empty((2, L), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    ctx.station_stage(F.PCC1, x.data_ptr(), N, 4, N, 0, F.F32, F.AMP_PURE, ph.data_ptr(), N)
+    ctx.pair_stage(F.PCC1, ph.data_ptr(), N, F.F32, pairs.data_ptr(), 2, N, 0, l1, l2, d_y=y.data_ptr(), ldy=L)
+    ctx.sync()
+    ctx.close()
+    assert relerr(y.cpu().numpy(), y64) < TOL
+
+
 def test_pccv_gpu_normalisation(F, orc):
     a, b = _data(2000, 2, 40, "pccv")
     y64 = orc.pccv(a, b, 1.5, -150, 150, norm_gpu=True)
