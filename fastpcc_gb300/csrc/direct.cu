@@ -515,7 +515,9 @@ cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st) {
   // packed launches (windows of any lengths) split each lag over 4 threads; the
   // choice depends on the launch form only, so a request's result does not
   // depend on the other windows in its launch
-  const bool split = a.desc != nullptr;
+  // k_pcc1 (v = 1) always splits each lag over 4 threads (128 lags per block),
+  // so that launches of few pairs still fill the GPU
+  const bool split = a.desc != nullptr || mode == 1;
   // lags per block: k_pccv one per thread (or sub-range), k_pcc1 two
   const int per = (split ? kLagBlock / 4 : kLagBlock) * (mode == 1 ? 2 : 1);
   const int lb = (a.L + per - 1) / per;

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <map>
+#include <atomic>
 #include <mutex>
 #include <tuple>
 #include <vector>
@@ -104,6 +105,9 @@ static int choose_nz_uncached(int N, int M, int mode);
 // Memoised: the serving loop asks once per request.
 static std::mutex g_memo_mu;
 static std::map<std::tuple<int, int, int>, int> g_memo;
+// generation of g_memo (bumped whenever it is cleared), so that a thread's
+// copy of its last answer is used only while the memo it came from stands
+static std::atomic<uint64_t> g_memo_gen{1};
 
 // Measured costs per padded length (autotuner): pair stage per correlation and
 // station stage per window, in ns; a length's cost is pair + station / reuse.
@@ -118,6 +122,7 @@ void tuned_set(int nz, double pair_ns, double station_ns) {
   }
   std::lock_guard<std::mutex> lk(g_memo_mu);
   g_memo.clear();
+  g_memo_gen.fetch_add(1);
 }
 
 void tuned_set_reuse(double reuse) {
@@ -127,6 +132,7 @@ void tuned_set_reuse(double reuse) {
   }
   std::lock_guard<std::mutex> lk(g_memo_mu);
   g_memo.clear();
+  g_memo_gen.fetch_add(1);
 }
 
 std::vector<std::tuple<int, double, double>> tuned_table(double* reuse) {
@@ -147,10 +153,21 @@ std::vector<int> usable_lengths(int lo, int hi) {
 
 int choose_nz(int N, int M, int mode) {
   const auto key = std::make_tuple(N, M, mode);
+  // requests in a row usually ask the same question (one per request when serving)
+  thread_local std::tuple<int, int, int> last_key{-1, -1, -1};
+  thread_local int last_nz = 0;
+  thread_local uint64_t last_gen = 0;
+  const uint64_t gen = g_memo_gen.load(std::memory_order_acquire);
+  if (gen == last_gen && key == last_key) return last_nz;
   {
     std::lock_guard<std::mutex> lk(g_memo_mu);
     auto it = g_memo.find(key);
-    if (it != g_memo.end()) return it->second;
+    if (it != g_memo.end()) {
+      last_key = key;
+      last_nz = it->second;
+      last_gen = gen;
+      return it->second;
+    }
   }
   int nz = choose_nz_uncached(N, M, mode);
   if (nz <= 0 && mode == FPCC_NZ_TUNED_MODE) nz = choose_nz_uncached(N, M, 1);

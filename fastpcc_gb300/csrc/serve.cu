@@ -242,7 +242,7 @@ struct Server {
   size_t arena_left = 0;
   char* arena_ptr = nullptr;
   std::deque<Req> pending;
-  std::unordered_map<int64_t, int> status;                     // id -> 0 pending, 1 done, <0 error
+  std::vector<int> status;        // by request id (ids count up from 0): 0 pending, 1 done, <0 error
   int64_t next_id = 0;
   bool stop = false;
   std::thread worker;
@@ -1250,7 +1250,7 @@ void deliver(Server* s, InFlight& fl) {
   {
     std::lock_guard<std::mutex> lk(s->mu);
     for (auto& q : fl.reqs) {
-      s->status[q.id] = err ? err : 1;
+      s->status[(size_t)q.id] = err ? err : 1;
       s->lat_ms.push_back(std::chrono::duration<double, std::milli>(now - q.t_submit).count());
     }
     s->completed += (int64_t)fl.reqs.size();
@@ -1755,17 +1755,31 @@ namespace {
 
 // Validates a request and fills its planning fields (window length, padded
 // length, lags).  `mu` is taken for the window and wavelet-setup lookups only.
+// Window length of a request's two windows (FPCC_EARG if either is missing or
+// they differ); the caller holds `mu`.
+int request_window_len(Server* s, const fpcc_request* req) {
+  auto a = s->windows.find({req->sta1, req->window});
+  auto b = s->windows.find({req->sta2, req->window});
+  if (a == s->windows.end() || b == s->windows.end()) return FPCC_EARG;
+  if (b->second.N != a->second.N) return FPCC_EARG;
+  return a->second.N;
+}
+
+// As prepare_request, for a window length already looked up.
+int prepare_request_n(Server* s, const fpcc_request* req, Req& q, int N);
+
 int prepare_request(Server* s, const fpcc_request* req, Req& q) {
-  q.r = *req;
   int N = 0;
   {
     std::lock_guard<std::mutex> lk(s->mu);
-    auto a = s->windows.find({req->sta1, req->window});
-    auto b = s->windows.find({req->sta2, req->window});
-    if (a == s->windows.end() || b == s->windows.end()) return FPCC_EARG;
-    N = a->second.N;
-    if (b->second.N != N) return FPCC_EARG;
+    N = request_window_len(s, req);
   }
+  if (N < 0) return N;
+  return prepare_request_n(s, req, q, N);
+}
+
+int prepare_request_n(Server* s, const fpcc_request* req, Req& q, int N) {
+  q.r = *req;
   const int M = std::max(std::abs(req->Lag1), std::abs(req->Lag2));
   if (M >= N) return FPCC_EARG;
   q.N = N;
@@ -1820,7 +1834,7 @@ extern "C" int64_t fpcc_submit(fpcc_server* h, const fpcc_request* req) {
   {
     std::lock_guard<std::mutex> lk(s->mu);
     q.id = s->next_id++;
-    s->status[q.id] = 0;
+    s->status.push_back(0);
     s->pending.push_back(q);
   }
   s->cv.notify_one();
@@ -1831,29 +1845,26 @@ extern "C" int fpcc_poll(fpcc_server* h, int64_t id) {
   Server* s = reinterpret_cast<Server*>(h);
   if (!s) return FPCC_EARG;
   std::lock_guard<std::mutex> lk(s->mu);
-  auto it = s->status.find(id);
-  if (it == s->status.end()) return FPCC_EARG;
-  if (it->second < 0) set_last_error(s->err_msg.c_str());
-  return it->second;
+  if (id < 0 || id >= (int64_t)s->status.size()) return FPCC_EARG;
+  const int st = s->status[(size_t)id];
+  if (st < 0) set_last_error(s->err_msg.c_str());
+  return st;
 }
 
 extern "C" int fpcc_wait(fpcc_server* h, int64_t id, double timeout_s) {
   Server* s = reinterpret_cast<Server*>(h);
   if (!s) return FPCC_EARG;
   std::unique_lock<std::mutex> lk(s->mu);
-  auto pred = [&] {
-    auto it = s->status.find(id);
-    return it == s->status.end() || it->second != 0;
-  };
+  if (id < 0 || id >= (int64_t)s->status.size()) return FPCC_EARG;
+  auto pred = [&] { return s->status[(size_t)id] != 0; };
   if (timeout_s > 0) {
     if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) return 0;
   } else {
     s->cv_done.wait(lk, pred);
   }
-  auto it = s->status.find(id);
-  if (it == s->status.end()) return FPCC_EARG;
-  if (it->second < 0) set_last_error(s->err_msg.c_str());
-  return it->second;
+  const int st = s->status[(size_t)id];
+  if (st < 0) set_last_error(s->err_msg.c_str());
+  return st;
 }
 
 extern "C" int fpcc_server_drain(fpcc_server* h) {
@@ -1901,14 +1912,21 @@ extern "C" int fpcc_submit_many(fpcc_server* h, const fpcc_request* reqs, int n,
   // that the worker can start on the first chunk while the rest are prepared
   constexpr int kChunk = 1024;
   std::vector<Req> qs;
+  std::vector<int> lens;
   qs.reserve(std::min(n, kChunk));
   for (int i0 = 0; i0 < n; i0 += kChunk) {
     const int i1 = std::min(n, i0 + kChunk);
     qs.clear();
     int rc = 0, bad = i1;
+    lens.resize((size_t)(i1 - i0));
+    {
+      std::lock_guard<std::mutex> lk(s->mu);   // the chunk's window lookups under one lock
+      for (int i = i0; i < i1; i++) lens[(size_t)(i - i0)] = request_window_len(s, reqs + i);
+    }
     for (int i = i0; i < i1; i++) {
       Req q;
-      if ((rc = prepare_request(s, reqs + i, q))) {
+      const int N = lens[(size_t)(i - i0)];
+      if ((rc = (N < 0) ? N : prepare_request_n(s, reqs + i, q, N))) {
         bad = i;
         break;
       }
@@ -1921,7 +1939,7 @@ extern "C" int fpcc_submit_many(fpcc_server* h, const fpcc_request* reqs, int n,
         Req& q = qs[k];
         q.t_submit = now;
         q.id = s->next_id++;
-        s->status[q.id] = 0;
+        s->status.push_back(0);
         if (ids) ids[i0 + (int)k] = q.id;
         s->pending.push_back(std::move(q));
       }
