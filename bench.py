@@ -54,6 +54,9 @@ def parse():
                          "to TRACE_JSON and print the kernel and stream summary")
     ap.add_argument("--stack-only", action="store_true",
                     help="run one all-pairs step, then only the stacking leg (profiling of the stacks)")
+    ap.add_argument("--methods-only", action="store_true",
+                    help="run the warm-up steps, then only the per-method kernel leg (profiling of one method's "
+                         "kernel: ncu -k)")
     return ap.parse_args()
 
 
@@ -879,11 +882,15 @@ def run_ours(args):
                           "serving": serving_leg(F, fmt=fmt, nz_mode=F.NZ_TUNED)}), flush=True)
         return
     n_sta, n_win = args.stations, args.windows
-    from fastpcc_gb300 import synth
-    # weak scaling: rank r correlates its own block of windows
-    x, _ = synth.all_pairs(n_stations=n_sta, n_windows=n_win, N=N_SAMP, tag=f"all-pairs/rank{rank}")
-    x = np.ascontiguousarray(x.reshape(n_sta * n_win, N_SAMP))
-    pairs = all_pairs_index(n_sta, n_win)
+    from fastpcc_gb300 import partition, synth
+    # weak scaling: the job is n_sta stations x (n_win x world) windows, and the
+    # partitioner deals each rank n_win of them (no product computed twice, no
+    # data-path collective); the rank synthesises and correlates its own windows
+    shard = partition.shard_all_pairs(n_sta, n_win * world, world)[rank]
+    x, _ = synth.all_pairs(n_stations=n_sta, n_windows=len(shard.windows), N=N_SAMP, tag=f"all-pairs/rank{rank}")
+    x = np.ascontiguousarray(x.reshape(n_sta * len(shard.windows), N_SAMP))
+    pairs = partition.shard_rows(shard, n_sta)
+    assert world > 1 or np.array_equal(pairs, all_pairs_index(n_sta, n_win))
     P = pairs.shape[0]
     L = 2 * LAG + 1
     fmt = {"f32": F.F32, "f16": F.F16, "i16": F.I16}[args.fmt]
@@ -915,6 +922,11 @@ def run_ours(args):
     for _ in range(args.warmup):
         step()
     barrier()
+    if args.methods_only:
+        print(json.dumps({"methods": method_legs(F, torch, ctx, stream, dev, x, d_x, pairs, Nz,
+                                                 measured_peaks()[0])}), flush=True)
+        ctx.close()
+        return
     if args.stack_only:
         print(json.dumps({"stacks": stack_leg(F, torch, ctx, stream, dev, d_y, n_sta, n_win, L,
                                               measured_peaks()[0])}), flush=True)
@@ -1052,7 +1064,7 @@ def run_ours(args):
             "config": {"workload": f"all-pairs PCC2: {n_sta} stations x {n_win} windows x {N_SAMP} samples, "
                                    f"{P} pair-windows per step, lags +-{LAG}",
                        "Nz": Nz, "spectra": args.fmt, "l2": f"inputs {x.nbytes / 1e6:.0f} MB and outputs {P * L * 4 / 1e9:.2f} GB exceed L2; no flush",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"window shards x{world}"},
             "max_rel_err": err,
             "latency_ms": {"p50": statistics.median(step_ms), "p99": float(np.percentile(step_ms, 99)),
                            "what": f"batched step ({x.shape[0]} station windows + {P} correlations)"},

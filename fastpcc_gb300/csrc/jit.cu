@@ -7,7 +7,8 @@
 // 24 complex values per thread), instantiates k_station_fused with it through
 // NVRTC for sm_103a, and caches the cubin in memory and under the disk cache
 // directory (FPCC_JIT_CACHE, default ~/.cache/fastpcc_gb300).  FPCC_JIT=0
-// disables the path.
+// disables the path.  For even N the real window's DFT_N runs as an N/2-point
+// complex transform (k_station_fused_real).
 #include <nvrtc.h>
 
 #include <cstdio>
@@ -147,8 +148,20 @@ Entry build(int dev, int N, int Nz) {
     return e;
   }
   e.T = T;
-  const std::string name = "fpcc::k_station_fused<" + std::to_string(T) + ", fpcc::Radices<" + list(rn) +
-                           ">, fpcc::Radices<" + list(rz) + ">>";
+  // even N: the real window's DFT_N as an N/2-point complex transform
+  // (k_station_fused_real); FPCC_STATION_REAL=0 keeps the N-point one
+  std::vector<int> rh;
+  const char* re = getenv("FPCC_STATION_REAL");
+  if (N % 2 == 0 && !(re && re[0] == '0') && fused_smem_bytes(N, Nz, N / 2) <= kMaxSmem) rh = schedule(N / 2, T);
+  std::string name;
+  if (!rh.empty()) {
+    e.smem = fused_smem_bytes(N, Nz, N / 2);
+    name = "fpcc::k_station_fused_real<" + std::to_string(T) + ", fpcc::Radices<" + list(rh) + ">, fpcc::Radices<" +
+           list(rn) + ">, fpcc::Radices<" + list(rz) + ">>";
+  } else {
+    name = "fpcc::k_station_fused<" + std::to_string(T) + ", fpcc::Radices<" + list(rn) + ">, fpcc::Radices<" +
+           list(rz) + ">>";
+  }
   // disk cache keyed by the kernel name and the source text
   const size_t h = std::hash<std::string>()(name + "|" + kJitSource);
   char file[128];

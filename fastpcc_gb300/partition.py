@@ -87,6 +87,26 @@ def shard_all_pairs(n_sta: int, n_win: int, world: int, block: int = 0) -> list:
     return shards
 
 
+def shard_rows(shard: Shard, n_sta: int) -> np.ndarray:
+    """The shard's pair list as (row of station 1, row of station 2), int32,
+    for a rank that holds its windows station-major: row = station * W + k,
+    where k is the window's position in ``shard.windows`` and W their number.
+    Ordered window-major (then station 1, station 2), the order in which one
+    window's station products are read by consecutive pairs."""
+    W = len(shard.windows)
+    if shard.n == 0 or W == 0:
+        return np.zeros((0, 2), np.int32)
+    local = np.full(max(shard.windows) + 1, -1, np.int64)
+    local[np.asarray(shard.windows, np.int64)] = np.arange(W)
+    p = shard.pairs.astype(np.int64)
+    k = local[p[:, 2]]
+    if np.any(k < 0) or np.any(p[:, :2] >= n_sta):
+        raise ValueError("shard pairs outside its windows or stations")
+    order = np.lexsort((p[:, 1], p[:, 0], k))
+    rows = np.stack([p[order, 0] * W + k[order], p[order, 1] * W + k[order]], axis=1)
+    return np.ascontiguousarray(rows.astype(np.int32))
+
+
 def stations_needed(shard: Shard) -> set:
     """(station, window) products a shard computes."""
     if shard.n == 0:

@@ -32,6 +32,27 @@ def test_window_split_duplicates_no_station_product():
     assert max(loads) - min(loads) <= 28
 
 
+@pytest.mark.parametrize("n_sta,n_win,world", [(6, 4, 2), (7, 5, 3), (9, 1, 4), (64, 8, 1)])
+def test_shard_rows_window_major(n_sta, n_win, world):
+    # each rank's station-major rows address exactly its shard's (i, j, w) triples,
+    # window-major; one rank over the whole job gives the plain all-pairs order
+    for sh in partition.shard_all_pairs(n_sta, n_win, world):
+        rows = partition.shard_rows(sh, n_sta)
+        W = len(sh.windows)
+        assert rows.shape == (sh.n, 2)
+        k = rows[:, 0] % W
+        assert np.array_equal(k, rows[:, 1] % W)
+        got = set(zip((rows[:, 0] // W).tolist(), (rows[:, 1] // W).tolist(),
+                      np.asarray(sh.windows)[k].tolist()))
+        assert got == set(map(tuple, sh.pairs.tolist()))
+        assert np.all(np.diff(k) >= 0)
+    if world == 1:
+        iu, ju = np.triu_indices(n_sta, k=1)
+        w = np.repeat(np.arange(n_win), iu.size)
+        ref = np.stack([np.tile(iu, n_win) * n_win + w, np.tile(ju, n_win) * n_win + w], axis=1)
+        assert np.array_equal(partition.shard_rows(partition.shard_all_pairs(n_sta, n_win, 1)[0], n_sta), ref)
+
+
 def test_route_is_stable_and_symmetric():
     for a in range(20):
         for b in range(20):
