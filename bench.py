@@ -544,16 +544,19 @@ def method_legs(F, torch, ctx, stream, dev, x, d_x, pairs, Nz, peak):
             out[f"pcc2_pairs_{tag}"]["max_rel_err"] = float(
                 O.relerr(d_y[torch.from_numpy(sel).to(dev)].cpu().numpy(), y64).max())
         del spec
-    # GNCC: half spectra + FP64 energy prefix sums
+    # GNCC: half spectra + energy rows (FP64 prefix sums and the float
+    # normalisation tables: two 4-byte table entries per lag); the same pairs
+    # with rows of prefix sums only (two FP64 sums per lag) beside it
     H = Nz // 2 + 1
     half = torch.empty((rows, 2 * H), dtype=torch.float32, device=dev)
-    E = torch.empty((rows, N + 1), dtype=torch.float64, device=dev)
+    E = torch.empty((rows, 2 * (N + 1)), dtype=torch.float64, device=dev)
     ctx.station_stage(F.GNCC, d_x.data_ptr(), N, rows, N, Nz, F.F32, 0, half.data_ptr(), H)
-    ctx.energy_stage(d_x.data_ptr(), N, rows, N, E.data_ptr(), N + 1)
-    ms = _time_ms(torch, stream, lambda: ctx.pair_stage(F.GNCC, half.data_ptr(), H, F.F32, d_pairs.data_ptr(), P, N,
-                                                        Nz, -LAG, LAG, d_E=E.data_ptr(), ldE=N + 1,
-                                                        d_y=d_y.data_ptr(), ldy=L))
-    hbm("gncc_pairs", ms, P * (2 * H * 8 + 2 * L * 8 + 4 * L), P)
+    for name, ldE, per_lag in (("gncc_pairs", 2 * (N + 1), 8), ("gncc_pairs_sums_only", N + 1, 16)):
+        ctx.energy_stage(d_x.data_ptr(), N, rows, N, E.data_ptr(), ldE)
+        ms = _time_ms(torch, stream, lambda: ctx.pair_stage(F.GNCC, half.data_ptr(), H, F.F32, d_pairs.data_ptr(),
+                                                            P, N, Nz, -LAG, LAG, d_E=E.data_ptr(), ldE=ldE,
+                                                            d_y=d_y.data_ptr(), ldy=L))
+        hbm(name, ms, P * (2 * H * 8 + per_lag * L + 4 * L), P)
     del E
     # 1-bit, DFT form: station 1 signs x >= 0, station 2 signs x > 0 (rows offset by `rows`)
     half2 = torch.empty((2 * rows, 2 * H), dtype=torch.float32, device=dev)

@@ -741,10 +741,12 @@ int run(const Options& o) {
     void* d_s = nullptr;
     double* d_E = nullptr;
     cudaMalloc(&d_s, (size_t)rows * H * 8);
-    cudaMalloc(&d_E, (size_t)rows * (N + 1) * 8);
+    // energy rows with room for the normalisation tables: 2 (N + 1) doubles
+    const int64_t ldE = 2 * ((int64_t)N + 1);
+    cudaMalloc(&d_E, (size_t)rows * ldE * 8);
     GCHECK(fpcc_station_stage(ctx, FPCC_GNCC, d_x, N, rows, N, Nz, FPCC_F32, 0, d_s, H));
-    GCHECK(fpcc_energy_stage(ctx, d_x, N, rows, N, d_E, N + 1));
-    GCHECK(fpcc_pair_stage(ctx, FPCC_GNCC, d_s, H, FPCC_F32, d_pairs, Tr, N, Nz, Lag1, Lag2, 0.f, d_E, N + 1, d_y,
+    GCHECK(fpcc_energy_stage(ctx, d_x, N, rows, N, d_E, ldE));
+    GCHECK(fpcc_pair_stage(ctx, FPCC_GNCC, d_s, H, FPCC_F32, d_pairs, Tr, N, Nz, Lag1, Lag2, 0.f, d_E, ldE, d_y,
                            L, nullptr));
     emit("ccgn");
     cudaFree(d_s);

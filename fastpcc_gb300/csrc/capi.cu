@@ -1105,11 +1105,13 @@ extern "C" int fpcc_energy_stage(fpcc_ctx* c, const float* d_x, int64_t ldx, int
   void* part;
   int rc = dev_buf(c, S_EPART, (size_t)blk * energy_chunks(N) * sizeof(double), &part);
   if (rc) return rc;
+  // rows with room for them also get the pair stage's normalisation tables
+  const bool tables = ldE >= 2 * ((int64_t)N + 1);
   for (int r0 = 0; r0 < nrows; r0 += blk) {
     const int n = std::min(blk, nrows - r0);
-    CK(launch_energy_prefix(d_x + (size_t)r0 * ldx, ldx, n, N, d_E + (size_t)r0 * ldE, ldE, (double*)part,
+    CK(launch_energy_prefix(d_x + (size_t)r0 * ldx, ldx, n, N, d_E + (size_t)r0 * ldE, ldE, (double*)part, tables,
                             c->stream));
-    g_launches += 2;
+    g_launches += tables ? 3 : 2;
   }
   return 0;
 }
@@ -1251,6 +1253,8 @@ struct Layout {
   int64_t lds;      // station row elements
   size_t esz;       // station element bytes
   bool two_rules;   // 1-bit: station 1 and 2 rows use different sign rules
+  // GNCC energy row: N + 1 FP64 prefix sums and the normalisation tables (2 (N + 1) floats)
+  int64_t ldE() const { return 2 * ((int64_t)N + 1); }
 };
 
 int make_layout(int method, int N, int Lag1, int Lag2, int nz_mode, int fmt, Layout* o) {
@@ -1338,13 +1342,13 @@ int run_device(fpcc_ctx* c, const Layout& Ly, const float* d_x, int nsta, const 
   double* d_E = nullptr;
   if (method == FPCC_GNCC) {
     void* p = nullptr;
-    if ((rc = dev_buf(c, S_ENERGY, (size_t)nsta * (Ly.N + 1) * sizeof(double), &p))) return rc;
+    if ((rc = dev_buf(c, S_ENERGY, (size_t)nsta * Ly.ldE() * sizeof(double), &p))) return rc;
     d_E = (double*)p;
-    if ((rc = fpcc_energy_stage(c, d_x, Ly.N, nsta, Ly.N, d_E, Ly.N + 1))) return rc;
+    if ((rc = fpcc_energy_stage(c, d_x, Ly.N, nsta, Ly.N, d_E, Ly.ldE()))) return rc;
   }
   if (!h_y)
     return fpcc_pair_stage(c, method, d_st, Ly.lds, Ly.fmt, d_pairs, npairs, Ly.N, Ly.Nz, Ly.lag0,
-                           Ly.lag0 + Ly.L - 1, v, d_E, Ly.N + 1, d_y, Ly.L, d_num);
+                           Ly.lag0 + Ly.L - 1, v, d_E, Ly.ldE(), d_y, Ly.L, d_num);
   // chunks of about 6000 correlations (at most 16): the first download starts
   // after a short first chunk, and the rest overlap the following chunks
   const int nch = (int)std::max<int64_t>(1, std::min<int64_t>(16, npairs / 6000));
@@ -1358,7 +1362,7 @@ int run_device(fpcc_ctx* c, const Layout& Ly, const float* d_x, int nsta, const 
     const int i0 = k * per, n = std::min(per, npairs - i0);
     if (n <= 0) break;
     if ((rc = fpcc_pair_stage(c, method, d_st, Ly.lds, Ly.fmt, d_pairs + 2 * (size_t)i0, n, Ly.N, Ly.Nz, Ly.lag0,
-                              Ly.lag0 + Ly.L - 1, v, d_E, Ly.N + 1, d_y + (size_t)i0 * Ly.L, Ly.L, nullptr)))
+                              Ly.lag0 + Ly.L - 1, v, d_E, Ly.ldE(), d_y + (size_t)i0 * Ly.L, Ly.L, nullptr)))
       return rc;
     CK(cudaEventRecord(c->chunk_ev[k], c->stream));
   }
@@ -1437,6 +1441,9 @@ extern "C" int fpcc_host_plain(int method, float** y, float** x1, float** x2, un
 extern "C" int fpcc_allpairs_host(fpcc_ctx* c, int method, const float* h_x, int nsta, int N, const int32_t* h_pairs,
                                   int npairs, int Lag1, int Lag2, float v, int nz_mode, int fmt, float* h_y) {
   if (!c || !h_x || !h_pairs || !h_y) return fail(FPCC_EARG, "null argument");
+  if (nsta < 0 || npairs < 0) return fail(FPCC_EARG, "negative count");
+  for (size_t i = 0; i < 2 * (size_t)npairs; i++)
+    if (h_pairs[i] < 0 || h_pairs[i] >= nsta) return fail(FPCC_EARG, "pair row index out of range");
   std::lock_guard<std::mutex> lk(c->mu);
   CK(cudaSetDevice(c->device));
   Layout Ly;

@@ -6,6 +6,7 @@
 //     (src/FFTapps.c:223-336, src/ccs_cuda.cu:260-321,388-453),
 //   - 1-bit GNCC numerators as exact popcounts of packed sign bits.
 #include "direct.cuh"
+#include "kernels.cuh"
 
 namespace fpcc {
 
@@ -83,6 +84,20 @@ __global__ void __launch_bounds__(256) k_energy_scan(const float* __restrict__ x
 #pragma unroll
   for (int j = 0; j < kEPer; j++)
     if (i0 + j < len) Er[i0 + j + 1] = off + v[j];
+}
+
+// Normalisation tables of each row (layout and rule: GnccNorm in
+// kernels.cuh): one thread per n = 0..N writes the prefix and suffix entries;
+// the thread of n = 0 sets the flag E[0] = -0.0 after reading E[0].
+__global__ void __launch_bounds__(256) k_energy_tables(double* __restrict__ E, int64_t ldE, int N) {
+  const int n = blockIdx.x * 256 + threadIdx.x;
+  if (n > N) return;
+  double* Er = E + (int64_t)blockIdx.y * ldE;
+  float* T = reinterpret_cast<float*>(Er + N + 1);
+  const double e = Er[n];
+  T[n] = energy_table_entry(e);
+  T[N + 1 + n] = energy_table_entry(Er[N] - e);
+  if (n == 0) Er[0] = -0.0;
 }
 
 // ---------------------------------------------------------------- PCC_v direct
@@ -499,12 +514,14 @@ __global__ void __launch_bounds__(256) k_cc1b_popcount(Cc1bArgs a) {
 int energy_chunks(int N) { return (N + kEChunk - 1) / kEChunk; }
 
 cudaError_t launch_energy_prefix(const float* x, int64_t ldx, int nrows, int N, double* E, int64_t ldE,
-                                 double* part, cudaStream_t st) {
+                                 double* part, bool tables, cudaStream_t st) {
   if (nrows <= 0 || N <= 0) return cudaSuccess;
   if (nrows > 65535) return cudaErrorInvalidValue;
+  if (tables && ldE < 2 * ((int64_t)N + 1)) return cudaErrorInvalidValue;
   const int nch = energy_chunks(N);
   k_energy_chunks<<<dim3(nch, nrows), 256, 0, st>>>(x, ldx, N, nch, part);
   k_energy_scan<<<dim3(nch, nrows), 256, 0, st>>>(x, ldx, N, nch, part, E, ldE);
+  if (tables) k_energy_tables<<<dim3(N / 256 + 1, nrows), 256, 0, st>>>(E, ldE, N);
   return cudaGetLastError();
 }
 

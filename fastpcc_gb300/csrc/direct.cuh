@@ -41,10 +41,12 @@ struct Cc1bArgs {
 };
 
 // FP64 prefix sums E[n] = sum_{m<n} x[m]^2 (N + 1 per row); `part` holds
-// nrows * energy_chunks(N) doubles of chunk totals.
+// nrows * energy_chunks(N) doubles of chunk totals.  With tables set (rows of
+// ldE >= 2 (N + 1)), each row also receives the GNCC normalisation tables of
+// GnccNorm (kernels.cuh) after its sums, and E[0] = -0.0 flags them.
 int energy_chunks(int N);
 cudaError_t launch_energy_prefix(const float* x, int64_t ldx, int nrows, int N, double* E, int64_t ldE,
-                                 double* part, cudaStream_t st);
+                                 double* part, bool tables, cudaStream_t st);
 cudaError_t launch_pccv(const PccvArgs& a, cudaStream_t st);
 cudaError_t launch_sign_bits(const float* x, int64_t ldx, int nrows, int N, uint32_t* bits, int64_t ldb,
                              int pos_ge, const int8_t* sel, cudaStream_t st);

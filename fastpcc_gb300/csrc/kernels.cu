@@ -236,13 +236,15 @@ __global__ void __launch_bounds__(T, 1) k_pairs(PairArgs a) {
         scale *= i16_row_scale(sp + (int64_t)pr.x * a.ldspec * 4) * i16_row_scale(sp + (int64_t)pr.y * a.ldspec * 4);
       }
     }
+    GnccNorm gn;
+    if (a.norm == 1) gn.init(E1, E2, N);
     for (int l = threadIdx.x; l < L; l += T) {
       const int lag = lag0 + l;
       const int idx = lag < 0 ? lag + NZ : lag;
       const float2 zz = res[PADI(idx >> 1)];
       float v = ((idx & 1) ? zz.y : zz.x) * (0.5f * scale);
       if (a.norm == 1) {
-        v = gncc_lag_norm(v, E1, E2, N, lag);
+        v = gn.apply(v, lag);
       } else if (a.norm == 2) {
         v = v / (float)(N - abs(lag));
       }

@@ -20,19 +20,71 @@ namespace fpcc {
 // conversion instruction, which would run on the FP64 pipe as well.
 __device__ __forceinline__ float energy_to_float(double d);
 
+// A prefix sum as stored: E[0] may hold -0.0 (the flag of rows that carry
+// normalisation tables), read as +0.0; every other prefix sum is >= 0.
+__device__ __forceinline__ double energy_at(const double* E, int i) {
+  return __longlong_as_double(__double_as_longlong(E[i]) & 0x7fffffffffffffffLL);
+}
+
 __device__ __forceinline__ float gncc_lag_norm(float v, const double* E1, const double* E2, int N, int lag) {
   double e1, e2;
   if (lag > 0) {
-    e1 = E1[N - lag];
-    e2 = E2[N] - E2[lag];
+    e1 = energy_at(E1, N - lag);
+    e2 = E2[N] - energy_at(E2, lag);
   } else {
-    e1 = E1[N] - E1[-lag];
-    e2 = E2[N + lag];
+    e1 = E1[N] - energy_at(E1, -lag);
+    e2 = energy_at(E2, N + lag);
   }
   const float f1 = energy_to_float(e1), f2 = energy_to_float(e2);
   if (f1 >= 1e-30f && f2 >= 1e-30f && f1 <= 1e30f && f2 <= 1e30f) return v * (rsqrtf(f1) * rsqrtf(f2));
   return (float)((double)v / sqrt(e1 * e2));
 }
+
+// Normalisation tables of one energy row (written by the energy stage when
+// the row has room for them, flagged by E[0] = -0.0): after the N + 1 prefix
+// sums, 2 (N + 1) floats
+//   T[n]         = 1/sqrt(prefix energy E[n])          (n = 0..N)
+//   T[N + 1 + n] = 1/sqrt(suffix energy E[N] - E[n])   (n = 0..N)
+// each the FP32 reciprocal square root of the energy narrowed as in
+// gncc_lag_norm, or 0 where that energy lies outside [1e-30, 1e30].  A lag then
+// costs two float loads and two multiplications, with results identical to
+// gncc_lag_norm: the same reciprocal square roots of the same narrowed
+// energies, multiplied in the same order, and gncc_lag_norm itself for any lag
+// whose energies are out of range.
+__device__ __forceinline__ float energy_table_entry(double e) {
+  const float f = energy_to_float(e);
+  return (f >= 1e-30f && f <= 1e30f) ? rsqrtf(f) : 0.0f;
+}
+
+// Holds the two rows by their table addresses (the sums sit N + 1 doubles
+// before), so that it keeps no more registers live than the two row pointers.
+struct GnccNorm {
+  const float *T1, *T2;
+  int N;
+  bool tab;
+  __device__ __forceinline__ void init(const double* e1, const double* e2, int n) {
+    N = n;
+    tab = (__double_as_longlong(e1[0]) < 0) && (__double_as_longlong(e2[0]) < 0);
+    T1 = reinterpret_cast<const float*>(e1 + n + 1);
+    T2 = reinterpret_cast<const float*>(e2 + n + 1);
+  }
+  __device__ __forceinline__ const double* E1() const { return reinterpret_cast<const double*>(T1) - (N + 1); }
+  __device__ __forceinline__ const double* E2() const { return reinterpret_cast<const double*>(T2) - (N + 1); }
+  // product of the two table entries of a lag: > 0, or 0 where gncc_lag_norm
+  // has to take the lag (an energy out of the tables' range)
+  __device__ __forceinline__ float table(int lag) const {
+    const float r1 = lag > 0 ? T1[N - lag] : T1[N + 1 - lag];
+    const float r2 = lag > 0 ? T2[N + 1 + lag] : T2[N + lag];
+    return r1 * r2;
+  }
+  __device__ __forceinline__ float apply(float v, int lag) const {
+    if (tab) {
+      const float p = table(lag);
+      if (p > 0.0f) return v * p;
+    }
+    return gncc_lag_norm(v, E1(), E2(), N, lag);
+  }
+};
 
 // A double narrowed to float by truncating its significand (relative error
 // below 2^-23), from the IEEE-754 fields with integer operations; magnitudes

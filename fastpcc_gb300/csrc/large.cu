@@ -223,6 +223,8 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
           }
         }
       }
+      GnccNorm gn;
+      if (a.norm == 1) gn.init(E1, E2, N);
 #pragma unroll
       for (int q = 0; q < 2; q++) {
         const int idx = 2 * k + q;
@@ -231,7 +233,7 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
         if (l < 0 || l >= L) continue;
         float val = (q ? v.y : v.x) * scale;
         if (a.norm == 1) {
-          val = gncc_lag_norm(val, E1, E2, N, lag);
+          val = gn.apply(val, lag);
         } else if (a.norm == 2) {
           val = val / (float)(N - abs(lag));
         }

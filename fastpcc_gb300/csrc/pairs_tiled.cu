@@ -372,15 +372,35 @@ __global__ void __launch_bounds__(kTM, 2) k_pairs_tiled(PairArgs a) {
     if constexpr (FMT == SPEC_I16) scale *= i16_row_scale(X1) * i16_row_scale(X2);
     // X[f] holds the lags of indices 2f (real part) and 2f + 1 (imaginary part),
     // index = lag mod Nz; output m covers lag numbers 2m - e and 2m - e + 1
+    // GNCC takes Hermitian spectra: the tables (GnccNorm) in those
+    // instantiations; the full-spectrum ones keep the plain form, which holds
+    // fewer registers
+    GnccNorm gn;
+    if constexpr (HERM) {
+      if (a.norm == 1) gn.init(E1, E2, N);
+    }
     const float hs = 0.5f * scale;
     const int idx0 = lag0 < 0 ? lag0 + NZ : lag0;
     const int e = idx0 & 1;
     const int nout = (L + e + 1) >> 1;
+    // GNCC: a lag the tables cannot take (energies out of their range, or rows
+    // without tables) is stored unnormalised and fixed after the loop, which
+    // keeps the FP64 branch out of the loop's registers
+    bool fix = false;
     auto put = [&](int l, float val) {
       const int lag = lag0 + l;
       val *= hs;
-      if (a.norm == 1) val = gncc_lag_norm(val, E1, E2, N, lag);
-      else if (a.norm == 2) val = val / (float)(N - abs(lag));
+      if (a.norm == 1) {
+        if constexpr (HERM) {
+          const float pr = gn.tab ? gn.table(lag) : 0.0f;
+          if (pr > 0.0f) val *= pr;
+          else fix = true;
+        } else {
+          val = gncc_lag_norm(val, E1, E2, N, lag);
+        }
+      } else if (a.norm == 2) {
+        val = val / (float)(N - abs(lag));
+      }
       y[l] = val;
     };
 #pragma unroll 2
@@ -392,6 +412,18 @@ __global__ void __launch_bounds__(kTM, 2) k_pairs_tiled(PairArgs a) {
       const int l = 2 * m - e;
       if (l >= 0) put(l, zz.x);
       if (l + 1 < L) put(l + 1, zz.y);
+    }
+    if constexpr (HERM) {
+      if (fix) {
+        // this thread's lags again: the ones the tables could not take
+        for (int m = threadIdx.x; m < nout; m += M)
+          for (int h = 0; h < 2; h++) {
+            const int l = 2 * m - e + h;
+            if (l < 0 || l >= L) continue;
+            const int lag = lag0 + l;
+            if (!(gn.tab && gn.table(lag) > 0.0f)) y[l] = gncc_lag_norm(y[l], E1, E2, N, lag);
+          }
+      }
     }
   }
 }

@@ -284,7 +284,7 @@ size_t product_row_bytes(const Product& p) {
     case 0: return (size_t)p.N * 4;
     case 1: return p.fmt == FPCC_I16 ? 16 + (size_t)p.Nz * 4 : (size_t)p.Nz * (p.fmt ? 4 : 8);
     case 2: case 3: case 4: return (size_t)(p.Nz / 2 + 1) * 8;
-    case 5: return (size_t)(p.N + 1) * 8;
+    case 5: return (size_t)(p.N + 1) * 16;   // FP64 prefix sums + the normalisation tables
     case 6: return (size_t)p.N * (p.fmt ? 4 : 8);
     case 9: return (size_t)p.S * p.Nz * (p.fmt ? 4 : 8);
     default: return (size_t)((p.N + 31) / 32) * 4;

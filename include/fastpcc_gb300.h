@@ -156,7 +156,11 @@ typedef struct {
 } fpcc_station_row;
 int fpcc_station_stage_multi(fpcc_ctx *ctx, int method, const fpcc_station_row *h_rows, int nrows, int fmt,
                              int rule, void *d_out, int64_t ldo);
-/* FP64 prefix sums E[n] = sum_{m<n} x[m]^2, N+1 per row (GNCC normalisation). */
+/* FP64 prefix sums E[n] = sum_{m<n} x[m]^2, N+1 per row (GNCC normalisation).
+ * Rows with ldE >= 2 (N+1) also receive, after the sums, 2 (N+1) floats of
+ * normalisation tables (reciprocal square roots of the prefix and suffix
+ * energies), and E[0] is written as -0.0 to flag them; the pair stage then reads
+ * two floats per lag instead of two FP64 sums, with identical results. */
 int fpcc_energy_stage(fpcc_ctx *ctx, const float *d_x, int64_t ldx, int nrows, int N, double *d_E,
                       int64_t ldE);
 /* Pair stage: output row p correlates station rows pairs[2p] (station 1) and
@@ -235,8 +239,11 @@ int fpcc_host_batched(int method, float **y, float **x1, float **x2, unsigned N,
 int fpcc_host_plain(int method, float **y, float **x1, float **x2, unsigned N, unsigned Tr, int Lag1,
                     int Lag2, float v, int nz_mode, int fmt);
 
-/* Contiguous host arrays (pinned or pageable): x is nsta x N, pairs 2*npairs,
- * y npairs x L.  Host<->device copies happen inside the call. */
+/* Contiguous host arrays (pinned or pageable): x is nsta x N, pairs 2*npairs
+ * (row indices in [0, nsta), else FPCC_EARG before any work), y npairs x L.
+ * Host<->device copies happen inside the call: the rows go up in chunks that
+ * the station stage consumes as they arrive, and the results come down in
+ * chunks while later pair chunks compute. */
 int fpcc_allpairs_host(fpcc_ctx *ctx, int method, const float *h_x, int nsta, int N,
                        const int32_t *h_pairs, int npairs, int Lag1, int Lag2, float v, int nz_mode,
                        int fmt, float *h_y);

@@ -50,6 +50,53 @@ def test_gncc(F, orc, N, Tr, l1, l2, d):
     assert relerr(F.ccgn_set(a, b, l1, l2), orc.gncc(a, b, l1, l2)) < TOL
 
 
+def test_gncc_normalisation_tables(F, orc):
+    # energy rows with room for the normalisation tables (ldE = 2 (N + 1)) give
+    # the pair stage the same results, bit for bit, as rows of FP64 prefix sums
+    # only (ldE = N + 1), over every lag of the window: rows of ordinary scale,
+    # a row ending in zeros (empty overlaps: the FP64 branch), rows scaled by
+    # 1e-17 and 1e15 (energies outside the tables' range: the FP64 branch)
+    import torch
+    N, lag = 1000, 999
+    a, b = _data(N, 3, 41, "gncc-tables")
+    x = np.concatenate([a, b]).astype(np.float32)
+    x[1, 800:] = 0.0
+    x[2] *= np.float32(1e-17)
+    x[3] *= np.float32(1e15)
+    rows = x.shape[0]
+    iu, ju = np.triu_indices(rows)
+    pairs = np.ascontiguousarray(np.stack([iu, ju], axis=1).astype(np.int32))
+    P, L = pairs.shape[0], 2 * lag + 1
+    Nz = F.choose_nz(N, -lag, lag, F.NZ_FAST)
+    H = Nz // 2 + 1
+    ctx = F.Context(0)
+    d_x = torch.from_numpy(x).cuda()
+    d_p = torch.from_numpy(pairs).cuda()
+    d_s = torch.empty((rows, 2 * H), dtype=torch.float32, device="cuda")
+    ctx.station_stage(F.GNCC, d_x.data_ptr(), N, rows, N, Nz, F.F32, 0, d_s.data_ptr(), H)
+    ys, Es = [], []
+    for ldE in (N + 1, 2 * (N + 1)):
+        E = torch.empty((rows, ldE), dtype=torch.float64, device="cuda")
+        d_y = torch.empty((P, L), dtype=torch.float32, device="cuda")
+        ctx.energy_stage(d_x.data_ptr(), N, rows, N, E.data_ptr(), ldE)
+        ctx.pair_stage(F.GNCC, d_s.data_ptr(), H, F.F32, d_p.data_ptr(), P, N, Nz, -lag, lag,
+                       d_E=E.data_ptr(), ldE=ldE, d_y=d_y.data_ptr(), ldy=L)
+        ctx.sync()
+        ys.append(d_y.cpu().numpy())
+        Es.append(E.cpu().numpy())
+    ctx.close()
+    assert np.array_equal(ys[0], ys[1], equal_nan=True)
+    # the sums are the same; E[0] carries the sign flag of the tables
+    assert np.array_equal(Es[0][:, 1:], Es[1][:, 1:N + 1])
+    assert np.all(Es[0][:, 0] == 0) and not np.any(np.signbit(Es[0][:, 0]))
+    assert np.all(np.signbit(Es[1][:, 0]))
+    # against the oracle on the lags whose overlaps are not empty
+    m = 700
+    sel = slice(lag - m, lag + m + 1)
+    y64 = orc.gncc(x[pairs[:, 0]], x[pairs[:, 1]], -m, m)
+    assert relerr(ys[1][:, sel], y64) < TOL
+
+
 @pytest.mark.parametrize("N,Tr,l1,l2,d", CASES)
 def test_cc1b_fft(F, orc, N, Tr, l1, l2, d):
     a, b = _data(N, Tr, d, "cc1b")
@@ -335,4 +382,15 @@ def test_allpairs_host_chunked_transfers(F, orc):
         y[:] = 0
         ctx.allpairs_host(method, x, pairs, -lag, lag, y)
         assert relerr(y[sel], ref(x[pairs[sel, 0]], x[pairs[sel, 1]], -lag, lag)) < TOL, method
+    # a shuffled pair list gives the same rows in its own order (the chunked
+    # downloads follow the caller's pair order)
+    perm = np.random.default_rng(11).permutation(P)
+    ys = np.zeros((P, L), np.float32)
+    ctx.allpairs_host(F.PCC2, x, np.ascontiguousarray(pairs[perm]), -lag, lag, ys)
+    assert np.array_equal(ys, d_y.cpu().numpy()[perm])
+    # a row index outside the station rows is refused before any work
+    bad = pairs.copy()
+    bad[5, 1] = x.shape[0]
+    with pytest.raises(F.FpccError):
+        ctx.allpairs_host(F.PCC2, x, bad, -lag, lag, ys)
     ctx.close()
