@@ -60,6 +60,37 @@ def parse():
     return ap.parse_args()
 
 
+def host_link_leg(torch, dev, hx, hy, d_x, d_y, t_e2e):
+    """The end-to-end roofline: copy rates between pinned host memory and the
+    device for the step's own buffers (uploads alone, downloads alone, both at
+    once on two streams), and the time the step's copies alone would take."""
+    up = torch.cuda.Stream(device=dev)
+    down = torch.cuda.Stream(device=dev)
+    dy = d_y.view(-1)[: hy.numel()]
+    hyv = hy.view(-1)
+
+    def run(h2d, d2h, reps=3):
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        for _ in range(reps):
+            if h2d:
+                with torch.cuda.stream(up):
+                    d_x.copy_(hx, non_blocking=True)
+            if d2h:
+                with torch.cuda.stream(down):
+                    hyv.copy_(dy, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        return (time.perf_counter() - t) / reps
+
+    run(True, True, 1)
+    bi, bo = hx.numel() * 4, hy.numel() * 4
+    t_up, t_down, t_both = run(True, False), run(False, True), run(True, True)
+    return {"h2d_GBs": bi / t_up / 1e9, "d2h_GBs": bo / t_down / 1e9, "both_GBs": (bi + bo) / t_both / 1e9,
+            "copies_ms": t_both * 1e3, "frac": t_both / t_e2e,
+            "what": "the step's upload and download alone (pinned, both directions at once on two streams): "
+                    "frac = their time / the end-to-end step"}
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1012,7 +1043,9 @@ def run_ours(args):
     barrier()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     e2e = {"value": P * world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(hxn.nbytes + hpn.nbytes),
-           "d2h_bytes_per_step": int(hyn.nbytes)}
+           "d2h_bytes_per_step": int(hyn.nbytes), "ms_per_step": t_e2e * 1e3}
+    if rank == 0:
+        e2e["host_link"] = host_link_leg(torch, dev, hx, hy, d_x, d_y, t_e2e)
 
     # --- plain per-pair drop-in (one launch sequence per pair-window), bounded sample ---
     plain = None
