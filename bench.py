@@ -233,11 +233,13 @@ def served_leg(F, x, pairs, n_win, L, rate_frac=0.5, poisson_max=60000):
     srv_err = float(O.relerr(out[sel], O.pcc2(x[pairs[sel, 0]], x[pairs[sel, 1]], -LAG, LAG)).max())
     return {
         "saturation": {"value": sat, "unit": UNIT, "batches": st_sat["batches"],
-                       "p50_ms": st_sat["p50_ms"], "p99_ms": st_sat["p99_ms"],
+                       "p50_ms": st_sat["p50_ms"], "p99_ms": st_sat["p99_ms"], "wall_ms": t_warm * 1e3,
+                       "worker_ms": st_sat["worker_ms"], "deliver_ms": st_sat["deliver_ms"],
                        "what": f"{P} requests submitted at once, station products resident, results copied "
                                f"straight into the caller's registered output array"},
         "saturation_pageable": {"value": P / t_pageable, "unit": UNIT, "batches": st_pg["batches"],
-                                "p50_ms": st_pg["p50_ms"], "p99_ms": st_pg["p99_ms"],
+                                "p50_ms": st_pg["p50_ms"], "p99_ms": st_pg["p99_ms"], "wall_ms": t_pageable * 1e3,
+                                "worker_ms": st_pg["worker_ms"], "deliver_ms": st_pg["deliver_ms"],
                                 "what": "the same with results delivered into unregistered (pageable) arrays by "
                                         "host copy threads"},
         "max_rel_err": srv_err,

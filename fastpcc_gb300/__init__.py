@@ -49,7 +49,7 @@ class PairDesc(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("batches", C.c_int64), ("station_rows", C.c_int64),
                 ("hbm_used", C.c_int64), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("max_ms", C.c_double),
-                ("pair_stages", C.c_int64)]
+                ("pair_stages", C.c_int64), ("worker_ms", C.c_double), ("deliver_ms", C.c_double)]
 
 
 class FpccError(RuntimeError):

@@ -134,6 +134,8 @@ struct Req {
   Clock::time_point t_submit;
   int N = 0, Nz = 0, lag0 = 0, L = 0;
   int aux = 0;    // WPCC: wavelet length cap
+  int f64 = 0;    // bit 0 / bit 1: the station-1 / station-2 window has enough zero
+                  // samples for an FP64 analytic signal (noted at submission)
 };
 
 struct InFlight {
@@ -141,6 +143,7 @@ struct InFlight {
   std::vector<Req> reqs;
   std::vector<int64_t> out_off;    // offset of each request's output in the pinned buffer (floats or int64)
   void* h_out = nullptr;           // pinned result buffer
+  void* d_out = nullptr;           // device results of the batch (group outputs at their offsets)
   size_t h_bytes = 0;
   char* h_up = nullptr;            // pinned upload staging (index arrays), bump-allocated
   size_t up_bytes = 0, up_used = 0;
@@ -213,6 +216,11 @@ struct Server {
   Lane dlane;                           // pair stages of direct-sum groups, started early
   int next_lane = 0;
   cudaEvent_t main_ev = nullptr;        // marks the server's stream for the lanes
+  // results go down on their own stream, so that one group's (and batch's)
+  // download overlaps the next pair stages; out_ev mark finished pair stages
+  cudaStream_t st_out = nullptr;
+  std::vector<cudaEvent_t> out_ev;
+  size_t out_used = 0;
   uint64_t lane_seq = 0;                // lane work items queued so far
   std::vector<int>* lane_rec = nullptr; // when set, lanes given work are noted here
   std::vector<cudaEvent_t> ev_pool;     // marks of lane progress for the pair stages
@@ -268,6 +276,7 @@ struct Server {
   // stats
   std::vector<double> lat_ms;
   int64_t completed = 0, batches = 0, station_rows = 0, pair_stages = 0;
+  std::atomic<int64_t> worker_ns{0}, deliver_ns{0};   // host time forming batches / completing them
   double busy_s = 0;
   int last_error = 0;
   std::string err_msg;                // message of last_error   [mu]
@@ -533,6 +542,13 @@ void* dbuf(Server* s, void** p, size_t* n, size_t need) {
 // ---------------------------------------------------------------- batch execution
 namespace {
 
+// Product rows of a group's requests, found by its products pass and kept
+// (pinned) for its pair pass, so that each request's rows are looked up once.
+struct GroupRows {
+  bool ok = false;
+  std::vector<int> r1, r2, e1, e2;
+};
+
 struct GroupKey {
   int method, N, Nz, lag0, L, fmt;
   float v;
@@ -764,41 +780,81 @@ cudaError_t d2h_results(InFlight& fl, const std::vector<Req*>& reqs, size_t firs
   return e;
 }
 
+// Device output of a group: its place in the batch's result buffer, or the
+// shared scratch buffer when the batch has none.
+char* group_out(Server* s, InFlight& fl, size_t out_base, size_t bytes) {
+  if (fl.d_out) return (char*)fl.d_out + out_base;
+  return (char*)dbuf(s, &s->d_y, &s->n_y, bytes);
+}
+
+// Results of a group whose pair stage was queued on `st`: downloaded on the
+// results stream after that pair stage (the batch's own result buffer is not
+// reused before the batch completes), else on `st` itself.
+cudaError_t results_down(Server* s, InFlight& fl, const std::vector<Req*>& reqs, size_t first, size_t out_base,
+                         const char* dy, cudaStream_t st) {
+  if (!fl.d_out || !s->st_out) return d2h_results(fl, reqs, first, out_base, dy, st);
+  if (s->out_used == s->out_ev.size()) {
+    cudaEvent_t e;
+    if (cudaError_t ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming)) return ce;
+    s->out_ev.push_back(e);
+  }
+  cudaEvent_t e = s->out_ev[s->out_used++];
+  if (cudaError_t ce = cudaEventRecord(e, st)) return ce;
+  if (cudaError_t ce = cudaStreamWaitEvent(s->st_out, e, 0)) return ce;
+  return d2h_results(fl, reqs, first, out_base, dy, s->st_out);
+}
+
 int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base,
-              bool products_only, size_t first = 0) {
+              bool products_only, size_t first = 0, GroupRows* gr = nullptr) {
   const int n = (int)reqs.size();
   const int m = g.method;
-  std::vector<int64_t> k1(n), k2(n);
-  for (int i = 0; i < n; i++) {
-    k1[i] = wkey(reqs[i]->r.sta1, reqs[i]->r.window);
-    k2[i] = wkey(reqs[i]->r.sta2, reqs[i]->r.window);
-  }
   int kind1, kind2;
   method_kinds(m, &kind1, &kind2);
   const int Nz = (m == FPCC_PCC1 || m == FPCC_PCCV || m == FPCC_CC1B_POPCOUNT) ? 0 : g.Nz;
   Product p1{kind1, g.N, Nz, g.fmt}, p2{kind2, g.N, Nz, g.fmt};
-  std::vector<int> r1, r2;
+  std::vector<int> r1, r2, e1, e2;
   int rc;
-  if (kind1 == kind2) {
-    std::vector<int64_t> all(k1);
-    all.insert(all.end(), k2.begin(), k2.end());
-    std::vector<int> rr;
-    if ((rc = ensure_products(s, p1, all, rr, fl))) return rc;
-    r1.assign(rr.begin(), rr.begin() + n);
-    r2.assign(rr.begin() + n, rr.end());
+  if (gr && gr->ok) {
+    r1.swap(gr->r1);
+    r2.swap(gr->r2);
+    e1.swap(gr->e1);
+    e2.swap(gr->e2);
+    gr->ok = false;
   } else {
-    if ((rc = ensure_products(s, p1, k1, r1, fl)) || (rc = ensure_products(s, p2, k2, r2, fl))) return rc;
+    std::vector<int64_t> k1(n), k2(n);
+    for (int i = 0; i < n; i++) {
+      k1[i] = wkey(reqs[i]->r.sta1, reqs[i]->r.window);
+      k2[i] = wkey(reqs[i]->r.sta2, reqs[i]->r.window);
+    }
+    if (kind1 == kind2) {
+      std::vector<int64_t> all(k1);
+      all.insert(all.end(), k2.begin(), k2.end());
+      std::vector<int> rr;
+      if ((rc = ensure_products(s, p1, all, rr, fl))) return rc;
+      r1.assign(rr.begin(), rr.begin() + n);
+      r2.assign(rr.begin() + n, rr.end());
+    } else {
+      if ((rc = ensure_products(s, p1, k1, r1, fl)) || (rc = ensure_products(s, p2, k2, r2, fl))) return rc;
+    }
+    if (m == FPCC_GNCC) {
+      std::vector<int64_t> all(k1);
+      all.insert(all.end(), k2.begin(), k2.end());
+      std::vector<int> rr;
+      if ((rc = ensure_products(s, Product{5, g.N, 0, 0}, all, rr, fl))) return rc;
+      e1.assign(rr.begin(), rr.begin() + n);
+      e2.assign(rr.begin() + n, rr.end());
+    }
   }
-  std::vector<int> e1, e2;
-  if (m == FPCC_GNCC) {
-    std::vector<int64_t> all(k1);
-    all.insert(all.end(), k2.begin(), k2.end());
-    std::vector<int> rr;
-    if ((rc = ensure_products(s, Product{5, g.N, 0, 0}, all, rr, fl))) return rc;
-    e1.assign(rr.begin(), rr.begin() + n);
-    e2.assign(rr.begin() + n, rr.end());
+  if (products_only) {
+    if (gr) {
+      gr->r1.swap(r1);
+      gr->r2.swap(r2);
+      gr->e1.swap(e1);
+      gr->e2.swap(e2);
+      gr->ok = true;
+    }
+    return 0;
   }
-  if (products_only) return 0;
   pair_join(s);
   // pair list: rows in one slab (both roles share a slab except the 1-bit methods,
   // whose station-2 rows are offset by the station-1 slab capacity after a merge)
@@ -852,7 +908,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
   // device pair list (its own buffer: the index buffer may still feed queued copies) and output
   const size_t ybytes = (size_t)n * g.L * (m == FPCC_CC1B_POPCOUNT ? 8 : 4);
   void* dpl = dbuf(s, &s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
-  void* dy = dbuf(s, &s->d_y, &s->n_y, ybytes);
+  void* dy = group_out(s, fl, out_base, ybytes);
   if (!dpl || !dy) return FPCC_ENOMEM;
   if (cudaError_t ue = upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st)) return cuda_err(ue, "upload");
   const int64_t lds = slab_of(s, p1).row_bytes / ((m == FPCC_CC1B_POPCOUNT) ? 4 : (g.fmt ? 4 : 8));
@@ -864,7 +920,8 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
                          g.lag0 + g.L - 1, g.v, E, ldE, (float*)dy, g.L, nullptr);
   }
   if (rc) return rc;
-  if (cudaError_t ce = d2h_results(fl, reqs, first, out_base, (const char*)dy, s->st)) return cuda_err(ce, "results");
+  if (cudaError_t ce = results_down(s, fl, reqs, first, out_base, (const char*)dy, s->st))
+    return cuda_err(ce, "results");
   return 0;
 }
 
@@ -888,21 +945,22 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
   };
   std::vector<Miss> miss;
   std::set<std::tuple<int, int, int64_t>> seen;
+  int lastN = -1;
+  bool smooth = false;
   for (const auto& set : sets)
   for (Req* q : *set.second) {
     const int Nz = set.first;
+    if (q->N != lastN) {
+      int a2, b3, c5;
+      lastN = q->N;
+      smooth = factor235(q->N, &a2, &b3, &c5);
+    }
     for (int side = 0; side < 2; side++) {
+      // the per-length path makes products of smooth lengths without gaps
+      const int f64 = (q->f64 >> side) & 1;
+      if (smooth && !f64) continue;
       const int64_t key = wkey(side ? q->r.sta2 : q->r.sta1, q->r.window);
       if (!seen.insert(std::make_tuple(q->N, Nz, key)).second) continue;
-      int zeros = 0;
-      {
-        std::lock_guard<std::mutex> lk(s->mu);
-        auto it = s->windows.find({(int)(key >> 32), (int)(uint32_t)key});
-        if (it != s->windows.end()) zeros = it->second.zeros;
-      }
-      int a2, b3, c5;
-      const int f64 = zeros >= FPCC_F64_ZERO_SAMPLES;
-      if (factor235(q->N, &a2, &b3, &c5) && !f64) continue;
       Slab& sl = slab_of(s, Product{kind, q->N, Nz, fmt});
       if (find_row(sl, key) >= 0) continue;
       const int r = claim_row(s, sl, key, 1);
@@ -999,17 +1057,25 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
 // vary per request; products are ensured per window length, then every
 // correlation of the group runs in one launch reading its rows in place.
 int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& fl, size_t out_base,
-                     bool products_only, Lane* on = nullptr, size_t first = 0) {
+                     bool products_only, Lane* on = nullptr, size_t first = 0, GroupRows* gr = nullptr) {
   const int n = (int)reqs.size();
   const int m = g.method;
   int kind1, kind2;
   method_kinds(m, &kind1, &kind2);
   const bool fft = (m == FPCC_PCC2 || m == FPCC_GNCC || m == FPCC_CC1B);
   const int Nz = fft ? g.Nz : 0;
-  std::map<int, std::vector<int>> byN;
-  for (int i = 0; i < n; i++) byN[reqs[i]->N].push_back(i);
   std::vector<int> r1(n), r2(n), e1(n), e2(n);
   int rc;
+  std::map<int, std::vector<int>> byN;
+  if (gr && gr->ok) {
+    r1.swap(gr->r1);
+    r2.swap(gr->r2);
+    e1.swap(gr->e1);
+    e2.swap(gr->e2);
+    gr->ok = false;
+  } else {
+    for (int i = 0; i < n; i++) byN[reqs[i]->N].push_back(i);
+  }
   for (auto& kv : byN) {
     const int N = kv.first;
     const std::vector<int>& ix = kv.second;
@@ -1036,7 +1102,16 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
       for (int j = 0; j < k; j++) { e1[ix[j]] = rr[j]; e2[ix[j]] = rr[k + j]; }
     }
   }
-  if (products_only) return 0;
+  if (products_only) {
+    if (gr) {
+      gr->r1.swap(r1);
+      gr->r2.swap(r2);
+      gr->e1.swap(e1);
+      gr->e2.swap(e2);
+      gr->ok = true;
+    }
+    return 0;
+  }
   // the pair stage runs on the server's stream, or on the lane `on` (its own
   // context, stream and output buffers), which first waits for the server's
   // stream and for the lane work that made the group's products
@@ -1066,7 +1141,7 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
   const size_t osz = (m == FPCC_CC1B_POPCOUNT) ? 8 : 4;
   size_t total = 0;
   for (int i = 0; i < n; i++) total += (size_t)reqs[i]->L * osz;
-  char* dy = (char*)(on ? lane_buf(s, *on, &on->d_tmp, &on->n_tmp, total) : dbuf(s, &s->d_y, &s->n_y, total));
+  char* dy = on ? (char*)lane_buf(s, *on, &on->d_tmp, &on->n_tmp, total) : group_out(s, fl, out_base, total);
   void* dd = on ? lane_buf(s, *on, &on->d_idx, &on->n_idx, (size_t)n * sizeof(fpcc_pair_desc))
                 : dbuf(s, &s->d_desc, &s->n_desc, (size_t)n * sizeof(fpcc_pair_desc));
   if (!dy || !dd) return FPCC_ENOMEM;
@@ -1109,7 +1184,10 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
   if (cudaError_t ue = upload(fl, dd, d.data(), d.size() * sizeof(fpcc_pair_desc), st)) return cuda_err(ue, "upload");
   rc = fpcc_pair_stage_packed(cx, m, g.fmt, Nz, (const fpcc_pair_desc*)dd, n, maxL, g.v, m == FPCC_CC1B_POPCOUNT);
   if (rc) return rc;
-  if (cudaError_t ce = d2h_results(fl, reqs, first, out_base, dy, st)) return cuda_err(ce, "results");
+  // a lane's output buffer is its own: its results go down on the lane
+  const cudaError_t ce = on ? d2h_results(fl, reqs, first, out_base, dy, st)
+                            : results_down(s, fl, reqs, first, out_base, dy, st);
+  if (ce) return cuda_err(ce, "results");
   return 0;
 }
 
@@ -1181,11 +1259,12 @@ int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlig
   for (int i = 0; i < n; i++) { pairs[2 * i] = rows[i]; pairs[2 * i + 1] = rows[n + i]; }
   const size_t ybytes = (size_t)n * g.L * 4;
   void* dpl = dbuf(s, &s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
-  void* dy = dbuf(s, &s->d_y, &s->n_y, ybytes);
+  void* dy = group_out(s, fl, out_base, ybytes);
   if (!dpl || !dy) return FPCC_ENOMEM;
   if (cudaError_t ue = upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st)) return cuda_err(ue, "upload");
   if ((rc = fpcc_wpcc_pair_stage(s->ctx, p, sl.base, g.fmt, (const int32_t*)dpl, n, (float*)dy, g.L))) return rc;
-  if (cudaError_t ce = d2h_results(fl, reqs, first, out_base, (const char*)dy, s->st)) return cuda_err(ce, "results");
+  if (cudaError_t ce = results_down(s, fl, reqs, first, out_base, (const char*)dy, s->st))
+    return cuda_err(ce, "results");
   return 0;
 }
 
@@ -1273,6 +1352,7 @@ void completer_main(Server* s) {
       fl = s->launched.front();
       s->launched.pop_front();
     }
+    const auto t_done = Clock::now();
     if (fl->done) {
       const cudaError_t e = cudaEventSynchronize(fl->done);
       if (e != cudaSuccess) {
@@ -1281,6 +1361,7 @@ void completer_main(Server* s) {
       }
     }
     deliver(s, *fl);
+    s->deliver_ns += std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t_done).count();
     {
       std::lock_guard<std::mutex> lk(s->mu_c);
       s->retired.push_back(fl);
@@ -1299,6 +1380,7 @@ void release_retired(Server* s) {
   }
   for (InFlight* fl : done) {
     for (auto& pr : fl->pinned_rows) pr.first->pin[pr.second]--;
+    if (fl->d_out) dfree(s, fl->d_out);   // the batch is complete: its downloads have ended
     if (fl->h_out) pinned_put(s, fl->h_out, fl->h_bytes);
     if (fl->h_up) pinned_put(s, fl->h_up, fl->up_bytes);
     for (auto& b : fl->up_full) pinned_put(s, b.first, b.second);
@@ -1357,6 +1439,7 @@ void worker_main(Server* s) {
     }
     // bound the number of batches in flight
     while (s->in_flight >= kMaxInFlight) wait_one_retired(s);
+    const auto t_form = Clock::now();
     InFlight* fl = new InFlight();
     fl->srv = s;
     {
@@ -1384,6 +1467,10 @@ void worker_main(Server* s) {
     size_t total = 0;
     for (auto& q : batch) total += (size_t)q.L * (q.r.method == FPCC_CC1B_POPCOUNT ? 8 : 4);
     fl->h_out = (char*)pinned_get(s, total, &fl->h_bytes);
+    // the batch's device results (freed when the batch retires); without it the
+    // groups share one scratch buffer and download on the server's stream
+    fl->d_out = s->st_out ? dalloc(s, std::max<size_t>(total, 256)) : nullptr;
+    s->out_used = 0;
     fl->h_up = (char*)pinned_get(s, (size_t)(16 * 4 + sizeof(fpcc_pair_desc)) * batch.size() +
                                      1024 * (groups.size() + 4 + 2 * s->lanes.size()),
                                  &fl->up_bytes);
@@ -1441,13 +1528,14 @@ void worker_main(Server* s) {
     // a packed direct-sum group starts its pair stage on the direct lane as
     // soon as its own products are queued, overlapping the later station stages
     std::vector<char> early(order.size(), 0);
+    std::vector<GroupRows> grows(order.size());
     for (size_t i = 0; i < order.size(); i++) {
       if (err) break;
       const GroupKey& g = order[i]->first;
       if (g.method == FPCC_WPCC) continue;
       s->lane_rec = &used;
-      err = (g.N < 0) ? run_group_packed(s, g, order[i]->second, *fl, 0, true)
-                      : run_group(s, g, order[i]->second, *fl, 0, true);
+      err = (g.N < 0) ? run_group_packed(s, g, order[i]->second, *fl, 0, true, nullptr, 0, &grows[i])
+                      : run_group(s, g, order[i]->second, *fl, 0, true, 0, &grows[i]);
       s->lane_rec = nullptr;
       lane_marks(s, used, waits[i]);
       if (g.N < 0 && g.method == FPCC_PCC2) waits[i].insert(waits[i].end(), marks1.begin(), marks1.end());
@@ -1457,7 +1545,7 @@ void worker_main(Server* s) {
       if (!err && direct && g.N < 0 && s->dlane.ctx) {
         s->pair_waits = &waits[i];
         s->pair_seq = s->lane_seq;
-        err = run_group_packed(s, g, order[i]->second, *fl, base[i], false, &s->dlane, first[i]);
+        err = run_group_packed(s, g, order[i]->second, *fl, base[i], false, &s->dlane, first[i], &grows[i]);
         s->pair_waits = nullptr;
         early[i] = 1;
         s->pair_stages++;
@@ -1472,8 +1560,8 @@ void worker_main(Server* s) {
       s->pair_waits = &waits[i];
       s->pair_seq = s->lane_seq;
       if (g.method == FPCC_WPCC) err = run_group_wpcc(s, g, kv.second, *fl, base_i, first[i]);
-      else if (g.N < 0) err = run_group_packed(s, g, kv.second, *fl, base_i, false, nullptr, first[i]);
-      else err = run_group(s, g, kv.second, *fl, base_i, false, first[i]);
+      else if (g.N < 0) err = run_group_packed(s, g, kv.second, *fl, base_i, false, nullptr, first[i], &grows[i]);
+      else err = run_group(s, g, kv.second, *fl, base_i, false, first[i], &grows[i]);
       s->pair_waits = nullptr;
       s->pair_stages++;
     }
@@ -1482,6 +1570,7 @@ void worker_main(Server* s) {
     if (err) {
       lanes_join(s);
       cudaStreamSynchronize(s->st);
+      if (s->st_out) cudaStreamSynchronize(s->st_out);
       fl->reqs.clear();
       for (auto& q : batch) fl->reqs.push_back(q);
       fl->direct.assign(fl->reqs.size(), 0);
@@ -1489,10 +1578,18 @@ void worker_main(Server* s) {
       fl->err_msg = fpcc_last_error();
     } else {
       cudaEventCreateWithFlags(&fl->done, cudaEventDisableTiming);
-      cudaEventRecord(fl->done, s->st);
+      if (fl->d_out) {
+        // done = the server's stream and the results stream both past this batch
+        cudaEventRecord(s->main_ev, s->st);
+        cudaStreamWaitEvent(s->st_out, s->main_ev, 0);
+        cudaEventRecord(fl->done, s->st_out);
+      } else {
+        cudaEventRecord(fl->done, s->st);
+      }
       s->batches++;
     }
     s->in_flight++;
+    s->worker_ns += std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t_form).count();
     {
       std::lock_guard<std::mutex> lk(s->mu_c);
       s->launched.push_back(fl);
@@ -1536,6 +1633,7 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
     if (s->dlane.ctx) fpcc_destroy(s->dlane.ctx);
     if (s->dlane.ev) cudaEventDestroy(s->dlane.ev);
     if (s->main_ev) cudaEventDestroy(s->main_ev);
+    if (s->st_out) cudaStreamDestroy(s->st_out);
     if (s->ctx) fpcc_destroy(s->ctx);
     cudaMemPoolDestroy(s->pool);
     delete s;
@@ -1549,6 +1647,10 @@ extern "C" int fpcc_server_create(fpcc_server** out, int device, size_t hbm_budg
   s->st = (cudaStream_t)fpcc_get_stream(s->ctx);
   if (cudaEventCreateWithFlags(&s->main_ev, cudaEventDisableTiming) != cudaSuccess) {
     s->main_ev = nullptr;
+    return undo();
+  }
+  if (cudaStreamCreateWithFlags(&s->st_out, cudaStreamNonBlocking) != cudaSuccess) {
+    s->st_out = nullptr;
     return undo();
   }
   // FPCC_SERVER_LANES sets the number of lanes (0: everything on the server's stream)
@@ -1678,12 +1780,17 @@ extern "C" int fpcc_server_destroy(fpcc_server* h) {
     cudaEventDestroy(s->dlane.ev);
   }
   cudaStreamSynchronize(s->st);
+  if (s->st_out) {
+    cudaStreamSynchronize(s->st_out);
+    cudaStreamDestroy(s->st_out);
+  }
   fpcc_destroy(s->ctx);
   cudaMemPoolDestroy(s->pool);
   for (size_t i = 0; i < s->pinned_pool.size(); i += 2) cudaFreeHost(s->pinned_pool[i]);
   for (char* a : s->arena) cudaFreeHost(a);
   if (s->main_ev) cudaEventDestroy(s->main_ev);
   for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
+  for (cudaEvent_t e : s->out_ev) cudaEventDestroy(e);
   delete s;
   return 0;
 }
@@ -1757,11 +1864,14 @@ namespace {
 // length, lags).  `mu` is taken for the window and wavelet-setup lookups only.
 // Window length of a request's two windows (FPCC_EARG if either is missing or
 // they differ); the caller holds `mu`.
-int request_window_len(Server* s, const fpcc_request* req) {
+// *f64 (when given) receives the windows' FP64 flags (Req::f64).
+int request_window_len(Server* s, const fpcc_request* req, int* f64 = nullptr) {
   auto a = s->windows.find({req->sta1, req->window});
   auto b = s->windows.find({req->sta2, req->window});
   if (a == s->windows.end() || b == s->windows.end()) return FPCC_EARG;
   if (b->second.N != a->second.N) return FPCC_EARG;
+  if (f64)
+    *f64 = (a->second.zeros >= FPCC_F64_ZERO_SAMPLES ? 1 : 0) | (b->second.zeros >= FPCC_F64_ZERO_SAMPLES ? 2 : 0);
   return a->second.N;
 }
 
@@ -1769,12 +1879,13 @@ int request_window_len(Server* s, const fpcc_request* req) {
 int prepare_request_n(Server* s, const fpcc_request* req, Req& q, int N);
 
 int prepare_request(Server* s, const fpcc_request* req, Req& q) {
-  int N = 0;
+  int N = 0, f64 = 0;
   {
     std::lock_guard<std::mutex> lk(s->mu);
-    N = request_window_len(s, req);
+    N = request_window_len(s, req, &f64);
   }
   if (N < 0) return N;
+  q.f64 = f64;
   return prepare_request_n(s, req, q, N);
 }
 
@@ -1831,13 +1942,17 @@ extern "C" int64_t fpcc_submit(fpcc_server* h, const fpcc_request* req) {
   Req q;
   if (int rc = prepare_request(s, req, q)) return rc;
   q.t_submit = Clock::now();
+  bool wake;
   {
     std::lock_guard<std::mutex> lk(s->mu);
     q.id = s->next_id++;
     s->status.push_back(0);
+    // the worker sleeps only on an empty queue (a batch it lingers over is
+    // re-checked on a short timeout), so only the first request wakes it
+    wake = s->pending.empty();
     s->pending.push_back(q);
   }
-  s->cv.notify_one();
+  if (wake) s->cv.notify_one();
   return q.id;
 }
 
@@ -1891,6 +2006,8 @@ extern "C" int fpcc_server_get_stats(fpcc_server* h, fpcc_server_stats* o) {
   o->p99_ms = pct(0.99);
   o->max_ms = v.empty() ? 0.0 : v.back();
   o->pair_stages = s->pair_stages;
+  o->worker_ms = (double)s->worker_ns.load() * 1e-6;
+  o->deliver_ms = (double)s->deliver_ns.load() * 1e-6;
   return 0;
 }
 
@@ -1902,6 +2019,8 @@ extern "C" int fpcc_server_reset_stats(fpcc_server* h) {
   s->batches = 0;
   s->station_rows = 0;
   s->pair_stages = 0;
+  s->worker_ns = 0;
+  s->deliver_ns = 0;
   return 0;
 }
 
@@ -1912,19 +2031,22 @@ extern "C" int fpcc_submit_many(fpcc_server* h, const fpcc_request* reqs, int n,
   // that the worker can start on the first chunk while the rest are prepared
   constexpr int kChunk = 1024;
   std::vector<Req> qs;
-  std::vector<int> lens;
+  std::vector<int> lens, f64s;
   qs.reserve(std::min(n, kChunk));
   for (int i0 = 0; i0 < n; i0 += kChunk) {
     const int i1 = std::min(n, i0 + kChunk);
     qs.clear();
     int rc = 0, bad = i1;
     lens.resize((size_t)(i1 - i0));
+    f64s.resize((size_t)(i1 - i0));
     {
       std::lock_guard<std::mutex> lk(s->mu);   // the chunk's window lookups under one lock
-      for (int i = i0; i < i1; i++) lens[(size_t)(i - i0)] = request_window_len(s, reqs + i);
+      for (int i = i0; i < i1; i++)
+        lens[(size_t)(i - i0)] = request_window_len(s, reqs + i, &f64s[(size_t)(i - i0)]);
     }
     for (int i = i0; i < i1; i++) {
       Req q;
+      q.f64 = f64s[(size_t)(i - i0)];
       const int N = lens[(size_t)(i - i0)];
       if ((rc = (N < 0) ? N : prepare_request_n(s, reqs + i, q, N))) {
         bad = i;
@@ -1933,8 +2055,10 @@ extern "C" int fpcc_submit_many(fpcc_server* h, const fpcc_request* reqs, int n,
       qs.push_back(q);
     }
     const auto now = Clock::now();
+    bool wake;
     {
       std::lock_guard<std::mutex> lk(s->mu);
+      wake = s->pending.empty();
       for (size_t k = 0; k < qs.size(); k++) {
         Req& q = qs[k];
         q.t_submit = now;
@@ -1944,7 +2068,7 @@ extern "C" int fpcc_submit_many(fpcc_server* h, const fpcc_request* reqs, int n,
         s->pending.push_back(std::move(q));
       }
     }
-    s->cv.notify_one();
+    if (wake) s->cv.notify_one();
     if (rc) {
       if (ids) ids[bad] = rc;
       return rc;

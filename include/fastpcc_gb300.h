@@ -312,6 +312,10 @@ typedef struct {
   int64_t completed, batches, station_rows, hbm_used;
   double p50_ms, p99_ms, max_ms;   /* submit -> result latency of completed requests */
   int64_t pair_stages;             /* pair-stage launches (one per group of a batch)  */
+  double worker_ms;                /* host time the worker spent forming and queueing
+                                      batches (taken off the pending queue -> launched) */
+  double deliver_ms;               /* host time of completion (wait for the batch, copy-out
+                                      into unregistered outputs, status), summed         */
 } fpcc_server_stats;
 int fpcc_server_create(fpcc_server **out, int device, size_t hbm_budget_bytes, int max_batch);
 /* Storage format (FPCC_F32 / FPCC_F16 / FPCC_I16) of the phase spectra and phase signals
