@@ -66,11 +66,13 @@ struct fpcc_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   bool own_pool = true;             // false: the pool belongs to a server sharing it
-  DevBuf dev[48];
+  DevBuf dev[56];
   DevBuf pin[8];
   cudaStream_t stream2 = nullptr;   // second stream of the pipelined drop-ins
   cudaEvent_t chunk_ev[16] = {};    // pair-stage chunks whose results stream2 downloads
   cudaEvent_t up_ev[4] = {};        // station-row chunks that stream2 has uploaded
+  cudaStream_t stream3 = nullptr;   // downloads of the first-use pipeline (uploads run on stream2)
+  std::vector<cudaEvent_t> pipe_ev; // events of the first-use pipeline
   // the context's device buffers and caches come from a pool of its own, allocated
   // and freed in the order of `stream` (no device synchronisation when a buffer
   // grows); ord_ev orders them against the second stream when it exists
@@ -256,6 +258,11 @@ extern "C" int fpcc_destroy(fpcc_ctx* c) {
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : c->up_ev)
     if (e) cudaEventDestroy(e);
+  if (c->stream3) {
+    cudaStreamSynchronize(c->stream3);
+    cudaStreamDestroy(c->stream3);
+  }
+  for (cudaEvent_t e : c->pipe_ev) cudaEventDestroy(e);
   {
     std::lock_guard<std::mutex> lk(g_default_mu);
     if (c == g_default) g_default = nullptr;
@@ -348,7 +355,7 @@ enum Slot { S_HOST_X = 0, S_STATION = 1, S_ENERGY = 2, S_PAIRS2 = 3, S_Y = 4, S_
             S_P64_CNT = 27, S_I16_Q = 28, S_MULTI_A = 29, S_MULTI_B = 30, S_MULTI_AN = 31, S_EPART = 32,
             S_CONV_X = 33, S_CONV_Y = 34, S_STK_SPEC = 35, S_STK_A = 36, S_STK_B = 37, S_STK_X = 38,
             S_STK_T = 39, S_STK_T2 = 40, S_STK_Y = 41, S_STK_Y2 = 42, S_STK_R = 43, S_STK_AN = 44,
-            S_HK_TAB = 45 };
+            S_HK_TAB = 45, S_PIPE_CNT = 46, S_GATHER_X = 47, S_GATHER_O = 48, S_GATHER_I = 49 };
 
 constexpr size_t kLargeChunkBytes = size_t(512) << 20;   // four-step intermediate per chunk
 
@@ -428,6 +435,28 @@ int large_pairs(fpcc_ctx* c, const PairArgs& q, int herm) {
     g_launches += 2;
   }
   return 0;
+}
+
+// Rows of 4-byte words: dst row didx[r] (r without didx) = src row sidx[r]
+// (r without sidx), `words` words each; strides in words.
+__global__ void k_rows_copy(const uint32_t* __restrict__ src, int64_t lds, const int* __restrict__ sidx,
+                            uint32_t* __restrict__ dst, int64_t ldd, const int* __restrict__ didx, int64_t words) {
+  const int r = blockIdx.y;
+  const int64_t sr = sidx ? sidx[r] : r, dr = didx ? didx[r] : r;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < words; i += (int64_t)gridDim.x * blockDim.x)
+    dst[dr * ldd + i] = src[sr * lds + i];
+}
+
+cudaError_t launch_rows_copy(const void* src, int64_t lds, const int* sidx, void* dst, int64_t ldd, const int* didx,
+                             int nrows, int64_t words, cudaStream_t st) {
+  const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(32, (words + 255) / 256));
+  for (int r0 = 0; r0 < nrows; r0 += 65535) {
+    const int n = std::min(65535, nrows - r0);
+    k_rows_copy<<<dim3(gx, n), 256, 0, st>>>((const uint32_t*)src + (sidx ? 0 : r0 * lds), lds, sidx ? sidx + r0 : nullptr,
+                                             (uint32_t*)dst + (didx ? 0 : r0 * ldd), ldd, didx ? didx + r0 : nullptr,
+                                             words);
+  }
+  return cudaGetLastError();
 }
 
 // Twiddle table exp(-2 pi i t / n), t < n, computed on the device in FP64
@@ -1015,6 +1044,11 @@ extern "C" int fpcc_station_stage(fpcc_ctx* c, int method, const float* d_x, int
   return fpcc_station_stage_ex(c, method, d_x, ldx, nrows, N, Nz, fmt, rule, d_out, ldo, nullptr, -1);
 }
 
+namespace {
+int station_general(fpcc_ctx* c, int method, const float* d_x, int64_t ldx, int nrows, int N, int Nz, int fmt,
+                    int rule, void* d_out, int64_t ldo, const std::vector<int>& p64);
+}  // namespace
+
 extern "C" int fpcc_station_stage_ex(fpcc_ctx* c, int method, const float* d_x, int64_t ldx, int nrows, int N,
                                      int Nz, int fmt, int rule, void* d_out, int64_t ldo, const int32_t* h_f64_rows,
                                      int n_f64_rows) {
@@ -1070,15 +1104,44 @@ extern "C" int fpcc_station_stage_ex(fpcc_ctx* c, int method, const float* d_x, 
     return large_station(c, method == FPCC_GNCC ? COL_REAL : COL_SIGN, d_x, sizeof(float), ldx, nrows, N, Nz, 0,
                          nullptr, rule == FPCC_SIGN_GE ? 1 : 0, FPCC_F32, 1, d_out, ldo);
   }
-  if (method == FPCC_PCC2 && p64.empty()) {
-    // one fused kernel per station window, specialised at run time for (N, Nz)
+  if (method == FPCC_PCC2) {
+    // one fused kernel per station window, specialised at run time for (N, Nz);
+    // windows with gaps (FP64 analytic signals) are then redone on their own
+    // through the general path, so that every window's spectrum depends on that
+    // window only, not on the others of the call
     const cudaError_t e = launch_station_fused(d_x, ldx, nrows, N, Nz, rule, fmt, d_out, ldo, c->stream);
     if (e == cudaSuccess) {
       g_launches++;
+      if (p64.empty()) return 0;
+      const int np = (int)p64.size();
+      const int64_t words = fpcc_station_row_bytes(method, N, Nz, fmt) / 4;
+      const int64_t ldo_w = ldo * (fmt == FPCC_F32 ? 2 : 1);
+      void *gx, *go, *gi;
+      if ((rc = dev_buf(c, S_GATHER_X, (size_t)np * N * sizeof(float), &gx)) ||
+          (rc = dev_buf(c, S_GATHER_O, (size_t)np * ldo_w * 4, &go)) ||
+          (rc = dev_buf(c, S_GATHER_I, (size_t)np * sizeof(int), &gi)))
+        return rc;
+      CK(cudaMemcpyAsync(gi, p64.data(), (size_t)np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+      CK(launch_rows_copy(d_x, ldx, (const int*)gi, gx, N, nullptr, np, N, c->stream));
+      std::vector<int> all((size_t)np);
+      for (int i = 0; i < np; i++) all[(size_t)i] = i;
+      if ((rc = station_general(c, method, (const float*)gx, N, np, N, Nz, fmt, rule, go, ldo, all))) return rc;
+      CK(launch_rows_copy(go, ldo_w, nullptr, d_out, ldo_w, (const int*)gi, np, words, c->stream));
+      g_launches += 2;
       return 0;
     }
     if (e != cudaErrorNotSupported) return cuda_fail(e, "fused station kernel");
   }
+  return station_general(c, method, d_x, ldx, nrows, N, Nz, fmt, rule, d_out, ldo, p64);
+}
+
+namespace {
+// The station stage of PCC2 (analytic signals, FP64 for the rows in p64, then
+// the phase spectra), GNCC and 1-bit (spectra of the real rows) by general
+// radix passes.
+int station_general(fpcc_ctx* c, int method, const float* d_x, int64_t ldx, int nrows, int N, int Nz, int fmt,
+                    int rule, void* d_out, int64_t ldo, const std::vector<int>& p64) {
+  int rc;
   SpecArgs a{};
   a.nrows = nrows; a.N = N; a.Nz = Nz; a.fmt = fmt; a.out = d_out; a.ldo = ldo;
   if (method == FPCC_PCC2) {
@@ -1095,6 +1158,7 @@ extern "C" int fpcc_station_stage_ex(fpcc_ctx* c, int method, const float* d_x, 
   g_launches++;
   return 0;
 }
+}  // namespace
 
 extern "C" int fpcc_energy_stage(fpcc_ctx* c, const float* d_x, int64_t ldx, int nrows, int N, double* d_E,
                                  int64_t ldE) {
@@ -1290,6 +1354,192 @@ int make_layout(int method, int N, int Lag1, int Lag2, int nz_mode, int fmt, Lay
 // chunk overlaps the correlation of the next; every kernel is queued before the
 // first download, so pageable host memory (whose copies return only when done)
 // does not hold back the launches.
+bool is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// All pairs with pinned host buffers, in the order the pair list first uses
+// the rows: the used rows are laid out on the device in first-use order (the
+// pair list is rewritten onto that order), so that the rows of the first pairs
+// go up first, each run of rows at one host stride as one strided copy; the
+// station stage runs on contiguous chunks of those rows as they arrive (a small
+// first chunk, then 768 rows), each chunk's gap counts come back on the upload
+// stream (the host never waits behind pair stages), the pairs whose rows are
+// all transformed run in pieces, and each piece's results go down on a third
+// stream while later pieces compute.  Results are the same as through
+// run_device: every row goes through the same station stage, with its FP64
+// rows chosen by the same rule.  Returns 1, with nothing queued, when the pair
+// list's first-use order breaks into too many runs (no row structure to use).
+int run_first_use(fpcc_ctx* c, const Layout& Ly, float* d_x, int nsta, const int32_t* h_pairs, int32_t* d_p,
+                  int npairs, float v, float* d_y, float* h_y, const float* h_x) {
+  const int method = Ly.method;
+  const int N = Ly.N;
+  std::vector<int> pos((size_t)nsta, -1), order;
+  order.reserve((size_t)nsta);
+  std::vector<int> need((size_t)npairs);   // rows first used by pairs 0..i
+  std::vector<int32_t> hp(2 * (size_t)npairs);
+  for (int i = 0; i < npairs; i++) {
+    for (int h = 0; h < 2; h++) {
+      const int r = h_pairs[2 * (size_t)i + h];
+      if (pos[(size_t)r] < 0) {
+        pos[(size_t)r] = (int)order.size();
+        order.push_back(r);
+      }
+      hp[2 * (size_t)i + h] = pos[(size_t)r];
+    }
+    need[(size_t)i] = (int)order.size();
+  }
+  const int nuse = (int)order.size();
+  // runs of rows at one host stride (device rows contiguous)
+  struct Run { int d0, r0, stride, len; };
+  std::vector<Run> runs;
+  for (int a = 0; a < nuse;) {
+    int b = a + 1;
+    int stride = b < nuse ? order[(size_t)b] - order[(size_t)a] : 1;
+    if (stride < 1 || (int64_t)stride * N * (int64_t)sizeof(float) > (1 << 30)) stride = 0;
+    if (stride) while (b < nuse && order[(size_t)b] - order[(size_t)b - 1] == stride) b++;
+    else b = a + 1;
+    runs.push_back({a, order[(size_t)a], stride ? stride : 1, b - a});
+    a = b;
+  }
+  if (runs.size() > (size_t)std::max(64, nuse / 8)) return 1;
+  // station chunks: rows [R[k], R[k+1]); the first one small so that results start early
+  std::vector<int> R{0};
+  for (int r = std::min(nuse, 256); ; r = std::min(nuse, r + 768)) {
+    R.push_back(r);
+    if (r == nuse) break;
+  }
+  const int nch = (int)R.size() - 1;
+  int rc;
+  void* d_st = nullptr;
+  const size_t rowb = (size_t)Ly.lds * Ly.esz;
+  if ((rc = dev_buf(c, S_STATION, (size_t)nuse * rowb, &d_st))) return rc;
+  double* d_E = nullptr;
+  if (method == FPCC_GNCC) {
+    void* p = nullptr;
+    if ((rc = dev_buf(c, S_ENERGY, (size_t)nuse * Ly.ldE() * sizeof(double), &p))) return rc;
+    d_E = (double*)p;
+  }
+  const bool phase = (method == FPCC_PCC2 || method == FPCC_PCC1 || method == FPCC_PCCV);
+  const bool counts = phase && c->precision == FPCC_ANALYTIC_AUTO;
+  int* d_cnt = nullptr;
+  int* h_cnt = nullptr;
+  if (counts) {
+    void *dp, *hp2;
+    if ((rc = dev_buf(c, S_PIPE_CNT, (size_t)nuse * sizeof(int), &dp)) ||
+        (rc = pin_buf(c, 6, (size_t)nuse * sizeof(int), &hp2)))
+      return rc;
+    d_cnt = (int*)dp;
+    h_cnt = (int*)hp2;
+  }
+  if (!c->stream2 && cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(FPCC_ECUDA, "stream creation failed");
+  if (!c->stream3 && cudaStreamCreateWithFlags(&c->stream3, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(FPCC_ECUDA, "stream creation failed");
+  // pieces of pairs: pair i is ready once rows [0, need[i]) are transformed
+  const int cp = std::max(1024, std::min(8192, npairs / 32));
+  std::vector<std::pair<int, int>> pieces;   // (first pair, chunk after which it is ready)
+  for (int i = 0, k = 0; i < npairs;) {
+    while (need[(size_t)i] > R[(size_t)k + 1]) k++;
+    int j = i + 1;
+    while (j < npairs && j - i < (pieces.empty() ? cp / 4 : cp) && need[(size_t)j] <= R[(size_t)k + 1]) j++;
+    pieces.push_back({i, k});
+    i = j;
+  }
+  pieces.push_back({npairs, nch});
+  const size_t nev = 2 * (size_t)nch + pieces.size() + 1;
+  while (c->pipe_ev.size() < nev) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return fail(FPCC_ECUDA, "event creation failed");
+    c->pipe_ev.push_back(e);
+  }
+  cudaEvent_t* ev_up = c->pipe_ev.data();          // chunk k uploaded
+  cudaEvent_t* ev_cnt = ev_up + nch;               // chunk k's gap counts on the host
+  cudaEvent_t* ev_pair = ev_cnt + nch;             // piece p computed
+  cudaEvent_t ev_upall = ev_pair[pieces.size()];   // every row uploaded
+  // the pair list, rewritten onto the device order, goes first on the main stream
+  void* hps = nullptr;
+  if ((rc = pin_buf(c, 7, hp.size() * sizeof(int32_t), &hps))) return rc;
+  memcpy(hps, hp.data(), hp.size() * sizeof(int32_t));
+  CK(cudaMemcpyAsync(d_p, hps, hp.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  // the copies follow everything queued on the main stream (buffer allocations included)
+  CK(cudaEventRecord(c->ord_ev, c->stream));
+  CK(cudaStreamWaitEvent(c->stream2, c->ord_ev, 0));
+  CK(cudaStreamWaitEvent(c->stream3, c->ord_ev, 0));
+  const size_t xrow = (size_t)N * sizeof(float);
+  // uploads of every chunk, in order, each followed by its gap counts
+  size_t ri = 0;
+  for (int k = 0; k < nch; k++) {
+    for (; ri < runs.size() && runs[ri].d0 < R[(size_t)k + 1]; ri++) {
+      // a run may cross a chunk boundary: copy the part in this chunk, keep the rest
+      Run& u = runs[ri];
+      const int len = std::min(u.len, R[(size_t)k + 1] - u.d0);
+      CK(cudaMemcpy2DAsync(d_x + (size_t)u.d0 * N, xrow, h_x + (size_t)u.r0 * N, xrow * u.stride, xrow, (size_t)len,
+                           cudaMemcpyHostToDevice, c->stream2));
+      if (len < u.len) {
+        u.d0 += len;
+        u.r0 += len * u.stride;
+        u.len -= len;
+        break;
+      }
+    }
+    CK(cudaEventRecord(ev_up[k], c->stream2));
+    if (counts) {
+      // the gap counts on the third stream (idle until the downloads), so that
+      // the uploads run back to back
+      const int r0 = R[(size_t)k], n = R[(size_t)k + 1] - r0;
+      CK(cudaStreamWaitEvent(c->stream3, ev_up[k], 0));
+      CK(launch_zero_count(d_x + (size_t)r0 * N, N, N, n, d_cnt + r0, c->stream3));
+      g_launches++;
+      CK(cudaMemcpyAsync(h_cnt + r0, d_cnt + r0, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, c->stream3));
+      CK(cudaEventRecord(ev_cnt[k], c->stream3));
+    }
+  }
+  // host-to-device and device-to-host copies share the host link, and a
+  // download running beside the uploads leaves them a small part of it (the
+  // last rows then arrive late and hold up the last pairs): the downloads start
+  // once every row is up
+  CK(cudaEventRecord(ev_upall, c->stream2));
+  CK(cudaStreamWaitEvent(c->stream3, ev_upall, 0));
+  size_t pi = 0;
+  std::vector<int32_t> f64;
+  for (int k = 0; k < nch; k++) {
+    const int r0 = R[(size_t)k], n = R[(size_t)k + 1] - r0;
+    CK(cudaStreamWaitEvent(c->stream, ev_up[k], 0));
+    f64.clear();
+    if (counts) {
+      CK(cudaEventSynchronize(ev_cnt[k]));
+      for (int i = 0; i < n; i++)
+        if (h_cnt[r0 + i] >= kZeroSamples) f64.push_back(i);
+    } else if (phase && c->precision == FPCC_ANALYTIC_F64) {
+      for (int i = 0; i < n; i++) f64.push_back(i);
+    }
+    if ((rc = fpcc_station_stage_ex(c, method, d_x + (size_t)r0 * N, N, n, N, Ly.Nz, Ly.fmt, FPCC_AMP_F_REG,
+                                    (char*)d_st + (size_t)r0 * rowb, Ly.lds, f64.data(), (int)f64.size())))
+      return rc;
+    if (d_E && (rc = fpcc_energy_stage(c, d_x + (size_t)r0 * N, N, n, N, d_E + (size_t)r0 * Ly.ldE(), Ly.ldE())))
+      return rc;
+    // the pieces ready after this chunk: compute, then download on the third stream
+    for (; pi + 1 < pieces.size() && pieces[pi].second == k; pi++) {
+      const int i0 = pieces[pi].first, np = pieces[pi + 1].first - i0;
+      if ((rc = fpcc_pair_stage(c, method, d_st, Ly.lds, Ly.fmt, d_p + 2 * (size_t)i0, np, N, Ly.Nz, Ly.lag0,
+                                Ly.lag0 + Ly.L - 1, v, d_E, Ly.ldE(), d_y + (size_t)i0 * Ly.L, Ly.L, nullptr)))
+        return rc;
+      CK(cudaEventRecord(ev_pair[pi], c->stream));
+      CK(cudaStreamWaitEvent(c->stream3, ev_pair[pi], 0));
+      CK(cudaMemcpyAsync(h_y + (size_t)i0 * Ly.L, d_y + (size_t)i0 * Ly.L, (size_t)np * Ly.L * sizeof(float),
+                         cudaMemcpyDeviceToHost, c->stream3));
+    }
+  }
+  CK(cudaStreamSynchronize(c->stream3));
+  return 0;
+}
+
 int run_device(fpcc_ctx* c, const Layout& Ly, const float* d_x, int nsta, const int32_t* d_pairs, int npairs,
                float v, float* d_y, int64_t* d_num, int split, float* h_y = nullptr, const float* h_x = nullptr) {
   void* d_st = nullptr;
@@ -1463,13 +1713,20 @@ extern "C" int fpcc_allpairs_host(fpcc_ctx* c, int method, const float* h_x, int
     for (int i = 0; i < npairs; i++) hp[2 * i + 1] += nsta;
     CK(cudaMemcpyAsync(d_p, hp.data(), pbytes, cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-  } else {
-    CK(cudaMemcpyAsync(d_p, h_pairs, pbytes, cudaMemcpyHostToDevice, c->stream));
   }
-  // one-rule methods: the windows go up in chunks that the station stage consumes as they arrive
-  if ((rc = run_device(c, Ly, (const float*)d_x, nsta, (const int32_t*)d_p, npairs, v, (float*)d_y, nullptr, -1,
-                       h_y, Ly.two_rules ? nullptr : h_x)))
-    return rc;
+  // one-rule methods with pinned buffers: rows in first-use order when the pair
+  // list has that structure (it uploads its own rewritten pair list); otherwise
+  // the windows go up in chunks that the station stage consumes as they arrive
+  rc = 1;
+  if (!Ly.two_rules && npairs >= 2048 && is_pinned(h_x) && is_pinned(h_y))
+    rc = run_first_use(c, Ly, (float*)d_x, nsta, h_pairs, (int32_t*)d_p, npairs, v, (float*)d_y, h_y, h_x);
+  if (rc < 0 || (rc > 1)) return rc;
+  if (rc == 1) {
+    if (!Ly.two_rules) CK(cudaMemcpyAsync(d_p, h_pairs, pbytes, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = run_device(c, Ly, (const float*)d_x, nsta, (const int32_t*)d_p, npairs, v, (float*)d_y, nullptr, -1,
+                         h_y, Ly.two_rules ? nullptr : h_x)))
+      return rc;
+  }
   CK(cudaStreamSynchronize(c->stream));
   return 0;
 }

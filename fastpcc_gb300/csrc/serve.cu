@@ -55,6 +55,12 @@ void set_last_error(const char* msg);
 
 namespace {
 // A failed CUDA call of the server itself: status FPCC_ECUDA with a message.
+// FPCC_ENOMEM with a message naming what could not be had.
+int no_mem(const char* what) {
+  set_last_error(what);
+  return FPCC_ENOMEM;
+}
+
 int cuda_err(cudaError_t e, const char* what) {
   char buf[256];
   snprintf(buf, sizeof buf, "server: %s: %s", what, cudaGetErrorString(e));
@@ -594,7 +600,7 @@ int ensure_raw(Server* s, int N, const std::vector<int64_t>& keys, std::vector<i
     int r = find_row(sl, keys[i]);
     if (r < 0) {
       r = claim_row(s, sl, keys[i], 1);
-      if (r < 0) return FPCC_ENOMEM;
+      if (r < 0) return no_mem("server: no free row for a raw window (every row held by this batch, budget reached)");
       miss.push_back((int)i);
     }
     rows[i] = r;
@@ -653,7 +659,7 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
     int r = find_row(sl, keys[i]);
     if (r < 0) {
       r = claim_row(s, sl, keys[i], (int)(keys.size() - i));
-      if (r < 0) return FPCC_ENOMEM;
+      if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
       miss_keys.push_back(keys[i]);
       miss_rows.push_back(r);
     }
@@ -682,7 +688,7 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   void* dp = in_place_p ? (char*)sl.base + (int64_t)miss_rows[0] * sl.row_bytes
                         : dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)n * sl.row_bytes);
   void* di = dbuf(s, &s->d_idx, &s->n_idx, (size_t)2 * n * sizeof(int) + 64);
-  if (!dx || !dp || !di) return FPCC_ENOMEM;
+  if (!dx || !dp || !di) return no_mem("server: device scratch of a station stage");
   if (!in_place_x || !in_place_p) {
     std::vector<int> idx(2 * n);
     for (int i = 0; i < n; i++) { idx[i] = raw_rows[i]; idx[n + i] = miss_rows[i]; }
@@ -867,7 +873,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
     const int64_t rb = s1.row_bytes;
     void* merged = dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)2 * n * rb);
     void* di = dbuf(s, &s->d_idx, &s->n_idx, (size_t)2 * n * sizeof(int) + 64);
-    if (!merged || !di) return FPCC_ENOMEM;
+    if (!merged || !di) return no_mem("server: device scratch of a pair stage");
     std::vector<int> idx(2 * n);
     for (int i = 0; i < n; i++) { idx[i] = r1[i]; idx[n + i] = r2[i]; }
     if (cudaError_t ue = upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st)) return cuda_err(ue, "upload");
@@ -891,7 +897,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
     const int64_t rb = s1.row_bytes, eb = se.row_bytes;
     void* tmp = dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)2 * n * (rb + eb));
     void* di = dbuf(s, &s->d_idx, &s->n_idx, (size_t)4 * n * sizeof(int) + 64);
-    if (!tmp || !di) return FPCC_ENOMEM;
+    if (!tmp || !di) return no_mem("server: device scratch of a GNCC pair stage");
     std::vector<int> idx(4 * n);
     for (int i = 0; i < n; i++) { idx[i] = r1[i]; idx[n + i] = r2[i]; idx[2 * n + i] = e1[i]; idx[3 * n + i] = e2[i]; }
     if (cudaError_t ue = upload(fl, di, idx.data(), idx.size() * sizeof(int), s->st)) return cuda_err(ue, "upload");
@@ -909,7 +915,7 @@ int run_group(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlight& f
   const size_t ybytes = (size_t)n * g.L * (m == FPCC_CC1B_POPCOUNT ? 8 : 4);
   void* dpl = dbuf(s, &s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
   void* dy = group_out(s, fl, out_base, ybytes);
-  if (!dpl || !dy) return FPCC_ENOMEM;
+  if (!dpl || !dy) return no_mem("server: device pair list or output of a pair stage");
   if (cudaError_t ue = upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st)) return cuda_err(ue, "upload");
   const int64_t lds = slab_of(s, p1).row_bytes / ((m == FPCC_CC1B_POPCOUNT) ? 4 : (g.fmt ? 4 : 8));
   if (m == FPCC_CC1B_POPCOUNT) {
@@ -964,7 +970,7 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
       Slab& sl = slab_of(s, Product{kind, q->N, Nz, fmt});
       if (find_row(sl, key) >= 0) continue;
       const int r = claim_row(s, sl, key, 1);
-      if (r < 0) return FPCC_ENOMEM;
+      if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
       sl.pin[r]++;
       fl.pinned_rows.push_back({&sl, r});
       miss.push_back({q->N, Nz, key, &sl, r, f64});
@@ -1031,7 +1037,7 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
                      : dbuf(s, &s->d_tmp_p, &s->n_tmp_p, (size_t)m * ldo * esz);
     void* dc = lane ? lane_buf(s, *ln, &ln->d_idx, &ln->n_idx, (size_t)m * sizeof(RowCopy) + 64)
                     : dbuf(s, &s->d_idx, &s->n_idx, (size_t)m * sizeof(RowCopy) + 64);
-    if (!tmp || !dc) return FPCC_ENOMEM;
+    if (!tmp || !dc) return no_mem("server: device scratch of a packed station stage");
     if ((rc = fpcc_station_stage_multi(cx, method, sub.data(), m, fmt, FPCC_AMP_F_REG, tmp, ldo))) return rc;
     std::vector<RowCopy> cp(m);
     for (int i = 0; i < m; i++) {
@@ -1144,7 +1150,7 @@ int run_group_packed(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFl
   char* dy = on ? (char*)lane_buf(s, *on, &on->d_tmp, &on->n_tmp, total) : group_out(s, fl, out_base, total);
   void* dd = on ? lane_buf(s, *on, &on->d_idx, &on->n_idx, (size_t)n * sizeof(fpcc_pair_desc))
                 : dbuf(s, &s->d_desc, &s->n_desc, (size_t)n * sizeof(fpcc_pair_desc));
-  if (!dy || !dd) return FPCC_ENOMEM;
+  if (!dy || !dd) return no_mem("server: device output or descriptors of a packed pair stage");
   std::vector<fpcc_pair_desc> d(n);
   size_t off = 0;
   int maxL = 0;
@@ -1235,7 +1241,7 @@ int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlig
     int r = find_row(sl, keys[i]);
     if (r < 0) {
       r = claim_row(s, sl, keys[i], 2 * n - i);
-      if (r < 0) return FPCC_ENOMEM;
+      if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
       miss_keys.push_back(keys[i]);
       miss_rows.push_back(r);
     }
@@ -1260,7 +1266,7 @@ int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlig
   const size_t ybytes = (size_t)n * g.L * 4;
   void* dpl = dbuf(s, &s->d_pl, &s->n_pl, (size_t)2 * n * sizeof(int32_t));
   void* dy = group_out(s, fl, out_base, ybytes);
-  if (!dpl || !dy) return FPCC_ENOMEM;
+  if (!dpl || !dy) return no_mem("server: device pair list or output of a pair stage");
   if (cudaError_t ue = upload(fl, dpl, pairs.data(), pairs.size() * sizeof(int32_t), s->st)) return cuda_err(ue, "upload");
   if ((rc = fpcc_wpcc_pair_stage(s->ctx, p, sl.base, g.fmt, (const int32_t*)dpl, n, (float*)dy, g.L))) return rc;
   if (cudaError_t ce = results_down(s, fl, reqs, first, out_base, (const char*)dy, s->st))
@@ -1474,7 +1480,7 @@ void worker_main(Server* s) {
     fl->h_up = (char*)pinned_get(s, (size_t)(16 * 4 + sizeof(fpcc_pair_desc)) * batch.size() +
                                      1024 * (groups.size() + 4 + 2 * s->lanes.size()),
                                  &fl->up_bytes);
-    int err = (fl->h_out && fl->h_up) ? 0 : FPCC_ENOMEM;
+    int err = (fl->h_out && fl->h_up) ? 0 : no_mem("server: pinned result or upload buffer of a batch");
     fl->reqs.reserve(batch.size());
     // Station products first, all on the lanes: the phase products of the
     // packed groups in packed stages (one kind at a time, the direct sums'

@@ -347,6 +347,48 @@ def test_example_records_against_reference_cli(F, orc):
     assert np.array_equal(F.cc1b_numerators(x1, x2, l1, l2), orc.cc1b_num(x1, x2, l1, l2))
 
 
+def test_allpairs_host_first_use_pipeline(F, orc):
+    # pinned host buffers: the rows go up in the order the pair list first uses
+    # them (one strided copy per window here), the station stage runs on chunks
+    # of them as they arrive, with each chunk's FP64 rows chosen from gap counts
+    # read back on the upload stream, and pieces of pairs start as soon as their
+    # rows are ready.  Every method's results equal the pageable-buffer path's bit
+    # for bit (same station and pair kernels, same FP64 rows), on windows with
+    # gaps as well, and agree with the oracle; a shuffled pair list (no row
+    # structure) falls back to the chunked path with the same results
+    import torch
+    n_sta, n_win, N, lag = 32, 25, 2000, 100
+    x, _ = synth.all_pairs(n_stations=n_sta, n_windows=n_win, N=N, max_delay=60, tag="gpu/allpairs-first-use")
+    x = np.ascontiguousarray(x.reshape(n_sta * n_win, N))
+    x[3 * n_win + 2, 500:900] = 0.0       # gaps: FP64 analytic signals for these rows
+    x[17 * n_win + 11, 0:40] = 0.0
+    iu, ju = np.triu_indices(n_sta, k=1)
+    w = np.repeat(np.arange(n_win), iu.size)
+    pairs = np.ascontiguousarray(np.stack([np.tile(iu, n_win) * n_win + w, np.tile(ju, n_win) * n_win + w],
+                                          axis=1).astype(np.int32))
+    P, L = pairs.shape[0], 2 * lag + 1
+    xp = torch.from_numpy(x).pin_memory()
+    yp = torch.zeros((P, L), dtype=torch.float32).pin_memory()
+    sel = np.concatenate([np.flatnonzero((pairs[:, 0] == 3 * n_win + 2) | (pairs[:, 1] == 3 * n_win + 2))[:3],
+                          np.random.default_rng(8).choice(P, 3, replace=False)])
+    ctx = F.Context(0)
+    refs = {F.PCC2: orc.pcc2, F.GNCC: orc.gncc, F.PCC1: orc.pcc1}
+    for method, ref in refs.items():
+        y = np.zeros((P, L), np.float32)
+        ctx.allpairs_host(method, x, pairs, -lag, lag, y)          # pageable: chunked path
+        yp.zero_()
+        ctx.allpairs_host(method, xp.numpy(), pairs, -lag, lag, yp.numpy())   # pinned: first-use order
+        assert np.array_equal(yp.numpy(), y), method
+        assert relerr(y[sel], ref(x[pairs[sel, 0]], x[pairs[sel, 1]], -lag, lag)) < TOL, method
+    perm = np.random.default_rng(12).permutation(P)
+    yp.zero_()
+    ctx.allpairs_host(F.PCC2, xp.numpy(), np.ascontiguousarray(pairs[perm]), -lag, lag, yp.numpy())
+    y = np.zeros((P, L), np.float32)
+    ctx.allpairs_host(F.PCC2, x, pairs, -lag, lag, y)
+    assert np.array_equal(yp.numpy(), y[perm])
+    ctx.close()
+
+
 def test_allpairs_host_chunked_transfers(F, orc):
     # all station pairs of every window with host buffers (fpcc_allpairs_host):
     # 32 stations x 25 windows -> 12,400 correlations, so the windows go up in
