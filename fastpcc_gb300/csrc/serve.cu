@@ -658,7 +658,10 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   for (size_t i = 0; i < keys.size(); i++) {
     int r = find_row(sl, keys[i]);
     if (r < 0) {
-      r = claim_row(s, sl, keys[i], (int)(keys.size() - i));
+      // room for one row at a time (the slab doubles as it grows): the keys
+      // repeat (both stations of many pairs), so their count would ask for more
+      // rows than the distinct windows need and fail under a tight budget
+      r = claim_row(s, sl, keys[i], 1);
       if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
       miss_keys.push_back(keys[i]);
       miss_rows.push_back(r);
@@ -968,7 +971,14 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
       const int64_t key = wkey(side ? q->r.sta2 : q->r.sta1, q->r.window);
       if (!seen.insert(std::make_tuple(q->N, Nz, key)).second) continue;
       Slab& sl = slab_of(s, Product{kind, q->N, Nz, fmt});
-      if (find_row(sl, key) >= 0) continue;
+      if (const int r = find_row(sl, key); r >= 0) {
+        // resident: pinned for the batch, so that the claims below (which may
+        // release idle product classes to stay in budget) cannot take it away
+        // before the batch's pair stages read it
+        sl.pin[r]++;
+        fl.pinned_rows.push_back({&sl, r});
+        continue;
+      }
       const int r = claim_row(s, sl, key, 1);
       if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
       sl.pin[r]++;
@@ -1240,7 +1250,7 @@ int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlig
   for (int i = 0; i < 2 * n; i++) {
     int r = find_row(sl, keys[i]);
     if (r < 0) {
-      r = claim_row(s, sl, keys[i], 2 * n - i);
+      r = claim_row(s, sl, keys[i], 1);   // one row at a time: the keys repeat
       if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
       miss_keys.push_back(keys[i]);
       miss_rows.push_back(r);
