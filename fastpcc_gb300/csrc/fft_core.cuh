@@ -179,10 +179,107 @@ __device__ __forceinline__ void dft16(float2* v) {
   for (int k1 = 0; k1 < 4; k1++) dft4<DIR>(v + 4 * k1);
 }
 
-// Position of output X[r] after dft<R> (radix 8/16 leave a transposed order).
+// Composite radices R = A x B done as two stages of small DFTs in registers
+// (dft_comp below): A for each.
+__host__ __device__ constexpr int comp_a(int R) {
+  return R == 6 ? 2 : R == 9 ? 3 : R == 10 ? 2 : R == 12 ? 4 : R == 15 ? 3 : R == 20 ? 4 : R == 24 ? 8 : 0;
+}
+
+// Position of output X[r] after dft<R> (radix 8/16 and the composite radices
+// leave a transposed order).
 template <int R>
 __host__ __device__ constexpr int dft_perm(int r) {
-  return R == 16 ? 4 * (r & 3) + (r >> 2) : (R == 8 ? 2 * (r & 3) + (r >> 2) : r);
+  if constexpr (comp_a(R) > 0) {
+    return r / (R / comp_a(R)) + comp_a(R) * (r % (R / comp_a(R)));
+  } else {
+    return R == 16 ? 4 * (r & 3) + (r >> 2) : (R == 8 ? 2 * (r & 3) + (r >> 2) : r);
+  }
+}
+
+// ---- compile-time twiddles
+constexpr double kPiD = 3.14159265358979323846264338327950288;
+// Taylor series of sin and cos, for arguments reduced to [-pi, pi]
+constexpr double cx_sin(double x) {
+  double x2 = x * x, term = x, sum = x;
+  for (int n = 1; n < 20; n++) {
+    term *= -x2 / ((2.0 * n) * (2.0 * n + 1.0));
+    sum += term;
+  }
+  return sum;
+}
+constexpr double cx_cos(double x) {
+  double x2 = x * x, term = 1.0, sum = 1.0;
+  for (int n = 1; n < 20; n++) {
+    term *= -x2 / ((2.0 * n - 1.0) * (2.0 * n));
+    sum += term;
+  }
+  return sum;
+}
+// v * exp(DIR 2 pi i T / N): exact quarter turns as swaps, otherwise a
+// constant computed at compile time (angle reduced to [-pi, pi]).
+template <int T, int N, int DIR>
+__device__ __forceinline__ float2 cmul_ct(float2 v) {
+  constexpr int t = ((T % N) + N) % N;
+  constexpr int q4 = ((4 * t) % N == 0) ? (4 * t) / N : -1;
+  if constexpr (q4 == 0) {
+    return v;
+  } else if constexpr (q4 == 1) {
+    return cmul_i<DIR>(v);
+  } else if constexpr (q4 == 2) {
+    return make_float2(-v.x, -v.y);
+  } else if constexpr (q4 == 3) {
+    return cmul_i<-DIR>(v);
+  } else {
+    constexpr double ang = 2.0 * kPiD * (double)(2 * t > N ? t - N : t) / (double)N;
+    constexpr float c = (float)cx_cos(ang);
+    constexpr float s = (float)((double)DIR * cx_sin(ang));
+    return cmul(v, make_float2(c, s));
+  }
+}
+
+template <int V>
+struct IntC {
+  static constexpr int value = V;
+};
+// fn(IntC<B>{}), ..., fn(IntC<E - 1>{}): a loop whose index is a constant
+template <int B, int E, typename Fn>
+__device__ __forceinline__ void sfor(Fn&& fn) {
+  if constexpr (B < E) {
+    fn(IntC<B>{});
+    sfor<B + 1, E>(static_cast<Fn&&>(fn));
+  }
+}
+
+template <int R, int DIR>
+__device__ __forceinline__ void dft(float2* v);
+
+// In-place DFT of R = A x B points: with n = r1 + A r2 and k = s2 + B s1,
+//   X[k] = sum_r1 w_A^(r1 s1) w_R^(r1 s2) sum_r2 v[r1 + A r2] w_B^(r2 s2);
+// the B-point DFTs (one per r1) and their twiddles first, then the A-point
+// DFTs (one per s2); X[k] is left at v[s1 + A s2] (dft_perm<R>).
+template <int A, int B, int DIR>
+__device__ __forceinline__ void dft_comp(float2* v) {
+  constexpr int R = A * B;
+  sfor<0, A>([&](auto i1) {
+    constexpr int r1 = decltype(i1)::value;
+    float2 t[B];
+#pragma unroll
+    for (int r2 = 0; r2 < B; r2++) t[r2] = v[r1 + A * r2];
+    dft<B, DIR>(t);
+    sfor<0, B>([&](auto i2) {
+      constexpr int s2 = decltype(i2)::value;
+      v[r1 + A * s2] = cmul_ct<r1 * s2, R, DIR>(t[dft_perm<B>(s2)]);
+    });
+  });
+#pragma unroll
+  for (int s2 = 0; s2 < B; s2++) {
+    float2 t[A];
+#pragma unroll
+    for (int r1 = 0; r1 < A; r1++) t[r1] = v[r1 + A * s2];
+    dft<A, DIR>(t);
+#pragma unroll
+    for (int s1 = 0; s1 < A; s1++) v[s1 + A * s2] = t[dft_perm<A>(s1)];
+  }
 }
 
 template <int R, int DIR>
@@ -193,6 +290,7 @@ __device__ __forceinline__ void dft(float2* v) {
   else if constexpr (R == 5) dft5<DIR>(v);
   else if constexpr (R == 8) dft8<DIR>(v);
   else if constexpr (R == 16) dft16<DIR>(v);
+  else if constexpr (comp_a(R) > 0) dft_comp<comp_a(R), R / comp_a(R), DIR>(v);
 }
 
 // ---------------------------------------------------------------- twiddles

@@ -3,14 +3,15 @@
 // The window length of a workload is data (18000 here, 36000 there, any length
 // in a serving stream), so the fused kernel's radix schedule for N cannot be
 // fixed when the library is built.  On first use of an (N, Nz) the host picks a
-// schedule for each length (largest radices whose register staging stays within
-// 24 complex values per thread), instantiates k_station_fused with it through
+// schedule for each length (fewest passes over the in-register radices whose
+// staging stays within 24 complex values per thread), instantiates k_station_fused with it through
 // NVRTC for sm_103a, and caches the cubin in memory and under the disk cache
 // directory (FPCC_JIT_CACHE, default ~/.cache/fastpcc_gb300).  FPCC_JIT=0
 // disables the path.  For even N the real window's DFT_N runs as an N/2-point
 // complex transform (k_station_fused_real).
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -55,28 +56,53 @@ int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
 bool stage_ok(int n, int R, int T) { return ceil_div(n / R, T) * R <= kStageCap; }
 
-// Radix schedule for n with T threads, or empty when none fits.
+// Radix schedule for n with T threads, or empty when none fits: the fewest
+// passes (each pass is a round trip through shared memory between two block
+// barriers) over the radices of the in-register DFTs (2, 3, 4, 5, 8, 16 and the
+// composites 6, 9, 10, 12, 15, 20, 24), each within the staging cap; among
+// equally short schedules, the one with the fewest radices that are not powers
+// of two (their butterflies cost more per point) and no radix-2 pass (a whole
+// pass for one butterfly stage).  Larger radices go first.
 std::vector<int> schedule(int n, int T) {
   int a, b, c;
+  if (!factor235(n, &a, &b, &c)) return {};
+  if (n == 1) return {1};
+  struct Rad { int r, x, y, z; };   // r = 2^x 3^y 5^z
+  const Rad rads[] = {{24, 3, 1, 0}, {20, 2, 0, 1}, {16, 4, 0, 0}, {15, 0, 1, 1}, {12, 2, 1, 0}, {10, 1, 0, 1},
+                      {9, 0, 2, 0},  {8, 3, 0, 0},  {6, 1, 1, 0},  {5, 0, 0, 1},  {4, 2, 0, 0},  {3, 0, 1, 0},
+                      {2, 1, 0, 0}};
+  // cost[(x, y, z)] of the exponents still to cover: passes * 64 + non-power-of-two radices
+  const int A = a + 1, B = b + 1, C = c + 1;
+  const int kInf = 1 << 29;
+  std::vector<int> cost((size_t)A * B * C, kInf), pick((size_t)A * B * C, -1);
+  auto id = [&](int x, int y, int z) { return ((size_t)x * B + y) * C + z; };
+  cost[id(0, 0, 0)] = 0;
+  for (int x = 0; x <= a; x++)
+    for (int y = 0; y <= b; y++)
+      for (int z = 0; z <= c; z++) {
+        if (!x && !y && !z) continue;
+        for (int i = 0; i < (int)(sizeof(rads) / sizeof(rads[0])); i++) {
+          const Rad& q = rads[i];
+          if (q.x > x || q.y > y || q.z > z || !stage_ok(n, q.r, T)) continue;
+          const int prev = cost[id(x - q.x, y - q.y, z - q.z)];
+          if (prev >= kInf) continue;
+          const int cst = prev + 64 + ((q.r & (q.r - 1)) ? 1 : 0) + (q.r == 2 ? 2 : 0);
+          if (cst < cost[id(x, y, z)]) {
+            cost[id(x, y, z)] = cst;
+            pick[id(x, y, z)] = i;
+          }
+        }
+      }
+  if (cost[id(a, b, c)] >= kInf) return {};
   std::vector<int> r;
-  if (!factor235(n, &a, &b, &c)) return r;
-  while (a > 0) {
-    int pick = 0;
-    for (int e : {4, 3, 2, 1})
-      if (e <= a && stage_ok(n, 1 << e, T)) { pick = e; break; }
-    if (!pick) return {};
-    r.push_back(1 << pick);
-    a -= pick;
+  for (int x = a, y = b, z = c; x || y || z;) {
+    const Rad& q = rads[pick[id(x, y, z)]];
+    r.push_back(q.r);
+    x -= q.x;
+    y -= q.y;
+    z -= q.z;
   }
-  for (int i = 0; i < c; i++) {
-    if (!stage_ok(n, 5, T)) return {};
-    r.push_back(5);
-  }
-  for (int i = 0; i < b; i++) {
-    if (!stage_ok(n, 3, T)) return {};
-    r.push_back(3);
-  }
-  if (r.empty()) r.push_back(1);
+  std::sort(r.rbegin(), r.rend());
   return r;
 }
 

@@ -22,8 +22,6 @@
 // The block synchronises three times per correlation and two 256-thread
 // blocks share an SM.  Blocks loop over correlations (grid = resident blocks),
 // so the twiddle tables are built once per block.
-#include <type_traits>
-
 #include "kernels.cuh"
 
 namespace fpcc {
@@ -36,54 +34,6 @@ __host__ __device__ __forceinline__ constexpr int P16(int i) { return i + (i >> 
 // Padded position of output q of a row after the in-place 16 x 16 transform
 // (X[k1 + 16 k2] sits at point k2 + 16 k1).
 __device__ __forceinline__ int out_pos(int q) { return (q >> 4) + 17 * (q & 15); }
-
-// ---- compile-time twiddles ------------------------------------------------
-constexpr double kPiD = 3.14159265358979323846264338327950288;
-constexpr double cx_sin(double x) {
-  double x2 = x * x, term = x, sum = x;
-  for (int n = 1; n < 20; n++) {
-    term *= -x2 / ((2.0 * n) * (2.0 * n + 1.0));
-    sum += term;
-  }
-  return sum;
-}
-constexpr double cx_cos(double x) {
-  double x2 = x * x, term = 1.0, sum = 1.0;
-  for (int n = 1; n < 20; n++) {
-    term *= -x2 / ((2.0 * n - 1.0) * (2.0 * n));
-    sum += term;
-  }
-  return sum;
-}
-// v * exp(DIR 2 pi i T / N): exact quarter turns as swaps, otherwise a
-// constant computed at compile time (angle reduced to [-pi, pi]).
-template <int T, int N, int DIR>
-__device__ __forceinline__ float2 cmul_ct(float2 v) {
-  constexpr int t = ((T % N) + N) % N;
-  constexpr int q4 = ((4 * t) % N == 0) ? (4 * t) / N : -1;
-  if constexpr (q4 == 0) {
-    return v;
-  } else if constexpr (q4 == 1) {
-    return cmul_i<DIR>(v);
-  } else if constexpr (q4 == 2) {
-    return make_float2(-v.x, -v.y);
-  } else if constexpr (q4 == 3) {
-    return cmul_i<-DIR>(v);
-  } else {
-    constexpr double ang = 2.0 * kPiD * (double)(2 * t > N ? t - N : t) / (double)N;
-    constexpr float c = (float)cx_cos(ang);
-    constexpr float s = (float)((double)DIR * cx_sin(ang));
-    return cmul(v, make_float2(c, s));
-  }
-}
-
-template <int B, int E, typename Fn>
-__device__ __forceinline__ void sfor(Fn&& fn) {
-  if constexpr (B < E) {
-    fn(std::integral_constant<int, B>{});
-    sfor<B + 1, E>(static_cast<Fn&&>(fn));
-  }
-}
 
 // In-register DFT of length A*B (A, B on the small-DFT list; B may be 1),
 // natural order in and out: X[s2 + B s1] = sum_{r1} w_A^(r1 s1) w_AB^(r1 s2)
