@@ -54,6 +54,8 @@ def parse():
                          "to TRACE_JSON and print the kernel and stream summary")
     ap.add_argument("--stack-only", action="store_true",
                     help="run one all-pairs step, then only the stacking leg (profiling of the stacks)")
+    ap.add_argument("--wpcc-only", action="store_true",
+                    help="run only the wavelet leg (profiling); --windows sets its windows per pair (24 by default)")
     ap.add_argument("--methods-only", action="store_true",
                     help="run the warm-up steps, then only the per-method kernel leg (profiling of one method's "
                          "kernel: ncu -k)")
@@ -895,6 +897,15 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     F.build()
+    if args.wpcc_only:
+        stream = torch.cuda.Stream(device=torch.device("cuda", local))
+        ctx = F.Context(local)
+        ctx.set_stream(stream.cuda_stream)
+        n_win = args.windows if args.windows != N_WIN else 24
+        print(json.dumps({"wpcc": wpcc_leg(F, torch, ctx, stream, torch.device("cuda", local), measured_peaks()[0],
+                                           n_win=n_win)}), flush=True)
+        ctx.close()
+        return
     if args.multi_only:
         stream = torch.cuda.Stream(device=torch.device("cuda", local))
         ctx = F.Context(local)

@@ -70,7 +70,9 @@ __device__ __forceinline__ float2 pair_bin(const LargeArgs& a, int row, int p) {
   return cconjmul(ld_bin(X1, a.fmt, p), ld_bin(X2, a.fmt, p));
 }
 
-__device__ __forceinline__ float2 col_load(const LargeArgs& a, int row, int j, float eps) {
+// prow / frow: for COL_PRODUCT the input row and the filter row of `row`
+// (row / filt_of_row_div and its remainder, computed once per block).
+__device__ __forceinline__ float2 col_load(const LargeArgs& a, int row, int j, float eps, int prow, int frow) {
   switch (a.cmode) {
     case COL_REAL:
     case COL_SIGN: {
@@ -92,9 +94,8 @@ __device__ __forceinline__ float2 col_load(const LargeArgs& a, int row, int j, f
       return cscale(v, factor_of(a.rule, v.x * v.x + v.y * v.y, eps));
     }
     case COL_PRODUCT: {
-      const int g = a.filt_of_row_div;
-      const float2 x = reinterpret_cast<const float2*>(a.in)[(int64_t)(row / g) * a.ldin + j];
-      float2 w = a.filt[(int64_t)(row % g) * a.ldfilt + j];
+      const float2 x = reinterpret_cast<const float2*>(a.in)[(int64_t)prow * a.ldin + j];
+      float2 w = a.filt[(int64_t)frow * a.ldfilt + j];
       if (a.filt_conj) w.y = -w.y;
       return cscale(cmul(x, w), a.in_scale);
     }
@@ -133,9 +134,11 @@ __global__ void __launch_bounds__(T) k_cols(LargeArgs a) {
   const int row = blockIdx.y;
   const int c0 = blockIdx.x * C;
   const float eps = (a.cmode == COL_PHASE || a.cmode == COL_NORMALISE) ? eps_of(a.rule, a.rowstat[row]) : 0.f;
+  const int prow = (a.cmode == COL_PRODUCT) ? row / a.filt_of_row_div : row;
+  const int frow = (a.cmode == COL_PRODUCT) ? row - prow * a.filt_of_row_div : 0;
   for (int e = threadIdx.x; e < C * N1; e += T) {
     const int c = e % C, j1 = e / C;
-    s[c * VS + PADI(j1)] = col_load(a, row, j1 * n2 + c0 + c, eps);
+    s[c * VS + PADI(j1)] = col_load(a, row, j1 * n2 + c0 + c, eps, prow, frow);
   }
   __syncthreads();
   ct_fft<DIR, T, C>(s, C, VS, TwTab{lo1, hi1}, RAD{});
@@ -144,8 +147,8 @@ __global__ void __launch_bounds__(T) k_cols(LargeArgs a) {
   for (int e = threadIdx.x; e < C * N1; e += T) {
     const int c = e % C, k1 = e / C;
     const int j2 = c0 + c;
-    const int t = (int)(((int64_t)j2 * k1) % n);
-    float2 w = twiddle(twN, t);
+    // j2 < n2 and k1 < N1, so j2 k1 < n: the twiddle index needs no reduction
+    float2 w = twiddle(twN, j2 * k1);
     if (DIR > 0) w.y = -w.y;
     out[(int64_t)k1 * n2 + j2] = cmul(s[c * VS + PADI(k1)], w);
   }
