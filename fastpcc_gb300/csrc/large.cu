@@ -71,15 +71,18 @@ __device__ __forceinline__ float2 pair_bin(const LargeArgs& a, int row, int p) {
 }
 
 // prow / frow: for COL_PRODUCT the input row and the filter row of `row`
-// (row / filt_of_row_div and its remainder, computed once per block).
+// (row / filt_of_row_div and its remainder, computed once per block).  MODE is
+// the column mode, a compile-time value so that a block's loads carry no branch
+// between them (cols_gather issues them all before the first is used).
+template <int MODE>
 __device__ __forceinline__ float2 col_load(const LargeArgs& a, int row, int j, float eps, int prow, int frow) {
-  switch (a.cmode) {
+  switch (MODE) {
     case COL_REAL:
     case COL_SIGN: {
       const int jj = j - a.in_off;
       if (jj < 0 || jj >= a.N) return make_float2(0.f, 0.f);
       float v = __ldg(reinterpret_cast<const float*>(a.in) + (int64_t)row * a.ldin + jj);
-      if (a.cmode == COL_SIGN) v = (a.sign_ge ? (v >= 0.0f) : (v > 0.0f)) ? 1.0f : -1.0f;
+      if (MODE == COL_SIGN) v = (a.sign_ge ? (v >= 0.0f) : (v > 0.0f)) ? 1.0f : -1.0f;
       return make_float2(v * a.in_scale, 0.f);
     }
     case COL_PHASE: {
@@ -117,6 +120,18 @@ __device__ __forceinline__ float2 col_load(const LargeArgs& a, int row, int j, f
   }
 }
 
+// The PER = C N1 / T column elements of a thread (element e = threadIdx.x + i T
+// is column e % C, point e / C), loaded into registers together.
+template <int MODE, int PER, int T, int C>
+__device__ __forceinline__ void cols_gather(const LargeArgs& a, int row, int c0, int n2, float eps, int prow, int frow,
+                                            float2* buf) {
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int e = threadIdx.x + i * T;
+    buf[i] = col_load<MODE>(a, row, (e / C) * n2 + c0 + e % C, eps, prow, frow);
+  }
+}
+
 template <int T, typename RAD, int DIR>
 __global__ void __launch_bounds__(T) k_cols(LargeArgs a) {
   constexpr int N1 = rlen(RAD{});
@@ -136,9 +151,22 @@ __global__ void __launch_bounds__(T) k_cols(LargeArgs a) {
   const float eps = (a.cmode == COL_PHASE || a.cmode == COL_NORMALISE) ? eps_of(a.rule, a.rowstat[row]) : 0.f;
   const int prow = (a.cmode == COL_PRODUCT) ? row / a.filt_of_row_div : row;
   const int frow = (a.cmode == COL_PRODUCT) ? row - prow * a.filt_of_row_div : 0;
-  for (int e = threadIdx.x; e < C * N1; e += T) {
-    const int c = e % C, j1 = e / C;
-    s[c * VS + PADI(j1)] = col_load(a, row, j1 * n2 + c0 + c, eps, prow, frow);
+  static_assert((C * N1) % T == 0, "column block: whole elements per thread");
+  constexpr int PER = C * N1 / T;
+  float2 buf[PER];
+  switch (a.cmode) {
+    case COL_REAL: cols_gather<COL_REAL, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
+    case COL_SIGN: cols_gather<COL_SIGN, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
+    case COL_PHASE: cols_gather<COL_PHASE, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
+    case COL_COMPLEX: cols_gather<COL_COMPLEX, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
+    case COL_PRODUCT: cols_gather<COL_PRODUCT, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
+    case COL_NORMALISE: cols_gather<COL_NORMALISE, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
+    default: cols_gather<COL_PAIR, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
+  }
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int e = threadIdx.x + i * T;
+    s[(e % C) * VS + PADI(e / C)] = buf[i];
   }
   __syncthreads();
   ct_fft<DIR, T, C>(s, C, VS, TwTab{lo1, hi1}, RAD{});
@@ -169,9 +197,21 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
   const int row = blockIdx.y;
   const int r0 = blockIdx.x * C;
   const float2* in = a.T + (int64_t)row * n;
-  for (int e = threadIdx.x; e < C * N2; e += T) {
-    const int c = e / N2, j2 = e - c * N2;
-    s[c * VS + PADI(j2)] = in[(int64_t)(r0 + c) * N2 + j2];
+  {
+    // every load of the thread first, then the stores into the tile
+    static_assert((C * N2) % T == 0, "row block: whole elements per thread");
+    constexpr int PER = C * N2 / T;
+    float2 buf[PER];
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+      const int e = threadIdx.x + i * T;
+      buf[i] = in[(int64_t)(r0 + e / N2) * N2 + e % N2];
+    }
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+      const int e = threadIdx.x + i * T;
+      s[(e / N2) * VS + PADI(e % N2)] = buf[i];
+    }
   }
   __syncthreads();
   ct_fft<DIR, T, C>(s, C, VS, TwTab{lo, hi}, RAD{});
