@@ -1379,13 +1379,18 @@ int run_first_use(fpcc_ctx* c, const Layout& Ly, float* d_x, int nsta, const int
                   int npairs, float v, float* d_y, float* h_y, const float* h_x) {
   const int method = Ly.method;
   const int N = Ly.N;
+  int rc;
+  // the rewritten pair list goes straight into pinned staging for its upload
+  void* hps = nullptr;
+  if ((rc = pin_buf(c, 7, 2 * (size_t)npairs * sizeof(int32_t), &hps))) return rc;
+  int32_t* hp = (int32_t*)hps;
   std::vector<int> pos((size_t)nsta, -1), order;
   order.reserve((size_t)nsta);
   std::vector<int> need((size_t)npairs);   // rows first used by pairs 0..i
-  std::vector<int32_t> hp(2 * (size_t)npairs);
   for (int i = 0; i < npairs; i++) {
     for (int h = 0; h < 2; h++) {
       const int r = h_pairs[2 * (size_t)i + h];
+      if (r < 0 || r >= nsta) return fail(FPCC_EARG, "pair row index out of range");
       if (pos[(size_t)r] < 0) {
         pos[(size_t)r] = (int)order.size();
         order.push_back(r);
@@ -1415,7 +1420,6 @@ int run_first_use(fpcc_ctx* c, const Layout& Ly, float* d_x, int nsta, const int
     if (r == nuse) break;
   }
   const int nch = (int)R.size() - 1;
-  int rc;
   void* d_st = nullptr;
   const size_t rowb = (size_t)Ly.lds * Ly.esz;
   if ((rc = dev_buf(c, S_STATION, (size_t)nuse * rowb, &d_st))) return rc;
@@ -1463,10 +1467,7 @@ int run_first_use(fpcc_ctx* c, const Layout& Ly, float* d_x, int nsta, const int
   cudaEvent_t* ev_pair = ev_cnt + nch;             // piece p computed
   cudaEvent_t ev_upall = ev_pair[pieces.size()];   // every row uploaded
   // the pair list, rewritten onto the device order, goes first on the main stream
-  void* hps = nullptr;
-  if ((rc = pin_buf(c, 7, hp.size() * sizeof(int32_t), &hps))) return rc;
-  memcpy(hps, hp.data(), hp.size() * sizeof(int32_t));
-  CK(cudaMemcpyAsync(d_p, hps, hp.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(d_p, hps, 2 * (size_t)npairs * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
   // the copies follow everything queued on the main stream (buffer allocations included)
   CK(cudaEventRecord(c->ord_ev, c->stream));
   CK(cudaStreamWaitEvent(c->stream2, c->ord_ev, 0));
@@ -1692,13 +1693,17 @@ extern "C" int fpcc_allpairs_host(fpcc_ctx* c, int method, const float* h_x, int
                                   int npairs, int Lag1, int Lag2, float v, int nz_mode, int fmt, float* h_y) {
   if (!c || !h_x || !h_pairs || !h_y) return fail(FPCC_EARG, "null argument");
   if (nsta < 0 || npairs < 0) return fail(FPCC_EARG, "negative count");
-  for (size_t i = 0; i < 2 * (size_t)npairs; i++)
-    if (h_pairs[i] < 0 || h_pairs[i] >= nsta) return fail(FPCC_EARG, "pair row index out of range");
   std::lock_guard<std::mutex> lk(c->mu);
   CK(cudaSetDevice(c->device));
   Layout Ly;
   int rc = make_layout(method, N, Lag1, Lag2, nz_mode, fmt, &Ly);
   if (rc) return rc;
+  // pinned buffers and one-rule methods try the first-use path, which checks
+  // the row indices as it reads the pair list; every other call checks them here
+  const bool first_use = !Ly.two_rules && npairs >= 2048 && is_pinned(h_x) && is_pinned(h_y);
+  if (!first_use)
+    for (size_t i = 0; i < 2 * (size_t)npairs; i++)
+      if (h_pairs[i] < 0 || h_pairs[i] >= nsta) return fail(FPCC_EARG, "pair row index out of range");
   const size_t xbytes = (size_t)nsta * N * sizeof(float);
   const size_t ybytes = (size_t)npairs * Ly.L * sizeof(float);
   const size_t pbytes = (size_t)npairs * 2 * sizeof(int32_t);
@@ -1718,7 +1723,7 @@ extern "C" int fpcc_allpairs_host(fpcc_ctx* c, int method, const float* h_x, int
   // list has that structure (it uploads its own rewritten pair list); otherwise
   // the windows go up in chunks that the station stage consumes as they arrive
   rc = 1;
-  if (!Ly.two_rules && npairs >= 2048 && is_pinned(h_x) && is_pinned(h_y))
+  if (first_use)
     rc = run_first_use(c, Ly, (float*)d_x, nsta, h_pairs, (int32_t*)d_p, npairs, v, (float*)d_y, h_y, h_x);
   if (rc < 0 || (rc > 1)) return rc;
   if (rc == 1) {

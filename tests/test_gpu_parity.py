@@ -386,6 +386,11 @@ def test_allpairs_host_first_use_pipeline(F, orc):
     y = np.zeros((P, L), np.float32)
     ctx.allpairs_host(F.PCC2, x, pairs, -lag, lag, y)
     assert np.array_equal(yp.numpy(), y[perm])
+    # a row index outside the station rows is refused before any work
+    bad = pairs.copy()
+    bad[7, 0] = -1
+    with pytest.raises(F.FpccError):
+        ctx.allpairs_host(F.PCC2, xp.numpy(), bad, -lag, lag, yp.numpy())
     ctx.close()
 
 
