@@ -215,6 +215,46 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
   }
   __syncthreads();
   ct_fft<DIR, T, C>(s, C, VS, TwTab{lo, hi}, RAD{});
+  // lag read-out (ROW_LAGS): the pair's lengths, scale, output row and energy
+  // rows are the block's (one pair per blockIdx.y), found once
+  int N = 0, lag0 = 0, L = 0;
+  float scale = 0.f;
+  float* yrow = nullptr;
+  GnccNorm gn;
+  const int Nz = 2 * n;
+  if (a.rmode == ROW_LAGS) {
+    const double* E1 = nullptr;
+    const double* E2 = nullptr;
+    if (a.desc) {
+      const PairDesc& d = a.desc[row];
+      N = d.N;
+      lag0 = d.lag0;
+      L = d.L;
+      scale = d.scale != 0.0f ? d.scale : (a.norm == 0 ? 1.0f / ((float)Nz * (float)N) : (float)(1.0 / (double)Nz));
+      if (a.fmt == SPEC_I16) scale *= i16_row_scale(d.a) * i16_row_scale(d.b);
+      yrow = reinterpret_cast<float*>(d.y);
+      if (a.norm == 1) { E1 = d.ea; E2 = d.eb; }
+    } else {
+      N = a.N;
+      lag0 = a.lag0;
+      L = a.L;
+      scale = a.scale;
+      yrow = a.y + (int64_t)row * a.ldy;
+      // station rows of the pair: only with a pair list (precomputed cross-spectrum rows have none)
+      if (a.herm != 2 && (a.fmt == SPEC_I16 || a.norm == 1)) {
+        const int2 pr = a.pairs[row];
+        if (a.fmt == SPEC_I16) {
+          const char* sp = reinterpret_cast<const char*>(a.spec);
+          scale *= i16_row_scale(sp + (int64_t)pr.x * a.ldspec * 4) * i16_row_scale(sp + (int64_t)pr.y * a.ldspec * 4);
+        }
+        if (a.norm == 1) {
+          E1 = a.energy + (int64_t)pr.x * a.ldE;
+          E2 = a.energy + (int64_t)pr.y * a.ldE;
+        }
+      }
+    }
+    if (a.norm == 1) gn.init(E1, E2, N);
+  }
   float mx = 0.f;
   for (int e = threadIdx.x; e < C * N2; e += T) {
     const int c = e % C, k2 = e / C;
@@ -231,43 +271,6 @@ __global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
       mx = fmaxf(mx, v.x * v.x + v.y * v.y);
     } else {
       // y_full[2k] = Re z[k], y_full[2k+1] = Im z[k]; lag = idx or idx - Nz
-      const int Nz = 2 * n;
-      int N, lag0, L;
-      float scale;
-      float* yrow;
-      const double* E1 = nullptr;
-      const double* E2 = nullptr;
-      if (a.desc) {
-        const PairDesc& d = a.desc[row];
-        N = d.N;
-        lag0 = d.lag0;
-        L = d.L;
-        scale = d.scale != 0.0f ? d.scale
-                                : (a.norm == 0 ? 1.0f / ((float)Nz * (float)N) : (float)(1.0 / (double)Nz));
-        if (a.fmt == SPEC_I16) scale *= i16_row_scale(d.a) * i16_row_scale(d.b);
-        yrow = reinterpret_cast<float*>(d.y);
-        if (a.norm == 1) { E1 = d.ea; E2 = d.eb; }
-      } else {
-        N = a.N;
-        lag0 = a.lag0;
-        L = a.L;
-        scale = a.scale;
-        yrow = a.y + (int64_t)row * a.ldy;
-        // station rows of the pair: only with a pair list (precomputed cross-spectrum rows have none)
-        if (a.herm != 2 && (a.fmt == SPEC_I16 || a.norm == 1)) {
-          const int2 pr = a.pairs[row];
-          if (a.fmt == SPEC_I16) {
-            const char* sp = reinterpret_cast<const char*>(a.spec);
-            scale *= i16_row_scale(sp + (int64_t)pr.x * a.ldspec * 4) * i16_row_scale(sp + (int64_t)pr.y * a.ldspec * 4);
-          }
-          if (a.norm == 1) {
-            E1 = a.energy + (int64_t)pr.x * a.ldE;
-            E2 = a.energy + (int64_t)pr.y * a.ldE;
-          }
-        }
-      }
-      GnccNorm gn;
-      if (a.norm == 1) gn.init(E1, E2, N);
 #pragma unroll
       for (int q = 0; q < 2; q++) {
         const int idx = 2 * k + q;
