@@ -1104,11 +1104,12 @@ extern "C" int fpcc_station_stage_ex(fpcc_ctx* c, int method, const float* d_x, 
     return large_station(c, method == FPCC_GNCC ? COL_REAL : COL_SIGN, d_x, sizeof(float), ldx, nrows, N, Nz, 0,
                          nullptr, rule == FPCC_SIGN_GE ? 1 : 0, FPCC_F32, 1, d_out, ldo);
   }
-  if (method == FPCC_PCC2) {
+  if (method == FPCC_PCC2 && (int)p64.size() < nrows) {
     // one fused kernel per station window, specialised at run time for (N, Nz);
     // windows with gaps (FP64 analytic signals) are then redone on their own
     // through the general path, so that every window's spectrum depends on that
-    // window only, not on the others of the call
+    // window only, not on the others of the call (a call whose windows all have
+    // gaps goes to the general path directly: no fused kernel to specialise)
     const cudaError_t e = launch_station_fused(d_x, ldx, nrows, N, Nz, rule, fmt, d_out, ldo, c->stream);
     if (e == cudaSuccess) {
       g_launches++;

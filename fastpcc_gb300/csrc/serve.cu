@@ -655,13 +655,22 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   rows.resize(keys.size());
   std::vector<int64_t> miss_keys;
   std::vector<int> miss_rows;
+  // room for every distinct missing key is asked for at the first claim (one
+  // growth of the slab), and one row fewer at each claim after it; the keys
+  // repeat (both stations of many pairs), so counting them would ask for more
+  // rows than the windows need and fail under a tight budget
+  int left = 0;
+  {
+    std::vector<int64_t> absent;
+    for (int64_t k : keys)
+      if (sl.row_of.find(k) == sl.row_of.end()) absent.push_back(k);
+    std::sort(absent.begin(), absent.end());
+    left = (int)(std::unique(absent.begin(), absent.end()) - absent.begin());
+  }
   for (size_t i = 0; i < keys.size(); i++) {
     int r = find_row(sl, keys[i]);
     if (r < 0) {
-      // room for one row at a time (the slab doubles as it grows): the keys
-      // repeat (both stations of many pairs), so their count would ask for more
-      // rows than the distinct windows need and fail under a tight budget
-      r = claim_row(s, sl, keys[i], 1);
+      r = claim_row(s, sl, keys[i], std::max(1, left--));
       if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
       miss_keys.push_back(keys[i]);
       miss_rows.push_back(r);
@@ -979,14 +988,22 @@ int prefetch_phase(Server* s, int kind, int fmt, const std::vector<std::pair<int
         fl.pinned_rows.push_back({&sl, r});
         continue;
       }
-      const int r = claim_row(s, sl, key, 1);
-      if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
-      sl.pin[r]++;
-      fl.pinned_rows.push_back({&sl, r});
-      miss.push_back({q->N, Nz, key, &sl, r, f64});
+      miss.push_back({q->N, Nz, key, &sl, -1, f64});
     }
   }
   if (miss.empty()) return 0;
+  // rows for the missing products, each slab growing once to what it needs
+  {
+    std::map<Slab*, int> left;
+    for (const Miss& m : miss) left[m.sl]++;
+    for (Miss& m : miss) {
+      const int r = claim_row(s, *m.sl, m.key, left[m.sl]--);
+      if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
+      m.sl->pin[r]++;
+      fl.pinned_rows.push_back({m.sl, r});
+      m.row = r;
+    }
+  }
   std::stable_sort(miss.begin(), miss.end(),
                    [](const Miss& a, const Miss& b) { return std::tie(a.N, a.Nz) < std::tie(b.N, b.Nz); });
   const int n = (int)miss.size();
@@ -1247,10 +1264,18 @@ int run_group_wpcc(Server* s, const GroupKey& g, std::vector<Req*>& reqs, InFlig
   std::vector<int> rows(2 * n);
   std::vector<int64_t> miss_keys;
   std::vector<int> miss_rows;
+  int left = 0;   // distinct missing keys (room asked for at the first claim, as ensure_products)
+  {
+    std::vector<int64_t> absent;
+    for (int64_t k : keys)
+      if (sl.row_of.find(k) == sl.row_of.end()) absent.push_back(k);
+    std::sort(absent.begin(), absent.end());
+    left = (int)(std::unique(absent.begin(), absent.end()) - absent.begin());
+  }
   for (int i = 0; i < 2 * n; i++) {
     int r = find_row(sl, keys[i]);
     if (r < 0) {
-      r = claim_row(s, sl, keys[i], 1);   // one row at a time: the keys repeat
+      r = claim_row(s, sl, keys[i], std::max(1, left--));
       if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
       miss_keys.push_back(keys[i]);
       miss_rows.push_back(r);

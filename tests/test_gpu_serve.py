@@ -342,14 +342,16 @@ def test_server_wpcc_requests(F, orc):
 
 
 def test_server_releases_idle_product_classes(F, orc):
-    # each window length is its own product class (5 spectra + 5 raw windows:
-    # 142, 150 and 179 KB).  A batch of 10 requests spans at most two windows,
-    # so the budget holds any two classes but not all three: classes are
-    # released and rebuilt as requests move on
+    # each window length is its own product class (5 spectra of 100, 100 and
+    # 120 KB, 5 raw windows of 40, 48 and 56 KB; slabs grow to the rows a batch
+    # needs).  A batch of 10 requests spans at most two windows, so the budget
+    # holds any two classes (at most 324 KB) but not the three classes' spectra
+    # beside a raw class (at least 360 KB): classes are released and rebuilt as
+    # requests move on
     lengths = [2000, 2400, 2800]
     xs = _uneven_windows(lengths, "serve/release")
     reqs = [(0, i, j, w, -100, 100, 0.0) for w in (0, 1, 2, 0) for i in range(5) for j in range(5) if i < j]
-    srv = F.Server(hbm_budget=400 << 10, max_batch=10)
+    srv = F.Server(hbm_budget=340 << 10, max_batch=10)
     for w, x in xs.items():
         for s in range(5):
             srv.put(s, w, x[s])
