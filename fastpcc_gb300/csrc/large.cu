@@ -132,8 +132,12 @@ __device__ __forceinline__ void cols_gather(const LargeArgs& a, int row, int c0,
   }
 }
 
-template <int T, typename RAD, int DIR>
-__global__ void __launch_bounds__(T) k_cols(LargeArgs a) {
+// BATCH: each thread's loads issued together (for the modes whose loads are
+// several reads and arithmetic: the wavelet band product and the pair
+// cross-spectrum); the other modes keep the loop, held to the registers of
+// five 256-thread blocks per SM (more warps to hide the loads' latency).
+template <int T, typename RAD, int DIR, bool BATCH>
+__global__ void __launch_bounds__(T, BATCH ? 1 : 1280 / T) k_cols(LargeArgs a) {
   constexpr int N1 = rlen(RAD{});
   constexpr int C = kColVecs;
   constexpr int VS = cpadded(N1);
@@ -153,20 +157,28 @@ __global__ void __launch_bounds__(T) k_cols(LargeArgs a) {
   const int frow = (a.cmode == COL_PRODUCT) ? row - prow * a.filt_of_row_div : 0;
   static_assert((C * N1) % T == 0, "column block: whole elements per thread");
   constexpr int PER = C * N1 / T;
-  float2 buf[PER];
-  switch (a.cmode) {
-    case COL_REAL: cols_gather<COL_REAL, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
-    case COL_SIGN: cols_gather<COL_SIGN, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
-    case COL_PHASE: cols_gather<COL_PHASE, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
-    case COL_COMPLEX: cols_gather<COL_COMPLEX, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
-    case COL_PRODUCT: cols_gather<COL_PRODUCT, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
-    case COL_NORMALISE: cols_gather<COL_NORMALISE, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
-    default: cols_gather<COL_PAIR, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf); break;
-  }
+  if constexpr (BATCH) {
+    float2 buf[PER];
+    if (a.cmode == COL_PRODUCT) cols_gather<COL_PRODUCT, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf);
+    else cols_gather<COL_PAIR, PER, T, C>(a, row, c0, n2, eps, prow, frow, buf);
 #pragma unroll
-  for (int i = 0; i < PER; i++) {
-    const int e = threadIdx.x + i * T;
-    s[(e % C) * VS + PADI(e / C)] = buf[i];
+    for (int i = 0; i < PER; i++) {
+      const int e = threadIdx.x + i * T;
+      s[(e % C) * VS + PADI(e / C)] = buf[i];
+    }
+  } else {
+    for (int e = threadIdx.x; e < C * N1; e += T) {
+      const int j = (e / C) * n2 + c0 + e % C;
+      float2 v;
+      switch (a.cmode) {
+        case COL_REAL: v = col_load<COL_REAL>(a, row, j, eps, prow, frow); break;
+        case COL_SIGN: v = col_load<COL_SIGN>(a, row, j, eps, prow, frow); break;
+        case COL_PHASE: v = col_load<COL_PHASE>(a, row, j, eps, prow, frow); break;
+        case COL_COMPLEX: v = col_load<COL_COMPLEX>(a, row, j, eps, prow, frow); break;
+        default: v = col_load<COL_NORMALISE>(a, row, j, eps, prow, frow); break;
+      }
+      s[(e % C) * VS + PADI(e / C)] = v;
+    }
   }
   __syncthreads();
   ct_fft<DIR, T, C>(s, C, VS, TwTab{lo1, hi1}, RAD{});
@@ -348,13 +360,18 @@ cudaError_t launch_large(const LargeArgs& a, cudaStream_t st) {
   cudaError_t e = cudaErrorInvalidValue;
   // column pass
   {
+    const bool batch = (a.cmode == COL_PRODUCT || a.cmode == COL_PAIR);
     dim3 grid(a.n2 / kColVecs, a.nrows);
     const size_t smem = ((size_t)kColVecs * cpadded(a.n1) + 128 + ctw_hi(a.n1) + 128 + ctw_hi(a.n)) * sizeof(float2);
     bool done = false;
 #define FPCC_CL(SZ, T, ...)                                                                            \
   if (!done && a.n1 == SZ) {                                                                         \
-    e = (a.dir < 0) ? launch_k2(k_cols<T, Radices<__VA_ARGS__>, -1>, grid, T, smem, st, a)             \
-                    : launch_k2(k_cols<T, Radices<__VA_ARGS__>, 1>, grid, T, smem, st, a);             \
+    if (batch)                                                                                        \
+      e = (a.dir < 0) ? launch_k2(k_cols<T, Radices<__VA_ARGS__>, -1, true>, grid, T, smem, st, a)     \
+                      : launch_k2(k_cols<T, Radices<__VA_ARGS__>, 1, true>, grid, T, smem, st, a);     \
+    else                                                                                              \
+      e = (a.dir < 0) ? launch_k2(k_cols<T, Radices<__VA_ARGS__>, -1, false>, grid, T, smem, st, a)    \
+                      : launch_k2(k_cols<T, Radices<__VA_ARGS__>, 1, false>, grid, T, smem, st, a);    \
     done = true;                                                                                     \
   }
     FPCC_COL_MENU(FPCC_CL)
