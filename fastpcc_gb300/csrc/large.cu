@@ -194,8 +194,11 @@ __global__ void __launch_bounds__(T, BATCH ? 1 : 1280 / T) k_cols(LargeArgs a) {
   }
 }
 
+// Row blocks of 160-256 threads are held to the registers of 1280 threads per
+// SM (eight blocks of 160): the row pass waits on its loads, and more resident
+// warps hide more of that wait than the few registers spilled cost.
 template <int T, typename RAD, int DIR>
-__global__ void __launch_bounds__(T) k_rows(LargeArgs a) {
+__global__ void __launch_bounds__(T, (T >= 160 && T <= 256) ? 1280 / T : 1) k_rows(LargeArgs a) {
   constexpr int N2 = rlen(RAD{});
   constexpr int C = kRowVecs;
   constexpr int VS = cpadded(N2);
