@@ -655,20 +655,33 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
   rows.resize(keys.size());
   std::vector<int64_t> miss_keys;
   std::vector<int> miss_rows;
+  // resident products first (pinned as found), then the claims for the rest:
   // room for every distinct missing key is asked for at the first claim (one
   // growth of the slab), and one row fewer at each claim after it; the keys
   // repeat (both stations of many pairs), so counting them would ask for more
   // rows than the windows need and fail under a tight budget
-  int left = 0;
-  {
-    std::vector<int64_t> absent;
-    for (int64_t k : keys)
-      if (sl.row_of.find(k) == sl.row_of.end()) absent.push_back(k);
-    std::sort(absent.begin(), absent.end());
-    left = (int)(std::unique(absent.begin(), absent.end()) - absent.begin());
-  }
+  std::vector<size_t> absent;
   for (size_t i = 0; i < keys.size(); i++) {
-    int r = find_row(sl, keys[i]);
+    const int r = find_row(sl, keys[i]);
+    if (r < 0) {
+      absent.push_back(i);
+      continue;
+    }
+    rows[i] = r;
+    sl.pin[r]++;
+    fl.pinned_rows.push_back({&sl, r});
+  }
+  if (absent.empty()) return 0;
+  int left;
+  {
+    std::vector<int64_t> ak;
+    ak.reserve(absent.size());
+    for (size_t i : absent) ak.push_back(keys[i]);
+    std::sort(ak.begin(), ak.end());
+    left = (int)(std::unique(ak.begin(), ak.end()) - ak.begin());
+  }
+  for (size_t i : absent) {
+    int r = find_row(sl, keys[i]);   // claimed already for an earlier repeat of the key
     if (r < 0) {
       r = claim_row(s, sl, keys[i], std::max(1, left--));
       if (r < 0) return no_mem("server: no free product row (every row held by this batch, budget reached)");
@@ -679,7 +692,6 @@ int ensure_products(Server* s, const Product& pk, const std::vector<int64_t>& ke
     sl.pin[r]++;
     fl.pinned_rows.push_back({&sl, r});
   }
-  if (miss_keys.empty()) return 0;
   const int n = (int)miss_keys.size();
   std::vector<int> raw_rows;
   int rc = ensure_raw(s, pk.N, miss_keys, raw_rows, fl);
