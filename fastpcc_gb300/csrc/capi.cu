@@ -1341,20 +1341,6 @@ int make_layout(int method, int N, int Lag1, int Lag2, int nz_mode, int fmt, Lay
   return 0;
 }
 
-// Station stage then pair stage on the context stream.  For the 1-bit methods
-// the sign rule depends on the role of the trace (src/FFTapps.c:1037,1042):
-// split >= 0 gives rows [0, split) the station-1 rule and the rest the station-2
-// rule; split < 0 computes both variants (rows [0,nsta) and [nsta,2 nsta)) and
-// expects each pair's station-2 index to point into the second half.
-// Station stage(s), then the pair stage.  With h_x (the station windows in host
-// memory, one method rule), the windows go up in four row chunks on the second
-// stream and the station stage of each chunk starts as soon as its rows have
-// arrived.  With h_y (FP32 results wanted in host memory) and enough pairs, the
-// pair stage runs in chunks of consecutive pairs and the second stream
-// downloads each chunk's rows once its kernels are done, so the download of one
-// chunk overlaps the correlation of the next; every kernel is queued before the
-// first download, so pageable host memory (whose copies return only when done)
-// does not hold back the launches.
 bool is_pinned(const void* p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -1369,10 +1355,11 @@ bool is_pinned(const void* p) {
 // pair list is rewritten onto that order), so that the rows of the first pairs
 // go up first, each run of rows at one host stride as one strided copy; the
 // station stage runs on contiguous chunks of those rows as they arrive (a small
-// first chunk, then 768 rows), each chunk's gap counts come back on the upload
+// first chunk, then 768 rows), each chunk's gap counts come back on a third
 // stream (the host never waits behind pair stages), the pairs whose rows are
-// all transformed run in pieces, and each piece's results go down on a third
-// stream while later pieces compute.  Results are the same as through
+// all transformed run in pieces, and each piece's results go down on the
+// third stream once every row is up (the two directions share the host link,
+// and downloads beside the uploads starve them) while later pieces compute.  Results are the same as through
 // run_device: every row goes through the same station stage, with its FP64
 // rows chosen by the same rule.  Returns 1, with nothing queued, when the pair
 // list's first-use order breaks into too many runs (no row structure to use).
@@ -1542,6 +1529,20 @@ int run_first_use(fpcc_ctx* c, const Layout& Ly, float* d_x, int nsta, const int
   return 0;
 }
 
+// Station stage then pair stage on the context stream.  For the 1-bit methods
+// the sign rule depends on the role of the trace (src/FFTapps.c:1037,1042):
+// split >= 0 gives rows [0, split) the station-1 rule and the rest the station-2
+// rule; split < 0 computes both variants (rows [0,nsta) and [nsta,2 nsta)) and
+// expects each pair's station-2 index to point into the second half.
+// Station stage(s), then the pair stage.  With h_x (the station windows in host
+// memory, one method rule), the windows go up in four row chunks on the second
+// stream and the station stage of each chunk starts as soon as its rows have
+// arrived.  With h_y (FP32 results wanted in host memory) and enough pairs, the
+// pair stage runs in chunks of consecutive pairs and the second stream
+// downloads each chunk's rows once its kernels are done, so the download of one
+// chunk overlaps the correlation of the next; every kernel is queued before the
+// first download, so pageable host memory (whose copies return only when done)
+// does not hold back the launches.
 int run_device(fpcc_ctx* c, const Layout& Ly, const float* d_x, int nsta, const int32_t* d_pairs, int npairs,
                float v, float* d_y, int64_t* d_num, int split, float* h_y = nullptr, const float* h_x = nullptr) {
   void* d_st = nullptr;
