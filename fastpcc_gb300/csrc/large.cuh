@@ -9,11 +9,34 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <float.h>
 #include <stdint.h>
 
 #include "kernels.cuh"
 
 namespace fpcc {
+
+__device__ __forceinline__ bool isnormal_pos(float v) { return v >= FLT_MIN && v <= FLT_MAX; }
+
+// Amplitude normalisation of a row from its statistic `ref` (max |x|^2): the
+// rule's epsilon, then the factor of a sample of |x|^2 = m2.
+__device__ __forceinline__ float eps_of(int rule, float ref) {
+  if (rule == AMP_F_REG) return (float)(1e-6 * sqrt((double)ref));
+  if (rule == AMP_PURE) return 0.0f;
+  return 1e-6f * ref;
+}
+
+__device__ __forceinline__ float factor_of(int rule, float m2, float eps) {
+  if (rule == AMP_F_REG) {
+    const float f = 1.0f / (sqrtf(m2) + eps);
+    return isnormal_pos(f) ? f : 0.0f;
+  }
+  if (rule == AMP_D_REG) {
+    const float f = rsqrtf(m2 + eps);
+    return isnormal_pos(f) ? f : 0.0f;
+  }
+  return (m2 > eps) ? rsqrtf(m2) : 0.0f;
+}
 
 // Column-kernel input modes.
 enum ColMode : int {

@@ -15,6 +15,7 @@
 // length than the reference's power of two.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -52,6 +53,201 @@ __global__ void __launch_bounds__(256) k_wpcc_accum(const void* __restrict__ P, 
     }
     Y[(int64_t)p * Nz + k] = acc;
   }
+}
+
+// ---------------------------------------------------------------- whole rows on a cluster
+// The band and phase-spectrum transforms of one (window, scale) row, N = 4Q
+// points, on a cluster of four blocks whose shared memories hold the row
+// between the transforms (no global-memory round trip):
+//   inverse, block k:  z_k[f] = w_N^(+k f) sum_j Y[f + Q j] i^(k j),  Y = X W_s,
+//                      x[4m + k] = IDFT_Q(z_k)[m]                       (in place)
+//   normalise:         x *= factor(|x|^2, eps(max over the four blocks))
+//   forward, block k:  Z_k = DFT_Q(x[4m + k]),  then block j writes
+//                      P[f + Q j] = sum_r (-i)^(r j) w_N^(-r f) Z_r[f]   (Z_r read from block r)
+// The same arithmetic as the four-step passes (`launch_large` with the band
+// product, the row maximum, the normalising load and the spectrum store) in
+// another order of the FFT's butterflies.
+template <int... Rs>
+__host__ __device__ constexpr int prod_radices_of(Radices<Rs...>) {
+  return prod_radices<Rs...>();
+}
+
+constexpr int kRowRanks = 4;      // blocks per row (the cluster)
+constexpr int kRowThreads = 1024;
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// all threads of all four blocks: shared-memory writes before it are seen by
+// the cluster's reads after it
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// address of the same shared-memory location in block `rank` of the cluster
+__device__ __forceinline__ uint32_t cluster_addr(const void* p, uint32_t rank) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float2 cluster_ld2(uint32_t addr) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ float cluster_ld(uint32_t addr) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+  return v;
+}
+// v * i^q
+__device__ __forceinline__ float2 rot_quarter(float2 v, int q) {
+  switch (q & 3) {
+    case 0: return v;
+    case 1: return make_float2(-v.y, v.x);
+    case 2: return make_float2(-v.x, -v.y);
+    default: return make_float2(v.y, -v.x);
+  }
+}
+
+struct WpccRowArgs {
+  const float2* X;     // window spectra of the chunk, Nz per row
+  const float2* W;     // S x Nz wavelet spectra
+  int S, filt_conj, rule, fmt;
+  void* out;           // phase spectra, row = window * S + scale, Nz per row (fmt F32 / F16)
+};
+
+__host__ __device__ constexpr int row_smem_floats2(int Q) {
+  return padded_len(Q) + 128 + tw_hi_len(Q) + 128 + tw_hi_len(4 * Q) + 17;
+}
+
+template <typename RADQ>
+__global__ void __cluster_dims__(kRowRanks, 1, 1) __launch_bounds__(kRowThreads, 1) k_wpcc_rows(WpccRowArgs a) {
+  constexpr int Q = prod_radices_of(RADQ{});
+  constexpr int N = kRowRanks * Q;
+  constexpr int T = kRowThreads;
+  extern __shared__ float4 smem_raw[];
+  float2* s = reinterpret_cast<float2*>(smem_raw);
+  float2* qlo = s + padded_len(Q);
+  float2* qhi = qlo + 128;
+  float2* nlo = qhi + tw_hi_len(Q);
+  float2* nhi = nlo + 128;
+  float* red = reinterpret_cast<float*>(nhi + tw_hi_len(N));   // 33 floats
+  const int k = (int)cluster_rank();
+  const int row = blockIdx.x / kRowRanks;
+  const float2* Xr = a.X + (int64_t)(row / a.S) * N;
+  const float2* Wr = a.W + (int64_t)(row % a.S) * N;
+  build_twiddles(qlo, qhi, Q);
+  build_twiddles(nlo, nhi, N);
+  __syncthreads();
+  const TwTab twN{nlo, nhi};
+  // inverse transform: this block's decimation of the band Y = X W_s (two
+  // points per thread at a time, so that sixteen loads are in flight)
+#pragma unroll 2
+  for (int f = threadIdx.x; f < Q; f += T) {
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < kRowRanks; j++) {
+      float2 w = __ldg(Wr + f + Q * j);
+      if (a.filt_conj) w.y = -w.y;
+      acc = cadd(acc, rot_quarter(cmul(__ldg(Xr + f + Q * j), w), k * j));
+    }
+    if (k) {
+      float2 t = twiddle(twN, k * f);   // exp(-2 pi i k f / N); k f < N
+      t.y = -t.y;
+      acc = cmul(acc, t);
+    }
+    s[PADI(f)] = acc;
+  }
+  __syncthreads();
+  ct_fft<+1, T, 1>(s, 1, 0, TwTab{qlo, qhi}, RADQ{});
+  // the row's maximum |x|^2 over the four blocks
+  float mx = 0.f;
+  for (int i = threadIdx.x; i < Q; i += T) {
+    const float2 v = s[PADI(i)];
+    mx = fmaxf(mx, v.x * v.x + v.y * v.y);
+  }
+  mx = warp_max(mx);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = red[threadIdx.x];   // T / 32 = 32 warps
+    v = warp_max(v);
+    if (threadIdx.x == 0) red[32] = v;
+  }
+  cluster_sync();
+  float gm = 0.f;
+#pragma unroll
+  for (int r = 0; r < kRowRanks; r++) gm = fmaxf(gm, cluster_ld(cluster_addr(red + 32, (uint32_t)r)));
+  const float eps = eps_of(a.rule, gm);
+  for (int i = threadIdx.x; i < Q; i += T) {
+    const float2 v = s[PADI(i)];
+    s[PADI(i)] = cscale(v, factor_of(a.rule, v.x * v.x + v.y * v.y, eps));
+  }
+  __syncthreads();
+  ct_fft<-1, T, 1>(s, 1, 0, TwTab{qlo, qhi}, RADQ{});
+  cluster_sync();   // every block's Z_r complete (and its maximum read)
+  uint32_t base[kRowRanks];
+#pragma unroll
+  for (int r = 0; r < kRowRanks; r++) base[r] = cluster_addr(s, (uint32_t)r);
+  const int64_t o = (int64_t)row * N + (int64_t)Q * k;
+#pragma unroll 2
+  for (int f = threadIdx.x; f < Q; f += T) {
+    float2 acc = cluster_ld2(base[0] + (uint32_t)PADI(f) * 8u);
+#pragma unroll
+    for (int r = 1; r < kRowRanks; r++) {
+      const float2 z = cmul(cluster_ld2(base[r] + (uint32_t)PADI(f) * 8u), twiddle(twN, r * f));
+      acc = cadd(acc, rot_quarter(z, -r * k));
+    }
+    if (a.fmt == SPEC_F16) reinterpret_cast<__half2*>(a.out)[o + f] = __float22half2_rn(acc);
+    else reinterpret_cast<float2*>(a.out)[o + f] = acc;
+  }
+  cluster_sync();   // no block leaves while the others read its shared memory
+}
+
+// The cluster kernel for row length Nz (Q = Nz / 4 on its menu), or null;
+// `smem` receives its dynamic shared memory.  The first call for a length sets
+// the kernel's shared-memory limit and checks that a cluster of four such
+// blocks can be resident.
+using RowKernel = void (*)(WpccRowArgs);
+RowKernel row_kernel(int Nz, size_t* smem) {
+  struct Entry { RowKernel fn; size_t smem; int ok; };
+  static Entry menu[3] = {{k_wpcc_rows<Radices<16, 16, 16, 4>>, 0, -1},
+                          {k_wpcc_rows<Radices<8, 8, 8, 8, 5>>, 0, -1},
+                          {k_wpcc_rows<Radices<8, 8, 8, 8, 6>>, 0, -1}};
+  static const int lens[3] = {16384, 20480, 24576};
+  if (const char* e = getenv("FPCC_WPCC_CLUSTER"))
+    if (e[0] == '0') return nullptr;
+  for (int i = 0; i < 3; i++) {
+    if (Nz != kRowRanks * lens[i]) continue;
+    Entry& en = menu[i];
+    if (en.ok < 0) {
+      en.smem = (size_t)row_smem_floats2(lens[i]) * sizeof(float2);
+      en.ok = 0;
+      if (cudaFuncSetAttribute(en.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)en.smem) == cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kRowRanks);
+        cfg.blockDim = dim3(kRowThreads);
+        cfg.dynamicSmemBytes = en.smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = kRowRanks;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, en.fn, &cfg) == cudaSuccess && n > 0) en.ok = 1;
+      }
+      cudaGetLastError();
+    }
+    if (en.ok != 1) return nullptr;
+    *smem = en.smem;
+    return en.fn;
+  }
+  return nullptr;
 }
 
 }  // namespace
@@ -121,6 +317,16 @@ cudaError_t wpcc_station(const WpccPlanDev& pl, const float* d_x, int64_t ldx, i
     if ((e = launch_large(a, st)) != cudaSuccess) return e;
     // bands: rows (window, scale)
     const int rows = cnt * S;
+    size_t rsmem = 0;
+    if (RowKernel rk = row_kernel(Nz, &rsmem)) {
+      // whole rows on clusters of four blocks
+      WpccRowArgs r{};
+      r.X = d_X; r.W = pl.d_W; r.S = S; r.filt_conj = pl.filt_conj; r.rule = pl.rule; r.fmt = fmt;
+      r.out = (char*)d_P + (size_t)r0 * S * Nz * pesz;
+      rk<<<dim3((unsigned)rows * kRowRanks), kRowThreads, rsmem, st>>>(r);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      continue;
+    }
     if ((e = cudaMemsetAsync(d_rowmax, 0, (size_t)rows * sizeof(float), st)) != cudaSuccess) return e;
     LargeArgs b{};
     b.n = Nz; b.n1 = n1; b.n2 = n2; b.dir = +1; b.nrows = rows;
