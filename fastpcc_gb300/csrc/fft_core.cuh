@@ -146,11 +146,11 @@ __device__ __forceinline__ void dft8(float2* v) {
   for (int k = 0; k < 4; k++) dft2<DIR>(v[2 * k], v[2 * k + 1]);
 }
 
+// 16 = 4 x 4 with n = 4 n1 + n2, k = k1 + 4 k2: DFT4 over n1 for each column
+// n2 (results k1 at v[4 k1 + n2]) and the twiddles exp(DIR*2*pi*i*n2*k1/16);
+// dft16 then takes a DFT4 over n2 for each k1 (k2 at v[4 k1 + k2]).
 template <int DIR>
-__device__ __forceinline__ void dft16(float2* v) {
-  // 16 = 4 x 4 with n = 4 n1 + n2, k = k1 + 4 k2:
-  // DFT4 over n1 for each column n2 (results k1 at v[4 k1 + n2]), twiddle
-  // exp(DIR*2*pi*i*n2*k1/16), DFT4 over n2 for each k1 (k2 at v[4 k1 + k2]).
+__device__ __forceinline__ void dft16_head(float2* v) {
 #pragma unroll
   for (int n2 = 0; n2 < 4; n2++) {
     float2 c[4] = {v[n2], v[4 + n2], v[8 + n2], v[12 + n2]};
@@ -175,6 +175,11 @@ __device__ __forceinline__ void dft16(float2* v) {
   v[7] = cmul(v[7], w3);
   v[11] = cmul(v[11], w6);
   v[15] = cmul(v[15], w9);
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft16(float2* v) {
+  dft16_head<DIR>(v);
 #pragma unroll
   for (int k1 = 0; k1 < 4; k1++) dft4<DIR>(v + 4 * k1);
 }

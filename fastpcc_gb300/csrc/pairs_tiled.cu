@@ -75,8 +75,12 @@ __host__ __device__ constexpr int split_b(int R1) { return R1 == 16 ? 1 : R1 / 8
 //   pass 2, butterfly k1: X[k1 + 16 k2] = sum_n1 Y[n1][k1] w_16^(n1 k2), stored at k2 + 16 k1.
 // A lane always has n1 (pass 1) and k1 (pass 2) equal to lane & 15, so its
 // fifteen twiddles are loaded once.  wm: exp(+2 pi i t / 256).
+// edges: only the outputs q in [-32, 32) mod 256 are read afterwards (k2 in
+// {14, 15, 0, 1}), so pass 2 forms those four of its sixteen: after the
+// column DFTs and twiddles of the 4 x 4 split (k2 = k1' + 4 k2'), the sums
+// over n2 for (k1', k2') = (0, 0), (1, 0), (2, 3) and (3, 3).
 template <int RW>
-__device__ __forceinline__ void warp_dft256(float2* rows0, const float2* __restrict__ wm, int lane) {
+__device__ __forceinline__ void warp_dft256(float2* rows0, const float2* __restrict__ wm, int lane, bool edges) {
   constexpr int NB = 16 * RW;   // butterflies per pass
   const int b = lane & 15;
   float2 tw[16];
@@ -105,9 +109,18 @@ __device__ __forceinline__ void warp_dft256(float2* rows0, const float2* __restr
       float2 v[16];
 #pragma unroll
       for (int r = 0; r < 16; r++) v[r] = x[r];
-      dft<16, 1>(v);
+      if (edges) {
+        dft16_head<1>(v);
+        x[0] = cadd(cadd(v[0], v[2]), cadd(v[1], v[3]));
+        x[1] = cadd(cadd(v[4], v[6]), cadd(v[5], v[7]));
+        // output 3 of a DFT4: (u0 - u2) - i (u1 - u3)
+        x[14] = csub(csub(v[8], v[10]), cmul_i<1>(csub(v[9], v[11])));
+        x[15] = csub(csub(v[12], v[14]), cmul_i<1>(csub(v[13], v[15])));
+      } else {
+        dft<16, 1>(v);
 #pragma unroll
-      for (int k2 = 0; k2 < 16; k2++) x[k2] = v[dft_perm<16>(k2)];
+        for (int k2 = 0; k2 < 16; k2++) x[k2] = v[dft_perm<16>(k2)];
+      }
     }
   }
 }
@@ -288,8 +301,17 @@ __global__ void __launch_bounds__(kTM, 2) k_pairs_tiled(PairArgs a) {
     for (int s = 0; s < R1; s++) rows[s * kTRowStride + P16(j)] = v[s];
     __syncthreads();
 
-    // ---- stage 2: M-point transforms of the warp's rows
-    warp_dft256<RW>(rows_w, wm, lane);
+    // ---- stage 2: M-point transforms of the warp's rows; when every output f
+    // that stage 3 reads lies within 32 R1 of 0 (lags within about +-64 R1),
+    // the rows' last pass forms only the outputs q in [-32, 32)
+    {
+      const int lag0 = a.desc ? a.desc[p].lag0 : a.lag0;
+      const int L = a.desc ? a.desc[p].L : a.L;
+      const int idx0 = lag0 < 0 ? lag0 + NZ : lag0;
+      const int f0 = (idx0 >> 1) >= HL / 2 ? (idx0 >> 1) - HL : (idx0 >> 1);
+      const int nout = (L + (idx0 & 1) + 1) >> 1;
+      warp_dft256<RW>(rows_w, wm, lane, f0 >= -32 * R1 && f0 + nout <= 32 * R1);
+    }
     __syncthreads();
 
     // ---- stage 3: the requested lags out of the tile
