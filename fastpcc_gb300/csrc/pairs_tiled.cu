@@ -75,52 +75,66 @@ __host__ __device__ constexpr int split_b(int R1) { return R1 == 16 ? 1 : R1 / 8
 //   pass 2, butterfly k1: X[k1 + 16 k2] = sum_n1 Y[n1][k1] w_16^(n1 k2), stored at k2 + 16 k1.
 // A lane always has n1 (pass 1) and k1 (pass 2) equal to lane & 15, so its
 // fifteen twiddles are loaded once.  wm: exp(+2 pi i t / 256).
+// Half-warps take one row each; with an odd row count the last row's pass 1
+// (lanes 0-15) and row 0's pass 2 (lanes 16-31) share one iteration, as one
+// instruction stream with per-lane strides and twiddles, so no lane idles.
 // edges: only the outputs q in [-32, 32) mod 256 are read afterwards (k2 in
-// {14, 15, 0, 1}), so pass 2 forms those four of its sixteen: after the
-// column DFTs and twiddles of the 4 x 4 split (k2 = k1' + 4 k2'), the sums
-// over n2 for (k1', k2') = (0, 0), (1, 0), (2, 3) and (3, 3).
+// {14, 15, 0, 1}), so the other pass-2 iterations form those four of their
+// sixteen: after the column DFTs and twiddles of the 4 x 4 split
+// (k2 = k1' + 4 k2'), the sums over n2 for (k1', k2') = (0, 0), (1, 0), (2, 3)
+// and (3, 3).
 template <int RW>
 __device__ __forceinline__ void warp_dft256(float2* rows0, const float2* __restrict__ wm, int lane, bool edges) {
-  constexpr int NB = 16 * RW;   // butterflies per pass
+  constexpr int PR = RW / 2;   // row pairs
   const int b = lane & 15;
+  const int h = lane >> 4;
   float2 tw[16];
 #pragma unroll
   for (int k = 1; k < 16; k++) tw[k] = wm[b * k];
 #pragma unroll
-  for (int t = 0; t < (NB + 31) / 32; t++) {
-    const int i = lane + 32 * t;
-    if (NB % 32 == 0 || i < NB) {
-      float2* x = rows0 + (i >> 4) * kTRowStride + b;   // P16(b + 16 r) = b + 17 r
-      float2 v[16];
+  for (int u = 0; u < PR; u++) {
+    float2* x = rows0 + ((lane + 32 * u) >> 4) * kTRowStride + b;   // P16(b + 16 r) = b + 17 r
+    float2 v[16];
 #pragma unroll
-      for (int r = 0; r < 16; r++) v[r] = x[17 * r];
-      dft<16, 1>(v);
-      x[0] = v[dft_perm<16>(0)];
+    for (int r = 0; r < 16; r++) v[r] = x[17 * r];
+    dft<16, 1>(v);
+    x[0] = v[dft_perm<16>(0)];
 #pragma unroll
-      for (int k1 = 1; k1 < 16; k1++) x[17 * k1] = cmul(v[dft_perm<16>(k1)], tw[k1]);
-    }
+    for (int k1 = 1; k1 < 16; k1++) x[17 * k1] = cmul(v[dft_perm<16>(k1)], tw[k1]);
   }
   __syncwarp();
+  if constexpr (RW % 2 == 1) {
+    // lanes 0-15: pass 1 of row RW-1 (stride 17, twiddles); lanes 16-31: pass 2
+    // of row 0 (stride 1, all sixteen outputs)
+    float2* x = h ? rows0 + 17 * b : rows0 + (RW - 1) * kTRowStride + b;
+    const int ls = h ? 1 : 17;
+    float2 v[16];
 #pragma unroll
-  for (int t = 0; t < (NB + 31) / 32; t++) {
-    const int i = lane + 32 * t;
-    if (NB % 32 == 0 || i < NB) {
-      float2* x = rows0 + (i >> 4) * kTRowStride + 17 * b;   // P16(16 b + n) = 17 b + n
-      float2 v[16];
+    for (int r = 0; r < 16; r++) v[r] = x[ls * r];
+    dft<16, 1>(v);
+    x[0] = v[dft_perm<16>(0)];
 #pragma unroll
-      for (int r = 0; r < 16; r++) v[r] = x[r];
-      if (edges) {
-        dft16_head<1>(v);
-        x[0] = cadd(cadd(v[0], v[2]), cadd(v[1], v[3]));
-        x[1] = cadd(cadd(v[4], v[6]), cadd(v[5], v[7]));
-        // output 3 of a DFT4: (u0 - u2) - i (u1 - u3)
-        x[14] = csub(csub(v[8], v[10]), cmul_i<1>(csub(v[9], v[11])));
-        x[15] = csub(csub(v[12], v[14]), cmul_i<1>(csub(v[13], v[15])));
-      } else {
-        dft<16, 1>(v);
+    for (int k = 1; k < 16; k++) x[ls * k] = h ? v[dft_perm<16>(k)] : cmul(v[dft_perm<16>(k)], tw[k]);
+    __syncwarp();
+  }
+  constexpr int R0 = RW % 2;   // first row left for pass 2
 #pragma unroll
-        for (int k2 = 0; k2 < 16; k2++) x[k2] = v[dft_perm<16>(k2)];
-      }
+  for (int u = 0; u < PR; u++) {
+    float2* x = rows0 + (R0 + ((lane + 32 * u) >> 4)) * kTRowStride + 17 * b;   // P16(16 b + n) = 17 b + n
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; r++) v[r] = x[r];
+    if (edges) {
+      dft16_head<1>(v);
+      x[0] = cadd(cadd(v[0], v[2]), cadd(v[1], v[3]));
+      x[1] = cadd(cadd(v[4], v[6]), cadd(v[5], v[7]));
+      // output 3 of a DFT4: (u0 - u2) - i (u1 - u3)
+      x[14] = csub(csub(v[8], v[10]), cmul_i<1>(csub(v[9], v[11])));
+      x[15] = csub(csub(v[12], v[14]), cmul_i<1>(csub(v[13], v[15])));
+    } else {
+      dft<16, 1>(v);
+#pragma unroll
+      for (int k2 = 0; k2 < 16; k2++) x[k2] = v[dft_perm<16>(k2)];
     }
   }
 }
