@@ -49,6 +49,21 @@ def test_pcc2_both_forms(F, orc, nz, N, l1, l2):
 
 
 @pytest.mark.parametrize("nz", NZS)
+def test_row_pass_pruning_edges(F, orc, nz):
+    """The tiled kernel's last row pass forms only the row outputs q in
+    [-32, 32) when every stored lag lies in [-64 R1, 64 R1) (R1 = Nz / 512):
+    lag windows exactly at that edge (even and odd first lag) and one lag past
+    it on either side (full pass)."""
+    e = nz // 8
+    a, b = synth.plain_pair(N=4000, n_windows=2, delay=120, tag="gpu/forms/edges")
+    for l1, l2 in ((-e, e - 1), (-e + 1, e - 2), (-e - 1, e - 1), (-e, e), (e - 700, e - 1), (-e, -e + 500)):
+        y64 = orc.pcc2(a, b, l1, l2)
+        yb, yt = both_forms(F, nz, lambda: F.pcc2_set(a, b, l1, l2, nz_mode=nz))
+        assert relerr(yb, y64) < TOL, (l1, l2)
+        assert relerr(yt, y64) < TOL, (l1, l2)
+
+
+@pytest.mark.parametrize("nz", NZS)
 def test_gncc_and_1bit_both_forms(F, orc, nz):
     a, b = synth.plain_pair(N=7000, n_windows=2, delay=-180, tag="gpu/forms/herm")
     for f, o in ((F.ccgn_set, orc.gncc), (F.cc1b_set, orc.cc1b)):
