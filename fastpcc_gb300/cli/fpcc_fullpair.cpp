@@ -268,7 +268,7 @@ int parse(int argc, char** argv, Options& o) {
 // ------------------------------------------------------------------ reading
 struct Station {
   std::vector<TraceHeader> hdr;
-  float* x = nullptr;        // Tr x N, pinned when the driver allows it
+  float* x = nullptr;        // Tr x N, pinned when the CUDA driver allows it
   bool pinned = false;
   int N = 0, Tr = 0;
   float dt = 0;

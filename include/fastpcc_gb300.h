@@ -36,7 +36,7 @@ extern "C" {
 #define FPCC_ECUDA (-1)    /* CUDA runtime failure (the reference's -1)          */
 #define FPCC_ENOMEM (-2)   /* allocation failure                                  */
 #define FPCC_EARG (-3)     /* invalid argument, e.g. |lag| >= N (reference's -3)  */
-#define FPCC_EUNSUP (-4)   /* size or option not supported by this build          */
+#define FPCC_EUNSUP (-4)   /* size or option not supported by this library        */
 
 enum fpcc_method {
   FPCC_PCC2 = 0,
@@ -109,7 +109,7 @@ int fpcc_choose_nz(int N, int Lag1, int Lag2, int mode);
  * lengths the table does not cover. */
 int fpcc_autotune(fpcc_ctx *ctx, int min_nz, int max_nz, double reuse, const char *json_path);
 int fpcc_autotune_load(const char *json_path);
-/* Largest length an in-block transform of this build supports. */
+/* Largest length an in-block transform of this library supports. */
 int fpcc_max_block_len(void);
 /* Pair kernel that runs the FFT methods' pair stage at padded length Nz:
  * FPCC_PAIR_BLOCK (one block per correlation, Stockham passes through shared
