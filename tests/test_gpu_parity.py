@@ -386,11 +386,18 @@ def test_allpairs_host_first_use_pipeline(F, orc):
     y = np.zeros((P, L), np.float32)
     ctx.allpairs_host(F.PCC2, x, pairs, -lag, lag, y)
     assert np.array_equal(yp.numpy(), y[perm])
-    # a row index outside the station rows is refused before any work
-    bad = pairs.copy()
-    bad[7, 0] = -1
-    with pytest.raises(F.FpccError):
-        ctx.allpairs_host(F.PCC2, xp.numpy(), bad, -lag, lag, yp.numpy())
+    # a row index outside the station rows is refused before any result is
+    # written, early or late in the pair list; the context stays usable
+    for at in ((7, 0), (P - 5, 1)):
+        bad = pairs.copy()
+        bad[at] = -1 if at[1] == 0 else n_sta * n_win
+        yp.fill_(7.0)
+        with pytest.raises(F.FpccError):
+            ctx.allpairs_host(F.PCC2, xp.numpy(), bad, -lag, lag, yp.numpy())
+        assert (yp.numpy() == 7.0).all()
+    yp.zero_()
+    ctx.allpairs_host(F.PCC2, xp.numpy(), pairs, -lag, lag, yp.numpy())
+    assert np.array_equal(yp.numpy(), y)
     ctx.close()
 
 
