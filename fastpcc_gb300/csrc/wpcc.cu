@@ -59,7 +59,9 @@ __global__ void __launch_bounds__(256) k_wpcc_accum(const void* __restrict__ P, 
 // The band and phase-spectrum transforms of one (window, scale) row, N = 4Q
 // points, on a cluster of four blocks whose shared memories hold the row
 // between the transforms (no global-memory round trip):
-//   inverse, block k:  z_k[f] = w_N^(+k f) sum_j Y[f + Q j] i^(k j),  Y = X W_s,
+//   inverse:           z_k[f] = w_N^(+k f) sum_j Y[f + Q j] i^(k j),  Y = X W_s
+//                      (block k reads the band at f in [k Q/4, (k+1) Q/4) only
+//                      and stores z_r[f] of every r into block r),
 //                      x[4m + k] = IDFT_Q(z_k)[m]                       (in place)
 //   normalise:         x *= factor(|x|^2, eps(max over the four blocks))
 //   forward, block k:  Z_k = DFT_Q(x[4m + k]),  then block j writes
@@ -96,6 +98,9 @@ __device__ __forceinline__ float2 cluster_ld2(uint32_t addr) {
   float2 v;
   asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
   return v;
+}
+__device__ __forceinline__ void cluster_st2(uint32_t addr, float2 v) {
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(v.x), "f"(v.y) : "memory");
 }
 __device__ __forceinline__ float cluster_ld(uint32_t addr) {
   float v;
@@ -143,25 +148,38 @@ __global__ void __cluster_dims__(kRowRanks, 1, 1) __launch_bounds__(kRowThreads,
   build_twiddles(nlo, nhi, N);
   __syncthreads();
   const TwTab twN{nlo, nhi};
-  // inverse transform: this block's decimation of the band Y = X W_s (two
-  // points per thread at a time, so that sixteen loads are in flight)
+  cluster_sync();   // every block of the cluster is running: its shared memory can be written
+  // inverse transform: the four decimations z_r of the band Y = X W_s at this
+  // block's quarter of f (two points per thread at a time, so that sixteen
+  // loads are in flight), each stored into block r
+  uint32_t base[kRowRanks];
+#pragma unroll
+  for (int r = 0; r < kRowRanks; r++) base[r] = cluster_addr(s, (uint32_t)r);
+  constexpr int QB = Q / kRowRanks;
+  static_assert(Q % kRowRanks == 0, "quarter of the row");
 #pragma unroll 2
-  for (int f = threadIdx.x; f < Q; f += T) {
-    float2 acc = make_float2(0.f, 0.f);
+  for (int f = k * QB + (int)threadIdx.x; f < (k + 1) * QB; f += T) {
+    float2 y[kRowRanks];
 #pragma unroll
     for (int j = 0; j < kRowRanks; j++) {
       float2 w = __ldg(Wr + f + Q * j);
       if (a.filt_conj) w.y = -w.y;
-      acc = cadd(acc, rot_quarter(cmul(__ldg(Xr + f + Q * j), w), k * j));
+      y[j] = cmul(__ldg(Xr + f + Q * j), w);
     }
-    if (k) {
-      float2 t = twiddle(twN, k * f);   // exp(-2 pi i k f / N); k f < N
-      t.y = -t.y;
-      acc = cmul(acc, t);
+#pragma unroll
+    for (int r = 0; r < kRowRanks; r++) {
+      float2 acc = y[0];
+#pragma unroll
+      for (int j = 1; j < kRowRanks; j++) acc = cadd(acc, rot_quarter(y[j], r * j));
+      if (r) {
+        float2 t = twiddle(twN, r * f);   // exp(-2 pi i r f / N); r f < N
+        t.y = -t.y;
+        acc = cmul(acc, t);
+      }
+      cluster_st2(base[r] + (uint32_t)PADI(f) * 8u, acc);
     }
-    s[PADI(f)] = acc;
   }
-  __syncthreads();
+  cluster_sync();   // every block's z_k complete
   ct_fft<+1, T, 1>(s, 1, 0, TwTab{qlo, qhi}, RADQ{});
   // the row's maximum |x|^2 over the four blocks
   float mx = 0.f;
@@ -189,9 +207,6 @@ __global__ void __cluster_dims__(kRowRanks, 1, 1) __launch_bounds__(kRowThreads,
   __syncthreads();
   ct_fft<-1, T, 1>(s, 1, 0, TwTab{qlo, qhi}, RADQ{});
   cluster_sync();   // every block's Z_r complete (and its maximum read)
-  uint32_t base[kRowRanks];
-#pragma unroll
-  for (int r = 0; r < kRowRanks; r++) base[r] = cluster_addr(s, (uint32_t)r);
   const int64_t o = (int64_t)row * N + (int64_t)Q * k;
 #pragma unroll 2
   for (int f = threadIdx.x; f < Q; f += T) {
