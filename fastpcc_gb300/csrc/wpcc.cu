@@ -64,8 +64,9 @@ __global__ void __launch_bounds__(256) k_wpcc_accum(const void* __restrict__ P, 
 //                      and stores z_r[f] of every r into block r),
 //                      x[4m + k] = IDFT_Q(z_k)[m]                       (in place)
 //   normalise:         x *= factor(|x|^2, eps(max over the four blocks))
-//   forward, block k:  Z_k = DFT_Q(x[4m + k]),  then block j writes
-//                      P[f + Q j] = sum_r (-i)^(r j) w_N^(-r f) Z_r[f]   (Z_r read from block r)
+//   forward, block k:  Z_k = DFT_Q(x[4m + k]),  then
+//                      P[f + Q j] = sum_r (-i)^(r j) w_N^(-r f) Z_r[f]   (Z_r read from block r;
+//                      block k writes every j at its quarter of f)
 // The same arithmetic as the four-step passes (`launch_large` with the band
 // product, the row maximum, the normalising load and the spectrum store) in
 // another order of the FFT's butterflies.
@@ -207,17 +208,23 @@ __global__ void __cluster_dims__(kRowRanks, 1, 1) __launch_bounds__(kRowThreads,
   __syncthreads();
   ct_fft<-1, T, 1>(s, 1, 0, TwTab{qlo, qhi}, RADQ{});
   cluster_sync();   // every block's Z_r complete (and its maximum read)
-  const int64_t o = (int64_t)row * N + (int64_t)Q * k;
+  // the spectrum at this block's quarter of f in all four output quarters j,
+  // from the four blocks' Z_r[f]
+  const int64_t o = (int64_t)row * N;
 #pragma unroll 2
-  for (int f = threadIdx.x; f < Q; f += T) {
-    float2 acc = cluster_ld2(base[0] + (uint32_t)PADI(f) * 8u);
+  for (int f = k * QB + (int)threadIdx.x; f < (k + 1) * QB; f += T) {
+    float2 z[kRowRanks];
+    z[0] = cluster_ld2(base[0] + (uint32_t)PADI(f) * 8u);
 #pragma unroll
-    for (int r = 1; r < kRowRanks; r++) {
-      const float2 z = cmul(cluster_ld2(base[r] + (uint32_t)PADI(f) * 8u), twiddle(twN, r * f));
-      acc = cadd(acc, rot_quarter(z, -r * k));
+    for (int r = 1; r < kRowRanks; r++) z[r] = cmul(cluster_ld2(base[r] + (uint32_t)PADI(f) * 8u), twiddle(twN, r * f));
+#pragma unroll
+    for (int j = 0; j < kRowRanks; j++) {
+      float2 acc = z[0];
+#pragma unroll
+      for (int r = 1; r < kRowRanks; r++) acc = cadd(acc, rot_quarter(z[r], -r * j));
+      if (a.fmt == SPEC_F16) reinterpret_cast<__half2*>(a.out)[o + f + (int64_t)Q * j] = __float22half2_rn(acc);
+      else reinterpret_cast<float2*>(a.out)[o + f + (int64_t)Q * j] = acc;
     }
-    if (a.fmt == SPEC_F16) reinterpret_cast<__half2*>(a.out)[o + f] = __float22half2_rn(acc);
-    else reinterpret_cast<float2*>(a.out)[o + f] = acc;
   }
   cluster_sync();   // no block leaves while the others read its shared memory
 }
