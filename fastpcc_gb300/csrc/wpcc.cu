@@ -56,17 +56,17 @@ __global__ void __launch_bounds__(256) k_wpcc_accum(const void* __restrict__ P, 
 }
 
 // ---------------------------------------------------------------- whole rows on a cluster
-// The band and phase-spectrum transforms of one (window, scale) row, N = 4Q
-// points, on a cluster of four blocks whose shared memories hold the row
-// between the transforms (no global-memory round trip):
-//   inverse:           z_k[f] = w_N^(+k f) sum_j Y[f + Q j] i^(k j),  Y = X W_s
-//                      (block k reads the band at f in [k Q/4, (k+1) Q/4) only
+// The band and phase-spectrum transforms of one (window, scale) row, N = R Q
+// points, on a cluster of R = 4 or 8 blocks whose shared memories hold the
+// row between the transforms (no global-memory round trip):
+//   inverse:           z_k[f] = w_N^(+k f) sum_j Y[f + Q j] w_R^(+k j),  Y = X W_s
+//                      (block k reads the band at f in [k Q/R, (k+1) Q/R) only
 //                      and stores z_r[f] of every r into block r),
-//                      x[4m + k] = IDFT_Q(z_k)[m]                       (in place)
-//   normalise:         x *= factor(|x|^2, eps(max over the four blocks))
-//   forward, block k:  Z_k = DFT_Q(x[4m + k]),  then
-//                      P[f + Q j] = sum_r (-i)^(r j) w_N^(-r f) Z_r[f]   (Z_r read from block r;
-//                      block k writes every j at its quarter of f)
+//                      x[R m + k] = IDFT_Q(z_k)[m]                      (in place)
+//   normalise:         x *= factor(|x|^2, eps(max over the R blocks))
+//   forward, block k:  Z_k = DFT_Q(x[R m + k]),  then
+//                      P[f + Q j] = sum_r w_R^(-r j) w_N^(-r f) Z_r[f]   (Z_r read from block r;
+//                      block k writes every j at its share of f)
 // The same arithmetic as the four-step passes (`launch_large` with the band
 // product, the row maximum, the normalising load and the spectrum store) in
 // another order of the FFT's butterflies.
@@ -75,7 +75,6 @@ __host__ __device__ constexpr int prod_radices_of(Radices<Rs...>) {
   return prod_radices<Rs...>();
 }
 
-constexpr int kRowRanks = 4;      // blocks per row (the cluster)
 constexpr int kRowThreads = 1024;
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -117,6 +116,19 @@ __device__ __forceinline__ float2 rot_quarter(float2 v, int q) {
     default: return make_float2(v.y, -v.x);
   }
 }
+// v * w_R^q = v * exp(2 pi i q / R) for R = 4 or 8
+template <int R>
+__device__ __forceinline__ float2 rot_root(float2 v, int q) {
+  static_assert(R == 4 || R == 8, "cluster sizes");
+  if constexpr (R == 4) {
+    return rot_quarter(v, q);
+  } else {
+    const float2 t = rot_quarter(v, (q & 7) >> 1);
+    if (!(q & 1)) return t;
+    const float h = 0.70710678118654752440f;   // w_8 = (1 + i) / sqrt(2)
+    return make_float2(h * (t.x - t.y), h * (t.x + t.y));
+  }
+}
 
 struct WpccRowArgs {
   const float2* X;     // window spectra of the chunk, Nz per row
@@ -125,12 +137,13 @@ struct WpccRowArgs {
   void* out;           // phase spectra, row = window * S + scale, Nz per row (fmt F32 / F16)
 };
 
-__host__ __device__ constexpr int row_smem_floats2(int Q) {
-  return padded_len(Q) + 128 + tw_hi_len(Q) + 128 + tw_hi_len(4 * Q) + 17;
+__host__ __device__ constexpr int row_smem_floats2(int R, int Q) {
+  return padded_len(Q) + 128 + tw_hi_len(Q) + 128 + tw_hi_len(R * Q) + 17;
 }
 
-template <typename RADQ>
-__global__ void __cluster_dims__(kRowRanks, 1, 1) __launch_bounds__(kRowThreads, 1) k_wpcc_rows(WpccRowArgs a) {
+template <int R, typename RADQ>
+__global__ void __cluster_dims__(R, 1, 1) __launch_bounds__(kRowThreads, 1) k_wpcc_rows(WpccRowArgs a) {
+  constexpr int kRowRanks = R;
   constexpr int Q = prod_radices_of(RADQ{});
   constexpr int N = kRowRanks * Q;
   constexpr int T = kRowThreads;
@@ -150,14 +163,14 @@ __global__ void __cluster_dims__(kRowRanks, 1, 1) __launch_bounds__(kRowThreads,
   __syncthreads();
   const TwTab twN{nlo, nhi};
   cluster_sync();   // every block of the cluster is running: its shared memory can be written
-  // inverse transform: the four decimations z_r of the band Y = X W_s at this
-  // block's quarter of f (two points per thread at a time, so that sixteen
-  // loads are in flight), each stored into block r
+  // inverse transform: the R decimations z_r of the band Y = X W_s at this
+  // block's share of f (two points per thread at a time, so that 4 R loads
+  // are in flight), each stored into block r
   uint32_t base[kRowRanks];
 #pragma unroll
   for (int r = 0; r < kRowRanks; r++) base[r] = cluster_addr(s, (uint32_t)r);
   constexpr int QB = Q / kRowRanks;
-  static_assert(Q % kRowRanks == 0, "quarter of the row");
+  static_assert(Q % kRowRanks == 0, "share of the row");
 #pragma unroll 2
   for (int f = k * QB + (int)threadIdx.x; f < (k + 1) * QB; f += T) {
     float2 y[kRowRanks];
@@ -171,7 +184,7 @@ __global__ void __cluster_dims__(kRowRanks, 1, 1) __launch_bounds__(kRowThreads,
     for (int r = 0; r < kRowRanks; r++) {
       float2 acc = y[0];
 #pragma unroll
-      for (int j = 1; j < kRowRanks; j++) acc = cadd(acc, rot_quarter(y[j], r * j));
+      for (int j = 1; j < kRowRanks; j++) acc = cadd(acc, rot_root<R>(y[j], r * j));
       if (r) {
         float2 t = twiddle(twN, r * f);   // exp(-2 pi i r f / N); r f < N
         t.y = -t.y;
@@ -208,8 +221,8 @@ __global__ void __cluster_dims__(kRowRanks, 1, 1) __launch_bounds__(kRowThreads,
   __syncthreads();
   ct_fft<-1, T, 1>(s, 1, 0, TwTab{qlo, qhi}, RADQ{});
   cluster_sync();   // every block's Z_r complete (and its maximum read)
-  // the spectrum at this block's quarter of f in all four output quarters j,
-  // from the four blocks' Z_r[f]
+  // the spectrum at this block's share of f in all R output parts j, from
+  // the R blocks' Z_r[f]
   const int64_t o = (int64_t)row * N;
 #pragma unroll 2
   for (int f = k * QB + (int)threadIdx.x; f < (k + 1) * QB; f += T) {
@@ -221,7 +234,7 @@ __global__ void __cluster_dims__(kRowRanks, 1, 1) __launch_bounds__(kRowThreads,
     for (int j = 0; j < kRowRanks; j++) {
       float2 acc = z[0];
 #pragma unroll
-      for (int r = 1; r < kRowRanks; r++) acc = cadd(acc, rot_quarter(z[r], -r * j));
+      for (int r = 1; r < kRowRanks; r++) acc = cadd(acc, rot_root<R>(z[r], -r * j));
       if (a.fmt == SPEC_F16) reinterpret_cast<__half2*>(a.out)[o + f + (int64_t)Q * j] = __float22half2_rn(acc);
       else reinterpret_cast<float2*>(a.out)[o + f + (int64_t)Q * j] = acc;
     }
@@ -229,33 +242,35 @@ __global__ void __cluster_dims__(kRowRanks, 1, 1) __launch_bounds__(kRowThreads,
   cluster_sync();   // no block leaves while the others read its shared memory
 }
 
-// The cluster kernel for row length Nz (Q = Nz / 4 on its menu), or null;
-// `smem` receives its dynamic shared memory.  The first call for a length sets
-// the kernel's shared-memory limit and checks that a cluster of four such
-// blocks can be resident.
+// The cluster kernel for row length Nz (Nz = R Q with R = 4 or 8 blocks and Q
+// on its menu), or null; `smem` and `ranks` receive its dynamic shared memory
+// and cluster size.  The first call for a length sets the kernel's
+// shared-memory limit and checks that a cluster of such blocks can be
+// resident.
 using RowKernel = void (*)(WpccRowArgs);
-RowKernel row_kernel(int Nz, size_t* smem) {
-  struct Entry { RowKernel fn; size_t smem; int ok; };
-  static Entry menu[3] = {{k_wpcc_rows<Radices<16, 16, 16, 4>>, 0, -1},
-                          {k_wpcc_rows<Radices<8, 8, 8, 8, 5>>, 0, -1},
-                          {k_wpcc_rows<Radices<8, 8, 8, 8, 6>>, 0, -1}};
-  static const int lens[3] = {16384, 20480, 24576};
+RowKernel row_kernel(int Nz, size_t* smem, int* ranks) {
+  struct Entry { RowKernel fn; int R, Q; size_t smem; int ok; };
+  static Entry menu[6] = {{k_wpcc_rows<4, Radices<16, 16, 16, 4>>, 4, 16384, 0, -1},
+                          {k_wpcc_rows<4, Radices<8, 8, 8, 8, 5>>, 4, 20480, 0, -1},
+                          {k_wpcc_rows<4, Radices<8, 8, 8, 8, 6>>, 4, 24576, 0, -1},
+                          {k_wpcc_rows<8, Radices<16, 16, 16, 4>>, 8, 16384, 0, -1},
+                          {k_wpcc_rows<8, Radices<8, 8, 8, 8, 5>>, 8, 20480, 0, -1},
+                          {k_wpcc_rows<8, Radices<8, 8, 8, 8, 6>>, 8, 24576, 0, -1}};
   if (const char* e = getenv("FPCC_WPCC_CLUSTER"))
     if (e[0] == '0') return nullptr;
-  for (int i = 0; i < 3; i++) {
-    if (Nz != kRowRanks * lens[i]) continue;
-    Entry& en = menu[i];
+  for (Entry& en : menu) {
+    if (Nz != en.R * en.Q) continue;
     if (en.ok < 0) {
-      en.smem = (size_t)row_smem_floats2(lens[i]) * sizeof(float2);
+      en.smem = (size_t)row_smem_floats2(en.R, en.Q) * sizeof(float2);
       en.ok = 0;
       if (cudaFuncSetAttribute(en.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)en.smem) == cudaSuccess) {
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(kRowRanks);
+        cfg.gridDim = dim3((unsigned)en.R);
         cfg.blockDim = dim3(kRowThreads);
         cfg.dynamicSmemBytes = en.smem;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = kRowRanks;
+        at[0].val.clusterDim.x = (unsigned)en.R;
         at[0].val.clusterDim.y = 1;
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
@@ -267,6 +282,7 @@ RowKernel row_kernel(int Nz, size_t* smem) {
     }
     if (en.ok != 1) return nullptr;
     *smem = en.smem;
+    *ranks = en.R;
     return en.fn;
   }
   return nullptr;
@@ -340,12 +356,13 @@ cudaError_t wpcc_station(const WpccPlanDev& pl, const float* d_x, int64_t ldx, i
     // bands: rows (window, scale)
     const int rows = cnt * S;
     size_t rsmem = 0;
-    if (RowKernel rk = row_kernel(Nz, &rsmem)) {
-      // whole rows on clusters of four blocks
+    int ranks = 0;
+    if (RowKernel rk = row_kernel(Nz, &rsmem, &ranks)) {
+      // whole rows on clusters of four or eight blocks
       WpccRowArgs r{};
       r.X = d_X; r.W = pl.d_W; r.S = S; r.filt_conj = pl.filt_conj; r.rule = pl.rule; r.fmt = fmt;
       r.out = (char*)d_P + (size_t)r0 * S * Nz * pesz;
-      rk<<<dim3((unsigned)rows * kRowRanks), kRowThreads, rsmem, st>>>(r);
+      rk<<<dim3((unsigned)rows * (unsigned)ranks), kRowThreads, rsmem, st>>>(r);
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
       continue;
     }

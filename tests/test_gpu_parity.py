@@ -269,13 +269,18 @@ def test_wpcc_gpu_rule(F, orc):
     assert relerr(F.wpcc_set(a, b, -300, 300, 4.0, 80.0, V=3, type=-1, rule=F.AMP_THRESH), y64) < TOL
 
 
-def test_wpcc_wavelet_config_size(F, orc):
-    """65,536 samples at 20 Hz, Morlet, 40 scales (V=5, 4 to 1000 samples), lags +-4000."""
+def test_wpcc_wavelet_config_size(F, orc, monkeypatch):
+    """65,536 samples at 20 Hz, Morlet, 40 scales (V=5, 4 to 1000 samples), lags +-4000,
+    at the fast padded length (81920: rows on clusters of four blocks) and the
+    reference's (2^17: clusters of eight), and both again as four-step passes."""
     x1, x2, _ = synth.wavelet_pairs(n_pairs=1, n_windows=1, tag="gpu/wpcc-c3")
     a, b = x1[0], x2[0]
     y64 = orc.wpcc(a, b, -4000, 4000, 4.0, 1000.0, V=5, wtype=-1)
-    y = F.wpcc_set(a, b, -4000, 4000, 4.0, 1000.0, V=5, type=-1)
-    assert relerr(y, y64) < TOL
+    for cluster in ("1", "0"):
+        monkeypatch.setenv("FPCC_WPCC_CLUSTER", cluster)
+        for nz_mode in (F.NZ_FAST, F.NZ_REFERENCE):
+            y = F.wpcc_set(a, b, -4000, 4000, 4.0, 1000.0, V=5, type=-1, nz_mode=nz_mode)
+            assert relerr(y, y64) < TOL, (cluster, nz_mode)
 
 
 # ---- window lengths with prime factors above 5 (Bluestein analytic signal) -----
