@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/fastpcc_gb300.h"
@@ -137,7 +138,7 @@ struct WpccRowArgs {
   void* out;           // phase spectra, row = window * S + scale, Nz per row (fmt F32 / F16)
 };
 
-__host__ __device__ constexpr int row_smem_floats2(int R, int Q) {
+inline int row_smem_floats2(int R, int Q) {
   return padded_len(Q) + 128 + tw_hi_len(Q) + 128 + tw_hi_len(R * Q) + 17;
 }
 
@@ -258,6 +259,9 @@ RowKernel row_kernel(int Nz, size_t* smem, int* ranks) {
                           {k_wpcc_rows<8, Radices<8, 8, 8, 8, 6>>, 8, 24576, 0, -1}};
   if (const char* e = getenv("FPCC_WPCC_CLUSTER"))
     if (e[0] == '0') return nullptr;
+  // one first-use check per entry, whichever host thread gets there first
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
   for (Entry& en : menu) {
     if (Nz != en.R * en.Q) continue;
     if (en.ok < 0) {
