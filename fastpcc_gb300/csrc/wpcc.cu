@@ -196,7 +196,7 @@ __global__ void __cluster_dims__(R, 1, 1) __launch_bounds__(kRowThreads, 1) k_wp
   }
   cluster_sync();   // every block's z_k complete
   ct_fft<+1, T, 1>(s, 1, 0, TwTab{qlo, qhi}, RADQ{});
-  // the row's maximum |x|^2 over the four blocks
+  // the row's maximum |x|^2 over the R blocks
   float mx = 0.f;
   for (int i = threadIdx.x; i < Q; i += T) {
     const float2 v = s[PADI(i)];
