@@ -83,7 +83,7 @@ __device__ __forceinline__ uint32_t cluster_rank() {
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
   return r;
 }
-// all threads of all four blocks: shared-memory writes before it are seen by
+// all threads of all blocks of the cluster: shared-memory writes before it are seen by
 // the cluster's reads after it
 __device__ __forceinline__ void cluster_sync() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
