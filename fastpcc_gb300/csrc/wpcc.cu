@@ -9,7 +9,10 @@
 // Pair stage (per pair window):
 //   Y = sum_s conj(P1_s) P2_s / (scale_s Nz)                            (:1217-1218)
 //   y = C Re IDFT_Nz(Y) at the lags, C = 1/(K0 N)                       (:1220-1224)
-// All transforms use the four-step kernels; P_s is the cached station product.
+// B_s and P_s of a (window, scale) row run on a thread-block cluster that holds
+// the row in its blocks' shared memories where Nz is on that kernel's menu
+// (k_wpcc_rows below), else as four-step kernels like every other transform
+// here; P_s is the cached station product.
 // Any length >= N + M + Ls0 gives the reference's values (every operation is a
 // linear convolution inside that support), so the planner may pick a shorter
 // length than the reference's power of two.
