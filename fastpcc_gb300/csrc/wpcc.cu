@@ -209,7 +209,7 @@ __global__ void __cluster_dims__(R, 1, 1) __launch_bounds__(kRowThreads, 1) k_wp
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
   __syncthreads();
   if (threadIdx.x < 32) {
-    float v = red[threadIdx.x];   // T / 32 = 32 warps
+    float v = (threadIdx.x < T / 32) ? red[threadIdx.x] : 0.f;
     v = warp_max(v);
     if (threadIdx.x == 0) red[32] = v;
   }
