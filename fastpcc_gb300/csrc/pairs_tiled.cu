@@ -114,7 +114,7 @@ __device__ __forceinline__ void warp_dft256(float2* rows0, const float2* __restr
     dft<16, 1>(v);
     x[0] = v[dft_perm<16>(0)];
 #pragma unroll
-    for (int k = 1; k < 16; k++) x[ls * k] = h ? v[dft_perm<16>(k)] : cmul(v[dft_perm<16>(k)], tw[k]);
+    for (int k = 1; k < 16; k++) x[ls * k] = cmul(v[dft_perm<16>(k)], h ? make_float2(1.f, 0.f) : tw[k]);
     __syncwarp();
   }
   constexpr int R0 = RW % 2;   // first row left for pass 2
